@@ -1,0 +1,254 @@
+/*
+ * trvg.h -- C ABI of the GB300-native mesh-based clustering estimators.
+ *
+ * Drop-in boundary for Triumvirate's FFT-based three-point (and two-point)
+ * estimators.  Every entry point replaces one reference C++ function of
+ * MikeSWang/Triumvirate (paths relative to src/triumvirate/):
+ *
+ *   trvg_compute_bispec_in_gpp_box  <- trv::compute_bispec_in_gpp_box
+ *                                      (include/threept.hpp:274)
+ *   trvg_compute_bispec             <- trv::compute_bispec
+ *                                      (include/threept.hpp:237)
+ *   trvg_compute_3pcf_in_gpp_box    <- trv::compute_3pcf_in_gpp_box
+ *                                      (include/threept.hpp:290)
+ *   trvg_compute_3pcf               <- trv::compute_3pcf
+ *                                      (include/threept.hpp:257)
+ *   trvg_compute_powspec_in_gpp_box <- trv::compute_powspec_in_gpp_box
+ *                                      (include/twopt.hpp:283)
+ *   trvg_compute_powspec            <- trv::compute_powspec
+ *                                      (include/twopt.hpp:246)
+ *   trvg_calc_grid_based_powlaw_norm<- trv::MeshField::
+ *                                      calc_grid_based_powlaw_norm
+ *                                      (include/field.hpp:426), the kernel of
+ *                                      calc_{bispec,powspec}_normalisation_
+ *                                      from_mesh (threept.hpp:150,
+ *                                      twopt.hpp:101)
+ *   trvg_assign_weighted_field_to_mesh <- trv::MeshField::
+ *                                      assign_weighted_field_to_mesh
+ *                                      (include/field.hpp:165)
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Particle arrays may live in host or
+ *    device memory (trvg_catalogue.memory); results are written to
+ *    caller-owned HOST arrays of length `dim` (complex values interleaved
+ *    re, im).  The reference returns the same vectors by value in
+ *    BispecMeasurements / ThreePCFMeasurements / PowspecMeasurements
+ *    (include/dataobjs.hpp:202-283).
+ *  - Errors: every function returns a TRVG_* status; the message of the
+ *    last failure on the calling thread is given by trvg_last_error().
+ *    TRVG_ERR_INVALID_PARAMETER maps to trv::sys::InvalidParameterError,
+ *    TRVG_ERR_INVALID_DATA to trv::sys::InvalidDataError and
+ *    TRVG_ERR_UNIMPLEMENTED to trv::sys::UnimplementedError
+ *    (include/monitor.hpp:683-780).
+ *  - Threading: a context owns one CUDA stream, its FFT plans and device
+ *    workspace; calls on one context must not overlap.  Different contexts
+ *    may be used from different threads.
+ *  - Parameters arrive already validated and derived as the reference's
+ *    ParameterSet::validate leaves them (parameters.cpp:466-1270): e.g.
+ *    interlacing is off for three-point statistics and 'full' form with
+ *    ell1 == ell2 is passed as TRVG_SHAPE_TRIU.
+ */
+#ifndef TRVG_H_INCLUDED
+#define TRVG_H_INCLUDED
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define TRVG_OK                     0
+#define TRVG_ERR_INVALID_PARAMETER  1
+#define TRVG_ERR_INVALID_DATA       2
+#define TRVG_ERR_UNIMPLEMENTED      3
+#define TRVG_ERR_CUDA               4
+#define TRVG_ERR_CUFFT              5
+#define TRVG_ERR_ALLOC              6
+
+/* Data-vector shapes (ParameterSet::shape, parameters.cpp:829-848). */
+#define TRVG_SHAPE_DIAG     0
+#define TRVG_SHAPE_OFFDIAG  1
+#define TRVG_SHAPE_ROW      2
+#define TRVG_SHAPE_FULL     3
+#define TRVG_SHAPE_TRIU     4
+
+/* Arithmetic of meshes and transforms.  FP64: all-double path.
+ * FP32_MIXED: float meshes and FFTs; particle offsets, Y_lm recurrences,
+ * mode counts, mesh-wide reductions, normalisation and shot-noise
+ * subtraction stay in double. */
+#define TRVG_PREC_FP64        0
+#define TRVG_PREC_FP32_MIXED  1
+
+/* Where the arrays of a trvg_catalogue live. */
+#define TRVG_MEM_HOST    0
+#define TRVG_MEM_DEVICE  1
+
+typedef struct trvg_context trvg_context;
+
+/* The subset of trv::ParameterSet (include/parameters.hpp:58-290) that
+ * the mesh estimators read. */
+typedef struct trvg_params {
+  double boxsize[3];
+  int ngrid[3];
+  int assignment_order;   /* 1 NGP, 2 CIC, 3 TSC, 4 PCS */
+  int interlace;          /* 0 or 1 */
+  int ell1, ell2, ELL;    /* multipole degrees */
+  int shape;              /* TRVG_SHAPE_* */
+  int idx_bin;            /* row / off-diagonal index */
+  int precision;          /* TRVG_PREC_* */
+  int verbose;            /* 0 silent; >= 20 stage log on stderr */
+} trvg_params;
+
+/* trv::Binning (include/dataobjs.hpp:58): edges and centres, host memory. */
+typedef struct trvg_binning {
+  int num_bins;
+  const double* bin_edges;    /* num_bins + 1 */
+  const double* bin_centres;  /* num_bins */
+} trvg_binning;
+
+/* A particle catalogue in structure-of-arrays form.  Replaces
+ * trv::ParticleCatalogue (include/particles.hpp:78) plus the
+ * LineOfSight arrays (include/dataobjs.hpp:186) of the survey estimators.
+ * Positions are box coordinates (the caller has centred / periodised).
+ * `w` is the overall weight ws * wc (NULL = unit weights).  `los_*` are
+ * unit line-of-sight vectors (survey estimators only; may be NULL for the
+ * periodic-box ones). */
+typedef struct trvg_catalogue {
+  int64_t n;
+  const double* x;
+  const double* y;
+  const double* z;
+  const double* w;
+  const double* los_x;
+  const double* los_y;
+  const double* los_z;
+  int memory;             /* TRVG_MEM_HOST or TRVG_MEM_DEVICE */
+} trvg_catalogue;
+
+/* trv::BispecMeasurements / trv::ThreePCFMeasurements
+ * (include/dataobjs.hpp:249-283).  For the 3PCF, coord/eff hold r values
+ * and counts hold npairs.  Caller-owned host arrays of length `dim`
+ * (2 * dim doubles for the complex ones). */
+typedef struct trvg_threept_out {
+  int dim;
+  double* coord1_bin;
+  double* coord1_eff;
+  int32_t* count_1;
+  double* coord2_bin;
+  double* coord2_eff;
+  int32_t* count_2;
+  double* raw;    /* complex, interleaved */
+  double* shot;   /* complex, interleaved */
+} trvg_threept_out;
+
+/* trv::PowspecMeasurements (include/dataobjs.hpp:202). */
+typedef struct trvg_powspec_out {
+  int dim;
+  double* kbin;
+  double* keff;
+  int32_t* nmodes;
+  double* pk_raw;   /* complex, interleaved */
+  double* pk_shot;  /* complex, interleaved */
+} trvg_powspec_out;
+
+/* Per-call counters of the last estimator call on a context. */
+typedef struct trvg_stats {
+  double ms_total;        /* wall time of the call on its stream (events) */
+  double ms_h2d;          /* host->device copies of particle arrays */
+  int64_t h2d_bytes;      /* bytes copied host->device */
+  int64_t kernel_launches;/* launches of this library's kernels */
+  int64_t fft_launches;   /* cuFFT executions */
+  int pruned_grid[3];     /* evaluation grid of the shell fields (== ngrid
+                             when the full mesh is used) */
+} trvg_stats;
+
+/* ---- Context -------------------------------------------------------- */
+
+/* Create a context on CUDA device `device`. */
+int trvg_context_create(int device, trvg_context** ctx);
+int trvg_context_destroy(trvg_context* ctx);
+/* Message of the last failure on this thread ("" if none). */
+const char* trvg_last_error(void);
+/* Library version string. */
+const char* trvg_version(void);
+/* Counters of the last estimator call on `ctx`. */
+int trvg_get_stats(const trvg_context* ctx, trvg_stats* out);
+/* Release cached device workspace and FFT plans of `ctx`. */
+int trvg_release_workspace(trvg_context* ctx);
+
+/* Length of the data vector of a three-point measurement
+ * (threept.cpp:1495-1521). */
+int trvg_data_vector_dim(int shape, int num_bins, int idx_bin, int* dim);
+
+/* ---- Estimators ------------------------------------------------------ */
+
+/* Bispectrum, periodic box, global plane-parallel line of sight. */
+int trvg_compute_bispec_in_gpp_box(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_binning* kbinning,
+  double norm_factor, trvg_threept_out* out);
+
+/* Bispectrum, survey-type catalogues, local plane-parallel line of sight.
+ * `alpha` = wstotal_data / wstotal_rand (threept.cpp:271). */
+int trvg_compute_bispec(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_catalogue* rand, double alpha,
+  const trvg_binning* kbinning, double norm_factor, trvg_threept_out* out);
+
+/* Three-point correlation function, periodic box. */
+int trvg_compute_3pcf_in_gpp_box(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_binning* rbinning,
+  double norm_factor, trvg_threept_out* out);
+
+/* Three-point correlation function, survey-type catalogues. */
+int trvg_compute_3pcf(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_catalogue* rand, double alpha,
+  const trvg_binning* rbinning, double norm_factor, trvg_threept_out* out);
+
+/* Power spectrum multipole (ELL = params->ELL), periodic box. */
+int trvg_compute_powspec_in_gpp_box(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_binning* kbinning,
+  double norm_factor, trvg_powspec_out* out);
+
+/* Power spectrum multipole, survey-type catalogues. */
+int trvg_compute_powspec(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* data, const trvg_catalogue* rand, double alpha,
+  const trvg_binning* kbinning, double norm_factor, trvg_powspec_out* out);
+
+/* 1 / (dV sum_x n(x)^order) of the weighted mesh n (no interlacing),
+ * the mesh normalisation of calc_*_normalisation_from_mesh. */
+int trvg_calc_grid_based_powlaw_norm(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* particles, int order, double* norm_factor);
+
+/* The weighted mesh n(x) = sum_i w_i W(x - x_i) / dV (real weights) or its
+ * interlacing shadow (`shadow` = 1), written to `mesh_out` (host, ngrid[0]
+ * * ngrid[1] * ngrid[2] doubles, row-major, z fastest). */
+int trvg_assign_weighted_field_to_mesh(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* particles, int shadow, double* mesh_out);
+
+/* ---- Host maths (no GPU needed) ------------------------------------- */
+
+/* Wigner 3-j symbol (maths.cpp:167-169). */
+double trvg_wigner_3j(int j1, int j2, int j3, int m1, int m2, int m3);
+/* j_ell(x) by the library's own evaluation (double). */
+double trvg_sph_bessel(int ell, double x);
+/* j_ell(x) through the natural-cubic-spline table the GPU kernels use
+ * (maths.cpp:309-375: dx = 0.05 up to max(1000, ell^2), direct above). */
+int trvg_sph_bessel_spline(int ell, const double* x, int64_t n, double* out);
+/* Reduced spherical harmonic y_lm(v) of n vectors (maths.cpp:171-220),
+ * evaluated by the same code the kernels use, on the host. */
+int trvg_reduced_ylm(int ell, int m, const double* v3, int64_t n,
+                     double* out_complex);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* TRVG_H_INCLUDED */

@@ -1,0 +1,404 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's
+golden files and against the CPU oracle on seeded inputs.
+
+Tolerances: FP64 path -- the reference tests' own ``np.allclose`` (rtol
+1e-5, atol 1e-8; shot noise atol 1e-6) against the goldens, and 1e-9
+relative to the complex modulus against the oracle.  FP32-mixed path --
+1e-5 relative to the complex modulus (the benchmark spec's bound), per bin.
+Mode / pair counts must be identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import BOX, KBINS, NMESH, RBINS, THREEPT_CASES, load_golden
+from oracle import trv_oracle as O
+from test_oracle import check_powspec, check_threept
+from triumvirate_gb300 import _engine, _lib
+from triumvirate_gb300.catalogue import ParticleCatalogue
+from triumvirate_gb300.dataobjs import Binning
+from triumvirate_gb300.threept import (compute_3pcf, compute_3pcf_in_gpp_box,
+                                       compute_bispec,
+                                       compute_bispec_in_gpp_box)
+from triumvirate_gb300.twopt import (compute_powspec,
+                                     compute_powspec_in_gpp_box)
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ['fp64', 'fp32mixed']
+
+
+def _sampling(precision, ngrid=NMESH, assignment='tsc', interlace=False,
+              box=BOX):
+    return {'boxsize': [box] * 3, 'ngrid': [ngrid] * 3,
+            'assignment': assignment, 'interlace': interlace,
+            'precision': precision}
+
+
+def _cats(d, r=None):
+    dc = ParticleCatalogue(d[:, 0], d[:, 1], d[:, 2], nz=d[:, 3])
+    if r is None:
+        return dc
+    return dc, ParticleCatalogue(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3])
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    scale = np.maximum(np.abs(b), 1e-300)
+    return float(np.max(np.abs(a - b) / scale))
+
+
+def assert_close_threept(res, ref, kind, rtol, shot_floor=0.):
+    keys = (['k1_bin', 'k1_eff', 'nmodes_1', 'k2_bin', 'k2_eff', 'nmodes_2',
+             'bk_raw', 'bk_shot'] if kind == 'bispec' else
+            ['r1_bin', 'r1_eff', 'npairs_1', 'r2_bin', 'r2_eff', 'npairs_2',
+             'zeta_raw', 'zeta_shot'])
+    assert np.array_equal(res[keys[2]], ref[keys[2]])
+    assert np.array_equal(res[keys[5]], ref[keys[5]])
+    assert np.allclose(res[keys[0]], ref[keys[0]], rtol=1e-15, atol=0)
+    assert np.allclose(res[keys[1]], ref[keys[1]], rtol=1e-12, atol=0)
+    assert rel_err(res[keys[6]], ref[keys[6]]) < rtol, keys[6]
+    err = np.abs(res[keys[7]] - ref[keys[7]])
+    assert np.all(err <= rtol * np.abs(ref[keys[7]]) + shot_floor), \
+        (keys[7], float(np.max(err / np.maximum(np.abs(ref[keys[7]]),
+                                                1e-300))))
+
+
+# ---------------------------------------------------------------------------
+# Golden files (reference tests/test_threept.py, tests/test_twopt.py)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kind, degrees, form, idx_bin, golden",
+                         THREEPT_CASES)
+def test_golden_gpp(precision, kind, degrees, form, idx_bin, golden,
+                    data_catalogue_array):
+    cat = _cats(data_catalogue_array)
+    bins = (Binning('fourier', 'lin', *KBINS) if kind == 'bispec'
+            else Binning('config', 'lin', *RBINS))
+    fn = compute_bispec_in_gpp_box if kind == 'bispec' \
+        else compute_3pcf_in_gpp_box
+    res = fn(cat, degrees=degrees, binning=bins, form=form, idx_bin=idx_bin,
+             sampling_params=_sampling(precision))
+    check_threept(res, load_golden(golden.format('gpp')), kind)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kind, degrees, form, idx_bin, golden",
+                         THREEPT_CASES)
+def test_golden_lpp(precision, kind, degrees, form, idx_bin, golden,
+                    data_catalogue_array, rand_catalogue_array):
+    dc, rc = _cats(data_catalogue_array, rand_catalogue_array)
+    bins = (Binning('fourier', 'lin', *KBINS) if kind == 'bispec'
+            else Binning('config', 'lin', *RBINS))
+    fn = compute_bispec if kind == 'bispec' else compute_3pcf
+    res = fn(dc, rc, degrees=degrees, binning=bins, form=form,
+             idx_bin=idx_bin, sampling_params=_sampling(precision))
+    check_threept(res, load_golden(golden.format('lpp')), kind)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("ell", [0, 2])
+def test_golden_powspec(precision, ell, data_catalogue_array,
+                        rand_catalogue_array):
+    bins = Binning('fourier', 'lin', *KBINS)
+    res = compute_powspec_in_gpp_box(_cats(data_catalogue_array), degree=ell,
+                                     binning=bins,
+                                     sampling_params=_sampling(precision))
+    check_powspec(res, load_golden(f"pk{ell}_gpp.txt"))
+    dc, rc = _cats(data_catalogue_array, rand_catalogue_array)
+    res = compute_powspec(dc, rc, degree=ell, binning=bins,
+                          sampling_params=_sampling(precision))
+    check_powspec(res, load_golden(f"pk{ell}_lpp.txt"))
+
+
+# ---------------------------------------------------------------------------
+# Seeded catalogues against the oracle
+# ---------------------------------------------------------------------------
+
+def _uniform(n, box, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0., box, size=(n, 3))
+
+
+def _oracle_gpp(kind, pos, box, ngrid, assignment, degrees, form, idx_bin,
+                bins):
+    x, y, z = O.periodise(pos[:, 0], pos[:, 1], pos[:, 2], [box] * 3)
+    p = O.Params(box, ngrid, assignment, False, *degrees, form=form,
+                 idx_bin=idx_bin)
+    edges, centres = O.lin_binning(*bins)
+    n = pos.shape[0]
+    norm = O.bispec_norm_from_particles(np.full(n, n / box ** 3), 1., 1.)
+    fn = (O.compute_bispec_in_gpp_box if kind == 'bispec'
+          else O.compute_3pcf_in_gpp_box)
+    return fn(np.stack([x, y, z], -1), p, edges, centres, norm)
+
+
+GPP_CASES = [
+    # kind, assignment, ngrid, degrees, form, idx_bin, bins
+    ('bispec', 'tsc', 32, (0, 0, 0), 'diag', None, (0.01, 0.1, 5)),
+    ('bispec', 'ngp', 32, (0, 0, 0), 'full', None, (0.01, 0.1, 4)),
+    ('bispec', 'cic', 32, (2, 0, 2), 'off-diag', 1, (0.01, 0.1, 5)),
+    ('bispec', 'pcs', 32, (2, 0, 2), 'row', 2, (0.01, 0.1, 4)),
+    ('bispec', 'tsc', 32, (1, 1, 0), 'full', None, (0.01, 0.1, 3)),
+    ('bispec', 'tsc', 32, (1, 1, 2), 'diag', None, (0.01, 0.1, 3)),
+    ('bispec', 'tsc', 32, (2, 2, 0), 'diag', None, (0.01, 0.1, 3)),
+    # pruned evaluation grid (4K + 1 < N)
+    ('bispec', 'tsc', 64, (0, 0, 0), 'diag', None, (0.005, 0.055, 5)),
+    ('bispec', 'pcs', 64, (2, 0, 2), 'full', None, (0.005, 0.045, 4)),
+    ('bispec', 'cic', 64, (1, 1, 2), 'triu', None, (0.005, 0.045, 3)),
+    ('3pcf', 'tsc', 32, (0, 0, 0), 'diag', None, (40., 160., 4)),
+    ('3pcf', 'cic', 32, (2, 0, 2), 'row', 1, (40., 160., 4)),
+    ('3pcf', 'tsc', 32, (1, 1, 0), 'full', None, (40., 160., 3)),
+]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kind, assignment, ngrid, degrees, form, idx_bin, "
+                         "bins", GPP_CASES)
+def test_oracle_gpp(precision, kind, assignment, ngrid, degrees, form,
+                    idx_bin, bins):
+    box, n = 800., 3000
+    pos = _uniform(n, box, seed=ngrid + sum(degrees) + len(form))
+    ref = _oracle_gpp(kind, pos, box, ngrid, assignment, degrees, form,
+                      idx_bin, bins)
+    cat = ParticleCatalogue(pos[:, 0], pos[:, 1], pos[:, 2],
+                            nz=n / box ** 3)
+    space = 'fourier' if kind == 'bispec' else 'config'
+    binning = Binning(space, 'lin', *bins)
+    fn = compute_bispec_in_gpp_box if kind == 'bispec' \
+        else compute_3pcf_in_gpp_box
+    res = fn(cat, degrees=degrees, binning=binning, form=form,
+             idx_bin=idx_bin,
+             sampling_params=_sampling(precision, ngrid, assignment,
+                                       box=box))
+    rtol = 1e-9 if precision == 'fp64' else 1e-5
+    shot_floor = 1e-9 * np.max(np.abs(ref['bk_shot' if kind == 'bispec'
+                                          else 'zeta_shot']))
+    assert_close_threept(res, ref, kind, rtol, shot_floor)
+
+
+def _survey_inputs(nd, nr, seed):
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(-300., 300., size=(nd, 3)) + [0., 0., 800.]
+    r = rng.uniform(-300., 300., size=(nr, 3)) + [0., 0., 800.]
+    wd = rng.uniform(0.5, 1.5, nd)
+    wr = rng.uniform(0.5, 1.5, nr)
+    return d, r, wd, wr
+
+
+def _oracle_survey(kind, d, r, wd, wr, box, ngrid, assignment, degrees,
+                   form, idx_bin, bins, interlace=False):
+    los_d = O.compute_los(*d.T)
+    los_r = O.compute_los(*r.T)
+    (dx, dy, dz), _ = O.centre(*d.T, [box] * 3, ref=tuple(r.T))
+    (rx, ry, rz), _ = O.centre(*r.T, [box] * 3)
+    data = dict(pos=np.stack([dx, dy, dz], -1), los=los_d, w=wd,
+                ws=np.ones_like(wd))
+    rand = dict(pos=np.stack([rx, ry, rz], -1), los=los_r, w=wr,
+                ws=np.ones_like(wr))
+    alpha = d.shape[0] / r.shape[0]
+    npoint = '2pt' if kind == 'powspec' else '3pt'
+    p = O.Params(box, ngrid, assignment, interlace, *degrees, form=form,
+                 idx_bin=idx_bin, npoint=npoint)
+    edges, centres = O.lin_binning(*bins)
+    nz = np.full(r.shape[0], 1e-4)
+    if kind == 'powspec':
+        norm = O.powspec_norm_from_particles(nz, 1., wr, alpha)
+        return O.compute_powspec(data, rand, p, edges, centres, norm)
+    norm = O.bispec_norm_from_particles(nz, 1., wr, alpha)
+    fn = O.compute_bispec if kind == 'bispec' else O.compute_3pcf
+    return fn(data, rand, p, edges, centres, norm)
+
+
+LPP_CASES = [
+    ('bispec', 'tsc', 32, (0, 0, 0), 'diag', None, (0.01, 0.1, 4)),
+    ('bispec', 'pcs', 32, (2, 0, 2), 'diag', None, (0.01, 0.1, 4)),
+    ('bispec', 'cic', 32, (1, 1, 2), 'full', None, (0.01, 0.1, 3)),
+    ('bispec', 'tsc', 64, (2, 0, 2), 'off-diag', -1, (0.005, 0.045, 4)),
+    ('3pcf', 'tsc', 32, (2, 0, 2), 'diag', None, (40., 160., 4)),
+    ('3pcf', 'cic', 32, (1, 1, 0), 'row', 0, (40., 160., 3)),
+]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kind, assignment, ngrid, degrees, form, idx_bin, "
+                         "bins", LPP_CASES)
+def test_oracle_lpp(precision, kind, assignment, ngrid, degrees, form,
+                    idx_bin, bins):
+    box = 1000.
+    d, r, wd, wr = _survey_inputs(1500, 6000, seed=ngrid + sum(degrees))
+    ref = _oracle_survey(kind, d, r, wd, wr, box, ngrid, assignment,
+                         degrees, form, idx_bin, bins)
+    dc = ParticleCatalogue(*d.T, nz=1e-4, wc=wd)
+    rc = ParticleCatalogue(*r.T, nz=1e-4, wc=wr)
+    space = 'fourier' if kind == 'bispec' else 'config'
+    fn = compute_bispec if kind == 'bispec' else compute_3pcf
+    res = fn(dc, rc, degrees=degrees, binning=Binning(space, 'lin', *bins),
+             form=form, idx_bin=idx_bin,
+             sampling_params=_sampling(precision, ngrid, assignment,
+                                       box=box))
+    rtol = 1e-9 if precision == 'fp64' else 1e-5
+    key = 'bk_shot' if kind == 'bispec' else 'zeta_shot'
+    assert_close_threept(res, ref, kind, rtol,
+                         1e-9 * np.max(np.abs(ref[key])))
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("assignment, interlace, ell",
+                         [('tsc', True, 0), ('cic', True, 2),
+                          ('pcs', False, 2), ('ngp', True, 0)])
+def test_oracle_powspec(precision, assignment, interlace, ell):
+    box, n, ngrid = 600., 4000, 32
+    pos = _uniform(n, box, seed=5 + ell)
+    bins = (0.01, 0.15, 6)
+    x, y, z = O.periodise(*pos.T, [box] * 3)
+    p = O.Params(box, ngrid, assignment, interlace, 0, 0, ell, npoint='2pt')
+    edges, centres = O.lin_binning(*bins)
+    norm = O.powspec_norm_from_particles(np.full(n, n / box ** 3), 1., 1.)
+    ref = O.compute_powspec_in_gpp_box(np.stack([x, y, z], -1), p, edges,
+                                       centres, norm)
+    res = compute_powspec_in_gpp_box(
+        ParticleCatalogue(*pos.T, nz=n / box ** 3), degree=ell,
+        binning=Binning('fourier', 'lin', *bins),
+        sampling_params=_sampling(precision, ngrid, assignment, interlace,
+                                  box))
+    rtol = 1e-9 if precision == 'fp64' else 1e-5
+    assert np.array_equal(res['nmodes'], ref['nmodes'])
+    assert rel_err(res['keff'], ref['keff']) < 1e-12
+    assert rel_err(res['pk_raw'], ref['pk_raw']) < rtol
+    assert rel_err(res['pk_shot'], ref['pk_shot']) < rtol
+
+    d, r, wd, wr = _survey_inputs(1200, 5000, seed=11 + ell)
+    ref = _oracle_survey('powspec', d, r, wd, wr, 1000., ngrid, assignment,
+                         (0, 0, ell), 'diag', None, bins, interlace)
+    res = compute_powspec(ParticleCatalogue(*d.T, nz=1e-4, wc=wd),
+                          ParticleCatalogue(*r.T, nz=1e-4, wc=wr),
+                          degree=ell,
+                          binning=Binning('fourier', 'lin', *bins),
+                          sampling_params=_sampling(precision, ngrid,
+                                                    assignment, interlace,
+                                                    1000.))
+    assert np.array_equal(res['nmodes'], ref['nmodes'])
+    assert rel_err(res['pk_raw'], ref['pk_raw']) < rtol
+    assert rel_err(res['pk_shot'], ref['pk_shot']) < rtol
+
+
+# ---------------------------------------------------------------------------
+# Mesh assignment (K1) against the oracle, mesh cell by mesh cell
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("assignment", ['ngp', 'cic', 'tsc', 'pcs'])
+@pytest.mark.parametrize("shadow", [False, True])
+def test_assignment_mesh(precision, assignment, shadow):
+    box, ngrid, n = 500., 16, 2500
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0., box, size=(n, 3))
+    # Particles on cell boundaries and at the box edge exercise the wraps.
+    pos[:8] = [[0., 0., 0.], [box * (1 - 1e-15), 0., 0.],
+               [box / ngrid * 3, box / 2, 0.],
+               [box / ngrid * 2.5, box / ngrid * 0.5, box / ngrid * 15.5],
+               [box / ngrid * 15.5, 0., 0.], [box / ngrid * 14.5, 0., 1.],
+               [box / ngrid * 15.999, 3., 7.], [1e-9, 1e-9, 1e-9]]
+    w = rng.uniform(0.5, 2., n)
+    p = O.Params(box, ngrid, assignment, True, npoint='2pt')
+    ref = O.assign_weighted_field_to_mesh(pos, w.astype(complex), p,
+                                          shadow=shadow).real
+    ctx = _lib.default_context()
+    pc = _engine.make_params({'boxsize': {'x': box, 'y': box, 'z': box},
+                              'ngrid': {'x': ngrid, 'y': ngrid, 'z': ngrid},
+                              'assignment_order': p.assignment_order,
+                              'interlace': True, 'degrees': {},
+                              'form': 'diag', 'precision': precision,
+                              'verbose': 0}, '2pt')
+    cat = _engine.HostCatalogue(pos[:, 0], pos[:, 1], pos[:, 2], w)
+    mesh = _engine.assign_mesh(ctx, pc, cat.c, shadow=shadow)
+    tol = 1e-12 if precision == 'fp64' else 1e-6
+    assert np.max(np.abs(mesh - ref)) <= tol * np.max(np.abs(ref))
+    assert abs(mesh.sum() - ref.sum()) <= tol * abs(ref.sum())
+
+
+def test_mesh_norm_matches_oracle():
+    box, ngrid, n = 500., 32, 3000
+    pos = _uniform(n, box, 9)
+    w = np.random.default_rng(9).uniform(0.5, 1.5, n)
+    p = O.Params(box, ngrid, 'tsc', False)
+    for order in (2, 3):
+        ref = O.grid_powlaw_norm(pos, w, p, order)
+        ctx = _lib.default_context()
+        pc = _engine.make_params({'boxsize': {'x': box, 'y': box, 'z': box},
+                                  'ngrid': {'x': ngrid, 'y': ngrid,
+                                            'z': ngrid},
+                                  'assignment_order': 3, 'interlace': False,
+                                  'degrees': {}, 'form': 'diag',
+                                  'precision': 'fp64', 'verbose': 0}, '2pt')
+        cat = _engine.HostCatalogue(pos[:, 0], pos[:, 1], pos[:, 2], w)
+        got = _engine.grid_powlaw_norm(ctx, pc, cat.c, order)
+        assert abs(got / ref - 1.) < 1e-10
+
+
+# ---------------------------------------------------------------------------
+# Edge cases and errors
+# ---------------------------------------------------------------------------
+
+def test_vanishing_multipole_raises():
+    cat = ParticleCatalogue(*_uniform(100, 500., 1).T, nz=1e-6)
+    with pytest.raises(_lib.InvalidParameterError, match="Wigner 3-j"):
+        compute_bispec_in_gpp_box(
+            cat, degrees=(1, 0, 0), binning=Binning('fourier', 'lin', 0.01,
+                                                    0.1, 3),
+            form='diag', sampling_params=_sampling('fp64', 16, box=500.))
+
+
+def test_empty_bin_gives_zero_modes_like_reference():
+    """A bin below the fundamental mode has no modes: nmodes = 0 and k_eff
+    = 0/0 as in field.cpp:1905."""
+    cat = ParticleCatalogue(*_uniform(500, 1000., 2).T, nz=5e-7)
+    res = compute_bispec_in_gpp_box(
+        cat, degrees=(0, 0, 0),
+        binning=Binning('fourier', 'lin', 0.0001, 0.0021, 2), form='diag',
+        sampling_params=_sampling('fp64', 16))
+    assert list(res['nmodes_1']) == [0, 0]
+    assert np.all(np.isnan(res['k1_eff']))
+
+
+def test_repeat_calls_are_reproducible():
+    pos = _uniform(5000, 700., 4)
+    out = []
+    for _ in range(3):
+        cat = ParticleCatalogue(*pos.T, nz=5000 / 700. ** 3)
+        out.append(compute_bispec_in_gpp_box(
+            cat, degrees=(0, 0, 0),
+            binning=Binning('fourier', 'lin', 0.01, 0.1, 5), form='diag',
+            sampling_params=_sampling('fp64', 32, box=700.)))
+    for o in out[1:]:
+        assert np.array_equal(o['nmodes_1'], out[0]['nmodes_1'])
+        assert rel_err(o['bk_raw'], out[0]['bk_raw']) < 1e-12
+        assert rel_err(o['bk_shot'], out[0]['bk_shot']) < 1e-12
+
+
+def test_device_inputs_match_host_inputs():
+    """Particle arrays already in device memory give the host result."""
+    torch = pytest.importorskip("torch")
+    box, n = 700., 4000
+    pos = _uniform(n, box, 12)
+    x, y, z = O.periodise(*pos.T, [box] * 3)
+    ctx = _lib.default_context()
+    pdict = {'boxsize': {'x': box, 'y': box, 'z': box},
+             'ngrid': {'x': 32, 'y': 32, 'z': 32}, 'assignment_order': 3,
+             'interlace': False, 'degrees': {'ell1': 0, 'ell2': 0, 'ELL': 0},
+             'form': 'diag', 'shape': 'diag', 'precision': 'fp32mixed',
+             'verbose': 0}
+    pc = _engine.make_params(pdict, '3pt')
+    binning = Binning('fourier', 'lin', 0.01, 0.1, 5)
+    host = _engine.HostCatalogue(x, y, z)
+    r1 = _engine.call_threept('trvg_compute_bispec_in_gpp_box', ctx, pc,
+                              host.c, binning, 1., 'bispec', shape='diag')
+    dev = [torch.as_tensor(a, dtype=torch.float64, device='cuda')
+           for a in (x, y, z)]
+    dc = _engine.device_catalogue(n, *(t.data_ptr() for t in dev))
+    torch.cuda.synchronize()
+    r2 = _engine.call_threept('trvg_compute_bispec_in_gpp_box', ctx, pc, dc,
+                              binning, 1., 'bispec', shape='diag')
+    assert np.array_equal(r1['nmodes_1'], r2['nmodes_1'])
+    assert rel_err(r1['bk_raw'], r2['bk_raw']) < 1e-5

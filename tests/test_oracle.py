@@ -1,0 +1,120 @@
+"""The CPU oracle against the reference's golden measurement files.
+
+Tolerances are the reference tests' own (tests/test_threept.py:49-75,
+tests/test_twopt.py:39-52): ``np.allclose`` defaults, plus ``atol=1e-6``
+on shot noise.
+"""
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import BOX, KBINS, NMESH, RBINS, THREEPT_CASES, load_golden
+from oracle import trv_oracle as O
+
+
+def _gpp_pos(d):
+    x, y, z = O.periodise(d[:, 0], d[:, 1], d[:, 2], [BOX] * 3)
+    return np.stack([x, y, z], -1)
+
+
+def _survey(d, r):
+    los_d = O.compute_los(d[:, 0], d[:, 1], d[:, 2])
+    los_r = O.compute_los(r[:, 0], r[:, 1], r[:, 2])
+    ref = (r[:, 0], r[:, 1], r[:, 2])
+    (dx, dy, dz), _ = O.centre(d[:, 0], d[:, 1], d[:, 2], [BOX] * 3, ref=ref)
+    (rx, ry, rz), _ = O.centre(*ref, [BOX] * 3)
+    nd, nr = d.shape[0], r.shape[0]
+    data = dict(pos=np.stack([dx, dy, dz], -1), los=los_d, w=np.ones(nd),
+                ws=np.ones(nd))
+    rand = dict(pos=np.stack([rx, ry, rz], -1), los=los_r, w=np.ones(nr),
+                ws=np.ones(nr))
+    return data, rand, nd / nr
+
+
+def check_threept(res, ext, kind):
+    keys = (['k1_bin', 'k1_eff', 'nmodes_1', 'k2_bin', 'k2_eff', 'nmodes_2',
+             'bk_raw', 'bk_shot'] if kind == 'bispec' else
+            ['r1_bin', 'r1_eff', 'npairs_1', 'r2_bin', 'r2_eff', 'npairs_2',
+             'zeta_raw', 'zeta_shot'])
+    for i, k in enumerate(keys[:6]):
+        assert np.allclose(res[k], ext[i]), k
+    assert np.allclose(res[keys[6]], ext[-4] + 1j * ext[-3]), keys[6]
+    assert np.allclose(res[keys[7]], ext[-2] + 1j * ext[-1], atol=1e-6), \
+        keys[7]
+
+
+def check_powspec(res, ext):
+    assert np.allclose(res['kbin'], ext[0])
+    assert np.allclose(res['keff'], ext[1])
+    assert np.allclose(res['nmodes'], ext[2])
+    assert np.allclose(res['pk_raw'], ext[3] + 1j * ext[4])
+    assert np.allclose(res['pk_shot'], ext[5] + 1j * ext[6], atol=1e-6)
+
+
+@pytest.mark.parametrize("kind, degrees, form, idx_bin, golden",
+                         THREEPT_CASES)
+def test_oracle_gpp(kind, degrees, form, idx_bin, golden,
+                    data_catalogue_array):
+    d = data_catalogue_array
+    p = O.Params(BOX, NMESH, 'tsc', False, *degrees, form=form,
+                 idx_bin=idx_bin)
+    bins = KBINS if kind == 'bispec' else RBINS
+    edges, centres = O.lin_binning(*bins)
+    norm = O.bispec_norm_from_particles(d[:, 3], 1., 1.)
+    fn = (O.compute_bispec_in_gpp_box if kind == 'bispec'
+          else O.compute_3pcf_in_gpp_box)
+    res = fn(_gpp_pos(d), p, edges, centres, norm)
+    check_threept(res, load_golden(golden.format('gpp')), kind)
+
+
+@pytest.mark.parametrize("kind, degrees, form, idx_bin, golden",
+                         THREEPT_CASES)
+def test_oracle_lpp(kind, degrees, form, idx_bin, golden,
+                    data_catalogue_array, rand_catalogue_array):
+    data, rand, alpha = _survey(data_catalogue_array, rand_catalogue_array)
+    p = O.Params(BOX, NMESH, 'tsc', False, *degrees, form=form,
+                 idx_bin=idx_bin)
+    bins = KBINS if kind == 'bispec' else RBINS
+    edges, centres = O.lin_binning(*bins)
+    norm = O.bispec_norm_from_particles(rand_catalogue_array[:, 3], 1., 1.,
+                                        alpha)
+    fn = O.compute_bispec if kind == 'bispec' else O.compute_3pcf
+    res = fn(data, rand, p, edges, centres, norm)
+    check_threept(res, load_golden(golden.format('lpp')), kind)
+
+
+@pytest.mark.parametrize("ell", [0, 2])
+def test_oracle_powspec(ell, data_catalogue_array, rand_catalogue_array):
+    d = data_catalogue_array
+    edges, centres = O.lin_binning(*KBINS)
+    p = O.Params(BOX, NMESH, 'tsc', False, 0, 0, ell, npoint='2pt')
+    norm = O.powspec_norm_from_particles(d[:, 3], 1., 1.)
+    res = O.compute_powspec_in_gpp_box(_gpp_pos(d), p, edges, centres, norm)
+    check_powspec(res, load_golden(f"pk{ell}_gpp.txt"))
+    data, rand, alpha = _survey(d, rand_catalogue_array)
+    norm = O.powspec_norm_from_particles(rand_catalogue_array[:, 3], 1., 1.,
+                                         alpha)
+    res = O.compute_powspec(data, rand, p, edges, centres, norm)
+    check_powspec(res, load_golden(f"pk{ell}_lpp.txt"))
+
+
+def test_random_catalogue_regeneration(rand_catalogue_array):
+    """The regenerated randoms equal the reference's file bit for bit."""
+    root = os.environ.get("TRIUMVIRATE_REFERENCE")
+    if not root:
+        pytest.skip("set TRIUMVIRATE_REFERENCE to the reference tree")
+    f = Path(root) / "tests" / "test_input" / "ctlgs" / \
+        "test_rand_catalogue.txt"
+    ref = np.loadtxt(f)
+    assert np.array_equal(ref, rand_catalogue_array)
+
+
+def test_wigner_3j_exact():
+    sympy = pytest.importorskip("sympy")
+    from sympy.physics.wigner import wigner_3j
+    for args in [(0, 0, 0, 0, 0, 0), (2, 0, 2, 0, 0, 0), (2, 0, 2, 1, 0, -1),
+                 (1, 1, 2, 1, -1, 0), (3, 2, 1, -2, 1, 1),
+                 (4, 4, 4, 2, -1, -1), (2, 2, 2, 0, 0, 0)]:
+        assert abs(O.wigner_3j(*args) - float(wigner_3j(*args))) < 1e-15

@@ -1,0 +1,258 @@
+"""ctypes bindings of ``libtrvg.so`` (declared in ``include/trvg.h``).
+
+The library is built in the source tree by ``triumvirate_gb300.build``.  No
+computation falls back to the CPU: if the library cannot be loaded, every
+estimator raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libtrvg.so"
+
+TRVG_OK = 0
+TRVG_ERR_INVALID_PARAMETER = 1
+TRVG_ERR_INVALID_DATA = 2
+TRVG_ERR_UNIMPLEMENTED = 3
+TRVG_ERR_CUDA = 4
+TRVG_ERR_CUFFT = 5
+TRVG_ERR_ALLOC = 6
+
+SHAPES = {'diag': 0, 'off-diag': 1, 'row': 2, 'full': 3, 'triu': 4}
+PRECISIONS = {'fp64': 0, 'fp32mixed': 1}
+MEM_HOST, MEM_DEVICE = 0, 1
+
+EXPORTED = [
+    "trvg_context_create", "trvg_context_destroy", "trvg_last_error",
+    "trvg_version", "trvg_get_stats", "trvg_release_workspace",
+    "trvg_data_vector_dim",
+    "trvg_compute_bispec_in_gpp_box", "trvg_compute_bispec",
+    "trvg_compute_3pcf_in_gpp_box", "trvg_compute_3pcf",
+    "trvg_compute_powspec_in_gpp_box", "trvg_compute_powspec",
+    "trvg_calc_grid_based_powlaw_norm", "trvg_assign_weighted_field_to_mesh",
+    "trvg_wigner_3j", "trvg_sph_bessel", "trvg_sph_bessel_spline",
+    "trvg_reduced_ylm",
+]
+
+
+class InvalidParameterError(ValueError):
+    """``trv::sys::InvalidParameterError`` (monitor.hpp:683-780)."""
+
+
+class InvalidDataError(RuntimeError):
+    """``trv::sys::InvalidDataError``."""
+
+
+class UnimplementedError(NotImplementedError):
+    """``trv::sys::UnimplementedError``."""
+
+
+class DeviceError(RuntimeError):
+    """CUDA / cuFFT failure or device allocation failure."""
+
+
+_ERRORS = {
+    TRVG_ERR_INVALID_PARAMETER: InvalidParameterError,
+    TRVG_ERR_INVALID_DATA: InvalidDataError,
+    TRVG_ERR_UNIMPLEMENTED: UnimplementedError,
+    TRVG_ERR_CUDA: DeviceError,
+    TRVG_ERR_CUFFT: DeviceError,
+    TRVG_ERR_ALLOC: DeviceError,
+}
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("boxsize", C.c_double * 3),
+        ("ngrid", C.c_int * 3),
+        ("assignment_order", C.c_int),
+        ("interlace", C.c_int),
+        ("ell1", C.c_int), ("ell2", C.c_int), ("ELL", C.c_int),
+        ("shape", C.c_int),
+        ("idx_bin", C.c_int),
+        ("precision", C.c_int),
+        ("verbose", C.c_int),
+    ]
+
+
+class BinningC(C.Structure):
+    _fields_ = [
+        ("num_bins", C.c_int),
+        ("bin_edges", C.POINTER(C.c_double)),
+        ("bin_centres", C.POINTER(C.c_double)),
+    ]
+
+
+class Catalogue(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+        ("w", C.c_void_p),
+        ("los_x", C.c_void_p), ("los_y", C.c_void_p), ("los_z", C.c_void_p),
+        ("memory", C.c_int),
+    ]
+
+
+class ThreeptOut(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int),
+        ("coord1_bin", C.POINTER(C.c_double)),
+        ("coord1_eff", C.POINTER(C.c_double)),
+        ("count_1", C.POINTER(C.c_int32)),
+        ("coord2_bin", C.POINTER(C.c_double)),
+        ("coord2_eff", C.POINTER(C.c_double)),
+        ("count_2", C.POINTER(C.c_int32)),
+        ("raw", C.POINTER(C.c_double)),
+        ("shot", C.POINTER(C.c_double)),
+    ]
+
+
+class PowspecOut(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int),
+        ("kbin", C.POINTER(C.c_double)),
+        ("keff", C.POINTER(C.c_double)),
+        ("nmodes", C.POINTER(C.c_int32)),
+        ("pk_raw", C.POINTER(C.c_double)),
+        ("pk_shot", C.POINTER(C.c_double)),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("ms_total", C.c_double),
+        ("ms_h2d", C.c_double),
+        ("h2d_bytes", C.c_int64),
+        ("kernel_launches", C.c_int64),
+        ("fft_launches", C.c_int64),
+        ("pruned_grid", C.c_int * 3),
+    ]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load(path: str | os.PathLike | None = None):
+    """Load the library (once); raise if it is missing."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise ImportError(
+                f"{p} is missing: build it with "
+                "`python -m triumvirate_gb300.build` (no CPU fallback).")
+        lib = C.CDLL(str(p))
+        _declare(lib)
+        _lib = lib
+        return lib
+
+
+def _declare(lib):
+    vp, ip, dp = C.c_void_p, C.c_int, C.c_double
+    P = C.POINTER
+    lib.trvg_context_create.argtypes = [ip, P(vp)]
+    lib.trvg_context_destroy.argtypes = [vp]
+    lib.trvg_last_error.restype = C.c_char_p
+    lib.trvg_version.restype = C.c_char_p
+    lib.trvg_get_stats.argtypes = [vp, P(Stats)]
+    lib.trvg_release_workspace.argtypes = [vp]
+    lib.trvg_data_vector_dim.argtypes = [ip, ip, ip, P(ip)]
+    for nm in ("trvg_compute_bispec_in_gpp_box",
+               "trvg_compute_3pcf_in_gpp_box"):
+        getattr(lib, nm).argtypes = [vp, P(Params), P(Catalogue),
+                                     P(BinningC), dp, P(ThreeptOut)]
+    for nm in ("trvg_compute_bispec", "trvg_compute_3pcf"):
+        getattr(lib, nm).argtypes = [vp, P(Params), P(Catalogue),
+                                     P(Catalogue), dp, P(BinningC), dp,
+                                     P(ThreeptOut)]
+    lib.trvg_compute_powspec_in_gpp_box.argtypes = [
+        vp, P(Params), P(Catalogue), P(BinningC), dp, P(PowspecOut)]
+    lib.trvg_compute_powspec.argtypes = [
+        vp, P(Params), P(Catalogue), P(Catalogue), dp, P(BinningC), dp,
+        P(PowspecOut)]
+    lib.trvg_calc_grid_based_powlaw_norm.argtypes = [
+        vp, P(Params), P(Catalogue), ip, P(dp)]
+    lib.trvg_assign_weighted_field_to_mesh.argtypes = [
+        vp, P(Params), P(Catalogue), ip, P(dp)]
+    lib.trvg_wigner_3j.argtypes = [ip] * 6
+    lib.trvg_wigner_3j.restype = dp
+    lib.trvg_sph_bessel.argtypes = [ip, dp]
+    lib.trvg_sph_bessel.restype = dp
+    lib.trvg_sph_bessel_spline.argtypes = [ip, P(dp), C.c_int64, P(dp)]
+    lib.trvg_reduced_ylm.argtypes = [ip, ip, P(dp), C.c_int64, P(dp)]
+
+
+def check(status: int):
+    """Raise the Python exception matching a TRVG_* status."""
+    if status == TRVG_OK:
+        return
+    msg = load().trvg_last_error().decode(errors='replace')
+    raise _ERRORS.get(status, RuntimeError)(msg or f"trvg status {status}")
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Context:
+    """A device context: one CUDA stream, FFT plans and cached workspace."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.trvg_context_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stats(self) -> dict:
+        s = Stats()
+        check(load().trvg_get_stats(self._h, C.byref(s)))
+        return dict(ms_total=s.ms_total, ms_h2d=s.ms_h2d,
+                    h2d_bytes=s.h2d_bytes, kernel_launches=s.kernel_launches,
+                    fft_launches=s.fft_launches,
+                    pruned_grid=tuple(s.pruned_grid))
+
+    def release_workspace(self):
+        check(load().trvg_release_workspace(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().trvg_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = {}
+
+
+def default_context(device: int | None = None) -> Context:
+    """Process-wide context of `device` (``TRVG_DEVICE``, default 0)."""
+    if device is None:
+        device = int(os.environ.get("TRVG_DEVICE", "0"))
+    ctx = _default_ctx.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _default_ctx[device] = ctx
+    return ctx

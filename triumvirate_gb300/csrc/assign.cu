@@ -1,0 +1,327 @@
+// K1: particle -> mesh assignment (NGP / CIC / TSC / PCS, with the
+// interlacing shadow in the same pass).
+//
+// Follows MeshField::assign_weighted_field_to_mesh_{ngp,cic,tsc,pcs}
+// (field.cpp:618-1112): per axis the covered cell indices and window values
+// are derived from loc = ngrid * x / L exactly as there (FP64, same
+// comparisons and periodic wrap), and the product window * weight is
+// accumulated with atomics.  The mesh stores the deposited weight per cell
+// (the reference's n(x) * dV), which is what its forward FFT consumes after
+// the vol_cell scaling (field.cpp:1503-1510).
+#include "kernels.h"
+
+namespace trvg {
+
+namespace {
+
+template <int ORDER>
+struct Stencil {
+  int idx[ORDER];
+  double win[ORDER];
+};
+
+// One axis of the assignment stencil.  `shadow` selects the half-cell-shifted
+// pass (field.cpp:673-726 etc.), including the reference's own index
+// arithmetic of the TSC shadow pass (field.cpp:940-945).
+template <int ORDER>
+__device__ __forceinline__ Stencil<ORDER> axis_stencil(double pos, int n,
+                                                       double L, bool shadow) {
+  Stencil<ORDER> st;
+  double loc = ddiv(dmul(double(n), pos), L);
+  if (shadow) {
+    loc = dadd(loc, 0.5);
+    if (loc > double(n)) loc = loc - double(n);
+  }
+  const int idx = int(loc);
+  double s = loc - double(idx);
+  if (ORDER == 1) {
+    int i0 = idx;
+    if (s >= 0.5) i0 = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[0] = i0;
+    st.win[0] = 1.;
+  } else if (ORDER == 2) {
+    st.idx[0] = idx;
+    st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+    st.win[0] = 1. - s;
+    st.win[1] = s;
+  } else if (ORDER == 3) {
+    if (s < 0.5) {
+      st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+      st.idx[1] = idx;
+      st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+      st.win[0] = 0.5 * (0.5 - s) * (0.5 - s);
+      st.win[1] = 0.75 - s * s;
+      st.win[2] = 0.5 * (0.5 + s) * (0.5 + s);
+    } else {
+      st.idx[0] = idx;
+      st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+      if (shadow) {
+        st.idx[2] = (idx == n - 1) ? 0 : st.idx[1] + 1;
+      } else {
+        st.idx[2] = (st.idx[1] == n - 1) ? 0 : st.idx[1] + 1;
+      }
+      const double t = 1. - s;
+      st.win[0] = 0.5 * (0.5 + t) * (0.5 + t);
+      st.win[1] = 0.75 - t * t;
+      st.win[2] = 0.5 * (0.5 - t) * (0.5 - t);
+    }
+  } else {
+    st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+    st.idx[1] = idx;
+    st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[3] = (st.idx[2] == n - 1) ? 0 : st.idx[2] + 1;
+    const double t = 1. - s;
+    st.win[0] = 1. / 6 * t * t * t;
+    st.win[1] = 1. / 6 * (4. - 6. * s * s + 3. * s * s * s);
+    st.win[2] = 1. / 6 * (4. - 6. * t * t + 3. * t * t * t);
+    st.win[3] = 1. / 6 * s * s * s;
+  }
+  return st;
+}
+
+__device__ __forceinline__ void atomic_add_real(float* p, double v) {
+  atomicAdd(p, float(v));
+}
+__device__ __forceinline__ void atomic_add_real(double* p, double v) {
+  atomicAdd(p, v);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct AssignArgs {
+  int n[3];
+  double L[3];
+  int64_t nmesh;
+  DevCatalogue cat;
+  WeightSpec ws;
+};
+
+// Deposit one stencil; returns the weight that landed inside the mesh.
+template <int ORDER, class Real>
+__device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
+                                      bool shadow, cd wgt, Real* re,
+                                      Real* im) {
+  Stencil<ORDER> sx = axis_stencil<ORDER>(pos[0], a.n[0], a.L[0], shadow);
+  Stencil<ORDER> sy = axis_stencil<ORDER>(pos[1], a.n[1], a.L[1], shadow);
+  Stencil<ORDER> sz = axis_stencil<ORDER>(pos[2], a.n[2], a.L[2], shadow);
+  cd landed = {0., 0.};
+#pragma unroll
+  for (int i = 0; i < ORDER; ++i) {
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) {
+      const int64_t row = (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
+      const double wij = sx.win[i] * sy.win[j];
+#pragma unroll
+      for (int k = 0; k < ORDER; ++k) {
+        const int64_t gid = row + sz.idx[k];
+        if (gid < 0 || gid >= a.nmesh) continue;
+        const double wv = wij * sz.win[k];
+        const double vre = wgt.re * wv;
+        atomic_add_real(re + gid, vre);
+        landed.re += vre;
+        if (im != nullptr) {
+          const double vim = wgt.im * wv;
+          atomic_add_real(im + gid, vim);
+          landed.im += vim;
+        }
+      }
+    }
+  }
+  return landed;
+}
+
+template <int ORDER, class Real>
+__global__ void __launch_bounds__(256)
+assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
+              double* sums) {
+  cd acc = {0., 0.}, acc_s = {0., 0.};
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       p < a.cat.n; p += int64_t(gridDim.x) * blockDim.x) {
+    const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
+    double w = (a.cat.w != nullptr) ? a.cat.w[p] : 1.0;
+    double wp = w;
+    for (int i = 1; i < a.ws.power; ++i) wp *= w;
+    cd wgt = {a.ws.scale * wp, 0.};
+    if (a.ws.use_ylm) {
+      cd y = reduced_ylm(a.ws.ell, a.ws.m, a.cat.lx[p], a.cat.ly[p],
+                         a.cat.lz[p]);
+      if (a.ws.conj_ylm) y = conjg(y);
+      wgt = (a.ws.scale * wp) * y;
+    }
+    cd l = deposit<ORDER, Real>(a, pos, false, wgt, re, im);
+    acc = acc + l;
+    if (sre != nullptr) {
+      cd ls = deposit<ORDER, Real>(a, pos, true, wgt, sre, sim);
+      acc_s = acc_s + ls;
+    }
+  }
+  // Block-wide FP64 sums of the deposited weight (k = 0 modes).
+  __shared__ double red[4][8];
+  double v[4] = {warp_sum(acc.re), warp_sum(acc.im), warp_sum(acc_s.re),
+                 warp_sum(acc_s.im)};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int q = 0; q < 4; ++q) red[q][wid] = v[q];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = 0.;
+    for (int q = 0; q < int(blockDim.x >> 5); ++q) s += red[threadIdx.x][q];
+    atomicAdd(sums + threadIdx.x, s);
+  }
+}
+
+template <class Real>
+__global__ void sum_pow_kernel(const Real* mesh, int64_t n, int order,
+                               double* out) {
+  double acc = 0.;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const double v = double(mesh[i]);
+    double p = 1.;
+    for (int q = 0; q < order; ++q) p *= v;
+    acc += p;
+  }
+  __shared__ double red[32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.;
+    for (int q = 0; q < int(blockDim.x >> 5); ++q) s += red[q];
+    atomicAdd(out, s);
+  }
+}
+
+template <class Real>
+__global__ void to_double_kernel(const Real* mesh, int64_t n, double scale,
+                                 double* out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = double(mesh[i]) * scale;
+}
+
+// sum_p scale * w_p^power * [conj] y_lm(los_p) in FP64
+// (calc_ylm_wgtd_shotnoise_amp_for_bispec, threept.cpp:156-208, and its
+// power-spectrum twin, twopt.cpp:298-350).
+__global__ void weight_sum_kernel(DevCatalogue cat, WeightSpec ws,
+                                  double* out) {
+  cd acc = {0., 0.};
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < cat.n;
+       p += int64_t(gridDim.x) * blockDim.x) {
+    const double w = (cat.w != nullptr) ? cat.w[p] : 1.0;
+    double wp = 1.;
+    for (int i = 0; i < ws.power; ++i) wp *= w;
+    cd y = {1., 0.};
+    if (ws.use_ylm) {
+      y = reduced_ylm(ws.ell, ws.m, cat.lx[p], cat.ly[p], cat.lz[p]);
+      if (ws.conj_ylm) y = conjg(y);
+    }
+    acc = acc + wp * y;
+  }
+  __shared__ double red[2][8];
+  const double v0 = warp_sum(acc.re), v1 = warp_sum(acc.im);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = v0;
+    red[1][wid] = v1;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double s = 0.;
+    for (int q = 0; q < int(blockDim.x >> 5); ++q) s += red[threadIdx.x][q];
+    atomicAdd(out + threadIdx.x, ws.scale * s);
+  }
+}
+
+int grid_for(int64_t work, int block) {
+  int64_t g = (work + block - 1) / block;
+  const int64_t cap = 152 * 16;  // a few waves of resident blocks
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return int(g);
+}
+
+}  // namespace
+
+template <class Real>
+void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
+                   const DevCatalogue& cat, const WeightSpec& ws,
+                   Real* mesh_re, Real* mesh_im, Real* shadow_re,
+                   Real* shadow_im, double* sums) {
+  if (cat.n == 0) return;
+  AssignArgs a;
+  for (int i = 0; i < 3; ++i) {
+    a.n[i] = g.n[i];
+    a.L[i] = g.L[i];
+  }
+  a.nmesh = g.nmesh;
+  a.cat = cat;
+  a.ws = ws;
+  Real* sre = interlace ? shadow_re : nullptr;
+  Real* sim = interlace ? shadow_im : nullptr;
+  const int block = 256;
+  const int grid = grid_for(cat.n, block);
+  switch (order) {
+    case 1:
+      assign_kernel<1, Real><<<grid, block, 0, ctx.stream>>>(
+          a, mesh_re, mesh_im, sre, sim, sums);
+      break;
+    case 2:
+      assign_kernel<2, Real><<<grid, block, 0, ctx.stream>>>(
+          a, mesh_re, mesh_im, sre, sim, sums);
+      break;
+    case 3:
+      assign_kernel<3, Real><<<grid, block, 0, ctx.stream>>>(
+          a, mesh_re, mesh_im, sre, sim, sums);
+      break;
+    case 4:
+      assign_kernel<4, Real><<<grid, block, 0, ctx.stream>>>(
+          a, mesh_re, mesh_im, sre, sim, sums);
+      break;
+    default:
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Unsupported mesh assignment order: %d.", order);
+  }
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
+                         double* out) {
+  sum_pow_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(mesh, n,
+                                                                 order, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
+                           double scale, double* out) {
+  to_double_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(
+      mesh, n, scale, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
+                       const WeightSpec& ws, double* out) {
+  if (cat.n == 0) return;
+  weight_sum_kernel<<<grid_for(cat.n, 256), 256, 0, ctx.stream>>>(cat, ws,
+                                                                  out);
+  TRVG_LAUNCHED(ctx);
+}
+
+#define TRVG_INST(R)                                                        \
+  template void launch_assign<R>(Context&, const Geom&, int, bool,          \
+                                 const DevCatalogue&, const WeightSpec&, R*, \
+                                 R*, R*, R*, double*);                      \
+  template void launch_mesh_sum_pow<R>(Context&, const R*, int64_t, int,    \
+                                       double*);                            \
+  template void launch_mesh_to_double<R>(Context&, const R*, int64_t,       \
+                                         double, double*);
+TRVG_INST(float)
+TRVG_INST(double)
+#undef TRVG_INST
+
+}  // namespace trvg

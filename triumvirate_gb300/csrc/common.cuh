@@ -1,0 +1,213 @@
+// Shared host/device arithmetic of the mesh estimators.
+//
+// The same functions run inside the CUDA kernels and in the host-side test
+// hooks of the C ABI, so the host tests exercise the device arithmetic.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#define TRVG_HD __host__ __device__ __forceinline__
+
+namespace trvg {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// Complex double arithmetic.
+// ---------------------------------------------------------------------------
+
+struct cd {
+  double re, im;
+};
+
+TRVG_HD cd cmk(double re, double im) { return cd{re, im}; }
+TRVG_HD cd operator+(cd a, cd b) { return cd{a.re + b.re, a.im + b.im}; }
+TRVG_HD cd operator-(cd a, cd b) { return cd{a.re - b.re, a.im - b.im}; }
+TRVG_HD cd operator*(cd a, cd b) {
+  return cd{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+TRVG_HD cd operator*(double s, cd a) { return cd{s * a.re, s * a.im}; }
+TRVG_HD cd conjg(cd a) { return cd{a.re, -a.im}; }
+// a / b for real b, component-wise as std::complex<double> operator/=(double).
+TRVG_HD cd cdivr(cd a, double b) { return cd{a.re / b, a.im / b}; }
+
+// ---------------------------------------------------------------------------
+// Round-to-nearest FP64 primitives.  Wavevector magnitudes decide integer
+// mode counts, so they are evaluated with the reference's operation order
+// and no fused multiply-add (maths.cpp:57-59, field.cpp:555-562).  Host code
+// is compiled with -ffp-contract=off for the same reason.
+// ---------------------------------------------------------------------------
+
+TRVG_HD double dmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+TRVG_HD double dadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+TRVG_HD double ddiv(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+TRVG_HD double dsqrt(double a) {
+#ifdef __CUDA_ARCH__
+  return __dsqrt_rn(a);
+#else
+  return std::sqrt(a);
+#endif
+}
+
+// sqrt(x*x + y*y + z*z) summed left to right.
+TRVG_HD double vec3_mag(double x, double y, double z) {
+  return dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+}
+
+// FFT-ordered index -> signed frequency / offset (field.cpp:538-542).
+TRVG_HD int shift_index(int i, int n) { return (i < n / 2) ? i : i - n; }
+
+// ---------------------------------------------------------------------------
+// Reduced spherical harmonics (maths.cpp:171-220).
+//
+// y_lm(v) = (-1)^m [m < 0] * conj(Y_l^m(v)) * sqrt(4 pi / (2l + 1)), with
+// y_00 = 1 and y_lm = 0 for |v| < 1e-9.  Y_l^m uses the normalised
+// associated Legendre function with the Condon-Shortley phase; the azimuthal
+// factor exp(i m phi) is formed from (x + i y) / r_xy, which equals the
+// reference's phi = arccos(x / r_xy) (reflected for y < 0) without the
+// inverse cosine.
+// ---------------------------------------------------------------------------
+
+// Normalised associated Legendre function
+//   sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) P_l^m(x),  0 <= m <= l,
+// from the standard stable recurrence in l at fixed m (start from P_m^m,
+// step with the normalised three-term relation).
+TRVG_HD double sph_plm(int l, int m, double x) {
+  double pmm = 1.0;
+  const double omx2 = (1.0 - x) * (1.0 + x);
+  double fact = 1.0;
+  for (int i = 1; i <= m; ++i) {
+    pmm *= omx2 * fact / (fact + 1.0);
+    fact += 2.0;
+  }
+  pmm = sqrt((2 * m + 1) * pmm / (4.0 * kPi));
+  if (m & 1) pmm = -pmm;
+  if (l == m) return pmm;
+  double pmmp1 = x * sqrt(2.0 * m + 3.0) * pmm;
+  if (l == m + 1) return pmmp1;
+  double oldfact = sqrt(2.0 * m + 3.0);
+  double pll = 0.0;
+  for (int ll = m + 2; ll <= l; ++ll) {
+    const double f = sqrt((4.0 * ll * ll - 1.0) / double(ll * ll - m * m));
+    pll = (x * pmmp1 - pmm / oldfact) * f;
+    oldfact = f;
+    pmm = pmmp1;
+    pmmp1 = pll;
+  }
+  return pll;
+}
+
+TRVG_HD cd reduced_ylm(int ell, int m, double x, double y, double z) {
+  if (ell == 0 && m == 0) return cmk(1.0, 0.0);
+  const double eps = 1.e-9;
+  const double r = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+  if (fabs(r) < eps) return cmk(0.0, 0.0);
+  const double mu = z / r;
+  const double rxy = dsqrt(dadd(dmul(x, x), dmul(y, y)));
+  double c = 1.0, s = 0.0;  // cos(phi), sin(phi)
+  if (fabs(rxy) >= eps) {
+    c = x / rxy;
+    s = y / rxy;
+  }
+  const int am = m < 0 ? -m : m;
+  // exp(i |m| phi) by repeated multiplication.
+  cd e = cmk(1.0, 0.0);
+  for (int i = 0; i < am; ++i) e = e * cmk(c, s);
+  if (m < 0) e = conjg(e);
+  const double p = sph_plm(ell, am, mu);
+  cd ylm = conjg(p * e);
+  if (m < 0 && (am & 1)) ylm = -1.0 * ylm;
+  return sqrt(4.0 * kPi / (2.0 * ell + 1.0)) * ylm;
+}
+
+// ---------------------------------------------------------------------------
+// Spherical Bessel functions (maths.cpp:309-375).
+// ---------------------------------------------------------------------------
+
+// j_l(x) by upward recurrence from j_0 and j_1; stable for x > l (used at
+// and beyond the spline split point max(1000, l^2)).
+TRVG_HD double sph_bessel_upward(int ell, double x) {
+  const double sx = sin(x), cx = cos(x);
+  const double j0 = sx / x;
+  if (ell == 0) return j0;
+  double j1 = sx / (x * x) - cx / x;
+  double jm = j0;
+  for (int l = 1; l < ell; ++l) {
+    const double jn = (2.0 * l + 1.0) / x * j1 - jm;
+    jm = j1;
+    j1 = jn;
+  }
+  return j1;
+}
+
+// Natural cubic spline of j_l on the nodes x_i = 0.05 i, i = 0..n-1
+// (second-derivative halves in `c`, node values in `y`).
+struct SplineTable {
+  const double* y;
+  const double* c;
+  int n;
+  int ell;
+  double split;
+};
+
+constexpr double kSplineStep = 0.05;
+
+TRVG_HD double spline_eval(const SplineTable& t, double x) {
+  if (x >= t.split) return sph_bessel_upward(t.ell, x);
+  const double h = kSplineStep;
+  int i = int(x / h);
+  if (i > t.n - 2) i = t.n - 2;
+  if (i < 0) i = 0;
+  double xlo = 0. + dmul(h, double(i));
+  if (x < xlo && i > 0) {
+    --i;
+    xlo = 0. + dmul(h, double(i));
+  }
+  double xhi = 0. + dmul(h, double(i + 1));
+  if (x >= xhi && i < t.n - 2) {
+    ++i;
+    xlo = xhi;
+    xhi = 0. + dmul(h, double(i + 1));
+  }
+  const double hh = xhi - xlo;
+  const double dx = x - xlo;
+  const double ylo = t.y[i], yhi = t.y[i + 1];
+  const double clo = t.c[i], chi = t.c[i + 1];
+  const double b = (yhi - ylo) / hh - hh * (chi + 2.0 * clo) / 3.0;
+  const double d = (chi - clo) / (3.0 * hh);
+  return ylo + dx * (b + dx * (clo + dx * d));
+}
+
+// ---------------------------------------------------------------------------
+// Per-axis Fourier-space factors (field.cpp:1114-1146, 3440-3520).
+// Products over the three axes are formed in the kernels.
+// ---------------------------------------------------------------------------
+
+struct AxisTables {
+  const double* sinc[3];   // sin(u)/u (1 at u = 0), u = pi * i_shift / n
+  const double* alias[3];  // per-axis shot-noise aliasing polynomial of sin^2
+  const double* u[3];      // u itself (interlaced isotropic approximation)
+};
+
+}  // namespace trvg

@@ -1,0 +1,236 @@
+// Context life cycle, device workspace, FFT plan cache, error reporting and
+// the host-side maths entry points of the C ABI.
+#include <cstdarg>
+#include <cstring>
+#include <string>
+
+#include "internal.h"
+#include "maths_host.h"
+
+namespace trvg {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+[[noreturn]] void throw_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw Error(code, buf);
+}
+
+void* Context::buffer(const std::string& name, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  DeviceBuffer& b = buffers[name];
+  if (b.bytes >= bytes) return b.ptr;
+  if (b.ptr != nullptr) {
+    TRVG_CUDA(cudaStreamSynchronize(stream));
+    TRVG_CUDA(cudaFree(b.ptr));
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    b.ptr = nullptr;
+    throw_error(TRVG_ERR_ALLOC,
+                "Device allocation of %.3f GiB for '%s' failed: %s",
+                double(bytes) / (1024. * 1024. * 1024.), name.c_str(),
+                cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  return b.ptr;
+}
+
+cufftHandle Context::plan(int type, const int n[3], int batch) {
+  PlanKey key{type, {n[0], n[1], n[2]}, batch};
+  auto it = plans.find(key);
+  if (it != plans.end()) return it->second;
+  cufftHandle h;
+  TRVG_CUFFT(cufftCreate(&h));
+  TRVG_CUFFT(cufftSetStream(h, stream));
+  long long nn[3] = {n[0], n[1], n[2]};
+  size_t work = 0;
+  long long odist = 0, idist = 0;
+  const long long nfull = nn[0] * nn[1] * nn[2];
+  const long long nhalf = nn[0] * nn[1] * (nn[2] / 2 + 1);
+  switch (type) {
+    case CUFFT_R2C:
+    case CUFFT_D2Z:
+      idist = nfull;
+      odist = nhalf;
+      break;
+    case CUFFT_C2R:
+    case CUFFT_Z2D:
+      idist = nhalf;
+      odist = nfull;
+      break;
+    default:
+      idist = odist = nfull;
+  }
+  cufftResult r = cufftMakePlanMany64(h, 3, nn, nullptr, 1, idist, nullptr, 1,
+                                      odist, cufftType(type), batch, &work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    throw_error(r == CUFFT_ALLOC_FAILED ? TRVG_ERR_ALLOC : TRVG_ERR_CUFFT,
+                "cuFFT plan (type %d, %d x %d x %d, batch %d) failed: %d",
+                type, n[0], n[1], n[2], batch, int(r));
+  }
+  plans[key] = h;
+  return h;
+}
+
+void Context::release() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (auto& kv : plans) cufftDestroy(kv.second);
+  plans.clear();
+  for (auto& kv : buffers)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  buffers.clear();
+}
+
+void Context::log(int level, const char* fmt, ...) const {
+  if (verbose < level) return;
+  va_list ap;
+  va_start(ap, fmt);
+  std::fprintf(stderr, "[trvg] ");
+  std::vfprintf(stderr, fmt, ap);
+  std::fprintf(stderr, "\n");
+  va_end(ap);
+}
+
+}  // namespace trvg
+
+extern "C" {
+
+const char* trvg_last_error(void) { return trvg::last_error(); }
+
+const char* trvg_version(void) { return "triumvirate-gb300 0.1.0 (sm_103a)"; }
+
+int trvg_context_create(int device, trvg_context** ctx) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null context pointer.");
+  int ndev = 0;
+  TRVG_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                      "CUDA device %d unavailable (%d devices).", device,
+                      ndev);
+  TRVG_CUDA(cudaSetDevice(device));
+  auto* c = new trvg_context();
+  c->impl.device = device;
+  TRVG_CUDA(cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking));
+  TRVG_CUDA(cudaEventCreate(&c->impl.ev_start));
+  TRVG_CUDA(cudaEventCreate(&c->impl.ev_h2d));
+  TRVG_CUDA(cudaEventCreate(&c->impl.ev_stop));
+  *ctx = c;
+  TRVG_API_END
+}
+
+int trvg_context_destroy(trvg_context* ctx) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr) return TRVG_OK;
+  cudaSetDevice(ctx->impl.device);
+  ctx->impl.release();
+  if (ctx->impl.ev_start) cudaEventDestroy(ctx->impl.ev_start);
+  if (ctx->impl.ev_h2d) cudaEventDestroy(ctx->impl.ev_h2d);
+  if (ctx->impl.ev_stop) cudaEventDestroy(ctx->impl.ev_stop);
+  if (ctx->impl.stream) cudaStreamDestroy(ctx->impl.stream);
+  delete ctx;
+  TRVG_API_END
+}
+
+int trvg_release_workspace(trvg_context* ctx) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null context.");
+  TRVG_CUDA(cudaSetDevice(ctx->impl.device));
+  ctx->impl.release();
+  TRVG_API_END
+}
+
+int trvg_get_stats(const trvg_context* ctx, trvg_stats* out) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || out == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  const trvg::Context& c = ctx->impl;
+  out->ms_total = c.ms_total;
+  out->ms_h2d = c.ms_h2d;
+  out->h2d_bytes = c.h2d_bytes;
+  out->kernel_launches = c.kernel_launches;
+  out->fft_launches = c.fft_launches;
+  for (int i = 0; i < 3; ++i) out->pruned_grid[i] = c.pruned_grid[i];
+  TRVG_API_END
+}
+
+double trvg_wigner_3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  return trvg::wigner_3j(j1, j2, j3, m1, m2, m3);
+}
+
+double trvg_sph_bessel(int ell, double x) { return trvg::sph_bessel(ell, x); }
+
+int trvg_sph_bessel_spline(int ell, const double* x, int64_t n,
+                           double* out) {
+  TRVG_API_BEGIN
+  if (ell < 0 || (n > 0 && (x == nullptr || out == nullptr)))
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid arguments.");
+  trvg::SplineHost s(ell);
+  trvg::SplineTable t = s.table(s.y.data(), s.c.data());
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(x[i] >= 0.))
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "Spline argument must be non-negative.");
+    out[i] = trvg::spline_eval(t, x[i]);
+  }
+  TRVG_API_END
+}
+
+int trvg_reduced_ylm(int ell, int m, const double* v3, int64_t n,
+                     double* out_complex) {
+  TRVG_API_BEGIN
+  if (ell < 0 || m < -ell || m > ell ||
+      (n > 0 && (v3 == nullptr || out_complex == nullptr)))
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid arguments.");
+  for (int64_t i = 0; i < n; ++i) {
+    trvg::cd y = trvg::reduced_ylm(ell, m, v3[3 * i], v3[3 * i + 1],
+                                   v3[3 * i + 2]);
+    out_complex[2 * i] = y.re;
+    out_complex[2 * i + 1] = y.im;
+  }
+  TRVG_API_END
+}
+
+int trvg_data_vector_dim(int shape, int num_bins, int idx_bin, int* dim) {
+  TRVG_API_BEGIN
+  if (dim == nullptr || num_bins <= 0)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid arguments.");
+  switch (shape) {
+    case TRVG_SHAPE_DIAG:
+    case TRVG_SHAPE_ROW:
+      *dim = num_bins;
+      break;
+    case TRVG_SHAPE_OFFDIAG:
+      *dim = num_bins - (idx_bin < 0 ? -idx_bin : idx_bin);
+      break;
+    case TRVG_SHAPE_FULL:
+      *dim = num_bins * num_bins;
+      break;
+    case TRVG_SHAPE_TRIU:
+      *dim = num_bins * (num_bins + 1) / 2;
+      break;
+    default:
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "Three-point statistic form is not recognised: %d.",
+                        shape);
+  }
+  TRVG_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,1368 @@
+// Estimator orchestration behind the C ABI.
+//
+// Each entry point follows one reference estimator (paths relative to
+// src/triumvirate/ of MikeSWang/Triumvirate):
+//   bispectrum  gpp  threept.cpp:1473-2188    survey  threept.cpp:248-1012
+//   3PCF        gpp  threept.cpp:2190-2619    survey  threept.cpp:1014-1471
+//   P_ell       gpp  twopt.cpp:609-701        survey  twopt.cpp:388-496
+//
+// GB300 structure.  All meshes stay in HBM for the whole call.  A catalogue
+// is assigned once per distinct weighting and transformed once (R2C); the
+// reference's repeated assignments/FFTs of identical fields are shared.
+// Shell-filtered fields F and the compensated field G are evaluated on the
+// smallest FFT-friendly grid M >= 4K + 1 (K: largest shell frequency per
+// axis), on which sum_x F_a F_b G over the full mesh equals
+// (N^3 / M^3) sum over the M grid exactly, since every triple
+// k_a + k_b + k_c = 0 mod N or mod M with |k_a|, |k_b| <= K, |k_c| <= 2K
+// is an exact triangle.  When 4K + 1 reaches the mesh size the full mesh is
+// used (M = N), which is the reference's own evaluation.  The pair-
+// independent shot-noise field is transformed once per term and reduced
+// per pair through a radial histogram.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "maths_host.h"
+
+namespace trvg {
+
+namespace {
+
+using std::vector;
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------------------------
+// cuFFT by precision.
+// ---------------------------------------------------------------------------
+
+template <class Real>
+struct FFT;
+
+template <>
+struct FFT<float> {
+  static constexpr int kR2C = CUFFT_R2C, kC2R = CUFFT_C2R, kC2C = CUFFT_C2C;
+  static void r2c(cufftHandle h, float* in, float2* out) {
+    TRVG_CUFFT(cufftExecR2C(h, in, reinterpret_cast<cufftComplex*>(out)));
+  }
+  static void c2r(cufftHandle h, float2* in, float* out) {
+    TRVG_CUFFT(cufftExecC2R(h, reinterpret_cast<cufftComplex*>(in), out));
+  }
+  static void c2c_inv(cufftHandle h, float2* io) {
+    auto* p = reinterpret_cast<cufftComplex*>(io);
+    TRVG_CUFFT(cufftExecC2C(h, p, p, CUFFT_INVERSE));
+  }
+};
+
+template <>
+struct FFT<double> {
+  static constexpr int kR2C = CUFFT_D2Z, kC2R = CUFFT_Z2D, kC2C = CUFFT_Z2Z;
+  static void r2c(cufftHandle h, double* in, double2* out) {
+    TRVG_CUFFT(
+        cufftExecD2Z(h, in, reinterpret_cast<cufftDoubleComplex*>(out)));
+  }
+  static void c2r(cufftHandle h, double2* in, double* out) {
+    TRVG_CUFFT(
+        cufftExecZ2D(h, reinterpret_cast<cufftDoubleComplex*>(in), out));
+  }
+  static void c2c_inv(cufftHandle h, double2* io) {
+    auto* p = reinterpret_cast<cufftDoubleComplex*>(io);
+    TRVG_CUFFT(cufftExecZ2Z(h, p, p, CUFFT_INVERSE));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Host helpers.
+// ---------------------------------------------------------------------------
+
+struct Pair {
+  int row, col;
+};
+
+// Bin pairs in data-vector order (threept.cpp:1675-1968).
+vector<Pair> dv_pairs(int shape, int nb, int idx_bin) {
+  vector<Pair> out;
+  switch (shape) {
+    case TRVG_SHAPE_DIAG:
+      for (int b = 0; b < nb; ++b) out.push_back({b, b});
+      break;
+    case TRVG_SHAPE_OFFDIAG: {
+      const int d = std::abs(idx_bin);
+      for (int i = 0; i < nb - d; ++i)
+        out.push_back(idx_bin >= 0 ? Pair{i, i + d} : Pair{i + d, i});
+      break;
+    }
+    case TRVG_SHAPE_ROW:
+      for (int c = 0; c < nb; ++c) out.push_back({idx_bin, c});
+      break;
+    case TRVG_SHAPE_FULL:
+      for (int r = 0; r < nb; ++r)
+        for (int c = 0; c < nb; ++c) out.push_back({r, c});
+      break;
+    case TRVG_SHAPE_TRIU:
+      for (int r = 0; r < nb; ++r)
+        for (int c = r; c < nb; ++c) out.push_back({r, c});
+      break;
+    default:
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Three-point statistic form is not recognised: %d.", shape);
+  }
+  return out;
+}
+
+struct Term {
+  int m1, m2, M;
+  double coupling;
+};
+
+// Non-redundant (m1, m2, 0) with nonzero coupling (threept.cpp:1580-1601).
+vector<Term> orders_gpp(int l1, int l2, int L) {
+  vector<Term> out;
+  for (int m1 = -l1; m1 <= l1; ++m1) {
+    for (int m2 = -l2; m2 <= l2; ++m2) {
+      const int M = 0;
+      bool redundant = false;
+      for (const Term& t : out)
+        if (m1 + t.m1 == 0 && m2 + t.m2 == 0 && M + t.M == 0)
+          redundant = true;
+      if (redundant) continue;
+      const double c = calc_coupling_coeff_3pt(l1, l2, L, m1, m2, M);
+      if (std::fabs(c) < kEpsCoupling) continue;
+      out.push_back({m1, m2, M, c});
+    }
+  }
+  return out;
+}
+
+// Non-redundant (m1, m2, M) (threept.cpp:354-404).
+vector<Term> orders_lpp(int l1, int l2, int L) {
+  vector<Term> out;
+  for (int m1 = -l1; m1 <= l1; ++m1) {
+    for (int m2 = -l2; m2 <= l2; ++m2) {
+      bool vanishing = true;
+      for (int M = -L; M <= L; ++M)
+        if (std::fabs(calc_coupling_coeff_3pt(l1, l2, L, m1, m2, M)) >
+            kEpsCoupling)
+          vanishing = false;
+      if (vanishing) continue;
+      for (int M = -L; M <= L; ++M) {
+        bool redundant = false;
+        for (const Term& t : out)
+          if (m1 + t.m1 == 0 && m2 + t.m2 == 0 && M + t.M == 0)
+            redundant = true;
+        if (redundant) continue;
+        const double c = calc_coupling_coeff_3pt(l1, l2, L, m1, m2, M);
+        if (std::fabs(c) < kEpsCoupling) continue;
+        out.push_back({m1, m2, M, c});
+      }
+    }
+  }
+  return out;
+}
+
+bool fft_friendly(int n) {
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+int good_fft_size(int n) {
+  while (!fft_friendly(n)) ++n;
+  return n;
+}
+
+cplx ipow(int n) {  // i^n
+  switch (((n % 4) + 4) % 4) {
+    case 0: return cplx(1., 0.);
+    case 1: return cplx(0., 1.);
+    case 2: return cplx(-1., 0.);
+    default: return cplx(0., -1.);
+  }
+}
+
+struct HostBins {
+  int nb = 0;
+  vector<double> lo, hi, centre;
+};
+
+HostBins host_bins(const trvg_binning* b) {
+  if (b == nullptr || b->num_bins <= 0 || b->bin_edges == nullptr ||
+      b->bin_centres == nullptr)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Binning must have a positive number of bins with edges "
+                "and centres.");
+  HostBins h;
+  h.nb = b->num_bins;
+  for (int i = 0; i < h.nb; ++i) {
+    h.lo.push_back(b->bin_edges[i]);
+    h.hi.push_back(b->bin_edges[i + 1]);
+    h.centre.push_back(b->bin_centres[i]);
+    if (!std::isfinite(h.lo.back()) || !std::isfinite(h.hi.back()))
+      throw_error(TRVG_ERR_INVALID_PARAMETER, "Bin edges must be finite.");
+  }
+  if (h.lo[0] < 0.)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Bin range must be non-negative.");
+  return h;
+}
+
+// Fine-sample index range [smin, smax) of each bin: sample i belongs to bin
+// b when lo_b <= i * step < hi_b (field.cpp:2671-2682, 3170-3181).
+void sample_ranges(const HostBins& hb, double step, int n_sample,
+                   vector<int>& smin, vector<int>& smax) {
+  smin.resize(hb.nb);
+  smax.resize(hb.nb);
+  auto first_at_least = [&](double v) {
+    if (!(v > 0.)) return 0;
+    double guess = std::floor(v / step) - 2.;
+    long long i = guess < 0. ? 0 : (long long)guess;
+    if (i > n_sample) return n_sample;
+    while (i < n_sample && double(i) * step < v) ++i;
+    return int(i);
+  };
+  for (int b = 0; b < hb.nb; ++b) {
+    smin[b] = first_at_least(hb.lo[b]);
+    smax[b] = std::max(smin[b], first_at_least(hb.hi[b]));
+  }
+}
+
+void validate_params(const trvg_params* p) {
+  if (p == nullptr)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Null parameter set.");
+  for (int i = 0; i < 3; ++i) {
+    if (p->ngrid[i] < 2)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Mesh number must be >= 2 in every dimension: %d.",
+                  p->ngrid[i]);
+    if (!(p->boxsize[i] > 0.) || !std::isfinite(p->boxsize[i]))
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Box size must be positive in every dimension.");
+  }
+  const double nmesh =
+      double(p->ngrid[0]) * double(p->ngrid[1]) * double(p->ngrid[2]);
+  if (nmesh > double(1LL << 40))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Mesh too large.");
+  if (p->assignment_order < 1 || p->assignment_order > 4)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Mesh assignment scheme must be 'ngp', 'cic', 'tsc' or "
+                "'pcs' (order %d given).",
+                p->assignment_order);
+  if (p->ell1 < 0 || p->ell2 < 0 || p->ELL < 0)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Degrees must be non-negative.");
+  if (p->precision != TRVG_PREC_FP64 && p->precision != TRVG_PREC_FP32_MIXED)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown precision %d.",
+                p->precision);
+}
+
+void validate_threept(const trvg_params* p, int nb) {
+  // threept.cpp:73-89.
+  if (std::fabs(wigner_3j(p->ell1, p->ell2, p->ELL, 0, 0, 0)) < kEpsCoupling)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Specified three-point correlator multipole vanishes "
+                "identically owing to zero-valued Wigner 3-j symbol.");
+  if (p->shape == TRVG_SHAPE_ROW && (p->idx_bin < 0 || p->idx_bin >= nb))
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Bin index `idx_bin` must be in [0, num_bins) for 'row'.");
+  if (p->shape == TRVG_SHAPE_OFFDIAG && std::abs(p->idx_bin) >= nb)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Bin index `idx_bin` must be < `num_bins` in absolute value.");
+}
+
+// ---------------------------------------------------------------------------
+// The engine.
+// ---------------------------------------------------------------------------
+
+template <class Real>
+struct Engine {
+  using C = typename CplxOf<Real>::type;
+
+  struct Field {
+    FieldSpec<Real> spec;
+    double sums[4] = {0., 0., 0., 0.};
+  };
+
+  struct Part {
+    DevCatalogue cat;
+    WeightSpec ws;
+  };
+
+  struct Stats {
+    vector<long long> nmodes;
+    vector<double> k;
+    vector<cplx> pk, sn;
+  };
+
+  Context& ctx;
+  trvg_params p;
+  Geom g;
+  AxisTablesDev ax;
+  bool interlace;
+
+  Engine(Context& c, const trvg_params& prm, bool allow_interlace)
+      : ctx(c), p(prm) {
+    interlace = allow_interlace && p.interlace != 0;
+    for (int i = 0; i < 3; ++i) {
+      g.n[i] = p.ngrid[i];
+      g.L[i] = p.boxsize[i];
+      g.dk[i] = 2. * M_PI / p.boxsize[i];
+      g.dr[i] = p.boxsize[i] / p.ngrid[i];
+    }
+    g.vol = p.boxsize[0] * p.boxsize[1] * p.boxsize[2];
+    g.nmesh = int64_t(g.n[0]) * g.n[1] * g.n[2];
+    g.vol_cell = g.vol / double(g.nmesh);
+    g.nzh = g.n[2] / 2 + 1;
+    g.nhalf = int64_t(g.n[0]) * g.n[1] * g.nzh;
+    setup_axis_tables();
+  }
+
+  void sync() { TRVG_CUDA(cudaStreamSynchronize(ctx.stream)); }
+
+  template <class T>
+  T* upload(const std::string& name, const vector<T>& v) {
+    T* d = ctx.buf<T>(name, v.size());
+    if (!v.empty())
+      TRVG_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T),
+                                cudaMemcpyHostToDevice, ctx.stream));
+    return d;
+  }
+
+  template <class T>
+  vector<T> download(const T* d, size_t n) {
+    vector<T> v(n);
+    if (n > 0) {
+      TRVG_CUDA(cudaMemcpyAsync(v.data(), d, n * sizeof(T),
+                                cudaMemcpyDeviceToHost, ctx.stream));
+      sync();
+    }
+    return v;
+  }
+
+  void zero(void* d, size_t bytes) {
+    TRVG_CUDA(cudaMemsetAsync(d, 0, bytes, ctx.stream));
+  }
+
+  // Per-axis sinc, aliasing and u tables (field.cpp:1127-1143, 3445-3458).
+  void setup_axis_tables() {
+    const int nmax = std::max({g.n[0], g.n[1], g.n[2]});
+    vector<double> host(size_t(9) * nmax, 0.);
+    for (int a = 0; a < 3; ++a) {
+      for (int i = 0; i < g.n[a]; ++i) {
+        const int s = shift_index(i, g.n[a]);
+        const double u = M_PI * s / double(g.n[a]);
+        const double sinc = (s != 0) ? std::sin(u) / u : 1.;
+        const double s2 = (s != 0) ? std::sin(u) * std::sin(u) : 0.;
+        double al = 1.;
+        switch (p.assignment_order) {
+          case 2: al = 1. - 2. / 3. * s2; break;
+          case 3: al = 1. - s2 + 2. / 15. * s2 * s2; break;
+          case 4:
+            al = 1. - 4. / 3. * s2 + 2. / 5. * s2 * s2 -
+                 4. / 315. * s2 * s2 * s2;
+            break;
+          default: al = 1.;
+        }
+        host[size_t(3 * a + 0) * nmax + i] = sinc;
+        host[size_t(3 * a + 1) * nmax + i] = al;
+        host[size_t(3 * a + 2) * nmax + i] = u;
+      }
+    }
+    double* d = upload("axis_tables", host);
+    for (int a = 0; a < 3; ++a) {
+      ax.t.sinc[a] = d + size_t(3 * a + 0) * nmax;
+      ax.t.alias[a] = d + size_t(3 * a + 1) * nmax;
+      ax.t.u[a] = d + size_t(3 * a + 2) * nmax;
+    }
+    ax.order = p.assignment_order;
+    ax.interlace = interlace;
+  }
+
+  DevCatalogue upload_catalogue(const trvg_catalogue* c,
+                                const std::string& tag, bool need_los) {
+    if (c == nullptr)
+      throw_error(TRVG_ERR_INVALID_DATA, "Particle data are uninitialised.");
+    if (c->n < 0)
+      throw_error(TRVG_ERR_INVALID_DATA, "Negative particle count.");
+    if (c->n > 0 && (c->x == nullptr || c->y == nullptr || c->z == nullptr))
+      throw_error(TRVG_ERR_INVALID_DATA, "Particle data are uninitialised.");
+    if (need_los && c->n > 0 &&
+        (c->los_x == nullptr || c->los_y == nullptr || c->los_z == nullptr))
+      throw_error(TRVG_ERR_INVALID_DATA,
+                  "Lines of sight are required for survey-type catalogues.");
+    DevCatalogue d;
+    d.n = c->n;
+    if (c->memory == TRVG_MEM_DEVICE) {
+      d.x = c->x;
+      d.y = c->y;
+      d.z = c->z;
+      d.w = c->w;
+      d.lx = c->los_x;
+      d.ly = c->los_y;
+      d.lz = c->los_z;
+      return d;
+    }
+    if (c->memory != TRVG_MEM_HOST)
+      throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown memory kind %d.",
+                  c->memory);
+    auto put = [&](const double* h, const char* nm) -> const double* {
+      if (h == nullptr || c->n == 0) return nullptr;
+      double* dd = ctx.buf<double>(tag + nm, size_t(c->n));
+      TRVG_CUDA(cudaMemcpyAsync(dd, h, size_t(c->n) * sizeof(double),
+                                cudaMemcpyHostToDevice, ctx.stream));
+      ctx.h2d_bytes += c->n * int64_t(sizeof(double));
+      return dd;
+    };
+    d.x = put(c->x, ".x");
+    d.y = put(c->y, ".y");
+    d.z = put(c->z, ".z");
+    d.w = put(c->w, ".w");
+    if (need_los) {
+      d.lx = put(c->los_x, ".lx");
+      d.ly = put(c->los_y, ".ly");
+      d.lz = put(c->los_z, ".lz");
+    }
+    return d;
+  }
+
+  // Assign all parts into one (complex if `cplx`) mesh, with the shadow when
+  // interlacing, and transform each component mesh once (R2C).
+  Field make_field(const std::string& name, const vector<Part>& parts,
+                   bool cplx) {
+    Field f;
+    Real* mre = ctx.buf<Real>("mesh.re", g.nmesh);
+    Real* mim = cplx ? ctx.buf<Real>("mesh.im", g.nmesh) : nullptr;
+    Real* sre = interlace ? ctx.buf<Real>("mesh.sre", g.nmesh) : nullptr;
+    Real* sim = (interlace && cplx) ? ctx.buf<Real>("mesh.sim", g.nmesh)
+                                    : nullptr;
+    const size_t mb = size_t(g.nmesh) * sizeof(Real);
+    zero(mre, mb);
+    if (mim) zero(mim, mb);
+    if (sre) zero(sre, mb);
+    if (sim) zero(sim, mb);
+    double* sums = ctx.buf<double>("assign.sums", 4);
+    zero(sums, 4 * sizeof(double));
+    for (const Part& part : parts)
+      launch_assign<Real>(ctx, g, p.assignment_order, interlace, part.cat,
+                          part.ws, mre, mim, sre, sim, sums);
+    cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
+    auto r2c = [&](Real* m, const char* suffix) -> const C* {
+      C* o = ctx.buf<C>(name + suffix, size_t(g.nhalf));
+      FFT<Real>::r2c(h, m, o);
+      ctx.fft_launches++;
+      return o;
+    };
+    f.spec.re = r2c(mre, ".re");
+    if (mim) f.spec.im = r2c(mim, ".im");
+    if (sre) f.spec.re_s = r2c(sre, ".sre");
+    if (sim) f.spec.im_s = r2c(sim, ".sim");
+    vector<double> hs = download(sums, 4);
+    for (int i = 0; i < 4; ++i) f.sums[i] = hs[i];
+    return f;
+  }
+
+  // Field spectrum with its exact k = 0 mode: (main sum + shift) combined
+  // with the shadow sum when interlacing.
+  FieldSpec<Real> k0_view(const Field& f, double shift) const {
+    FieldSpec<Real> s = f.spec;
+    cd k0 = {f.sums[0] + shift, f.sums[1]};
+    if (interlace) k0 = cd{(k0.re + f.sums[2]) / 2., (k0.im + f.sums[3]) / 2.};
+    s.k0 = k0;
+    s.k0_set = true;
+    return s;
+  }
+
+  cplx weight_sum(const DevCatalogue& cat, const WeightSpec& ws) {
+    double* d = ctx.buf<double>("wsum", 2);
+    zero(d, 2 * sizeof(double));
+    launch_weight_sum(ctx, cat, ws, d);
+    vector<double> h = download(d, 2);
+    return cplx(h[0], h[1]);
+  }
+
+  // Frequencies of all modes with |k| < kmax: |s| <= floor(kmax/dk) + 1 per
+  // axis, or the whole axis.
+  Cube make_cube(double kmax) const {
+    Cube c;
+    c.count = 1;
+    for (int a = 0; a < 3; ++a) {
+      const double kk = kmax / g.dk[a];
+      int K = (kk >= double(g.n[a])) ? g.n[a] : int(std::floor(kk)) + 1;
+      c.dense[a] = (2 * int64_t(K) + 1 >= g.n[a]);
+      c.K[a] = c.dense[a] ? g.n[a] / 2 : K;
+      c.ext[a] = c.dense[a] ? g.n[a] : 2 * K + 1;
+      c.count *= c.ext[a];
+    }
+    return c;
+  }
+
+  BinsDev bins_dev(const std::string& tag, const HostBins& hb,
+                   const vector<int>* smin, const vector<int>* smax) {
+    BinsDev b;
+    b.nbins = hb.nb;
+    b.lo = upload(tag + ".lo", hb.lo);
+    b.hi = upload(tag + ".hi", hb.hi);
+    if (smin) b.smin = upload(tag + ".smin", *smin);
+    if (smax) b.smax = upload(tag + ".smax", *smax);
+    return b;
+  }
+
+  // nmodes and k_eff per bin (field.cpp:1812-1847, 1904-1905).
+  void count_modes(const HostBins& hb, vector<long long>& nmodes,
+                   vector<double>& keff) {
+    const double kmax = *std::max_element(hb.hi.begin(), hb.hi.end());
+    Cube cube = make_cube(kmax);
+    BinsDev bd = bins_dev("cm", hb, nullptr, nullptr);
+    long long* dn = ctx.buf<long long>("cm.n", hb.nb);
+    double* dk = ctx.buf<double>("cm.k", hb.nb);
+    zero(dn, hb.nb * sizeof(long long));
+    zero(dk, hb.nb * sizeof(double));
+    launch_count_modes(ctx, g, cube, bd, dn, dk);
+    nmodes = download(dn, hb.nb);
+    vector<double> ks = download(dk, hb.nb);
+    keff.resize(hb.nb);
+    for (int b = 0; b < hb.nb; ++b) keff[b] = ks[b] / double(nmodes[b]);
+  }
+
+  // Fine-binned two-point statistics (field.cpp:2511-2703).
+  Stats twopt_stats(const HostBins& hb, const FieldSpec<Real>& fa,
+                    const FieldSpec<Real>& fb, cplx shot, int ell, int m) {
+    vector<int> smin, smax;
+    const int n_sample = 1000000;
+    const double dk_sample = 1.e-5;
+    sample_ranges(hb, dk_sample, n_sample, smin, smax);
+    const int smax_all = *std::max_element(smax.begin(), smax.end());
+    Cube cube = make_cube(double(smax_all + 1) * dk_sample);
+    BinsDev bd = bins_dev("st", hb, &smin, &smax);
+    long long* dn = ctx.buf<long long>("st.n", hb.nb);
+    double* dk = ctx.buf<double>("st.k", hb.nb);
+    double* dpk = ctx.buf<double>("st.pk", 2 * hb.nb);
+    double* dsn = ctx.buf<double>("st.sn", 2 * hb.nb);
+    zero(dn, hb.nb * sizeof(long long));
+    zero(dk, hb.nb * sizeof(double));
+    zero(dpk, 2 * hb.nb * sizeof(double));
+    zero(dsn, 2 * hb.nb * sizeof(double));
+    launch_twopt_stats<Real>(ctx, g, cube, fa, fb, cd{shot.real(), shot.imag()},
+                             ell, m, ax, bd, dn, dk, dpk, dsn);
+    Stats s;
+    s.nmodes = download(dn, hb.nb);
+    vector<double> k = download(dk, hb.nb), pk = download(dpk, 2 * hb.nb),
+                   sn = download(dsn, 2 * hb.nb);
+    s.k.resize(hb.nb);
+    s.pk.resize(hb.nb);
+    s.sn.resize(hb.nb);
+    for (int b = 0; b < hb.nb; ++b) {
+      const double n = double(s.nmodes[b]);
+      if (s.nmodes[b] != 0) {
+        s.k[b] = k[b] / n;
+        s.pk[b] = cplx(pk[2 * b], pk[2 * b + 1]) / n;
+        s.sn[b] = cplx(sn[2 * b], sn[2 * b + 1]) / n;
+      } else {
+        s.k[b] = hb.centre[b];
+        s.pk[b] = 0.;
+        s.sn[b] = 0.;
+      }
+    }
+    return s;
+  }
+
+  // Shot-noise two-point field xi(x) = IFFT[(fa fb^*/W - S C_1/W) / V]
+  // (field.cpp:3269-3345) into the real meshes xi.re (and xi.im).
+  void twopt_xi(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                cplx shot, Real*& xi_re, Real*& xi_im) {
+    const bool hermitian = fa.im == nullptr && fb.im == nullptr &&
+                           fa.im_s == nullptr && fb.im_s == nullptr &&
+                           shot.imag() == 0.;
+    C* hre = ctx.buf<C>("xi.h.re", size_t(g.nhalf));
+    C* him = hermitian ? nullptr : ctx.buf<C>("xi.h.im", size_t(g.nhalf));
+    launch_twopt_field<Real>(ctx, g, fa, fb, cd{shot.real(), shot.imag()}, ax,
+                             hre, him);
+    cufftHandle h = ctx.plan(FFT<Real>::kC2R, g.n, 1);
+    xi_re = ctx.buf<Real>("xi.re", size_t(g.nmesh));
+    FFT<Real>::c2r(h, hre, xi_re);
+    ctx.fft_launches++;
+    xi_im = nullptr;
+    if (him) {
+      xi_im = ctx.buf<Real>("xi.im", size_t(g.nmesh));
+      FFT<Real>::c2r(h, him, xi_im);
+      ctx.fft_launches++;
+    }
+  }
+
+  struct SplineDev {
+    SplineTable t;
+  };
+
+  SplineTable spline(int ell) {
+    SplineHost s(ell);
+    const std::string tag = "spline." + std::to_string(ell);
+    const double* y = upload(tag + ".y", s.y);
+    const double* c = upload(tag + ".c", s.c);
+    return s.table(y, c);
+  }
+
+  // Uncoupled shot noise per pair (field.cpp:3349-3396):
+  // vol_cell sum_x j_a(k_a r) j_b(k_b r) y_a y_b xi(x).
+  vector<cplx> shotnoise_pairs(const Real* xi_re, const Real* xi_im, int la,
+                               int ma, int lb, int mb, const SplineTable& sja,
+                               const SplineTable& sjb,
+                               const vector<double>& ka,
+                               const vector<double>& kb) {
+    const int np = int(ka.size());
+    const double* dka = upload("sn.ka", ka);
+    const double* dkb = upload("sn.kb", kb);
+    double* out = ctx.buf<double>("sn.out", 2 * size_t(np));
+    zero(out, 2 * np * sizeof(double));
+    const bool cubic = g.dr[0] == g.dr[1] && g.dr[1] == g.dr[2];
+    if (cubic) {
+      int64_t nkeys = 1;
+      for (int a = 0; a < 3; ++a) {
+        const int64_t smx = g.n[a] - g.n[a] / 2;
+        nkeys += smx * smx;
+      }
+      double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
+      zero(hist, 2 * nkeys * sizeof(double));
+      launch_radial_hist<Real>(ctx, g, xi_re, xi_im, la, ma, lb, mb, hist);
+      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
+                              out);
+    } else {
+      launch_pair_bessel_direct<Real>(ctx, g, xi_re, xi_im, la, ma, lb, mb,
+                                      sja, sjb, dka, dkb, np, out);
+    }
+    vector<double> h = download(out, 2 * size_t(np));
+    vector<cplx> res(np);
+    for (int i = 0; i < np; ++i)
+      res[i] = cplx(h[2 * i], h[2 * i + 1]) * g.vol_cell;
+    return res;
+  }
+
+  // Evaluation grid of the shell fields.
+  void eval_grid(double kmax, int M[3], int K[3], int Kg[3]) {
+    Cube c = make_cube(kmax);
+    for (int a = 0; a < 3; ++a) {
+      K[a] = c.K[a];
+      Kg[a] = 2 * c.K[a];
+      M[a] = g.n[a];
+      if (!c.dense[a]) {
+        const int need = good_fft_size(4 * c.K[a] + 1);
+        if (need < g.n[a]) M[a] = need;
+      }
+    }
+  }
+
+  C* build_G(const FieldSpec<Real>& f, const int M[3], const int Kg[3]) {
+    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+    C* G = ctx.buf<C>("G", size_t(Mc));
+    launch_build_G<Real>(ctx, g, M, Kg, f, ax, G);
+    FFT<Real>::c2c_inv(ctx.plan(FFT<Real>::kC2C, M, 1), G);
+    ctx.fft_launches++;
+    return G;
+  }
+
+  // Leg of shell fields: either band-limited shells (lo/hi) or j_l(k r)
+  // weights (radii), one field per listed bin.
+  struct Leg {
+    int ell, m;
+    bool sjl = false;
+    SplineTable sj;
+  };
+
+  void build_leg(const FieldSpec<Real>& src, const Leg& leg,
+                 const vector<int>& bins, const HostBins& hb,
+                 const vector<double>& radii, const int M[3], const int K[3],
+                 const std::string& tag, C* out) {
+    const int nb = int(bins.size());
+    if (leg.sjl) {
+      vector<double> r(nb);
+      for (int i = 0; i < nb; ++i) r[i] = radii[bins[i]];
+      const double* dr = upload(tag + ".r", r);
+      launch_build_F_sjl<Real>(ctx, g, src, ax, leg.ell, leg.m, leg.sj, dr,
+                               nb, out);
+    } else {
+      vector<double> lo(nb), hi(nb);
+      double hmax = 0.;
+      for (int i = 0; i < nb; ++i) {
+        lo[i] = hb.lo[bins[i]];
+        hi[i] = hb.hi[bins[i]];
+        hmax = std::max(hmax, hi[i]);
+      }
+      const double* dlo = upload(tag + ".lo", lo);
+      const double* dhi = upload(tag + ".hi", hi);
+      launch_build_F<Real>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo, dhi,
+                           nb, hmax, out);
+    }
+    FFT<Real>::c2c_inv(ctx.plan(FFT<Real>::kC2C, M, nb), out);
+    ctx.fft_launches++;
+  }
+
+  // sum over the evaluation grid of F_a(row) F_b(col) G for every pair.
+  vector<cplx> pair_sums(const FieldSpec<Real>& src, const C* G,
+                         const Leg& la, const Leg& lb,
+                         const vector<Pair>& pairs, const HostBins& hb,
+                         const vector<double>& radii, const int M[3],
+                         const int K[3]) {
+    const int np = int(pairs.size());
+    vector<cplx> res(np, cplx(0., 0.));
+    const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;
+    vector<int> A, B;
+    for (const Pair& q : pairs) {
+      A.push_back(q.row);
+      B.push_back(q.col);
+    }
+    if (shared) {
+      A.insert(A.end(), B.begin(), B.end());
+      B = A;
+    }
+    auto uniq = [](vector<int>& v) {
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+    };
+    uniq(A);
+    uniq(B);
+    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+    const size_t perF = size_t(Mc) * sizeof(C);
+    size_t free_b = 0, total_b = 0;
+    TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    size_t have = 0;
+    for (const char* nm : {"F.A", "F.B"}) {
+      auto it = ctx.buffers.find(nm);
+      if (it != ctx.buffers.end()) have += it->second.bytes;
+    }
+    const double budget = 0.7 * double(free_b + have);
+    int SA, SB;
+    if (shared) {
+      SA = int(std::min<double>(A.size(), budget / perF));
+      if (SA < int(A.size())) SA = int(std::min<double>(A.size(),
+                                                         budget / (2. * perF)));
+      SB = SA;
+    } else {
+      SA = int(std::min<double>(A.size(), budget / (2. * perF)));
+      SB = int(std::min<double>(B.size(), budget / (2. * perF)));
+    }
+    if (SA < 1 || SB < 1)
+      throw_error(TRVG_ERR_ALLOC,
+                  "Insufficient device memory for shell fields "
+                  "(%.2f GiB each).",
+                  double(perF) / 1073741824.);
+    auto chunk = [](const vector<int>& v, int s) {
+      vector<vector<int>> out;
+      for (size_t i = 0; i < v.size(); i += s)
+        out.emplace_back(v.begin() + i,
+                         v.begin() + std::min(v.size(), i + size_t(s)));
+      return out;
+    };
+    const auto blocksA = chunk(A, SA);
+    const auto blocksB = shared ? blocksA : chunk(B, SB);
+    for (size_t I = 0; I < blocksA.size(); ++I) {
+      const vector<int>& bA = blocksA[I];
+      C* FA = ctx.buf<C>("F.A", bA.size() * size_t(Mc));
+      build_leg(src, la, bA, hb, radii, M, K, "legA", FA);
+      for (size_t J = 0; J < blocksB.size(); ++J) {
+        const vector<int>& bB = blocksB[J];
+        vector<int> pa, pb, idx;
+        for (int i = 0; i < np; ++i) {
+          auto ia = std::lower_bound(bA.begin(), bA.end(), pairs[i].row);
+          auto ib = std::lower_bound(bB.begin(), bB.end(), pairs[i].col);
+          if (ia == bA.end() || *ia != pairs[i].row) continue;
+          if (ib == bB.end() || *ib != pairs[i].col) continue;
+          pa.push_back(int(ia - bA.begin()));
+          pb.push_back(int(ib - bB.begin()));
+          idx.push_back(i);
+        }
+        if (idx.empty()) continue;
+        const C* FB = FA;
+        if (!(shared && I == J)) {
+          C* fb = ctx.buf<C>("F.B", bB.size() * size_t(Mc));
+          build_leg(src, lb, bB, hb, radii, M, K, "legB", fb);
+          FB = fb;
+        }
+        const int* dpa = upload("pairs.a", pa);
+        const int* dpb = upload("pairs.b", pb);
+        double* dout = ctx.buf<double>("pairs.out", 2 * idx.size());
+        zero(dout, 2 * idx.size() * sizeof(double));
+        launch_reduce_pairs<Real>(ctx, Mc, G, FA, FB, dpa, dpb,
+                                  int(idx.size()), dout);
+        vector<double> h = download(dout, 2 * idx.size());
+        for (size_t q = 0; q < idx.size(); ++q)
+          res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);
+      }
+    }
+    return res;
+  }
+
+  // -------------------------------------------------------------------------
+  // Bispectrum.
+  // -------------------------------------------------------------------------
+  void bispec(const trvg_catalogue* data, const trvg_catalogue* rand,
+              double alpha, const trvg_binning* kb, double norm,
+              trvg_threept_out* out, bool survey) {
+    const HostBins hb = host_bins(kb);
+    validate_threept(&p, hb.nb);
+    const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
+    const int ndv = int(pairs.size());
+    if (out == nullptr || out->dim != ndv)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Output data vector has dimension %d, expected %d.",
+                  out ? out->dim : -1, ndv);
+    const vector<Term> terms = survey ? orders_lpp(p.ell1, p.ell2, p.ELL)
+                                      : orders_gpp(p.ell1, p.ell2, p.ELL);
+    const DevCatalogue dd = upload_catalogue(data, "data", survey);
+    DevCatalogue dr;
+    if (survey) dr = upload_catalogue(rand, "rand", true);
+    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+
+    auto ylm_ws = [](double scale, int power, int ell, int m, bool conj) {
+      WeightSpec w;
+      w.scale = scale;
+      w.power = power;
+      w.use_ylm = !(ell == 0 && m == 0);
+      w.ell = ell;
+      w.m = m;
+      w.conj_ylm = conj;
+      return w;
+    };
+
+    // delta n_00 and N_00 (gpp: one unit-weight assignment serves both).
+    FieldSpec<Real> dn, nf;
+    if (!survey) {
+      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      const double nbar = double(dd.n) / g.vol;
+      dn = k0_view(base, -nbar * g.vol);
+      nf = k0_view(base, 0.);
+    } else {
+      Field f0 = make_field("dn00", {{dd, ylm_ws(1., 1, 0, 0, false)},
+                                     {dr, ylm_ws(-alpha, 1, 0, 0, false)}},
+                            false);
+      dn = k0_view(f0, 0.);
+      Field n0 = make_field("N00", {{dd, ylm_ws(1., 2, 0, 0, true)},
+                                    {dr, ylm_ws(alpha * alpha, 2, 0, 0, true)}},
+                            false);
+      nf = k0_view(n0, 0.);
+    }
+
+    vector<long long> nmodes;
+    vector<double> keff;
+    count_modes(hb, nmodes, keff);
+    vector<double> ka(ndv), kbv(ndv);
+    for (int i = 0; i < ndv; ++i) {
+      ka[i] = keff[pairs[i].row];
+      kbv[i] = keff[pairs[i].col];
+    }
+
+    int M[3], K[3], Kg[3];
+    eval_grid(*std::max_element(hb.hi.begin(), hb.hi.end()), M, K, Kg);
+    for (int a = 0; a < 3; ++a) ctx.pruned_grid[a] = M[a];
+    const double fac = double(g.nmesh) / (double(M[0]) * M[1] * M[2]);
+    ctx.log(20, "bispectrum: mesh %d^3 -> evaluation grid %d x %d x %d",
+            g.n[0], M[0], M[1], M[2]);
+
+    const SplineTable sja = spline(p.ell1);
+    const SplineTable sjb = spline(p.ell2);
+    const cplx phase = ipow(p.ell1 + p.ell2);
+
+    vector<cplx> bk(ndv, 0.), sn(ndv, 0.);
+
+    C* G = nullptr;
+    Real *xi_re = nullptr, *xi_im = nullptr;
+    if (!survey) {
+      G = build_G(dn, M, Kg);
+      twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
+    }
+    vector<double> no_radii;
+
+    for (const Term& t : terms) {
+      const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
+      const double mirror = zero_t ? 0. : ((p.ELL & 1) ? -1. : 1.);
+      const double mirror_w3j = zero_t ? 0. : 1.;
+      FieldSpec<Real> dnLM, NLM;
+      cplx Sbar;
+      if (survey) {
+        const bool cplxM = (t.M != 0);
+        Field fdn = make_field("dnLM",
+                               {{dd, ylm_ws(1., 1, p.ELL, t.M, false)},
+                                {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
+                               cplxM);
+        dnLM = k0_view(fdn, 0.);
+        G = build_G(dnLM, M, Kg);
+        Field fN = make_field(
+            "NLM",
+            {{dd, ylm_ws(1., 2, p.ELL, t.M, true)},
+             {dr, ylm_ws(alpha * alpha, 2, p.ELL, t.M, true)}},
+            cplxM);
+        NLM = k0_view(fN, 0.);
+        Sbar = weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false)) +
+               alpha * alpha * alpha *
+                   weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
+      } else {
+        NLM = nf;
+        Sbar = cplx(double(dd.n), 0.);
+      }
+
+      // Raw bispectrum (threept.cpp:1675-1968).
+      Leg la{p.ell1, t.m1}, lb{p.ell2, t.m2};
+      const vector<cplx> comp =
+          pair_sums(dn, G, la, lb, pairs, hb, no_radii, M, K);
+      for (int i = 0; i < ndv; ++i) {
+        const cplx B = comp[i] * fac /
+                       (double(nmodes[pairs[i].row]) *
+                        double(nmodes[pairs[i].col]));
+        bk[i] += t.coupling * g.vol_cell * (B + mirror * std::conj(B));
+      }
+
+      // Shot noise (threept.cpp:1974-2140).
+      if (p.ell1 == 0 && p.ell2 == 0)
+        for (int i = 0; i < ndv; ++i) sn[i] += t.coupling * Sbar;
+      if (p.ell2 == 0) {
+        Stats st = twopt_stats(hb, dn, NLM, Sbar, p.ell1, t.m1);
+        for (int i = 0; i < ndv; ++i) {
+          const int b = pairs[i].row;
+          const cplx S = t.coupling * (st.pk[b] - st.sn[b]);
+          sn[i] += S + mirror * std::conj(S);
+        }
+      }
+      if (p.ell1 == 0) {
+        Stats st = twopt_stats(hb, dn, NLM, Sbar, p.ell2, t.m2);
+        for (int i = 0; i < ndv; ++i) {
+          const int b = pairs[i].col;
+          const cplx S = t.coupling * (st.pk[b] - st.sn[b]);
+          sn[i] += S + mirror * std::conj(S);
+        }
+      }
+      if (survey) twopt_xi(dnLM, nf, Sbar, xi_re, xi_im);
+      const vector<cplx> Sij = shotnoise_pairs(
+          xi_re, xi_im, p.ell1, t.m1, p.ell2, t.m2, sja, sjb, ka, kbv);
+      for (int i = 0; i < ndv; ++i) {
+        const cplx S = t.coupling * Sij[i];
+        sn[i] += phase * (S + mirror_w3j * std::conj(S));
+      }
+    }
+
+    for (int i = 0; i < ndv; ++i) {
+      const Pair& q = pairs[i];
+      out->coord1_bin[i] = hb.centre[q.row];
+      out->coord2_bin[i] = hb.centre[q.col];
+      out->coord1_eff[i] = keff[q.row];
+      out->coord2_eff[i] = keff[q.col];
+      out->count_1[i] = int32_t(nmodes[q.row]);
+      out->count_2[i] = int32_t(nmodes[q.col]);
+      const cplx r = norm * bk[i], s = norm * sn[i];
+      out->raw[2 * i] = r.real();
+      out->raw[2 * i + 1] = r.imag();
+      out->shot[2 * i] = s.real();
+      out->shot[2 * i + 1] = s.imag();
+    }
+  }
+
+  // -------------------------------------------------------------------------
+  // Three-point correlation function.
+  // -------------------------------------------------------------------------
+  void threepcf(const trvg_catalogue* data, const trvg_catalogue* rand,
+                double alpha, const trvg_binning* rbin, double norm,
+                trvg_threept_out* out, bool survey) {
+    const HostBins hb = host_bins(rbin);
+    validate_threept(&p, hb.nb);
+    const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
+    const int ndv = int(pairs.size());
+    if (out == nullptr || out->dim != ndv)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Output data vector has dimension %d, expected %d.",
+                  out ? out->dim : -1, ndv);
+    const vector<Term> terms = survey ? orders_lpp(p.ell1, p.ell2, p.ELL)
+                                      : orders_gpp(p.ell1, p.ell2, p.ELL);
+    const DevCatalogue dd = upload_catalogue(data, "data", survey);
+    DevCatalogue dr;
+    if (survey) dr = upload_catalogue(rand, "rand", true);
+    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+
+    auto ylm_ws = [](double scale, int power, int ell, int m, bool conj) {
+      WeightSpec w;
+      w.scale = scale;
+      w.power = power;
+      w.use_ylm = !(ell == 0 && m == 0);
+      w.ell = ell;
+      w.m = m;
+      w.conj_ylm = conj;
+      return w;
+    };
+
+    FieldSpec<Real> dn, nf;
+    if (!survey) {
+      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      const double nbar = double(dd.n) / g.vol;
+      dn = k0_view(base, -nbar * g.vol);
+      nf = k0_view(base, 0.);
+    } else {
+      Field f0 = make_field("dn00", {{dd, ylm_ws(1., 1, 0, 0, false)},
+                                     {dr, ylm_ws(-alpha, 1, 0, 0, false)}},
+                            false);
+      dn = k0_view(f0, 0.);
+      Field n0 = make_field("N00", {{dd, ylm_ws(1., 2, 0, 0, true)},
+                                    {dr, ylm_ws(alpha * alpha, 2, 0, 0, true)}},
+                            false);
+      nf = k0_view(n0, 0.);
+    }
+
+    const int M[3] = {g.n[0], g.n[1], g.n[2]};
+    const int K[3] = {g.n[0] / 2, g.n[1] / 2, g.n[2] / 2};
+    for (int a = 0; a < 3; ++a) ctx.pruned_grid[a] = M[a];
+
+    const SplineTable sja = spline(p.ell1);
+    const SplineTable sjb = spline(p.ell2);
+    const cplx phase = ipow(p.ell1 + p.ell2);
+    const double parity = ((p.ell1 + p.ell2) & 1) ? -1. : 1.;
+
+    vector<int> smin, smax;
+    sample_ranges(hb, 1., 100000, smin, smax);
+    BinsDev bd = bins_dev("rb", hb, &smin, &smax);
+
+    vector<cplx> zeta(ndv, 0.), sn(ndv, 0.);
+    vector<long long> npairs(hb.nb, 0);
+    vector<double> reff(hb.nb, 0.);
+
+    C* G = nullptr;
+    Real *xi_re = nullptr, *xi_im = nullptr;
+    if (!survey) {
+      G = build_G(dn, M, K);
+      twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
+    }
+
+    bool first = true;
+    for (const Term& t : terms) {
+      const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
+      const double mirror = zero_t ? 0. : ((p.ELL & 1) ? -1. : 1.);
+      const double mirror_w3j = zero_t ? 0. : 1.;
+      if (survey) {
+        const bool cplxM = (t.M != 0);
+        Field fdn = make_field("dnLM",
+                               {{dd, ylm_ws(1., 1, p.ELL, t.M, false)},
+                                {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
+                               cplxM);
+        FieldSpec<Real> dnLM = k0_view(fdn, 0.);
+        const cplx Sbar = weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false)) +
+                          alpha * alpha * alpha *
+                              weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
+        twopt_xi(dnLM, nf, Sbar, xi_re, xi_im);
+        G = build_G(dnLM, M, K);
+      }
+
+      // Shot noise (field.cpp:3090-3196; threept.cpp:2307-2345).
+      long long* dnp = ctx.buf<long long>("z.n", hb.nb);
+      double* drs = ctx.buf<double>("z.r", hb.nb);
+      double* dxi = ctx.buf<double>("z.xi", 2 * hb.nb);
+      zero(dnp, hb.nb * sizeof(long long));
+      zero(drs, hb.nb * sizeof(double));
+      zero(dxi, 2 * hb.nb * sizeof(double));
+      launch_shotnoise_3pcf_bins<Real>(ctx, g, xi_re, xi_im, p.ell1, t.m1,
+                                       p.ell2, t.m2, bd, dnp, drs, dxi);
+      vector<long long> np = download(dnp, hb.nb);
+      vector<double> rs = download(drs, hb.nb), xs = download(dxi, 2 * hb.nb);
+      vector<cplx> xib(hb.nb);
+      const double norm_f = 1. / g.vol_cell * parity;
+      for (int b = 0; b < hb.nb; ++b) {
+        if (np[b] != 0) {
+          xib[b] = cplx(xs[2 * b], xs[2 * b + 1]) / double(np[b]);
+          xib[b] *= norm_f / double(np[b]);
+          if (first) reff[b] = rs[b] / double(np[b]);
+        } else {
+          xib[b] = 0.;
+          if (first) reff[b] = hb.centre[b];
+        }
+        if (first) npairs[b] = np[b];
+      }
+      for (int i = 0; i < ndv; ++i) {
+        if (pairs[i].row != pairs[i].col) continue;
+        if (p.shape == TRVG_SHAPE_OFFDIAG && p.idx_bin != 0) continue;
+        const int b = pairs[i].row;
+        sn[i] += t.coupling * parity *
+                 (xib[b] + mirror_w3j * std::conj(xib[b]));
+      }
+      first = false;
+
+      // Raw 3PCF with j_l(k r)-weighted transforms (field.cpp:1908-2010).
+      Leg la{p.ell1, t.m1, true, sja}, lb{p.ell2, t.m2, true, sjb};
+      const vector<cplx> comp =
+          pair_sums(dn, G, la, lb, pairs, hb, reff, M, K);
+      for (int i = 0; i < ndv; ++i)
+        zeta[i] += t.coupling * g.vol_cell * phase *
+                   (comp[i] + mirror * std::conj(comp[i]));
+    }
+
+    for (int i = 0; i < ndv; ++i) {
+      const Pair& q = pairs[i];
+      out->coord1_bin[i] = hb.centre[q.row];
+      out->coord2_bin[i] = hb.centre[q.col];
+      out->coord1_eff[i] = reff[q.row];
+      out->coord2_eff[i] = reff[q.col];
+      out->count_1[i] = int32_t(npairs[q.row]);
+      out->count_2[i] = int32_t(npairs[q.col]);
+      const cplx r = norm * zeta[i], s = norm * sn[i];
+      out->raw[2 * i] = r.real();
+      out->raw[2 * i + 1] = r.imag();
+      out->shot[2 * i] = s.real();
+      out->shot[2 * i + 1] = s.imag();
+    }
+  }
+
+  // -------------------------------------------------------------------------
+  // Power spectrum.
+  // -------------------------------------------------------------------------
+  void powspec(const trvg_catalogue* data, const trvg_catalogue* rand,
+               double alpha, const trvg_binning* kb, double norm,
+               trvg_powspec_out* out, bool survey) {
+    const HostBins hb = host_bins(kb);
+    if (out == nullptr || out->dim != hb.nb)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Output data vector has dimension %d, expected %d.",
+                  out ? out->dim : -1, hb.nb);
+    const DevCatalogue dd = upload_catalogue(data, "data", survey);
+    DevCatalogue dr;
+    if (survey) dr = upload_catalogue(rand, "rand", true);
+    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+    for (int a = 0; a < 3; ++a) ctx.pruned_grid[a] = g.n[a];
+
+    auto ylm_ws = [](double scale, int power, int ell, int m, bool conj) {
+      WeightSpec w;
+      w.scale = scale;
+      w.power = power;
+      w.use_ylm = !(ell == 0 && m == 0);
+      w.ell = ell;
+      w.m = m;
+      w.conj_ylm = conj;
+      return w;
+    };
+
+    vector<long long> nmodes(hb.nb, 0);
+    vector<double> keff(hb.nb, 0.);
+    vector<cplx> pk(hb.nb, 0.), sn(hb.nb, 0.);
+    if (!survey) {
+      // twopt.cpp:609-701.
+      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      const double nbar = double(dd.n) / g.vol;
+      FieldSpec<Real> dn = k0_view(base, -nbar * g.vol);
+      Stats st = twopt_stats(hb, dn, dn, cplx(double(dd.n), 0.), p.ELL, 0);
+      const double f = double(2 * p.ELL + 1);
+      for (int b = 0; b < hb.nb; ++b) {
+        nmodes[b] = st.nmodes[b];
+        keff[b] = st.k[b];
+        pk[b] = f * st.pk[b];
+        sn[b] = f * st.sn[b];
+      }
+    } else {
+      // twopt.cpp:388-496.
+      Field f0 = make_field("dn00", {{dd, ylm_ws(1., 1, 0, 0, false)},
+                                     {dr, ylm_ws(-alpha, 1, 0, 0, false)}},
+                            false);
+      const FieldSpec<Real> dn00 = k0_view(f0, 0.);
+      const int ell1 = p.ELL;
+      for (int M = -p.ELL; M <= p.ELL; ++M) {
+        Field fl = make_field("dnLM",
+                              {{dd, ylm_ws(1., 1, p.ELL, M, false)},
+                               {dr, ylm_ws(-alpha, 1, p.ELL, M, false)}},
+                              M != 0);
+        const FieldSpec<Real> dnLM = k0_view(fl, 0.);
+        const cplx amp = weight_sum(dd, ylm_ws(1., 2, p.ELL, M, false)) +
+                         alpha * alpha *
+                             weight_sum(dr, ylm_ws(1., 2, p.ELL, M, false));
+        for (int m1 = -ell1; m1 <= ell1; ++m1) {
+          const double c = calc_coupling_coeff_2pt(ell1, p.ELL, m1, M);
+          if (std::fabs(c) < kEpsCoupling) continue;
+          Stats st = twopt_stats(hb, dnLM, dn00, amp, ell1, m1);
+          for (int b = 0; b < hb.nb; ++b) {
+            pk[b] += c * st.pk[b];
+            sn[b] += c * st.sn[b];
+          }
+          if (M == 0 && m1 == 0) {
+            nmodes = st.nmodes;
+            keff = st.k;
+          }
+        }
+      }
+    }
+    for (int b = 0; b < hb.nb; ++b) {
+      out->kbin[b] = hb.centre[b];
+      out->keff[b] = keff[b];
+      out->nmodes[b] = int32_t(nmodes[b]);
+      const cplx r = norm * pk[b], s = norm * sn[b];
+      out->pk_raw[2 * b] = r.real();
+      out->pk_raw[2 * b + 1] = r.imag();
+      out->pk_shot[2 * b] = s.real();
+      out->pk_shot[2 * b + 1] = s.imag();
+    }
+  }
+
+  // -------------------------------------------------------------------------
+  // Mesh utilities.
+  // -------------------------------------------------------------------------
+  double powlaw_norm(const trvg_catalogue* cat, int order) {
+    const DevCatalogue d = upload_catalogue(cat, "data", false);
+    Real* m = ctx.buf<Real>("mesh.re", g.nmesh);
+    zero(m, size_t(g.nmesh) * sizeof(Real));
+    double* sums = ctx.buf<double>("assign.sums", 4);
+    zero(sums, 4 * sizeof(double));
+    launch_assign<Real>(ctx, g, p.assignment_order, false, d, WeightSpec(), m,
+                        nullptr, nullptr, nullptr, sums);
+    double* acc = ctx.buf<double>("powlaw", 1);
+    zero(acc, sizeof(double));
+    launch_mesh_sum_pow<Real>(ctx, m, g.nmesh, order, acc);
+    const double s = download(acc, 1)[0];
+    // The mesh holds n dV; field.cpp:2050-2062 sums n^order then * dV.
+    const double vint = s / std::pow(g.vol_cell, order) * g.vol_cell;
+    return 1. / vint;
+  }
+
+  void assign_to_host(const trvg_catalogue* cat, bool shadow, double* host) {
+    const DevCatalogue d = upload_catalogue(cat, "data", false);
+    Real* m = ctx.buf<Real>("mesh.re", g.nmesh);
+    Real* s = ctx.buf<Real>("mesh.sre", g.nmesh);
+    zero(m, size_t(g.nmesh) * sizeof(Real));
+    zero(s, size_t(g.nmesh) * sizeof(Real));
+    double* sums = ctx.buf<double>("assign.sums", 4);
+    zero(sums, 4 * sizeof(double));
+    launch_assign<Real>(ctx, g, p.assignment_order, shadow, d, WeightSpec(),
+                        m, nullptr, s, nullptr, sums);
+    double* dd = ctx.buf<double>("mesh.dbl", g.nmesh);
+    launch_mesh_to_double<Real>(ctx, shadow ? s : m, g.nmesh,
+                                1. / g.vol_cell, dd);
+    TRVG_CUDA(cudaMemcpyAsync(host, dd, size_t(g.nmesh) * sizeof(double),
+                              cudaMemcpyDeviceToHost, ctx.stream));
+    sync();
+  }
+};
+
+// Run `fn` on an engine of the requested precision with call accounting.
+template <class Fn>
+void run(trvg_context* c, const trvg_params* prm, bool allow_interlace,
+         Fn&& fn) {
+  if (c == nullptr) throw_error(TRVG_ERR_INVALID_PARAMETER, "Null context.");
+  validate_params(prm);
+  Context& ctx = c->impl;
+  TRVG_CUDA(cudaSetDevice(ctx.device));
+  ctx.verbose = prm->verbose;
+  ctx.kernel_launches = 0;
+  ctx.fft_launches = 0;
+  ctx.h2d_bytes = 0;
+  TRVG_CUDA(cudaEventRecord(ctx.ev_start, ctx.stream));
+  TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+  if (prm->precision == TRVG_PREC_FP64) {
+    Engine<double> e(ctx, *prm, allow_interlace);
+    fn(e);
+  } else {
+    Engine<float> e(ctx, *prm, allow_interlace);
+    fn(e);
+  }
+  TRVG_CUDA(cudaEventRecord(ctx.ev_stop, ctx.stream));
+  TRVG_CUDA(cudaEventSynchronize(ctx.ev_stop));
+  TRVG_CUDA(cudaGetLastError());
+  float ms = 0.f, ms_h = 0.f;
+  TRVG_CUDA(cudaEventElapsedTime(&ms, ctx.ev_start, ctx.ev_stop));
+  TRVG_CUDA(cudaEventElapsedTime(&ms_h, ctx.ev_start, ctx.ev_h2d));
+  ctx.ms_total = ms;
+  ctx.ms_h2d = ms_h;
+}
+
+}  // namespace
+
+}  // namespace trvg
+
+using trvg::run;
+
+extern "C" {
+
+int trvg_compute_bispec_in_gpp_box(trvg_context* ctx,
+                                   const trvg_params* params,
+                                   const trvg_catalogue* data,
+                                   const trvg_binning* kbinning,
+                                   double norm_factor,
+                                   trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.bispec(data, nullptr, 1., kbinning, norm_factor, out, false);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_bispec(trvg_context* ctx, const trvg_params* params,
+                        const trvg_catalogue* data,
+                        const trvg_catalogue* rand, double alpha,
+                        const trvg_binning* kbinning, double norm_factor,
+                        trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.bispec(data, rand, alpha, kbinning, norm_factor, out, true);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_3pcf_in_gpp_box(trvg_context* ctx, const trvg_params* params,
+                                 const trvg_catalogue* data,
+                                 const trvg_binning* rbinning,
+                                 double norm_factor, trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.threepcf(data, nullptr, 1., rbinning, norm_factor, out, false);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_3pcf(trvg_context* ctx, const trvg_params* params,
+                      const trvg_catalogue* data, const trvg_catalogue* rand,
+                      double alpha, const trvg_binning* rbinning,
+                      double norm_factor, trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.threepcf(data, rand, alpha, rbinning, norm_factor, out, true);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_powspec_in_gpp_box(trvg_context* ctx,
+                                    const trvg_params* params,
+                                    const trvg_catalogue* data,
+                                    const trvg_binning* kbinning,
+                                    double norm_factor,
+                                    trvg_powspec_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, true, [&](auto& e) {
+    e.powspec(data, nullptr, 1., kbinning, norm_factor, out, false);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_powspec(trvg_context* ctx, const trvg_params* params,
+                         const trvg_catalogue* data,
+                         const trvg_catalogue* rand, double alpha,
+                         const trvg_binning* kbinning, double norm_factor,
+                         trvg_powspec_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, true, [&](auto& e) {
+    e.powspec(data, rand, alpha, kbinning, norm_factor, out, true);
+  });
+  TRVG_API_END
+}
+
+int trvg_calc_grid_based_powlaw_norm(trvg_context* ctx,
+                                     const trvg_params* params,
+                                     const trvg_catalogue* particles,
+                                     int order, double* norm_factor) {
+  TRVG_API_BEGIN
+  if (norm_factor == nullptr || order < 1)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid arguments.");
+  run(ctx, params, false,
+      [&](auto& e) { *norm_factor = e.powlaw_norm(particles, order); });
+  TRVG_API_END
+}
+
+int trvg_assign_weighted_field_to_mesh(trvg_context* ctx,
+                                       const trvg_params* params,
+                                       const trvg_catalogue* particles,
+                                       int shadow, double* mesh_out) {
+  TRVG_API_BEGIN
+  if (mesh_out == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null output mesh.");
+  run(ctx, params, true, [&](auto& e) {
+    e.assign_to_host(particles, shadow != 0, mesh_out);
+  });
+  TRVG_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+// Host-side internals: errors, device workspace, FFT plans, the context.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include "trvg.h"
+
+namespace trvg {
+
+// Error carrying a C-ABI status code.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+[[noreturn]] void throw_error(int code, const char* fmt, ...);
+void set_last_error(const std::string& msg);
+const char* last_error();
+
+// Body wrappers of the C-ABI functions: exceptions become status codes and
+// the thread's last-error message.
+#define TRVG_API_BEGIN try {
+#define TRVG_API_END                                        \
+  }                                                         \
+  catch (const ::trvg::Error& e) {                          \
+    ::trvg::set_last_error(e.what());                       \
+    return e.code;                                          \
+  }                                                         \
+  catch (const std::bad_alloc&) {                           \
+    ::trvg::set_last_error("Host allocation failed.");      \
+    return TRVG_ERR_ALLOC;                                  \
+  }                                                         \
+  catch (const std::exception& e) {                         \
+    ::trvg::set_last_error(e.what());                       \
+    return TRVG_ERR_INVALID_DATA;                           \
+  }                                                         \
+  ::trvg::set_last_error("");                               \
+  return TRVG_OK;
+
+#define TRVG_CUDA(call)                                                     \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess)                                                  \
+      ::trvg::throw_error(TRVG_ERR_CUDA, "%s failed at %s:%d: %s", #call,   \
+                          __FILE_NAME__, __LINE__, cudaGetErrorString(e_));      \
+  } while (0)
+
+#define TRVG_CUFFT(call)                                                    \
+  do {                                                                      \
+    cufftResult r_ = (call);                                                \
+    if (r_ != CUFFT_SUCCESS)                                                \
+      ::trvg::throw_error(TRVG_ERR_CUFFT, "%s failed at %s:%d: cufft %d",   \
+                          #call, __FILE_NAME__, __LINE__, int(r_));              \
+  } while (0)
+
+// Check the launch just made (configuration errors surface here; faults in
+// the kernel surface at the next synchronising call).
+#define TRVG_LAUNCHED(ctx)                                                  \
+  do {                                                                      \
+    TRVG_CUDA(cudaGetLastError());                                          \
+    (ctx).kernel_launches++;                                                \
+  } while (0)
+
+// A named, grow-only device buffer.  Buffers persist across calls on one
+// context so that repeated estimates allocate nothing.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+// cuFFT plan key.
+struct PlanKey {
+  int type;       // cufftType
+  int n[3];
+  int batch;
+  bool operator<(const PlanKey& o) const {
+    if (type != o.type) return type < o.type;
+    for (int i = 0; i < 3; ++i)
+      if (n[i] != o.n[i]) return n[i] < o.n[i];
+    return batch < o.batch;
+  }
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::map<std::string, DeviceBuffer> buffers;
+  std::map<PlanKey, cufftHandle> plans;
+  cudaEvent_t ev_start = nullptr, ev_h2d = nullptr, ev_stop = nullptr;
+  int verbose = 0;
+  // Counters of the current / last call.
+  int64_t kernel_launches = 0;
+  int64_t fft_launches = 0;
+  int64_t h2d_bytes = 0;
+  double ms_total = 0., ms_h2d = 0.;
+  int pruned_grid[3] = {0, 0, 0};
+
+  // Grow-only named buffer of at least `bytes` bytes.
+  void* buffer(const std::string& name, size_t bytes);
+  template <class T>
+  T* buf(const std::string& name, size_t count) {
+    return static_cast<T*>(buffer(name, count * sizeof(T)));
+  }
+  cufftHandle plan(int type, const int n[3], int batch);
+  void release();
+  void log(int level, const char* fmt, ...) const;
+};
+
+}  // namespace trvg
+
+struct trvg_context {
+  trvg::Context impl;
+};

@@ -1,0 +1,174 @@
+// Host launchers of the CUDA kernels.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace trvg {
+
+template <class Real> struct CplxOf;
+template <> struct CplxOf<float> { using type = float2; };
+template <> struct CplxOf<double> { using type = double2; };
+
+// Mesh geometry of one estimate.
+struct Geom {
+  int n[3];
+  double L[3];
+  double dk[3];        // 2 pi / L (field.cpp:358-360)
+  double dr[3];        // L / n   (field.cpp:353-355)
+  double vol, vol_cell;
+  int64_t nmesh;
+  int nzh;             // n[2] / 2 + 1 (half-spectrum extent)
+  int64_t nhalf;       // n[0] * n[1] * nzh
+};
+
+// Particle arrays in device memory.
+struct DevCatalogue {
+  int64_t n = 0;
+  const double* x = nullptr;
+  const double* y = nullptr;
+  const double* z = nullptr;
+  const double* w = nullptr;
+  const double* lx = nullptr;
+  const double* ly = nullptr;
+  const double* lz = nullptr;
+};
+
+// Per-particle weight scale * w^power * [conj] y_lm(los).
+struct WeightSpec {
+  double scale = 1.0;
+  int power = 1;
+  bool use_ylm = false;
+  int ell = 0, m = 0;
+  bool conj_ylm = false;
+};
+
+// Spectrum of a (possibly complex) mesh field stored as the half spectra
+// of its real and imaginary part meshes, with an optional interlacing
+// shadow and an exact override of the k = 0 mode.
+template <class Real>
+struct FieldSpec {
+  using C = typename CplxOf<Real>::type;
+  const C* re = nullptr;
+  const C* im = nullptr;
+  const C* re_s = nullptr;
+  const C* im_s = nullptr;
+  cd k0 = {0., 0.};
+  bool k0_set = false;
+};
+
+// Device copies of the per-axis Fourier factor tables.
+struct AxisTablesDev {
+  AxisTables t;
+  int order;           // assignment order
+  bool interlace;
+};
+
+// Bin edges and the fine-sample index ranges of each bin.
+struct BinsDev {
+  int nbins = 0;
+  const double* lo = nullptr;
+  const double* hi = nullptr;
+  const int* smin = nullptr;   // first fine sample index in the bin
+  const int* smax = nullptr;   // one past the last
+};
+
+// ---- assign.cu -----------------------------------------------------------
+template <class Real>
+void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
+                   const DevCatalogue& cat, const WeightSpec& ws,
+                   Real* mesh_re, Real* mesh_im, Real* shadow_re,
+                   Real* shadow_im, double* sums /* [4]: re, im, s_re, s_im */);
+void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
+                       const WeightSpec& ws, double* out /* [2] */);
+template <class Real>
+void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
+                         double* out);
+template <class Real>
+void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
+                           double scale, double* out);
+
+// ---- spectral.cu ---------------------------------------------------------
+// Mode cube: frequencies s in [-K, K] per axis, or the whole axis when
+// dense[ax].
+struct Cube {
+  int K[3];
+  bool dense[3];
+  int ext[3];
+  int64_t count;
+};
+
+void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
+                        const BinsDev& bins, long long* nmodes,
+                        double* ksum);
+
+template <class Real>
+void launch_build_G(Context& ctx, const Geom& g, const int M[3],
+                    const int Kg[3], const FieldSpec<Real>& f,
+                    const AxisTablesDev& ax,
+                    typename CplxOf<Real>::type* out);
+
+template <class Real>
+void launch_build_F(Context& ctx, const Geom& g, const int M[3],
+                    const int K[3], const FieldSpec<Real>& f,
+                    const AxisTablesDev& ax, int ell, int m,
+                    const double* lo, const double* hi, int nb,
+                    double hi_max, typename CplxOf<Real>::type* out);
+
+template <class Real>
+void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
+                        const AxisTablesDev& ax, int ell, int m,
+                        const SplineTable& sj, const double* radii, int nb,
+                        typename CplxOf<Real>::type* out);
+
+template <class Real>
+void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
+                        const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                        cd shot, int ell, int m, const AxisTablesDev& ax,
+                        const BinsDev& bins, long long* nmodes, double* ksum,
+                        double* pk, double* sn);
+
+template <class Real>
+void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
+                        const FieldSpec<Real>& fb, cd shot,
+                        const AxisTablesDev& ax,
+                        typename CplxOf<Real>::type* out_re,
+                        typename CplxOf<Real>::type* out_im);
+
+// ---- reduce.cu -----------------------------------------------------------
+template <class Real>
+void launch_reduce_pairs(Context& ctx, int64_t ncell,
+                         const typename CplxOf<Real>::type* G,
+                         const typename CplxOf<Real>::type* Fa,
+                         const typename CplxOf<Real>::type* Fb,
+                         const int* pa, const int* pb, int npairs,
+                         double* out /* 2 * npairs */);
+
+template <class Real>
+void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
+                        const Real* xi_im, int ell_a, int m_a, int ell_b,
+                        int m_b, double* hist /* 2 * nkeys */);
+
+void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
+                             const double* hist, const SplineTable& sja,
+                             const SplineTable& sjb, const double* ka,
+                             const double* kb, int npairs, double* out);
+
+template <class Real>
+void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,
+                               const Real* xi_im, int ell_a, int m_a,
+                               int ell_b, int m_b, const SplineTable& sja,
+                               const SplineTable& sjb, const double* ka,
+                               const double* kb, int npairs, double* out);
+
+template <class Real>
+void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
+                                const Real* xi_im, int ell_a, int m_a,
+                                int ell_b, int m_b, const BinsDev& bins,
+                                long long* npairs, double* rsum, double* xi);
+
+}  // namespace trvg

@@ -1,0 +1,329 @@
+// Configuration-space reductions.
+//
+//  * reduce_pairs: sum_x F_a(x) F_b(x) G(x) for many bin pairs in one launch
+//    (the triple-product loops of threept.cpp:1703-1723 and its copies),
+//    accumulated in FP64.
+//  * radial_hist + pair_bessel_sums: the uncoupled shot noise of the
+//    bispectrum, vol_cell sum_x j_la(k_a r) j_lb(k_b r) y_a(r) y_b(r) xi(x)
+//    (field.cpp:3349-3396).  With cubic cells r depends on x only through
+//    the integer key s_x^2 + s_y^2 + s_z^2, so xi * y_a * y_b is first
+//    summed per key and the Bessel weights are applied per key and pair.
+//  * pair_bessel_direct: the same sum evaluated cell by cell (any cells).
+//  * shotnoise_3pcf_bins: r-binned sums of the 3PCF shot noise
+//    (field.cpp:3090-3196) with exact per-cell separations.
+#include "kernels.h"
+
+namespace trvg {
+
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+int grid_for(int64_t work, int block, int64_t cap = 152 * 16) {
+  int64_t g = (work + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return int(g);
+}
+
+// Block-wide sum of `n` per-thread values, atomically added to out[0..n).
+// Only the first `limit` sums are written (the tail of the last chunk of
+// pairs has no output slots).
+template <int N>
+__device__ __forceinline__ void block_add(double (&v)[N], double* out,
+                                          double* red /* [N][32] */,
+                                          int limit = N) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double s = warp_sum(v[q]);
+    if (lane == 0) red[q * 32 + wid] = s;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    double s = 0.;
+    for (int w = 0; w < nw; ++w) s += red[q * 32 + w];
+    if (out != nullptr && q < limit) atomicAdd(out + q, s);
+  }
+  __syncthreads();
+}
+
+template <class C>
+__device__ __forceinline__ C cmulc(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+
+constexpr int kPairChunk = 8;
+
+template <class Real>
+__global__ void __launch_bounds__(256)
+reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
+                    const typename CplxOf<Real>::type* Fa,
+                    const typename CplxOf<Real>::type* Fb, const int* pa,
+                    const int* pb, int npairs, double* out) {
+  using C = typename CplxOf<Real>::type;
+  __shared__ double red[2 * kPairChunk * 32];
+  const int p0 = blockIdx.y * kPairChunk;
+  int ia[kPairChunk], ib[kPairChunk];
+  bool ok[kPairChunk];
+#pragma unroll
+  for (int q = 0; q < kPairChunk; ++q) {
+    ok[q] = (p0 + q) < npairs;
+    ia[q] = ok[q] ? pa[p0 + q] : 0;
+    ib[q] = ok[q] ? pb[p0 + q] : 0;
+  }
+  double acc[2 * kPairChunk];
+#pragma unroll
+  for (int q = 0; q < 2 * kPairChunk; ++q) acc[q] = 0.;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const C g = G[t];
+#pragma unroll
+    for (int q = 0; q < kPairChunk; ++q) {
+      if (!ok[q]) continue;
+      const C a = Fa[int64_t(ia[q]) * ncell + t];
+      const C b = Fb[int64_t(ib[q]) * ncell + t];
+      const C p = cmulc(cmulc(a, b), g);
+      acc[2 * q] += double(p.x);
+      acc[2 * q + 1] += double(p.y);
+    }
+  }
+  block_add<2 * kPairChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
+}
+
+// Sum of xi * y_a * y_b per integer key s_x^2 + s_y^2 + s_z^2 (cubic cells).
+template <class Real>
+__global__ void __launch_bounds__(256)
+radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
+                   int m_a, int ell_b, int m_b, double* hist) {
+  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
+              sz = shift_index(k, g.n[2]);
+    const int64_t key = int64_t(sx) * sx + int64_t(sy) * sy + int64_t(sz) * sz;
+    cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
+    if (!trivial) {
+      const double rx = dmul(double(sx), g.dr[0]);
+      const double ry = dmul(double(sy), g.dr[1]);
+      const double rz = dmul(double(sz), g.dr[2]);
+      const cd ya = reduced_ylm(ell_a, m_a, rx, ry, rz);
+      const cd yb = reduced_ylm(ell_b, m_b, rx, ry, rz);
+      v = v * (ya * yb);
+    }
+    atomicAdd(hist + 2 * key, v.re);
+    if (v.im != 0.) atomicAdd(hist + 2 * key + 1, v.im);
+  }
+}
+
+struct PairBesselArgs {
+  SplineTable ja, jb;
+  const double* ka;
+  const double* kb;
+};
+
+__global__ void __launch_bounds__(256)
+pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* hist,
+                        PairBesselArgs a, double* out) {
+  __shared__ double red[2 * 32];
+  const int p = blockIdx.y;
+  const double ka = a.ka[p], kb = a.kb[p];
+  double acc[2] = {0., 0.};
+  for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
+    const double hr = hist[2 * key], hi = hist[2 * key + 1];
+    if (hr == 0. && hi == 0.) continue;
+    const double r = dr * sqrt(double(key));
+    const double w = spline_eval(a.ja, ka * r) * spline_eval(a.jb, kb * r);
+    acc[0] += w * hr;
+    acc[1] += w * hi;
+  }
+  block_add<2>(acc, out + 2 * p, red);
+}
+
+constexpr int kBesselChunk = 4;
+
+template <class Real>
+__global__ void __launch_bounds__(256)
+pair_bessel_direct_kernel(Geom g, const Real* xi_re, const Real* xi_im,
+                          int ell_a, int m_a, int ell_b, int m_b,
+                          PairBesselArgs a, int npairs, double* out) {
+  __shared__ double red[2 * kBesselChunk * 32];
+  const int p0 = blockIdx.y * kBesselChunk;
+  double acc[2 * kBesselChunk];
+#pragma unroll
+  for (int q = 0; q < 2 * kBesselChunk; ++q) acc[q] = 0.;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
+    const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
+    const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
+    const double r = vec3_mag(rx, ry, rz);
+    cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
+    v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
+             reduced_ylm(ell_b, m_b, rx, ry, rz));
+#pragma unroll
+    for (int q = 0; q < kBesselChunk; ++q) {
+      if (p0 + q >= npairs) continue;
+      const double w = spline_eval(a.ja, a.ka[p0 + q] * r) *
+                       spline_eval(a.jb, a.kb[p0 + q] * r);
+      acc[2 * q] += w * v.re;
+      acc[2 * q + 1] += w * v.im;
+    }
+  }
+  block_add<2 * kBesselChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256)
+shotnoise_3pcf_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
+                      int m_a, int ell_b, int m_b, BinsDev bins,
+                      long long* npairs, double* rsum, double* xi) {
+  extern __shared__ unsigned char smem_raw[];
+  double* s_r = reinterpret_cast<double*>(smem_raw);
+  double* s_xi = s_r + bins.nbins;
+  long long* s_n = reinterpret_cast<long long*>(s_xi + 2 * bins.nbins);
+  for (int q = threadIdx.x; q < bins.nbins; q += blockDim.x) {
+    s_r[q] = 0.;
+    s_xi[2 * q] = s_xi[2 * q + 1] = 0.;
+    s_n[q] = 0;
+  }
+  __syncthreads();
+  const int n_sample = 100000;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
+    const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
+    const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
+    const double r = vec3_mag(rx, ry, rz);
+    const int idx_r = int(ddiv(r, 1.));
+    if (idx_r < 0 || idx_r >= n_sample) continue;
+    bool any = false;
+    for (int q = 0; q < bins.nbins; ++q)
+      any |= (bins.smin[q] <= idx_r && idx_r < bins.smax[q]);
+    if (!any) continue;
+    cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
+    v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
+             reduced_ylm(ell_b, m_b, rx, ry, rz));
+    for (int q = 0; q < bins.nbins; ++q) {
+      if (bins.smin[q] <= idx_r && idx_r < bins.smax[q]) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(s_n + q), 1ull);
+        atomicAdd(s_r + q, r);
+        atomicAdd(s_xi + 2 * q, v.re);
+        atomicAdd(s_xi + 2 * q + 1, v.im);
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < bins.nbins; q += blockDim.x) {
+    if (s_n[q] == 0) continue;
+    atomicAdd(reinterpret_cast<unsigned long long*>(npairs + q),
+              (unsigned long long)s_n[q]);
+    atomicAdd(rsum + q, s_r[q]);
+    atomicAdd(xi + 2 * q, s_xi[2 * q]);
+    atomicAdd(xi + 2 * q + 1, s_xi[2 * q + 1]);
+  }
+}
+
+}  // namespace
+
+template <class Real>
+void launch_reduce_pairs(Context& ctx, int64_t ncell,
+                         const typename CplxOf<Real>::type* G,
+                         const typename CplxOf<Real>::type* Fa,
+                         const typename CplxOf<Real>::type* Fb,
+                         const int* pa, const int* pb, int npairs,
+                         double* out) {
+  if (npairs <= 0) return;
+  const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
+  dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
+  reduce_pairs_kernel<Real><<<grid, 256, 0, ctx.stream>>>(ncell, G, Fa, Fb,
+                                                          pa, pb, npairs, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
+                        const Real* xi_im, int ell_a, int m_a, int ell_b,
+                        int m_b, double* hist) {
+  radial_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+      g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, hist);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
+                             const double* hist, const SplineTable& sja,
+                             const SplineTable& sjb, const double* ka,
+                             const double* kb, int npairs, double* out) {
+  if (npairs <= 0) return;
+  PairBesselArgs a{sja, sjb, ka, kb};
+  dim3 grid(grid_for(nkeys, 256, 64), npairs);
+  pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(nkeys, g.dr[0], hist,
+                                                        a, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,
+                               const Real* xi_im, int ell_a, int m_a,
+                               int ell_b, int m_b, const SplineTable& sja,
+                               const SplineTable& sjb, const double* ka,
+                               const double* kb, int npairs, double* out) {
+  if (npairs <= 0) return;
+  PairBesselArgs a{sja, sjb, ka, kb};
+  dim3 grid(grid_for(g.nmesh, 256, 152 * 4),
+            (npairs + kBesselChunk - 1) / kBesselChunk);
+  pair_bessel_direct_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
+      g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, a, npairs, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
+                                const Real* xi_im, int ell_a, int m_a,
+                                int ell_b, int m_b, const BinsDev& bins,
+                                long long* npairs, double* rsum, double* xi) {
+  const size_t smem = bins.nbins * (3 * sizeof(double) + sizeof(long long));
+  shotnoise_3pcf_kernel<Real><<<grid_for(g.nmesh, 256), 256, smem,
+                                ctx.stream>>>(g, xi_re, xi_im, ell_a, m_a,
+                                              ell_b, m_b, bins, npairs, rsum,
+                                              xi);
+  TRVG_LAUNCHED(ctx);
+}
+
+#define TRVG_INST(R)                                                          \
+  template void launch_reduce_pairs<R>(Context&, int64_t,                     \
+                                       const CplxOf<R>::type*,                \
+                                       const CplxOf<R>::type*,                \
+                                       const CplxOf<R>::type*, const int*,    \
+                                       const int*, int, double*);             \
+  template void launch_radial_hist<R>(Context&, const Geom&, const R*,        \
+                                      const R*, int, int, int, int, double*); \
+  template void launch_pair_bessel_direct<R>(                                 \
+      Context&, const Geom&, const R*, const R*, int, int, int, int,          \
+      const SplineTable&, const SplineTable&, const double*, const double*,   \
+      int, double*);                                                          \
+  template void launch_shotnoise_3pcf_bins<R>(                                \
+      Context&, const Geom&, const R*, const R*, int, int, int, int,          \
+      const BinsDev&, long long*, double*, double*);
+TRVG_INST(float)
+TRVG_INST(double)
+#undef TRVG_INST
+
+}  // namespace trvg

@@ -1,0 +1,512 @@
+// Fourier-space kernels: mode counting, shell-filtered field spectra on the
+// evaluation grid, fine-binned two-point statistics and the shot-noise
+// two-point field.
+//
+// Spectra of real meshes are stored as cuFFT half spectra
+// (n0 x n1 x (n2/2 + 1)); a complex field is the pair (re, im) of the half
+// spectra of its real and imaginary part meshes, read back at any full-grid
+// index through Hermitian symmetry.  Interlacing (field.cpp:1615-1653) is
+// applied on read from the raw main and shadow spectra.
+#include "kernels.h"
+
+namespace trvg {
+
+namespace {
+
+template <class C>
+__device__ __forceinline__ cd ld(const C* p, int64_t i) {
+  const C v = p[i];
+  return cd{double(v.x), double(v.y)};
+}
+
+template <class C>
+__device__ __forceinline__ cd half_value(const C* h, const Geom& g, int i,
+                                         int j, int k) {
+  if (k < g.nzh) return ld(h, (int64_t(i) * g.n[1] + j) * g.nzh + k);
+  const int ii = (i == 0) ? 0 : g.n[0] - i;
+  const int jj = (j == 0) ? 0 : g.n[1] - j;
+  const int kk = g.n[2] - k;
+  return conjg(ld(h, (int64_t(ii) * g.n[1] + jj) * g.nzh + kk));
+}
+
+template <class C>
+__device__ __forceinline__ cd pair_value(const C* re, const C* im,
+                                         const Geom& g, int i, int j, int k) {
+  cd v = half_value(re, g, i, j, k);
+  if (im != nullptr) {
+    const cd b = half_value(im, g, i, j, k);
+    v = v + cd{-b.im, b.re};  // v + i b
+  }
+  return v;
+}
+
+// Value of field `f` at full-grid index (i, j, k).
+template <class Real>
+__device__ __forceinline__ cd field_value(const FieldSpec<Real>& f,
+                                          const Geom& g, int i, int j,
+                                          int k) {
+  if (f.k0_set && i == 0 && j == 0 && k == 0) return f.k0;
+  cd v = pair_value(f.re, f.im, g, i, j, k);
+  if (f.re_s != nullptr) {
+    const cd vs = pair_value(f.re_s, f.im_s, g, i, j, k);
+    const double mx = (i < g.n[0] / 2) ? double(i) / g.n[0]
+                                       : double(i) / g.n[0] - 1;
+    const double my = (j < g.n[1] / 2) ? double(j) / g.n[1]
+                                       : double(j) / g.n[1] - 1;
+    const double mz = (k < g.n[2] / 2) ? double(k) / g.n[2]
+                                       : double(k) / g.n[2] - 1;
+    const double arg = kPi * (mx + my + mz);
+    double sa, ca;
+    sincos(arg, &sa, &ca);
+    v = cd{(v.re + (ca * vs.re - sa * vs.im)) / 2.,
+           (v.im + (sa * vs.re + ca * vs.im)) / 2.};
+  }
+  return v;
+}
+
+// W(k)^order (field.cpp:1114-1146).
+__device__ __forceinline__ double window_pow(const AxisTablesDev& ax, int i,
+                                             int j, int k) {
+  const double wk = ax.t.sinc[0][i] * ax.t.sinc[1][j] * ax.t.sinc[2][k];
+  double r = 1.;
+  for (int q = 0; q < ax.order; ++q) r *= wk;
+  return r;
+}
+
+// Shot-noise aliasing C_1(k) (field.cpp:3463-3509).
+__device__ __forceinline__ double alias_sn(const AxisTablesDev& ax, int i,
+                                           int j, int k) {
+  if (!ax.interlace)
+    return ax.t.alias[0][i] * ax.t.alias[1][j] * ax.t.alias[2][k];
+  const double ux = ax.t.u[0][i], uy = ax.t.u[1][j], uz = ax.t.u[2][k];
+  const double uhalf = sqrt(ux * ux + uy * uy + uz * uz) / 2.;
+  const double sh = sin(uhalf), ch = cos(uhalf);
+  const double s2h = sh * sh, c2h = ch * ch;
+  double cc = 1.;
+  for (int q = 0; q < ax.order; ++q) cc *= c2h;
+  double cs = 1.;
+  if (ax.order == 2) {
+    cs = 1. - 2. / 3. * s2h;
+  } else if (ax.order == 3) {
+    cs = 1. - s2h + 2. / 15. * s2h * s2h;
+  } else if (ax.order == 4) {
+    cs = 1. - 4. / 3. * s2h + 2. / 5. * s2h * s2h -
+         4. / 315. * s2h * s2h * s2h;
+  }
+  return cc * cs;
+}
+
+__device__ __forceinline__ int wrap(int s, int n) { return s < 0 ? s + n : s; }
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+int grid_for(int64_t work, int block, int64_t cap = 152 * 16) {
+  int64_t g = (work + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return int(g);
+}
+
+// ---------------------------------------------------------------------------
+
+__global__ void count_modes_kernel(Geom g, Cube cube, BinsDev bins,
+                                   long long* nmodes, double* ksum) {
+  extern __shared__ unsigned char smem_raw[];
+  double* s_k = reinterpret_cast<double*>(smem_raw);
+  long long* s_n = reinterpret_cast<long long*>(s_k + bins.nbins);
+  for (int b = threadIdx.x; b < bins.nbins; b += blockDim.x) {
+    s_k[b] = 0.;
+    s_n[b] = 0;
+  }
+  __syncthreads();
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < cube.count; t += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(t % cube.ext[2]);
+    const int b = int((t / cube.ext[2]) % cube.ext[1]);
+    const int a = int(t / (int64_t(cube.ext[2]) * cube.ext[1]));
+    const int sx = cube.dense[0] ? shift_index(a, g.n[0]) : a - cube.K[0];
+    const int sy = cube.dense[1] ? shift_index(b, g.n[1]) : b - cube.K[1];
+    const int sz = cube.dense[2] ? shift_index(c, g.n[2]) : c - cube.K[2];
+    const double k = vec3_mag(dmul(double(sx), g.dk[0]),
+                              dmul(double(sy), g.dk[1]),
+                              dmul(double(sz), g.dk[2]));
+    for (int q = 0; q < bins.nbins; ++q) {
+      if (bins.lo[q] <= k && k < bins.hi[q]) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(s_n + q), 1ull);
+        atomicAdd(s_k + q, k);
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < bins.nbins; q += blockDim.x) {
+    if (s_n[q] != 0) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(nmodes + q),
+                (unsigned long long)s_n[q]);
+      atomicAdd(ksum + q, s_k[q]);
+    }
+  }
+}
+
+// G on the evaluation grid: dn(k) / W(k) / V for |s| <= Kg on pruned axes,
+// every mode on dense axes (G_LM: threept.cpp:1665-1670, field.cpp:1657-1785).
+template <class Real>
+__global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
+                               int Kg1, int Kg2, FieldSpec<Real> f,
+                               AxisTablesDev ax,
+                               typename CplxOf<Real>::type* out) {
+  using C = typename CplxOf<Real>::type;
+  const int64_t count = int64_t(M0) * M1 * M2;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(t % M2);
+    const int b = int((t / M2) % M1);
+    const int a = int(t / (int64_t(M2) * M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
+                    (M1 == g.n[1] || abs(sy) <= Kg1) &&
+                    (M2 == g.n[2] || abs(sz) <= Kg2);
+    C o;
+    o.x = 0;
+    o.y = 0;
+    if (in) {
+      const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                k = wrap(sz, g.n[2]);
+      const cd v = field_value(f, g, i, j, k);
+      const double w = window_pow(ax, i, j, k);
+      const cd r = cdivr(cdivr(v, w), g.vol);
+      o.x = Real(r.re);
+      o.y = Real(r.im);
+    }
+    out[t] = o;
+  }
+}
+
+// Shell-filtered spectra y_lm(k) f(k) / W(k), one per bin, on the
+// evaluation grid (field.cpp:1812-1847).  The 1/nmodes of the reference is
+// applied to the reduced sums instead of the fields.
+template <class Real>
+__global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
+                               int K2, FieldSpec<Real> f, AxisTablesDev ax,
+                               int ell, int m, const double* lo,
+                               const double* hi, int nb, double hi_max,
+                               typename CplxOf<Real>::type* out) {
+  using C = typename CplxOf<Real>::type;
+  const int64_t count = int64_t(M0) * M1 * M2;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(t % M2);
+    const int b = int((t / M2) % M1);
+    const int a = int(t / (int64_t(M2) * M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= K0) &&
+                    (M1 == g.n[1] || abs(sy) <= K1) &&
+                    (M2 == g.n[2] || abs(sz) <= K2);
+    double k = -1.;
+    cd val = {0., 0.};
+    if (in) {
+      const double kx = dmul(double(sx), g.dk[0]);
+      const double ky = dmul(double(sy), g.dk[1]);
+      const double kz = dmul(double(sz), g.dk[2]);
+      k = vec3_mag(kx, ky, kz);
+      if (k < hi_max) {
+        const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                  kk = wrap(sz, g.n[2]);
+        const cd v = field_value(f, g, i, j, kk);
+        const double w = window_pow(ax, i, j, kk);
+        const cd y = reduced_ylm(ell, m, kx, ky, kz);
+        val = y * cdivr(v, w);
+      }
+    }
+    for (int q = 0; q < nb; ++q) {
+      C o;
+      const bool sel = in && (lo[q] <= k) && (k < hi[q]);
+      o.x = sel ? Real(val.re) : Real(0);
+      o.y = sel ? Real(val.im) : Real(0);
+      out[int64_t(q) * count + t] = o;
+    }
+  }
+}
+
+struct SjlArgs {
+  SplineTable sj;
+  const double* radii;
+  int nb;
+};
+
+// j_l(k r) y_lm(k) f(k) / W(k) / V on the full mesh, one per radius
+// (field.cpp:1908-2010).
+template <class Real>
+__global__ void build_F_sjl_kernel(Geom g, FieldSpec<Real> f,
+                                   AxisTablesDev ax, int ell, int m,
+                                   SjlArgs sa,
+                                   typename CplxOf<Real>::type* out) {
+  using C = typename CplxOf<Real>::type;
+  const int64_t count = g.nmesh;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int kk = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const double kx = dmul(double(shift_index(i, g.n[0])), g.dk[0]);
+    const double ky = dmul(double(shift_index(j, g.n[1])), g.dk[1]);
+    const double kz = dmul(double(shift_index(kk, g.n[2])), g.dk[2]);
+    const double k = vec3_mag(kx, ky, kz);
+    const cd v = field_value(f, g, i, j, kk);
+    const double w = window_pow(ax, i, j, kk);
+    const cd y = reduced_ylm(ell, m, kx, ky, kz);
+    const cd val = y * cdivr(v, w);
+    for (int q = 0; q < sa.nb; ++q) {
+      const double jl = spline_eval(sa.sj, k * sa.radii[q]);
+      C o;
+      o.x = Real(jl * val.re / g.vol);
+      o.y = Real(jl * val.im / g.vol);
+      out[int64_t(q) * count + t] = o;
+    }
+  }
+}
+
+// Fine-binned two-point statistics (field.cpp:2586-2702).  Each mode goes
+// to fine sample int(k / 1e-5); bin b collects samples i with
+// lo_b <= i * 1e-5 < hi_b (precomputed as [smin_b, smax_b)).
+template <class Real>
+__global__ void twopt_stats_kernel(Geom g, Cube cube, FieldSpec<Real> fa,
+                                   FieldSpec<Real> fb, cd shot, int ell,
+                                   int m, AxisTablesDev ax, BinsDev bins,
+                                   long long* nmodes, double* ksum,
+                                   double* pk, double* sn) {
+  extern __shared__ unsigned char smem_raw[];
+  double* s_k = reinterpret_cast<double*>(smem_raw);
+  double* s_pk = s_k + bins.nbins;          // 2 * nbins
+  double* s_sn = s_pk + 2 * bins.nbins;     // 2 * nbins
+  long long* s_n = reinterpret_cast<long long*>(s_sn + 2 * bins.nbins);
+  for (int q = threadIdx.x; q < bins.nbins; q += blockDim.x) {
+    s_k[q] = 0.;
+    s_pk[2 * q] = s_pk[2 * q + 1] = 0.;
+    s_sn[2 * q] = s_sn[2 * q + 1] = 0.;
+    s_n[q] = 0;
+  }
+  __syncthreads();
+  const int n_sample = 1000000;
+  const double dk_sample = 1.e-5;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < cube.count; t += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(t % cube.ext[2]);
+    const int b = int((t / cube.ext[2]) % cube.ext[1]);
+    const int a = int(t / (int64_t(cube.ext[2]) * cube.ext[1]));
+    const int sx = cube.dense[0] ? shift_index(a, g.n[0]) : a - cube.K[0];
+    const int sy = cube.dense[1] ? shift_index(b, g.n[1]) : b - cube.K[1];
+    const int sz = cube.dense[2] ? shift_index(c, g.n[2]) : c - cube.K[2];
+    const double kx = dmul(double(sx), g.dk[0]);
+    const double ky = dmul(double(sy), g.dk[1]);
+    const double kz = dmul(double(sz), g.dk[2]);
+    const double k = vec3_mag(kx, ky, kz);
+    const int idx_k = int(ddiv(k, dk_sample));
+    if (idx_k < 0 || idx_k >= n_sample) continue;
+    bool any = false;
+    for (int q = 0; q < bins.nbins; ++q)
+      any |= (bins.smin[q] <= idx_k && idx_k < bins.smax[q]);
+    if (!any) continue;
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              kk = wrap(sz, g.n[2]);
+    const cd va = field_value(fa, g, i, j, kk);
+    const cd vb = field_value(fb, g, i, j, kk);
+    const double al = alias_sn(ax, i, j, kk);
+    double win_pk, win_sn;
+    if (ax.interlace) {
+      const double w = window_pow(ax, i, j, kk);
+      win_pk = w * w;
+      win_sn = win_pk;
+    } else {
+      win_pk = al;
+      win_sn = al;
+    }
+    const cd y = reduced_ylm(ell, m, kx, ky, kz);
+    const cd pkm = cdivr(va * conjg(vb), win_pk) * y;
+    const cd snm = cdivr(al * shot, win_sn) * y;
+    for (int q = 0; q < bins.nbins; ++q) {
+      if (bins.smin[q] <= idx_k && idx_k < bins.smax[q]) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(s_n + q), 1ull);
+        atomicAdd(s_k + q, k);
+        atomicAdd(s_pk + 2 * q, pkm.re);
+        atomicAdd(s_pk + 2 * q + 1, pkm.im);
+        atomicAdd(s_sn + 2 * q, snm.re);
+        atomicAdd(s_sn + 2 * q + 1, snm.im);
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < bins.nbins; q += blockDim.x) {
+    if (s_n[q] == 0) continue;
+    atomicAdd(reinterpret_cast<unsigned long long*>(nmodes + q),
+              (unsigned long long)s_n[q]);
+    atomicAdd(ksum + q, s_k[q]);
+    atomicAdd(pk + 2 * q, s_pk[2 * q]);
+    atomicAdd(pk + 2 * q + 1, s_pk[2 * q + 1]);
+    atomicAdd(sn + 2 * q, s_sn[2 * q]);
+    atomicAdd(sn + 2 * q + 1, s_sn[2 * q + 1]);
+  }
+}
+
+// Shot-noise two-point field spectrum (fa fb^* / win_pk - S C_1 / win_sn) / V
+// (field.cpp:3273-3298) on the half-spectrum grid.  When `out_im` is given
+// the spectrum is split into its Hermitian parts so that both halves
+// transform with C2R: P = H_re + i H_im.
+template <class Real>
+__device__ __forceinline__ cd twopt_mode(const Geom& g, const FieldSpec<Real>& fa,
+                                         const FieldSpec<Real>& fb, cd shot,
+                                         const AxisTablesDev& ax, int i,
+                                         int j, int k) {
+  const cd va = field_value(fa, g, i, j, k);
+  const cd vb = field_value(fb, g, i, j, k);
+  const double al = alias_sn(ax, i, j, k);
+  double win_pk, win_sn;
+  if (ax.interlace) {
+    const double w = window_pow(ax, i, j, k);
+    win_pk = w * w;
+    win_sn = win_pk;
+  } else {
+    win_pk = al;
+    win_sn = al;
+  }
+  const cd p = cdivr(va * conjg(vb), win_pk) - cdivr(al * shot, win_sn);
+  return cdivr(p, g.vol);
+}
+
+template <class Real>
+__global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
+                                   FieldSpec<Real> fb, cd shot,
+                                   AxisTablesDev ax,
+                                   typename CplxOf<Real>::type* out_re,
+                                   typename CplxOf<Real>::type* out_im) {
+  using C = typename CplxOf<Real>::type;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nhalf; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.nzh);
+    const int j = int((t / g.nzh) % g.n[1]);
+    const int i = int(t / (int64_t(g.nzh) * g.n[1]));
+    const cd p = twopt_mode(g, fa, fb, shot, ax, i, j, k);
+    C o;
+    if (out_im == nullptr) {
+      o.x = Real(p.re);
+      o.y = Real(p.im);
+      out_re[t] = o;
+    } else {
+      const int ii = (i == 0) ? 0 : g.n[0] - i;
+      const int jj = (j == 0) ? 0 : g.n[1] - j;
+      const int kk = (k == 0) ? 0 : g.n[2] - k;
+      const cd q = conjg(twopt_mode(g, fa, fb, shot, ax, ii, jj, kk));
+      const cd s = p + q, d = p - q;
+      o.x = Real(s.re / 2.);
+      o.y = Real(s.im / 2.);
+      out_re[t] = o;
+      C oi;
+      oi.x = Real(d.im / 2.);
+      oi.y = Real(-d.re / 2.);
+      out_im[t] = oi;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
+                        const BinsDev& bins, long long* nmodes,
+                        double* ksum) {
+  const size_t smem = bins.nbins * (sizeof(double) + sizeof(long long));
+  count_modes_kernel<<<grid_for(cube.count, 256), 256, smem, ctx.stream>>>(
+      g, cube, bins, nmodes, ksum);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_build_G(Context& ctx, const Geom& g, const int M[3],
+                    const int Kg[3], const FieldSpec<Real>& f,
+                    const AxisTablesDev& ax,
+                    typename CplxOf<Real>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  build_G_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, ax, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_build_F(Context& ctx, const Geom& g, const int M[3],
+                    const int K[3], const FieldSpec<Real>& f,
+                    const AxisTablesDev& ax, int ell, int m,
+                    const double* lo, const double* hi, int nb,
+                    double hi_max, typename CplxOf<Real>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  build_F_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
+      hi_max, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
+                        const AxisTablesDev& ax, int ell, int m,
+                        const SplineTable& sj, const double* radii, int nb,
+                        typename CplxOf<Real>::type* out) {
+  SjlArgs sa{sj, radii, nb};
+  build_F_sjl_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+      g, f, ax, ell, m, sa, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
+                        const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                        cd shot, int ell, int m, const AxisTablesDev& ax,
+                        const BinsDev& bins, long long* nmodes, double* ksum,
+                        double* pk, double* sn) {
+  const size_t smem = bins.nbins * (5 * sizeof(double) + sizeof(long long));
+  twopt_stats_kernel<Real><<<grid_for(cube.count, 256), 256, smem,
+                             ctx.stream>>>(g, cube, fa, fb, shot, ell, m, ax,
+                                           bins, nmodes, ksum, pk, sn);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
+                        const FieldSpec<Real>& fb, cd shot,
+                        const AxisTablesDev& ax,
+                        typename CplxOf<Real>::type* out_re,
+                        typename CplxOf<Real>::type* out_im) {
+  twopt_field_kernel<Real><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+      g, fa, fb, shot, ax, out_re, out_im);
+  TRVG_LAUNCHED(ctx);
+}
+
+#define TRVG_INST(R)                                                         \
+  template void launch_build_G<R>(Context&, const Geom&, const int*,         \
+                                  const int*, const FieldSpec<R>&,           \
+                                  const AxisTablesDev&, CplxOf<R>::type*);   \
+  template void launch_build_F<R>(Context&, const Geom&, const int*,         \
+                                  const int*, const FieldSpec<R>&,           \
+                                  const AxisTablesDev&, int, int,            \
+                                  const double*, const double*, int, double, \
+                                  CplxOf<R>::type*);                         \
+  template void launch_build_F_sjl<R>(Context&, const Geom&,                 \
+                                      const FieldSpec<R>&,                   \
+                                      const AxisTablesDev&, int, int,        \
+                                      const SplineTable&, const double*,     \
+                                      int, CplxOf<R>::type*);                \
+  template void launch_twopt_stats<R>(                                       \
+      Context&, const Geom&, const Cube&, const FieldSpec<R>&,               \
+      const FieldSpec<R>&, cd, int, int, const AxisTablesDev&,               \
+      const BinsDev&, long long*, double*, double*, double*);                \
+  template void launch_twopt_field<R>(Context&, const Geom&,                 \
+                                      const FieldSpec<R>&,                   \
+                                      const FieldSpec<R>&, cd,               \
+                                      const AxisTablesDev&, CplxOf<R>::type*,\
+                                      CplxOf<R>::type*);
+TRVG_INST(float)
+TRVG_INST(double)
+#undef TRVG_INST
+
+}  // namespace trvg

@@ -1,0 +1,259 @@
+"""Three-point clustering statistics (mirrors ``triumvirate.threept``,
+threept.py:1-1723): bispectrum and 3PCF from periodic-box ('sim') and
+survey-type catalogues, computed on the GPU through ``libtrvg.so``."""
+from __future__ import annotations
+
+import warnings
+from pathlib import Path
+
+import numpy as np
+
+from . import _engine, _lib
+from .dataobjs import Binning
+from .parameters import (ParameterSet, _as_dict,
+                         _modify_measurement_parameters,
+                         _modify_sampling_parameters, _set_ngrid_from_cutoff,
+                         fetch_paramset_template)
+
+
+def _amalgamate_parameters(paramset=None, params_sampling=None, degrees=None,
+                           wa_orders=None, binning=None, form=None,
+                           idx_bin=None, **type_kwargs):
+    """Parameter set with sampling / measurement overrides
+    (threept.py:53-172)."""
+    if paramset is None and params_sampling is None:
+        raise ValueError(
+            "Either `paramset` or `sampling_params` must be provided.")
+    if paramset is None and None in [degrees, binning, form]:
+        raise ValueError("`degrees`, `binning` and `form` must be provided "
+                         "when `paramset` is None.")
+    if paramset is None and form in ['row', 'off-diag'] and idx_bin is None:
+        raise ValueError("`idx_bin` must be provided when `paramset` is None "
+                         "and `form` is 'row' or 'off-diag'.")
+    if paramset is None:
+        pdict, defaults = fetch_paramset_template('dict', ret_defaults=True)
+    else:
+        pdict, defaults = _as_dict(paramset), None
+    if params_sampling is not None:
+        pdict, defaults = _modify_sampling_parameters(
+            pdict, params_sampling, params_default=defaults,
+            ret_defaults=True)
+    measure = {}
+    if degrees is not None:
+        ell1, ell2, ELL = degrees
+        measure.update({'ell1': int(ell1), 'ell2': int(ell2),
+                        'ELL': int(ELL)})
+    if wa_orders is not None:
+        i_wa, j_wa = wa_orders
+        measure.update({'i_wa': int(i_wa), 'j_wa': int(j_wa)})
+    if binning is not None:
+        measure.update({'bin_min': binning.bin_min,
+                        'bin_max': binning.bin_max,
+                        'num_bins': binning.num_bins})
+    if form is not None:
+        measure['form'] = form
+    if idx_bin is not None:
+        measure['idx_bin'] = idx_bin
+    pdict, defaults = _modify_measurement_parameters(
+        pdict, measure, params_default=defaults, ret_defaults=True)
+    pdict.update(type_kwargs)
+    if defaults:
+        warnings.warn("The following parameter default values are "
+                      f"unchanged: {defaults}. Not all parameters are "
+                      "necessarily used.", stacklevel=3)
+    return ParameterSet(param_dict=pdict)
+
+
+def _boxsize(paramset):
+    return [float(paramset['boxsize'][ax]) for ax in ['x', 'y', 'z']]
+
+
+def _norm_factor(paramset, ctx, params_c, cat_c, nz, ws, wc, alpha, order):
+    """Particle / mesh normalisation (threept.cpp:96-149,
+    twopt.cpp:56-130)."""
+    conv = paramset['norm_convention']
+    if conv == 'none':
+        return 1.
+    if conv == 'particle':
+        if order == 3:
+            norm = float(np.sum(ws * nz ** 2 * wc ** 3))
+        else:
+            norm = float(np.sum(ws * nz * wc ** 2))
+        if norm == 0.:
+            raise _lib.InvalidDataError(
+                "Particle 'nz' values appear to be all zeros. Check the "
+                "input catalogue contains valid 'nz' field.")
+        return 1. / (alpha * norm)
+    if conv == 'mesh':
+        return _engine.grid_powlaw_norm(ctx, params_c, cat_c, order) \
+            / alpha ** order
+    raise ValueError(f"Unsupported normalisation convention: {conv}.")
+
+
+def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
+                                params_sampling=None, degrees=None,
+                                binning=None, form=None, idx_bin=None,
+                                save=False, logger=None, device=None):
+    """Periodic-box three-point statistics (threept.py:1312-1621)."""
+    stat = 'bispec' if kind == 'bispec' else '3pcf'
+    paramset = _amalgamate_parameters(
+        paramset=paramset, params_sampling=params_sampling, degrees=degrees,
+        binning=binning, form=form, idx_bin=idx_bin,
+        catalogue_type='sim', statistic_type=stat)
+    if binning is None:
+        binning = Binning.from_parameter_set(paramset)
+    if None in paramset['boxsize'].values():
+        paramset['boxsize'] = {
+            ax: (catalogue_data.bounds[ax][1] - catalogue_data.bounds[ax][0])
+            * paramset['expand'] for ax in ['x', 'y', 'z']}
+    if None in paramset['ngrid'].values():
+        pd = _as_dict(paramset)
+        _set_ngrid_from_cutoff(pd)
+        paramset['ngrid'] = pd['ngrid']
+    catalogue_data.periodise(_boxsize(paramset))
+    if not catalogue_data['nz'].any():
+        catalogue_data.compute_mean_density(boxsize=_boxsize(paramset))
+
+    ctx = _lib.default_context(device)
+    params_c = _engine.make_params(paramset, '3pt')
+    x, y, z, w = catalogue_data._columns()
+    cat = _engine.HostCatalogue(x, y, z, w)
+    norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data['nz'],
+                        catalogue_data['ws'], catalogue_data['wc'], 1., 3)
+    fn = ('trvg_compute_bispec_in_gpp_box' if kind == 'bispec'
+          else 'trvg_compute_3pcf_in_gpp_box')
+    results = _engine.call_threept(
+        fn, ctx, params_c, cat.c, binning, norm, kind,
+        shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
+    if save:
+        _save(results, paramset, save, kind, norm)
+    return results
+
+
+def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
+                                   los_data=None, los_rand=None,
+                                   paramset=None, params_sampling=None,
+                                   degrees=None, binning=None, form=None,
+                                   idx_bin=None, save=False, logger=None,
+                                   device=None):
+    """Survey-type three-point statistics (threept.py:384-740)."""
+    stat = 'bispec' if kind == 'bispec' else '3pcf'
+    paramset = _amalgamate_parameters(
+        paramset=paramset, params_sampling=params_sampling, degrees=degrees,
+        binning=binning, form=form, idx_bin=idx_bin,
+        catalogue_type='survey', statistic_type=stat)
+    if binning is None:
+        binning = Binning.from_parameter_set(paramset)
+    if los_data is None:
+        los_data = catalogue_data.compute_los()
+    if los_rand is None:
+        los_rand = catalogue_rand.compute_los()
+    los_data = np.ascontiguousarray(los_data)
+    los_rand = np.ascontiguousarray(los_rand)
+    if None in paramset['boxsize'].values():
+        paramset['boxsize'] = {
+            ax: (catalogue_rand.bounds[ax][1] - catalogue_rand.bounds[ax][0])
+            * paramset['expand'] for ax in ['x', 'y', 'z']}
+    if None in paramset['ngrid'].values():
+        pd = _as_dict(paramset)
+        _set_ngrid_from_cutoff(pd)
+        paramset['ngrid'] = pd['ngrid']
+    if paramset['alignment'] == 'centre':
+        catalogue_data.centre(_boxsize(paramset), catalogue_ref=catalogue_rand)
+    if paramset['alignment'] == 'pad':
+        if paramset['padscale'] == 'box':
+            kw = {'boxsize_pad': paramset['padfactor']}
+        else:
+            kw = {'ngrid': [paramset['ngrid'][ax] for ax in 'xyz'],
+                  'ngrid_pad': paramset['padfactor']}
+        catalogue_data.pad(_boxsize(paramset), catalogue_ref=catalogue_rand,
+                           **kw)
+    ctx = _lib.default_context(device)
+    params_c = _engine.make_params(paramset, '3pt')
+    alpha = catalogue_data.wstotal / catalogue_rand.wstotal
+    xd, yd, zd, wd = catalogue_data._columns()
+    xr, yr, zr, wr = catalogue_rand._columns()
+    dcat = _engine.HostCatalogue(xd, yd, zd, wd, los_data)
+    rcat = _engine.HostCatalogue(xr, yr, zr, wr, los_rand)
+    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
+                        catalogue_rand['ws'], catalogue_rand['wc'], alpha, 3)
+    fn = 'trvg_compute_bispec' if kind == 'bispec' else 'trvg_compute_3pcf'
+    results = _engine.call_threept(
+        fn, ctx, params_c, dcat.c, binning, norm, kind, rand_c=rcat.c,
+        alpha=alpha, shape=paramset['shape'],
+        idx_bin=paramset.get('idx_bin') or 0)
+    if save:
+        _save(results, paramset, save, kind, norm)
+    return results
+
+
+def _save(results, paramset, save, kind, norm):
+    """Measurement file in the reference's layout (threept.py:707-735)."""
+    odir = paramset['directories'].get('measurements') or ""
+    tag = paramset['tags'].get('output') or ""
+    deg = paramset['degrees']
+    name = (f"{'bk' if kind == 'bispec' else 'zeta'}"
+            f"{deg['ell1']}{deg['ell2']}{deg['ELL']}_{paramset['form']}{tag}")
+    path = Path(odir, name)
+    header = f"Normalisation factor: {norm:.9e} " \
+             f"({paramset['norm_convention']})"
+    if str(save).lower() == '.txt':
+        keys = list(results.keys())
+        raw, shot = results[keys[6]], results[keys[7]]
+        tab = np.column_stack([results[k] for k in keys[:6]] +
+                              [raw.real, raw.imag, shot.real, shot.imag])
+        fmt = '\t'.join((['%.9e'] * 2 + ['%10d']) * 2 + ['% .9e'] * 4)
+        np.savetxt(path.with_suffix('.txt'), tab, fmt=fmt, header=header,
+                   delimiter='\t')
+    elif str(save).lower().endswith('.npz'):
+        np.savez(path.with_suffix('.npz'), header=header, **results)
+    else:
+        raise ValueError(f"Unrecognised save format for measurements: {save}.")
+
+
+def compute_bispec(catalogue_data, catalogue_rand, los_data=None,
+                   los_rand=None, degrees=None, binning=None, form=None,
+                   idx_bin=None, sampling_params=None, paramset=None,
+                   save=False, logger=None, device=None):
+    """Bispectrum from survey-type catalogues in the local plane-parallel
+    approximation (threept.py:743-865)."""
+    return _compute_3pt_stats_survey_like(
+        'bispec', catalogue_data, catalogue_rand, los_data=los_data,
+        los_rand=los_rand, paramset=paramset, params_sampling=sampling_params,
+        degrees=degrees, binning=binning, form=form, idx_bin=idx_bin,
+        save=save, logger=logger, device=device)
+
+
+def compute_3pcf(catalogue_data, catalogue_rand, los_data=None,
+                 los_rand=None, degrees=None, binning=None, form=None,
+                 idx_bin=None, sampling_params=None, paramset=None,
+                 save=False, logger=None, device=None):
+    """3PCF from survey-type catalogues (threept.py:868-990)."""
+    return _compute_3pt_stats_survey_like(
+        '3pcf', catalogue_data, catalogue_rand, los_data=los_data,
+        los_rand=los_rand, paramset=paramset, params_sampling=sampling_params,
+        degrees=degrees, binning=binning, form=form, idx_bin=idx_bin,
+        save=save, logger=logger, device=device)
+
+
+def compute_bispec_in_gpp_box(catalogue_data, degrees=None, binning=None,
+                              form=None, idx_bin=None, sampling_params=None,
+                              paramset=None, save=False, logger=None,
+                              device=None):
+    """Bispectrum from a periodic-box catalogue in the global plane-parallel
+    approximation (threept.py:1624-1723)."""
+    return _compute_3pt_stats_sim_like(
+        'bispec', catalogue_data, paramset=paramset,
+        params_sampling=sampling_params, degrees=degrees, binning=binning,
+        form=form, idx_bin=idx_bin, save=save, logger=logger, device=device)
+
+
+def compute_3pcf_in_gpp_box(catalogue_data, degrees=None, binning=None,
+                            form=None, idx_bin=None, sampling_params=None,
+                            paramset=None, save=False, logger=None,
+                            device=None):
+    """3PCF from a periodic-box catalogue (threept.py:1726-1830)."""
+    return _compute_3pt_stats_sim_like(
+        '3pcf', catalogue_data, paramset=paramset,
+        params_sampling=sampling_params, degrees=degrees, binning=binning,
+        form=form, idx_bin=idx_bin, save=save, logger=logger, device=device)
