@@ -1,0 +1,441 @@
+"""Benchmark of the periodic-box bispectrum on GB300.
+
+Workload (the headline metric): ``compute_bispec_in_gpp_box``, B_000 diag,
+20 linear bins 0.005-0.205 h/Mpc, 4 194 304 particles uniform in a
+1000 Mpc/h box (numpy ``default_rng(42)``, float64), unit weights,
+nz = N/V, 512^3 mesh, TSC, no interlacing (three-point statistics force it
+off), particle normalisation.  One step = one estimate.
+
+Lines printed by rank 0 (one JSON object):
+  value  -- s/estimate of the FP32-mixed path with particles resident in
+            device memory (CUDA events on the stream the library runs on);
+  e2e    -- the same through the C ABI with pinned host particle arrays,
+            host->device copies inside the timed region;
+  fp64   -- the FP64 path on the same inputs, its time and the FP32-mixed
+            error against it;
+  roofline, cpu_baseline, clocks, gpu_launches.
+``--impl reference`` times the CPU oracle (a numpy restatement of the
+reference algorithm) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("bispectrum s/estimate @512³, 4M pts: FP32-mixed vs FP64 on "
+          "1 GB300 @1e-5 err")
+UNIT = "s/estimate"
+FALLBACK_HBM_GBS = 6800.
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--ngrid', type=int, default=512)
+    ap.add_argument('--npart', type=int, default=4194304)
+    ap.add_argument('--boxsize', type=float, default=1000.)
+    ap.add_argument('--nbins', type=int, default=20)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--profile-only', action='store_true',
+                    help='run two estimates (for an ncu launch list)')
+    return ap.parse_args()
+
+
+def workload(args):
+    return {
+        "workload": (f"gpp B_000 diag, {args.ngrid}^3 mesh, TSC, "
+                     f"{args.npart} uniform particles, L={args.boxsize:g} "
+                     f"Mpc/h, {args.nbins} lin k-bins 0.005-0.205 h/Mpc"),
+        "ngrid": args.ngrid, "npart": args.npart, "boxsize": args.boxsize,
+        "bins": [0.005, 0.205, args.nbins], "assignment": "tsc",
+        "degrees": [0, 0, 0], "form": "diag", "norm": "particle",
+        "l2": ("inputs larger than L2 (mesh >= 512 MiB) and a 256 MiB L2 "
+               "flush before every timed step"),
+    }
+
+
+def make_particles(n, box, seed=42):
+    rng = np.random.default_rng(seed)
+    x, y, z = rng.uniform(0., box, size=(3, n))
+    # ParticleCatalogue.periodise (catalogue.py:648-676), as the Python
+    # entry point does before handing positions to the estimator.
+    out = []
+    for c in (x, y, z):
+        out.append(np.ascontiguousarray(
+            (c + box / 2. - (c.max() + c.min()) / 2.) % box))
+    return out
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed
+    region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.device),
+                 f'--query-gpu={self.QUERY}', '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_traffic.json"
+    if not f.exists():
+        return None
+    try:
+        return json.loads(f.read_text()).get(kernel)
+    except ValueError:
+        return None
+
+
+def algorithmic_bytes(kernel, args, real_bytes):
+    """Compulsory HBM bytes of one launch of `kernel` on the workload."""
+    nm = args.ngrid ** 3
+    nh = args.ngrid * args.ngrid * (args.ngrid // 2 + 1)
+    if kernel == 'assign_kernel':
+        # x, y, z read once; every mesh cell written once.
+        return 24 * args.npart + real_bytes * nm
+    if kernel == 'twopt_field_kernel':
+        # FP32 half spectrum read, FP64 half spectrum written.
+        return 2 * real_bytes * nh + 16 * nh
+    if kernel == 'radial_hist_kernel':
+        return 8 * nm          # FP64 shot-noise field read once
+    if kernel == 'cufft.r2c.mesh':
+        return real_bytes * nm + 2 * real_bytes * nh
+    if kernel == 'cufft.c2r.xi':
+        return 16 * nh + 8 * nm
+    return None
+
+
+def run_gb300(args):
+    import torch
+
+    from triumvirate_gb300 import _engine, _lib
+    from triumvirate_gb300.dataobjs import Binning
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    box, n, N = args.boxsize, args.npart, args.ngrid
+    x, y, z = make_particles(n, box, seed=42 + rank)
+    binning = Binning('fourier', 'lin', 0.005, 0.205, args.nbins)
+    nbar = n / box ** 3
+    norm = 1. / (n * nbar ** 2)        # threept.cpp:96-136, alpha = 1
+
+    ctx = _lib.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    def params(precision):
+        pd = {'boxsize': {'x': box, 'y': box, 'z': box},
+              'ngrid': {'x': N, 'y': N, 'z': N}, 'assignment_order': 3,
+              'interlace': False,
+              'degrees': {'ell1': 0, 'ell2': 0, 'ELL': 0},
+              'form': 'diag', 'shape': 'diag', 'precision': precision,
+              'verbose': 0}
+        return _engine.make_params(pd, '3pt')
+
+    p32, p64 = params('fp32mixed'), params('fp64')
+    xd, yd, zd = (torch.from_numpy(a).to(dev) for a in (x, y, z))
+    dcat = _engine.device_catalogue(n, xd.data_ptr(), yd.data_ptr(),
+                                    zd.data_ptr())
+    xh, yh, zh = (torch.from_numpy(a).pin_memory() for a in (x, y, z))
+    hcat = _engine.device_catalogue(n, xh.data_ptr(), yh.data_ptr(),
+                                    zh.data_ptr())
+    hcat.memory = _lib.MEM_HOST
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device=dev)
+
+    def estimate(p, cat):
+        return _engine.call_threept('trvg_compute_bispec_in_gpp_box', ctx, p,
+                                    cat, binning, norm, 'bispec',
+                                    shape='diag')
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(p, cat, steps, profile=False):
+        ctx.set_option('profiling', int(profile))
+        ms, launches, ktimes, res = [], 0, {}, None
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = estimate(p, cat)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+            st = ctx.stats()
+            launches += st['kernel_launches']
+            if profile:
+                for k, (t, c) in ctx.kernel_times().items():
+                    a = ktimes.setdefault(k, [0., 0])
+                    a[0] += t
+                    a[1] += c
+        ctx.set_option('profiling', 0)
+        return ms, launches, ktimes, res, st
+
+    if args.profile_only:
+        for _ in range(2):
+            estimate(p32, dcat)
+        torch.cuda.synchronize(dev)
+        return
+
+    for _ in range(args.warmup):
+        estimate(p32, dcat)
+    estimate(p32, hcat)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, launches, ktimes, res32, st = timed(p32, dcat, args.steps,
+                                            profile=True)
+    clk = clocks.stop()
+    ms_e2e, _, _, _, st_e2e = timed(p32, hcat, args.steps)
+
+    # Max over ranks of the summed device time.
+    total_s = sum(ms) / 1e3
+    total_e2e = sum(ms_e2e) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_s, total_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s, total_e2e = float(t[0]), float(t[1])
+    value = total_s / (args.steps * world)
+    value_e2e = total_e2e / (args.steps * world)
+
+    fp64 = None
+    if not args.no_fp64:
+        estimate(p64, dcat)
+        n64 = max(1, min(args.steps, 3))
+        ms64, _, _, res64, _ = timed(p64, dcat, n64)
+        err = {}
+        for key in ('bk_raw', 'bk_shot'):
+            a, b = res32[key], res64[key]
+            err[key] = float(np.max(np.abs(a - b) / np.abs(b)))
+        fp64 = {"s_per_estimate": sum(ms64) / 1e3 / n64,
+                "fp32mixed_speedup": (sum(ms64) / n64) / (sum(ms) / len(ms)),
+                "max_rel_err_fp32mixed": err,
+                "nmodes_equal": bool(np.array_equal(res32['nmodes_1'],
+                                                    res64['nmodes_1']))}
+        ctx.set_option('full_mesh_shells', 1)
+        try:
+            estimate(p64, dcat)
+            msd, _, _, resd, _ = timed(p64, dcat, 1)
+            fp64["plain_full_mesh_s_per_estimate"] = sum(msd) / 1e3
+            fp64["fp32mixed_speedup_vs_plain"] = sum(msd) / (sum(ms) / len(ms))
+            fp64["plain_vs_pruned_max_rel"] = float(max(
+                np.max(np.abs(resd[k] - res64[k]) / np.abs(res64[k]))
+                for k in ('bk_raw', 'bk_shot')))
+        except _lib.DeviceError as e:
+            fp64["plain_full_mesh_s_per_estimate"] = None
+            fp64["plain_error"] = str(e)[:200]
+        finally:
+            ctx.set_option('full_mesh_shells', 0)
+
+    # Roofline of the dominant kernel of this library.
+    peak, peak_kind = hbm_peak()
+    mine = {k: v for k, v in ktimes.items() if not k.startswith('cufft')}
+    total_k = sum(v[0] for v in ktimes.values())
+    dom = max(mine, key=lambda k: mine[k][0])
+    dom_ms = mine[dom][0] / mine[dom][1]
+    alg = algorithmic_bytes(dom, args, 4)
+    roof = None
+    if alg is not None:
+        ach = alg / (dom_ms * 1e-3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": round(ach, 1),
+                "peak": peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                "unit": "GB/s", "frac": round(ach / peak, 4),
+                "traffic": ncu_traffic(dom), "algorithmic_bytes": alg,
+                "ms_per_launch": round(dom_ms, 4)}
+    shares = {k: round(v[0] / total_k, 4) for k, v in
+              sorted(ktimes.items(), key=lambda kv: -kv[1][0])}
+
+    line = {
+        "metric": METRIC, "value": round(value, 6), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total_s / args.steps, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 meshes/FFTs, f64 offsets/Ylm/reductions/shot noise",
+        "data": "synthetic (seeded uniform catalogue)",
+        "config": {**workload(args), "parallelism": f"replicas x{world}",
+                   "evaluation_grid": list(st.get('pruned_grid', []))},
+        "e2e": {"value": round(value_e2e, 6), "unit": UNIT,
+                "h2d_bytes_per_step": int(st_e2e['h2d_bytes']),
+                "d2h_bytes_per_step": int(res32['k1_bin'].size * 72)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "kernel_time_shares": shares,
+        "fp64": fp64,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, pair_steps=1):
+    """The CPU oracle on a bounded sample of the workload: the mesh set-up
+    once plus `pair_steps` bin pairs, extrapolated to the whole estimate."""
+    from oracle.sample import GppBispecSample
+    s = GppBispecSample(args.npart, args.boxsize, args.ngrid, args.nbins)
+    t0 = time.perf_counter()
+    s.setup()
+    t_setup = time.perf_counter() - t0
+    tp = []
+    for i in range(pair_steps):
+        t0 = time.perf_counter()
+        s.pair(args.nbins // 2 + i)
+        tp.append(time.perf_counter() - t0)
+    t_pair = statistics.median(tp)
+    return {"value": round(t_setup + args.nbins * t_pair, 3), "unit": UNIT,
+            "cores": s.threads, "kind": "port",
+            "sample": (f"oracle set-up ({t_setup:.1f} s: assignment, "
+                       f"forward FFTs, G) + {pair_steps} of {args.nbins} bin "
+                       f"pairs ({t_pair:.1f} s each), extrapolated")}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.sample import GppBispecSample
+    s = GppBispecSample(args.npart, args.boxsize, args.ngrid, args.nbins)
+    t0 = time.perf_counter()
+    s.setup()
+    t_setup = time.perf_counter() - t0
+    for i in range(args.warmup):
+        s.pair(i % args.nbins)
+    tp = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        s.pair((args.warmup + i) % args.nbins)
+        tp.append(time.perf_counter() - t0)
+    value = t_setup + args.nbins * statistics.mean(tp)
+    sample = (f"oracle (numpy restatement of threept.cpp:1473-2188) set-up "
+              f"{t_setup:.1f} s once + mean of {args.steps} bin pairs "
+              f"({statistics.mean(tp):.1f} s) x {args.nbins}")
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * statistics.mean(tp), 1),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded uniform catalogue)",
+        "config": {**workload(args), "parallelism": "cpu"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT,
+                         "cores": s.threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == '__main__':
+    main()

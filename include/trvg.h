@@ -177,6 +177,21 @@ int trvg_get_stats(const trvg_context* ctx, trvg_stats* out);
 /* Release cached device workspace and FFT plans of `ctx`. */
 int trvg_release_workspace(trvg_context* ctx);
 
+/* Run the context's work on `stream` (a cudaStream_t of the calling
+ * framework, e.g. its current stream); NULL restores the context's own
+ * stream.  No counterpart in the reference (which has no streams). */
+int trvg_context_set_stream(trvg_context* ctx, void* stream);
+/* Context options (no counterpart in the reference):
+ *   "full_mesh_shells" 0/1: evaluate the shell-filtered fields on the full
+ *                           mesh instead of the smallest exact grid;
+ *   "profiling"        0/1: time every kernel / FFT launch with CUDA events
+ *                           (read back with trvg_kernel_time_*). */
+int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
+/* Per-kernel device time of the last call (profiling on). */
+int trvg_kernel_time_count(const trvg_context* ctx, int* count);
+int trvg_kernel_time_get(const trvg_context* ctx, int index, char* name,
+                         int name_len, double* ms, int64_t* launches);
+
 /* Length of the data vector of a three-point measurement
  * (threept.cpp:1495-1521). */
 int trvg_data_vector_dim(int shape, int num_bins, int idx_bin, int* dim);

@@ -37,7 +37,8 @@ EXPORTED = [
     "trvg_compute_powspec_in_gpp_box", "trvg_compute_powspec",
     "trvg_calc_grid_based_powlaw_norm", "trvg_assign_weighted_field_to_mesh",
     "trvg_wigner_3j", "trvg_sph_bessel", "trvg_sph_bessel_spline",
-    "trvg_reduced_ylm",
+    "trvg_reduced_ylm", "trvg_context_set_stream", "trvg_set_option",
+    "trvg_kernel_time_count", "trvg_kernel_time_get",
 ]
 
 
@@ -189,6 +190,11 @@ def _declare(lib):
     lib.trvg_sph_bessel.restype = dp
     lib.trvg_sph_bessel_spline.argtypes = [ip, P(dp), C.c_int64, P(dp)]
     lib.trvg_reduced_ylm.argtypes = [ip, ip, P(dp), C.c_int64, P(dp)]
+    lib.trvg_context_set_stream.argtypes = [vp, vp]
+    lib.trvg_set_option.argtypes = [vp, C.c_char_p, C.c_int64]
+    lib.trvg_kernel_time_count.argtypes = [vp, P(ip)]
+    lib.trvg_kernel_time_get.argtypes = [vp, ip, C.c_char_p, ip, P(dp),
+                                         P(C.c_int64)]
 
 
 def check(status: int):
@@ -228,6 +234,28 @@ class Context:
                     h2d_bytes=s.h2d_bytes, kernel_launches=s.kernel_launches,
                     fft_launches=s.fft_launches,
                     pruned_grid=tuple(s.pruned_grid))
+
+    def set_stream(self, stream_ptr):
+        """Run on a caller's cudaStream_t (None: the context's own)."""
+        check(load().trvg_context_set_stream(
+            self._h, None if stream_ptr is None else C.c_void_p(stream_ptr)))
+
+    def set_option(self, key: str, value: int):
+        check(load().trvg_set_option(self._h, key.encode(), int(value)))
+
+    def kernel_times(self) -> dict:
+        """{name: (ms, launches)} of the last call (profiling on)."""
+        lib = load()
+        n = C.c_int()
+        check(lib.trvg_kernel_time_count(self._h, C.byref(n)))
+        out = {}
+        buf = C.create_string_buffer(64)
+        for i in range(n.value):
+            ms, cnt = C.c_double(), C.c_int64()
+            check(lib.trvg_kernel_time_get(self._h, i, buf, 64, C.byref(ms),
+                                           C.byref(cnt)))
+            out[buf.value.decode()] = (ms.value, cnt.value)
+        return out
 
     def release_workspace(self):
         check(load().trvg_release_workspace(self._h))

@@ -266,18 +266,22 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
   const int grid = grid_for(cat.n, block);
   switch (order) {
     case 1:
+      TRVG_KBEGIN(ctx, "assign_kernel");
       assign_kernel<1, Real><<<grid, block, 0, ctx.stream>>>(
           a, mesh_re, mesh_im, sre, sim, sums);
       break;
     case 2:
+      TRVG_KBEGIN(ctx, "assign_kernel");
       assign_kernel<2, Real><<<grid, block, 0, ctx.stream>>>(
           a, mesh_re, mesh_im, sre, sim, sums);
       break;
     case 3:
+      TRVG_KBEGIN(ctx, "assign_kernel");
       assign_kernel<3, Real><<<grid, block, 0, ctx.stream>>>(
           a, mesh_re, mesh_im, sre, sim, sums);
       break;
     case 4:
+      TRVG_KBEGIN(ctx, "assign_kernel");
       assign_kernel<4, Real><<<grid, block, 0, ctx.stream>>>(
           a, mesh_re, mesh_im, sre, sim, sums);
       break;
@@ -291,6 +295,7 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
 template <class Real>
 void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
                          double* out) {
+  TRVG_KBEGIN(ctx, "sum_pow_kernel");
   sum_pow_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(mesh, n,
                                                                  order, out);
   TRVG_LAUNCHED(ctx);
@@ -299,6 +304,7 @@ void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
 template <class Real>
 void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
                            double scale, double* out) {
+  TRVG_KBEGIN(ctx, "to_double_kernel");
   to_double_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(
       mesh, n, scale, out);
   TRVG_LAUNCHED(ctx);
@@ -307,6 +313,7 @@ void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
                        const WeightSpec& ws, double* out) {
   if (cat.n == 0) return;
+  TRVG_KBEGIN(ctx, "weight_sum_kernel");
   weight_sum_kernel<<<grid_for(cat.n, 256), 256, 0, ctx.stream>>>(cat, ws,
                                                                   out);
   TRVG_LAUNCHED(ctx);

@@ -86,6 +86,65 @@ cufftHandle Context::plan(int type, const int n[3], int batch) {
   return h;
 }
 
+namespace {
+cudaEvent_t next_event(Context& c) {
+  if (c.events_used == c.event_pool.size()) {
+    cudaEvent_t e;
+    TRVG_CUDA(cudaEventCreate(&e));
+    c.event_pool.push_back(e);
+  }
+  return c.event_pool[c.events_used++];
+}
+}  // namespace
+
+void Context::kbegin(const char* name) {
+  if (!profiling) return;
+  pending = name;
+  pending_begin = next_event(*this);
+  TRVG_CUDA(cudaEventRecord(pending_begin, stream));
+}
+
+void Context::kend() {
+  if (!profiling || pending == nullptr) return;
+  cudaEvent_t e = next_event(*this);
+  TRVG_CUDA(cudaEventRecord(e, stream));
+  records.push_back({pending, pending_begin, e});
+  pending = nullptr;
+}
+
+void Context::begin_call() {
+  kernel_launches = 0;
+  fft_launches = 0;
+  h2d_bytes = 0;
+  records.clear();
+  events_used = 0;
+  pending = nullptr;
+}
+
+void Context::finish_call() {
+  ktimes.clear();
+  for (const KernelRecord& r : records) {
+    float ms = 0.f;
+    TRVG_CUDA(cudaEventElapsedTime(&ms, r.begin, r.end));
+    bool found = false;
+    for (auto& kv : ktimes) {
+      if (kv.first == r.name) {
+        kv.second.first += ms;
+        kv.second.second += 1;
+        found = true;
+        break;
+      }
+    }
+    if (!found) ktimes.push_back({r.name, {double(ms), int64_t(1)}});
+  }
+  records.clear();
+}
+
+void Context::set_stream(cudaStream_t s) {
+  stream = (s != nullptr) ? s : own_stream;
+  for (auto& kv : plans) TRVG_CUFFT(cufftSetStream(kv.second, stream));
+}
+
 void Context::release() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto& kv : plans) cufftDestroy(kv.second);
@@ -93,6 +152,12 @@ void Context::release() {
   for (auto& kv : buffers)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   buffers.clear();
+}
+
+void destroy_events(Context& c) {
+  for (cudaEvent_t e : c.event_pool) cudaEventDestroy(e);
+  c.event_pool.clear();
+  c.events_used = 0;
 }
 
 void Context::log(int level, const char* fmt, ...) const {
@@ -126,7 +191,9 @@ int trvg_context_create(int device, trvg_context** ctx) {
   TRVG_CUDA(cudaSetDevice(device));
   auto* c = new trvg_context();
   c->impl.device = device;
-  TRVG_CUDA(cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking));
+  TRVG_CUDA(cudaStreamCreateWithFlags(&c->impl.own_stream,
+                                      cudaStreamNonBlocking));
+  c->impl.stream = c->impl.own_stream;
   TRVG_CUDA(cudaEventCreate(&c->impl.ev_start));
   TRVG_CUDA(cudaEventCreate(&c->impl.ev_h2d));
   TRVG_CUDA(cudaEventCreate(&c->impl.ev_stop));
@@ -142,7 +209,8 @@ int trvg_context_destroy(trvg_context* ctx) {
   if (ctx->impl.ev_start) cudaEventDestroy(ctx->impl.ev_start);
   if (ctx->impl.ev_h2d) cudaEventDestroy(ctx->impl.ev_h2d);
   if (ctx->impl.ev_stop) cudaEventDestroy(ctx->impl.ev_stop);
-  if (ctx->impl.stream) cudaStreamDestroy(ctx->impl.stream);
+  trvg::destroy_events(ctx->impl);
+  if (ctx->impl.own_stream) cudaStreamDestroy(ctx->impl.own_stream);
   delete ctx;
   TRVG_API_END
 }
@@ -167,6 +235,55 @@ int trvg_get_stats(const trvg_context* ctx, trvg_stats* out) {
   out->kernel_launches = c.kernel_launches;
   out->fft_launches = c.fft_launches;
   for (int i = 0; i < 3; ++i) out->pruned_grid[i] = c.pruned_grid[i];
+  TRVG_API_END
+}
+
+int trvg_context_set_stream(trvg_context* ctx, void* stream) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null context.");
+  TRVG_CUDA(cudaSetDevice(ctx->impl.device));
+  TRVG_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+  ctx->impl.set_stream(static_cast<cudaStream_t>(stream));
+  TRVG_API_END
+}
+
+int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || key == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  const std::string k(key);
+  if (k == "full_mesh_shells") {
+    ctx->impl.full_mesh_shells = value != 0;
+  } else if (k == "profiling") {
+    ctx->impl.profiling = value != 0;
+  } else {
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown option '%s'.",
+                      key);
+  }
+  TRVG_API_END
+}
+
+int trvg_kernel_time_count(const trvg_context* ctx, int* count) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || count == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  *count = int(ctx->impl.ktimes.size());
+  TRVG_API_END
+}
+
+int trvg_kernel_time_get(const trvg_context* ctx, int index, char* name,
+                         int name_len, double* ms, int64_t* launches) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || name == nullptr || name_len <= 0 || ms == nullptr ||
+      launches == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  const auto& kt = ctx->impl.ktimes;
+  if (index < 0 || index >= int(kt.size()))
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Index out of range.");
+  std::snprintf(name, size_t(name_len), "%s", kt[index].first.c_str());
+  *ms = kt[index].second.first;
+  *launches = kt[index].second.second;
   TRVG_API_END
 }
 

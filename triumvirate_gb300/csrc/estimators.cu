@@ -448,7 +448,9 @@ struct Engine {
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
     auto r2c = [&](Real* m, const char* suffix) -> const C* {
       C* o = ctx.buf<C>(name + suffix, size_t(g.nhalf));
+      ctx.kbegin("cufft.r2c.mesh");
       FFT<Real>::r2c(h, m, o);
+      ctx.kend();
       ctx.fft_launches++;
       return o;
     };
@@ -567,24 +569,31 @@ struct Engine {
   }
 
   // Shot-noise two-point field xi(x) = IFFT[(fa fb^*/W - S C_1/W) / V]
-  // (field.cpp:3269-3345) into the real meshes xi.re (and xi.im).
+  // (field.cpp:3269-3345) into the FP64 meshes xi.re (and xi.im).  It is
+  // a difference of nearly equal quantities, so it is formed and
+  // transformed in FP64 at every precision.
   void twopt_xi(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
-                cplx shot, Real*& xi_re, Real*& xi_im) {
+                cplx shot, double*& xi_re, double*& xi_im) {
     const bool hermitian = fa.im == nullptr && fb.im == nullptr &&
                            fa.im_s == nullptr && fb.im_s == nullptr &&
                            shot.imag() == 0.;
-    C* hre = ctx.buf<C>("xi.h.re", size_t(g.nhalf));
-    C* him = hermitian ? nullptr : ctx.buf<C>("xi.h.im", size_t(g.nhalf));
+    double2* hre = ctx.buf<double2>("xi.h.re", size_t(g.nhalf));
+    double2* him =
+        hermitian ? nullptr : ctx.buf<double2>("xi.h.im", size_t(g.nhalf));
     launch_twopt_field<Real>(ctx, g, fa, fb, cd{shot.real(), shot.imag()}, ax,
                              hre, him);
-    cufftHandle h = ctx.plan(FFT<Real>::kC2R, g.n, 1);
-    xi_re = ctx.buf<Real>("xi.re", size_t(g.nmesh));
-    FFT<Real>::c2r(h, hre, xi_re);
+    cufftHandle h = ctx.plan(FFT<double>::kC2R, g.n, 1);
+    xi_re = ctx.buf<double>("xi.re", size_t(g.nmesh));
+    ctx.kbegin("cufft.c2r.xi");
+    FFT<double>::c2r(h, hre, xi_re);
+    ctx.kend();
     ctx.fft_launches++;
     xi_im = nullptr;
     if (him) {
-      xi_im = ctx.buf<Real>("xi.im", size_t(g.nmesh));
-      FFT<Real>::c2r(h, him, xi_im);
+      xi_im = ctx.buf<double>("xi.im", size_t(g.nmesh));
+      ctx.kbegin("cufft.c2r.xi");
+      FFT<double>::c2r(h, him, xi_im);
+      ctx.kend();
       ctx.fft_launches++;
     }
   }
@@ -603,7 +612,8 @@ struct Engine {
 
   // Uncoupled shot noise per pair (field.cpp:3349-3396):
   // vol_cell sum_x j_a(k_a r) j_b(k_b r) y_a y_b xi(x).
-  vector<cplx> shotnoise_pairs(const Real* xi_re, const Real* xi_im, int la,
+  vector<cplx> shotnoise_pairs(const double* xi_re, const double* xi_im,
+                               int la,
                                int ma, int lb, int mb, const SplineTable& sja,
                                const SplineTable& sjb,
                                const vector<double>& ka,
@@ -622,11 +632,11 @@ struct Engine {
       }
       double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
       zero(hist, 2 * nkeys * sizeof(double));
-      launch_radial_hist<Real>(ctx, g, xi_re, xi_im, la, ma, lb, mb, hist);
+      launch_radial_hist<double>(ctx, g, xi_re, xi_im, la, ma, lb, mb, hist);
       launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
                               out);
     } else {
-      launch_pair_bessel_direct<Real>(ctx, g, xi_re, xi_im, la, ma, lb, mb,
+      launch_pair_bessel_direct<double>(ctx, g, xi_re, xi_im, la, ma, lb, mb,
                                       sja, sjb, dka, dkb, np, out);
     }
     vector<double> h = download(out, 2 * size_t(np));
@@ -643,7 +653,7 @@ struct Engine {
       K[a] = c.K[a];
       Kg[a] = 2 * c.K[a];
       M[a] = g.n[a];
-      if (!c.dense[a]) {
+      if (!c.dense[a] && !ctx.full_mesh_shells) {
         const int need = good_fft_size(4 * c.K[a] + 1);
         if (need < g.n[a]) M[a] = need;
       }
@@ -654,7 +664,10 @@ struct Engine {
     const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
     C* G = ctx.buf<C>("G", size_t(Mc));
     launch_build_G<Real>(ctx, g, M, Kg, f, ax, G);
-    FFT<Real>::c2c_inv(ctx.plan(FFT<Real>::kC2C, M, 1), G);
+    cufftHandle h = ctx.plan(FFT<Real>::kC2C, M, 1);
+    ctx.kbegin("cufft.c2c.G");
+    FFT<Real>::c2c_inv(h, G);
+    ctx.kend();
     ctx.fft_launches++;
     return G;
   }
@@ -691,7 +704,10 @@ struct Engine {
       launch_build_F<Real>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo, dhi,
                            nb, hmax, out);
     }
-    FFT<Real>::c2c_inv(ctx.plan(FFT<Real>::kC2C, M, nb), out);
+    cufftHandle h = ctx.plan(FFT<Real>::kC2C, M, nb);
+    ctx.kbegin("cufft.c2c.F");
+    FFT<Real>::c2c_inv(h, out);
+    ctx.kend();
     ctx.fft_launches++;
   }
 
@@ -863,7 +879,7 @@ struct Engine {
     vector<cplx> bk(ndv, 0.), sn(ndv, 0.);
 
     C* G = nullptr;
-    Real *xi_re = nullptr, *xi_im = nullptr;
+    double *xi_re = nullptr, *xi_im = nullptr;
     if (!survey) {
       G = build_G(dn, M, Kg);
       twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
@@ -1020,7 +1036,7 @@ struct Engine {
     vector<double> reff(hb.nb, 0.);
 
     C* G = nullptr;
-    Real *xi_re = nullptr, *xi_im = nullptr;
+    double *xi_re = nullptr, *xi_im = nullptr;
     if (!survey) {
       G = build_G(dn, M, K);
       twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
@@ -1052,7 +1068,7 @@ struct Engine {
       zero(dnp, hb.nb * sizeof(long long));
       zero(drs, hb.nb * sizeof(double));
       zero(dxi, 2 * hb.nb * sizeof(double));
-      launch_shotnoise_3pcf_bins<Real>(ctx, g, xi_re, xi_im, p.ell1, t.m1,
+      launch_shotnoise_3pcf_bins<double>(ctx, g, xi_re, xi_im, p.ell1, t.m1,
                                        p.ell2, t.m2, bd, dnp, drs, dxi);
       vector<long long> np = download(dnp, hb.nb);
       vector<double> rs = download(drs, hb.nb), xs = download(dxi, 2 * hb.nb);
@@ -1238,9 +1254,7 @@ void run(trvg_context* c, const trvg_params* prm, bool allow_interlace,
   Context& ctx = c->impl;
   TRVG_CUDA(cudaSetDevice(ctx.device));
   ctx.verbose = prm->verbose;
-  ctx.kernel_launches = 0;
-  ctx.fft_launches = 0;
-  ctx.h2d_bytes = 0;
+  ctx.begin_call();
   TRVG_CUDA(cudaEventRecord(ctx.ev_start, ctx.stream));
   TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
   if (prm->precision == TRVG_PREC_FP64) {
@@ -1258,6 +1272,7 @@ void run(trvg_context* c, const trvg_params* prm, bool allow_interlace,
   TRVG_CUDA(cudaEventElapsedTime(&ms_h, ctx.ev_start, ctx.ev_h2d));
   ctx.ms_total = ms;
   ctx.ms_h2d = ms_h;
+  ctx.finish_call();
 }
 
 }  // namespace

@@ -61,12 +61,16 @@ const char* last_error();
                           #call, __FILE_NAME__, __LINE__, int(r_));              \
   } while (0)
 
-// Check the launch just made (configuration errors surface here; faults in
-// the kernel surface at the next synchronising call).
+// Bracket a launch: TRVG_KBEGIN records the start event when profiling,
+// TRVG_LAUNCHED checks the launch (configuration errors surface here;
+// faults in the kernel surface at the next synchronising call), counts it
+// and records the end event.
+#define TRVG_KBEGIN(ctx, name) (ctx).kbegin(name)
 #define TRVG_LAUNCHED(ctx)                                                  \
   do {                                                                      \
     TRVG_CUDA(cudaGetLastError());                                          \
     (ctx).kernel_launches++;                                                \
+    (ctx).kend();                                                           \
   } while (0)
 
 // A named, grow-only device buffer.  Buffers persist across calls on one
@@ -89,9 +93,16 @@ struct PlanKey {
   }
 };
 
+// One timed launch of the current call (profiling mode).
+struct KernelRecord {
+  const char* name;
+  cudaEvent_t begin, end;
+};
+
 struct Context {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // stream in use
+  cudaStream_t own_stream = nullptr;   // stream created with the context
   std::map<std::string, DeviceBuffer> buffers;
   std::map<PlanKey, cufftHandle> plans;
   cudaEvent_t ev_start = nullptr, ev_h2d = nullptr, ev_stop = nullptr;
@@ -102,6 +113,23 @@ struct Context {
   int64_t h2d_bytes = 0;
   double ms_total = 0., ms_h2d = 0.;
   int pruned_grid[3] = {0, 0, 0};
+  // Options.
+  bool full_mesh_shells = false;  // evaluate shell fields on the full mesh
+  // Profiling: per-launch events of the current call, per-name totals of
+  // the last call.
+  bool profiling = false;
+  std::vector<cudaEvent_t> event_pool;
+  size_t events_used = 0;
+  std::vector<KernelRecord> records;
+  const char* pending = nullptr;
+  cudaEvent_t pending_begin = nullptr;
+  std::vector<std::pair<std::string, std::pair<double, int64_t>>> ktimes;
+
+  void kbegin(const char* name);
+  void kend();
+  void begin_call();
+  void finish_call();   // after the stream is synchronised
+  void set_stream(cudaStream_t s);
 
   // Grow-only named buffer of at least `bytes` bytes.
   void* buffer(const std::string& name, size_t bytes);
@@ -113,6 +141,8 @@ struct Context {
   void release();
   void log(int level, const char* fmt, ...) const;
 };
+
+void destroy_events(Context& c);
 
 }  // namespace trvg
 

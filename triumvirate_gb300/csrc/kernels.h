@@ -132,12 +132,13 @@ void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const BinsDev& bins, long long* nmodes, double* ksum,
                         double* pk, double* sn);
 
+// The shot-noise field spectrum is formed and transformed in FP64 at every
+// precision (it is a difference of nearly equal quantities).
 template <class Real>
 void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         const FieldSpec<Real>& fb, cd shot,
-                        const AxisTablesDev& ax,
-                        typename CplxOf<Real>::type* out_re,
-                        typename CplxOf<Real>::type* out_im);
+                        const AxisTablesDev& ax, double2* out_re,
+                        double2* out_im);
 
 // ---- reduce.cu -----------------------------------------------------------
 template <class Real>

@@ -253,6 +253,7 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
   if (npairs <= 0) return;
   const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
   dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
+  TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
   reduce_pairs_kernel<Real><<<grid, 256, 0, ctx.stream>>>(ncell, G, Fa, Fb,
                                                           pa, pb, npairs, out);
   TRVG_LAUNCHED(ctx);
@@ -262,6 +263,7 @@ template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                         const Real* xi_im, int ell_a, int m_a, int ell_b,
                         int m_b, double* hist) {
+  TRVG_KBEGIN(ctx, "radial_hist_kernel");
   radial_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
       g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, hist);
   TRVG_LAUNCHED(ctx);
@@ -274,6 +276,7 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
   if (npairs <= 0) return;
   PairBesselArgs a{sja, sjb, ka, kb};
   dim3 grid(grid_for(nkeys, 256, 64), npairs);
+  TRVG_KBEGIN(ctx, "pair_bessel_sums_kernel");
   pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(nkeys, g.dr[0], hist,
                                                         a, out);
   TRVG_LAUNCHED(ctx);
@@ -289,6 +292,7 @@ void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,
   PairBesselArgs a{sja, sjb, ka, kb};
   dim3 grid(grid_for(g.nmesh, 256, 152 * 4),
             (npairs + kBesselChunk - 1) / kBesselChunk);
+  TRVG_KBEGIN(ctx, "pair_bessel_direct_kernel");
   pair_bessel_direct_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
       g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, a, npairs, out);
   TRVG_LAUNCHED(ctx);
@@ -300,6 +304,7 @@ void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
                                 int ell_b, int m_b, const BinsDev& bins,
                                 long long* npairs, double* rsum, double* xi) {
   const size_t smem = bins.nbins * (3 * sizeof(double) + sizeof(long long));
+  TRVG_KBEGIN(ctx, "shotnoise_3pcf_kernel");
   shotnoise_3pcf_kernel<Real><<<grid_for(g.nmesh, 256), 256, smem,
                                 ctx.stream>>>(g, xi_re, xi_im, ell_a, m_a,
                                               ell_b, m_b, bins, npairs, rsum,

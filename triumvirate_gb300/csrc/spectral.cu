@@ -380,10 +380,9 @@ __device__ __forceinline__ cd twopt_mode(const Geom& g, const FieldSpec<Real>& f
 template <class Real>
 __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
                                    FieldSpec<Real> fb, cd shot,
-                                   AxisTablesDev ax,
-                                   typename CplxOf<Real>::type* out_re,
-                                   typename CplxOf<Real>::type* out_im) {
-  using C = typename CplxOf<Real>::type;
+                                   AxisTablesDev ax, double2* out_re,
+                                   double2* out_im) {
+  using C = double2;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        t < g.nhalf; t += int64_t(gridDim.x) * blockDim.x) {
     const int k = int(t % g.nzh);
@@ -392,8 +391,8 @@ __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
     const cd p = twopt_mode(g, fa, fb, shot, ax, i, j, k);
     C o;
     if (out_im == nullptr) {
-      o.x = Real(p.re);
-      o.y = Real(p.im);
+      o.x = p.re;
+      o.y = p.im;
       out_re[t] = o;
     } else {
       const int ii = (i == 0) ? 0 : g.n[0] - i;
@@ -401,12 +400,12 @@ __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
       const int kk = (k == 0) ? 0 : g.n[2] - k;
       const cd q = conjg(twopt_mode(g, fa, fb, shot, ax, ii, jj, kk));
       const cd s = p + q, d = p - q;
-      o.x = Real(s.re / 2.);
-      o.y = Real(s.im / 2.);
+      o.x = s.re / 2.;
+      o.y = s.im / 2.;
       out_re[t] = o;
       C oi;
-      oi.x = Real(d.im / 2.);
-      oi.y = Real(-d.re / 2.);
+      oi.x = d.im / 2.;
+      oi.y = -d.re / 2.;
       out_im[t] = oi;
     }
   }
@@ -418,6 +417,7 @@ void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
                         const BinsDev& bins, long long* nmodes,
                         double* ksum) {
   const size_t smem = bins.nbins * (sizeof(double) + sizeof(long long));
+  TRVG_KBEGIN(ctx, "count_modes_kernel");
   count_modes_kernel<<<grid_for(cube.count, 256), 256, smem, ctx.stream>>>(
       g, cube, bins, nmodes, ksum);
   TRVG_LAUNCHED(ctx);
@@ -429,6 +429,7 @@ void launch_build_G(Context& ctx, const Geom& g, const int M[3],
                     const AxisTablesDev& ax,
                     typename CplxOf<Real>::type* out) {
   const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  TRVG_KBEGIN(ctx, "build_G_kernel");
   build_G_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, ax, out);
   TRVG_LAUNCHED(ctx);
@@ -441,6 +442,7 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const double* lo, const double* hi, int nb,
                     double hi_max, typename CplxOf<Real>::type* out) {
   const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  TRVG_KBEGIN(ctx, "build_F_kernel");
   build_F_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
       hi_max, out);
@@ -453,6 +455,7 @@ void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const SplineTable& sj, const double* radii, int nb,
                         typename CplxOf<Real>::type* out) {
   SjlArgs sa{sj, radii, nb};
+  TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
   build_F_sjl_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
       g, f, ax, ell, m, sa, out);
   TRVG_LAUNCHED(ctx);
@@ -465,6 +468,7 @@ void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const BinsDev& bins, long long* nmodes, double* ksum,
                         double* pk, double* sn) {
   const size_t smem = bins.nbins * (5 * sizeof(double) + sizeof(long long));
+  TRVG_KBEGIN(ctx, "twopt_stats_kernel");
   twopt_stats_kernel<Real><<<grid_for(cube.count, 256), 256, smem,
                              ctx.stream>>>(g, cube, fa, fb, shot, ell, m, ax,
                                            bins, nmodes, ksum, pk, sn);
@@ -474,9 +478,9 @@ void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
 template <class Real>
 void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         const FieldSpec<Real>& fb, cd shot,
-                        const AxisTablesDev& ax,
-                        typename CplxOf<Real>::type* out_re,
-                        typename CplxOf<Real>::type* out_im) {
+                        const AxisTablesDev& ax, double2* out_re,
+                        double2* out_im) {
+  TRVG_KBEGIN(ctx, "twopt_field_kernel");
   twopt_field_kernel<Real><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
       g, fa, fb, shot, ax, out_re, out_im);
   TRVG_LAUNCHED(ctx);
@@ -503,8 +507,8 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
   template void launch_twopt_field<R>(Context&, const Geom&,                 \
                                       const FieldSpec<R>&,                   \
                                       const FieldSpec<R>&, cd,               \
-                                      const AxisTablesDev&, CplxOf<R>::type*,\
-                                      CplxOf<R>::type*);
+                                      const AxisTablesDev&, double2*,        \
+                                      double2*);
 TRVG_INST(float)
 TRVG_INST(double)
 #undef TRVG_INST
