@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument('--no-fp64', action='store_true')
     ap.add_argument('--profile-only', action='store_true',
                     help='run two estimates (for an ncu launch list)')
+    ap.add_argument('--variants', action='store_true',
+                    help='also time the FP32-mixed precision options')
     return ap.parse_args()
 
 
@@ -326,6 +328,25 @@ def run_gb300(args):
         finally:
             ctx.set_option('full_mesh_shells', 0)
 
+    variants = None
+    if args.variants and fp64 is not None:
+        variants = {}
+        for shell64 in (0, 1):
+            for shot64 in (0, 1):
+                ctx.set_option('shell_fields_fp64', shell64)
+                ctx.set_option('shotnoise_fp64', shot64)
+                estimate(p32, dcat)
+                msv, _, _, resv, _ = timed(p32, dcat, 2)
+                errs = {k: [float(e) for e in
+                            np.abs(resv[k] - res64[k]) / np.abs(res64[k])]
+                        for k in ('bk_raw', 'bk_shot')}
+                variants[f"shell64={shell64},shot64={shot64}"] = {
+                    "s_per_estimate": sum(msv) / 2e3,
+                    "max_rel_err": {k: max(v) for k, v in errs.items()},
+                    "per_bin_rel_err": errs}
+        ctx.set_option('shell_fields_fp64', 0)
+        ctx.set_option('shotnoise_fp64', 0)
+
     # Roofline of the dominant kernel of this library.
     peak, peak_kind = hbm_peak()
     mine = {k: v for k, v in ktimes.items() if not k.startswith('cufft')}
@@ -360,6 +381,7 @@ def run_gb300(args):
         "roofline": roof,
         "kernel_time_shares": shares,
         "fp64": fp64,
+        "precision_variants": variants,
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -185,7 +185,11 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *   "full_mesh_shells" 0/1: evaluate the shell-filtered fields on the full
  *                           mesh instead of the smallest exact grid;
  *   "profiling"        0/1: time every kernel / FFT launch with CUDA events
- *                           (read back with trvg_kernel_time_*). */
+ *                           (read back with trvg_kernel_time_*);
+ *   "shotnoise_fp64"   0/1: FP32-mixed: transform the shot-noise field in
+ *                           FP64 (default FP32);
+ *   "shell_fields_fp64" 0/1: FP32-mixed: evaluate the shell-filtered and
+ *                           compensated fields in FP64 (default FP32). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
 /* Per-kernel device time of the last call (profiling on). */
 int trvg_kernel_time_count(const trvg_context* ctx, int* count);

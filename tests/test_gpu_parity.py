@@ -430,3 +430,54 @@ def test_device_inputs_match_host_inputs():
                               binning, 1., 'bispec', shape='diag')
     assert np.array_equal(r1['nmodes_1'], r2['nmodes_1'])
     assert rel_err(r1['bk_raw'], r2['bk_raw']) < 1e-5
+
+
+@pytest.mark.parametrize("boxsize, ngrid", [((800., 800., 1000.), (32, 32, 32)),
+                                            ((700., 700., 700.), (27, 27, 27)),
+                                            ((600., 700., 800.), (24, 28, 32))])
+def test_oracle_gpp_noncubic_and_odd(boxsize, ngrid):
+    """Non-cubic cells use the cell-by-cell Bessel sum, odd meshes the
+    cell-by-cell histogram, unequal x/y meshes the orbit sum without the
+    x <-> y swap."""
+    n = 2500
+    rng = np.random.default_rng(21)
+    pos = rng.uniform(0., 1., size=(n, 3)) * np.array(boxsize)
+    bins = (0.01, 0.1, 4)
+    x, y, z = O.periodise(*pos.T, list(boxsize))
+    p = O.Params(list(boxsize), list(ngrid), 'tsc', False, 0, 0, 0,
+                 form='diag')
+    edges, centres = O.lin_binning(*bins)
+    vol = float(np.prod(boxsize))
+    norm = O.bispec_norm_from_particles(np.full(n, n / vol), 1., 1.)
+    ref = O.compute_bispec_in_gpp_box(np.stack([x, y, z], -1), p, edges,
+                                      centres, norm)
+    for precision in PRECISIONS:
+        res = compute_bispec_in_gpp_box(
+            ParticleCatalogue(*pos.T, nz=n / vol), degrees=(0, 0, 0),
+            binning=Binning('fourier', 'lin', *bins), form='diag',
+            sampling_params={'boxsize': list(boxsize), 'ngrid': list(ngrid),
+                             'assignment': 'tsc', 'precision': precision})
+        assert_close_threept(res, ref, 'bispec', precision)
+
+
+@pytest.mark.parametrize("shell64, shot64", [(0, 1), (1, 0), (1, 1)])
+def test_fp32mixed_precision_options(shell64, shot64):
+    """The FP64 evaluation-grid / shot-noise options of the FP32-mixed path
+    stay within its tolerance of the oracle."""
+    box, n, ngrid = 800., 3000, 32
+    pos = _uniform(n, box, seed=31)
+    bins = (0.01, 0.1, 5)
+    ref = _oracle_gpp('bispec', pos, box, ngrid, 'tsc', (2, 0, 2), 'diag',
+                      None, bins)
+    ctx = _lib.default_context()
+    ctx.set_option('shell_fields_fp64', shell64)
+    ctx.set_option('shotnoise_fp64', shot64)
+    try:
+        res = compute_bispec_in_gpp_box(
+            ParticleCatalogue(*pos.T, nz=n / box ** 3), degrees=(2, 0, 2),
+            binning=Binning('fourier', 'lin', *bins), form='diag',
+            sampling_params=_sampling('fp32mixed', ngrid, box=box))
+    finally:
+        ctx.set_option('shell_fields_fp64', 0)
+        ctx.set_option('shotnoise_fp64', 0)
+    assert_close_threept(res, ref, 'bispec', 'fp32mixed')

@@ -161,11 +161,14 @@ TRVG_HD double sph_bessel_upward(int ell, double x) {
   return j1;
 }
 
-// Natural cubic spline of j_l on the nodes x_i = 0.05 i, i = 0..n-1
-// (second-derivative halves in `c`, node values in `y`).
+// Natural cubic spline of j_l on the nodes x_i = 0.05 i, i = 0..n-1, as
+// the per-interval polynomial y_i + b_i dx + c_i dx^2 + d_i dx^3
+// (c: half the second derivative at the nodes).
 struct SplineTable {
   const double* y;
+  const double* b;
   const double* c;
+  const double* d;
   int n;
   int ell;
   double split;
@@ -173,30 +176,25 @@ struct SplineTable {
 
 constexpr double kSplineStep = 0.05;
 
+// The interval is the one with x_i <= x < x_{i+1} (the last interval for
+// x at the last node), found from x / 0.05 and corrected against the node
+// values themselves.
 TRVG_HD double spline_eval(const SplineTable& t, double x) {
   if (x >= t.split) return sph_bessel_upward(t.ell, x);
   const double h = kSplineStep;
-  int i = int(x / h);
+  int i = int(x * (1. / h));
   if (i > t.n - 2) i = t.n - 2;
   if (i < 0) i = 0;
-  double xlo = 0. + dmul(h, double(i));
+  double xlo = dmul(h, double(i));
   if (x < xlo && i > 0) {
     --i;
-    xlo = 0. + dmul(h, double(i));
-  }
-  double xhi = 0. + dmul(h, double(i + 1));
-  if (x >= xhi && i < t.n - 2) {
+    xlo = dmul(h, double(i));
+  } else if (i < t.n - 2 && x >= dmul(h, double(i + 1))) {
     ++i;
-    xlo = xhi;
-    xhi = 0. + dmul(h, double(i + 1));
+    xlo = dmul(h, double(i));
   }
-  const double hh = xhi - xlo;
   const double dx = x - xlo;
-  const double ylo = t.y[i], yhi = t.y[i + 1];
-  const double clo = t.c[i], chi = t.c[i + 1];
-  const double b = (yhi - ylo) / hh - hh * (chi + 2.0 * clo) / 3.0;
-  const double d = (chi - clo) / (3.0 * hh);
-  return ylo + dx * (b + dx * (clo + dx * d));
+  return t.y[i] + dx * (t.b[i] + dx * (t.c[i] + dx * t.d[i]));
 }
 
 // ---------------------------------------------------------------------------
@@ -208,6 +206,7 @@ struct AxisTables {
   const double* sinc[3];   // sin(u)/u (1 at u = 0), u = pi * i_shift / n
   const double* alias[3];  // per-axis shot-noise aliasing polynomial of sin^2
   const double* u[3];      // u itself (interlaced isotropic approximation)
+  const double* inv_alias[3];  // 1 / alias
 };
 
 }  // namespace trvg

@@ -257,6 +257,10 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     ctx->impl.full_mesh_shells = value != 0;
   } else if (k == "profiling") {
     ctx->impl.profiling = value != 0;
+  } else if (k == "shotnoise_fp64") {
+    ctx->impl.shotnoise_fp64 = value != 0;
+  } else if (k == "shell_fields_fp64") {
+    ctx->impl.shell_fields_fp64 = value != 0;
   } else {
     trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown option '%s'.",
                       key);
@@ -299,7 +303,8 @@ int trvg_sph_bessel_spline(int ell, const double* x, int64_t n,
   if (ell < 0 || (n > 0 && (x == nullptr || out == nullptr)))
     trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid arguments.");
   trvg::SplineHost s(ell);
-  trvg::SplineTable t = s.table(s.y.data(), s.c.data());
+  trvg::SplineTable t =
+      s.table(s.y.data(), s.b.data(), s.c.data(), s.d.data());
   for (int64_t i = 0; i < n; ++i) {
     if (!(x[i] >= 0.))
       trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,

@@ -346,7 +346,7 @@ struct Engine {
   // Per-axis sinc, aliasing and u tables (field.cpp:1127-1143, 3445-3458).
   void setup_axis_tables() {
     const int nmax = std::max({g.n[0], g.n[1], g.n[2]});
-    vector<double> host(size_t(9) * nmax, 0.);
+    vector<double> host(size_t(12) * nmax, 0.);
     for (int a = 0; a < 3; ++a) {
       for (int i = 0; i < g.n[a]; ++i) {
         const int s = shift_index(i, g.n[a]);
@@ -363,16 +363,18 @@ struct Engine {
             break;
           default: al = 1.;
         }
-        host[size_t(3 * a + 0) * nmax + i] = sinc;
-        host[size_t(3 * a + 1) * nmax + i] = al;
-        host[size_t(3 * a + 2) * nmax + i] = u;
+        host[size_t(4 * a + 0) * nmax + i] = sinc;
+        host[size_t(4 * a + 1) * nmax + i] = al;
+        host[size_t(4 * a + 2) * nmax + i] = u;
+        host[size_t(4 * a + 3) * nmax + i] = 1. / al;
       }
     }
     double* d = upload("axis_tables", host);
     for (int a = 0; a < 3; ++a) {
-      ax.t.sinc[a] = d + size_t(3 * a + 0) * nmax;
-      ax.t.alias[a] = d + size_t(3 * a + 1) * nmax;
-      ax.t.u[a] = d + size_t(3 * a + 2) * nmax;
+      ax.t.sinc[a] = d + size_t(4 * a + 0) * nmax;
+      ax.t.alias[a] = d + size_t(4 * a + 1) * nmax;
+      ax.t.u[a] = d + size_t(4 * a + 2) * nmax;
+      ax.t.inv_alias[a] = d + size_t(4 * a + 3) * nmax;
     }
     ax.order = p.assignment_order;
     ax.interlace = interlace;
@@ -569,33 +571,51 @@ struct Engine {
   }
 
   // Shot-noise two-point field xi(x) = IFFT[(fa fb^*/W - S C_1/W) / V]
-  // (field.cpp:3269-3345) into the FP64 meshes xi.re (and xi.im).  It is
-  // a difference of nearly equal quantities, so it is formed and
-  // transformed in FP64 at every precision.
-  void twopt_xi(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
-                cplx shot, double*& xi_re, double*& xi_im) {
+  // (field.cpp:3269-3345) into the real meshes xi.re (and xi.im), in FP64
+  // for the FP64 path or when the "shotnoise_fp64" option is set, else in
+  // FP32.
+  struct Xi {
+    const void* re = nullptr;
+    const void* im = nullptr;
+    bool dbl = false;
+  };
+
+  template <class XR>
+  Xi twopt_xi_t(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                cplx shot) {
+    using XC = typename CplxOf<XR>::type;
     const bool hermitian = fa.im == nullptr && fb.im == nullptr &&
                            fa.im_s == nullptr && fb.im_s == nullptr &&
                            shot.imag() == 0.;
-    double2* hre = ctx.buf<double2>("xi.h.re", size_t(g.nhalf));
-    double2* him =
-        hermitian ? nullptr : ctx.buf<double2>("xi.h.im", size_t(g.nhalf));
-    launch_twopt_field<Real>(ctx, g, fa, fb, cd{shot.real(), shot.imag()}, ax,
-                             hre, him);
-    cufftHandle h = ctx.plan(FFT<double>::kC2R, g.n, 1);
-    xi_re = ctx.buf<double>("xi.re", size_t(g.nmesh));
+    XC* hre = ctx.buf<XC>("xi.h.re", size_t(g.nhalf));
+    XC* him = hermitian ? nullptr : ctx.buf<XC>("xi.h.im", size_t(g.nhalf));
+    launch_twopt_field<Real, XR>(ctx, g, fa, fb, cd{shot.real(), shot.imag()},
+                                 ax, hre, him);
+    cufftHandle h = ctx.plan(FFT<XR>::kC2R, g.n, 1);
+    Xi xi;
+    xi.dbl = sizeof(XR) == 8;
+    XR* re = ctx.buf<XR>("xi.re", size_t(g.nmesh));
     ctx.kbegin("cufft.c2r.xi");
-    FFT<double>::c2r(h, hre, xi_re);
+    FFT<XR>::c2r(h, hre, re);
     ctx.kend();
     ctx.fft_launches++;
-    xi_im = nullptr;
+    xi.re = re;
     if (him) {
-      xi_im = ctx.buf<double>("xi.im", size_t(g.nmesh));
+      XR* im = ctx.buf<XR>("xi.im", size_t(g.nmesh));
       ctx.kbegin("cufft.c2r.xi");
-      FFT<double>::c2r(h, him, xi_im);
+      FFT<XR>::c2r(h, him, im);
       ctx.kend();
       ctx.fft_launches++;
+      xi.im = im;
     }
+    return xi;
+  }
+
+  Xi twopt_xi(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+              cplx shot) {
+    if (sizeof(Real) == 8 || ctx.shotnoise_fp64)
+      return twopt_xi_t<double>(fa, fb, shot);
+    return twopt_xi_t<float>(fa, fb, shot);
   }
 
   struct SplineDev {
@@ -606,15 +626,16 @@ struct Engine {
     SplineHost s(ell);
     const std::string tag = "spline." + std::to_string(ell);
     const double* y = upload(tag + ".y", s.y);
+    const double* b = upload(tag + ".b", s.b);
     const double* c = upload(tag + ".c", s.c);
-    return s.table(y, c);
+    const double* d = upload(tag + ".d", s.d);
+    return s.table(y, b, c, d);
   }
 
   // Uncoupled shot noise per pair (field.cpp:3349-3396):
   // vol_cell sum_x j_a(k_a r) j_b(k_b r) y_a y_b xi(x).
-  vector<cplx> shotnoise_pairs(const double* xi_re, const double* xi_im,
-                               int la,
-                               int ma, int lb, int mb, const SplineTable& sja,
+  vector<cplx> shotnoise_pairs(const Xi& xi, int la, int ma, int lb, int mb,
+                               const SplineTable& sja,
                                const SplineTable& sjb,
                                const vector<double>& ka,
                                const vector<double>& kb) {
@@ -632,12 +653,27 @@ struct Engine {
       }
       double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
       zero(hist, 2 * nkeys * sizeof(double));
-      launch_radial_hist<double>(ctx, g, xi_re, xi_im, la, ma, lb, mb, hist);
+      if (xi.dbl)
+        launch_radial_hist<double>(ctx, g, static_cast<const double*>(xi.re),
+                                   static_cast<const double*>(xi.im), la, ma,
+                                   lb, mb, hist);
+      else
+        launch_radial_hist<float>(ctx, g, static_cast<const float*>(xi.re),
+                                  static_cast<const float*>(xi.im), la, ma, lb,
+                                  mb, hist);
       launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
                               out);
     } else {
-      launch_pair_bessel_direct<double>(ctx, g, xi_re, xi_im, la, ma, lb, mb,
-                                      sja, sjb, dka, dkb, np, out);
+      if (xi.dbl)
+        launch_pair_bessel_direct<double>(
+            ctx, g, static_cast<const double*>(xi.re),
+            static_cast<const double*>(xi.im), la, ma, lb, mb, sja, sjb, dka,
+            dkb, np, out);
+      else
+        launch_pair_bessel_direct<float>(
+            ctx, g, static_cast<const float*>(xi.re),
+            static_cast<const float*>(xi.im), la, ma, lb, mb, sja, sjb, dka,
+            dkb, np, out);
     }
     vector<double> h = download(out, 2 * size_t(np));
     vector<cplx> res(np);
@@ -660,13 +696,16 @@ struct Engine {
     }
   }
 
-  C* build_G(const FieldSpec<Real>& f, const int M[3], const int Kg[3]) {
+  template <class FR>
+  typename CplxOf<FR>::type* build_G(const FieldSpec<Real>& f, const int M[3],
+                                     const int Kg[3]) {
+    using FC = typename CplxOf<FR>::type;
     const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
-    C* G = ctx.buf<C>("G", size_t(Mc));
-    launch_build_G<Real>(ctx, g, M, Kg, f, ax, G);
-    cufftHandle h = ctx.plan(FFT<Real>::kC2C, M, 1);
+    FC* G = ctx.buf<FC>("G", size_t(Mc));
+    launch_build_G<Real, FR>(ctx, g, M, Kg, f, ax, G);
+    cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, 1);
     ctx.kbegin("cufft.c2c.G");
-    FFT<Real>::c2c_inv(h, G);
+    FFT<FR>::c2c_inv(h, G);
     ctx.kend();
     ctx.fft_launches++;
     return G;
@@ -680,17 +719,18 @@ struct Engine {
     SplineTable sj;
   };
 
+  template <class FR>
   void build_leg(const FieldSpec<Real>& src, const Leg& leg,
                  const vector<int>& bins, const HostBins& hb,
                  const vector<double>& radii, const int M[3], const int K[3],
-                 const std::string& tag, C* out) {
+                 const std::string& tag, typename CplxOf<FR>::type* out) {
     const int nb = int(bins.size());
     if (leg.sjl) {
       vector<double> r(nb);
       for (int i = 0; i < nb; ++i) r[i] = radii[bins[i]];
       const double* dr = upload(tag + ".r", r);
-      launch_build_F_sjl<Real>(ctx, g, src, ax, leg.ell, leg.m, leg.sj, dr,
-                               nb, out);
+      launch_build_F_sjl<Real, FR>(ctx, g, src, ax, leg.ell, leg.m, leg.sj,
+                                   dr, nb, out);
     } else {
       vector<double> lo(nb), hi(nb);
       double hmax = 0.;
@@ -701,24 +741,40 @@ struct Engine {
       }
       const double* dlo = upload(tag + ".lo", lo);
       const double* dhi = upload(tag + ".hi", hi);
-      launch_build_F<Real>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo, dhi,
-                           nb, hmax, out);
+      launch_build_F<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo,
+                               dhi, nb, hmax, out);
     }
-    cufftHandle h = ctx.plan(FFT<Real>::kC2C, M, nb);
+    cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, nb);
     ctx.kbegin("cufft.c2c.F");
-    FFT<Real>::c2c_inv(h, out);
+    FFT<FR>::c2c_inv(h, out);
     ctx.kend();
     ctx.fft_launches++;
   }
 
-  // sum over the evaluation grid of F_a(row) F_b(col) G for every pair.
-  vector<cplx> pair_sums(const FieldSpec<Real>& src, const C* G,
-                         const Leg& la, const Leg& lb,
-                         const vector<Pair>& pairs, const HostBins& hb,
-                         const vector<double>& radii, const int M[3],
-                         const int K[3]) {
+  // sum over the evaluation grid of F_a(row) F_b(col) G for every pair, G
+  // being the compensated field of `gsrc`; evaluation-grid fields in FP64
+  // for the FP64 path or with the "shell_fields_fp64" option.
+  vector<cplx> pair_sums(const FieldSpec<Real>& src,
+                         const FieldSpec<Real>& gsrc, const Leg& la,
+                         const Leg& lb, const vector<Pair>& pairs,
+                         const HostBins& hb, const vector<double>& radii,
+                         const int M[3], const int K[3], const int Kg[3]) {
+    if (sizeof(Real) == 8 || ctx.shell_fields_fp64)
+      return pair_sums_t<double>(src, gsrc, la, lb, pairs, hb, radii, M, K,
+                                 Kg);
+    return pair_sums_t<float>(src, gsrc, la, lb, pairs, hb, radii, M, K, Kg);
+  }
+
+  template <class FR>
+  vector<cplx> pair_sums_t(const FieldSpec<Real>& src,
+                           const FieldSpec<Real>& gsrc, const Leg& la,
+                           const Leg& lb, const vector<Pair>& pairs,
+                           const HostBins& hb, const vector<double>& radii,
+                           const int M[3], const int K[3], const int Kg[3]) {
+    using FC = typename CplxOf<FR>::type;
     const int np = int(pairs.size());
     vector<cplx> res(np, cplx(0., 0.));
+    const FC* G = build_G<FR>(gsrc, M, Kg);
     const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;
     vector<int> A, B;
     for (const Pair& q : pairs) {
@@ -736,7 +792,7 @@ struct Engine {
     uniq(A);
     uniq(B);
     const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
-    const size_t perF = size_t(Mc) * sizeof(C);
+    const size_t perF = size_t(Mc) * sizeof(FC);
     size_t free_b = 0, total_b = 0;
     TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     size_t have = 0;
@@ -748,8 +804,8 @@ struct Engine {
     int SA, SB;
     if (shared) {
       SA = int(std::min<double>(A.size(), budget / perF));
-      if (SA < int(A.size())) SA = int(std::min<double>(A.size(),
-                                                         budget / (2. * perF)));
+      if (SA < int(A.size()))
+        SA = int(std::min<double>(A.size(), budget / (2. * perF)));
       SB = SA;
     } else {
       SA = int(std::min<double>(A.size(), budget / (2. * perF)));
@@ -771,8 +827,8 @@ struct Engine {
     const auto blocksB = shared ? blocksA : chunk(B, SB);
     for (size_t I = 0; I < blocksA.size(); ++I) {
       const vector<int>& bA = blocksA[I];
-      C* FA = ctx.buf<C>("F.A", bA.size() * size_t(Mc));
-      build_leg(src, la, bA, hb, radii, M, K, "legA", FA);
+      FC* FA = ctx.buf<FC>("F.A", bA.size() * size_t(Mc));
+      build_leg<FR>(src, la, bA, hb, radii, M, K, "legA", FA);
       for (size_t J = 0; J < blocksB.size(); ++J) {
         const vector<int>& bB = blocksB[J];
         vector<int> pa, pb, idx;
@@ -786,18 +842,18 @@ struct Engine {
           idx.push_back(i);
         }
         if (idx.empty()) continue;
-        const C* FB = FA;
+        const FC* FB = FA;
         if (!(shared && I == J)) {
-          C* fb = ctx.buf<C>("F.B", bB.size() * size_t(Mc));
-          build_leg(src, lb, bB, hb, radii, M, K, "legB", fb);
+          FC* fb = ctx.buf<FC>("F.B", bB.size() * size_t(Mc));
+          build_leg<FR>(src, lb, bB, hb, radii, M, K, "legB", fb);
           FB = fb;
         }
         const int* dpa = upload("pairs.a", pa);
         const int* dpb = upload("pairs.b", pb);
         double* dout = ctx.buf<double>("pairs.out", 2 * idx.size());
         zero(dout, 2 * idx.size() * sizeof(double));
-        launch_reduce_pairs<Real>(ctx, Mc, G, FA, FB, dpa, dpb,
-                                  int(idx.size()), dout);
+        launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb, int(idx.size()),
+                                dout);
         vector<double> h = download(dout, 2 * idx.size());
         for (size_t q = 0; q < idx.size(); ++q)
           res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);
@@ -878,19 +934,15 @@ struct Engine {
 
     vector<cplx> bk(ndv, 0.), sn(ndv, 0.);
 
-    C* G = nullptr;
-    double *xi_re = nullptr, *xi_im = nullptr;
-    if (!survey) {
-      G = build_G(dn, M, Kg);
-      twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
-    }
+    Xi xi;
+    if (!survey) xi = twopt_xi(dn, nf, cplx(double(dd.n), 0.));
     vector<double> no_radii;
 
     for (const Term& t : terms) {
       const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
       const double mirror = zero_t ? 0. : ((p.ELL & 1) ? -1. : 1.);
       const double mirror_w3j = zero_t ? 0. : 1.;
-      FieldSpec<Real> dnLM, NLM;
+      FieldSpec<Real> dnLM = dn, NLM;
       cplx Sbar;
       if (survey) {
         const bool cplxM = (t.M != 0);
@@ -899,7 +951,6 @@ struct Engine {
                                 {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
                                cplxM);
         dnLM = k0_view(fdn, 0.);
-        G = build_G(dnLM, M, Kg);
         Field fN = make_field(
             "NLM",
             {{dd, ylm_ws(1., 2, p.ELL, t.M, true)},
@@ -917,7 +968,7 @@ struct Engine {
       // Raw bispectrum (threept.cpp:1675-1968).
       Leg la{p.ell1, t.m1}, lb{p.ell2, t.m2};
       const vector<cplx> comp =
-          pair_sums(dn, G, la, lb, pairs, hb, no_radii, M, K);
+          pair_sums(dn, dnLM, la, lb, pairs, hb, no_radii, M, K, Kg);
       for (int i = 0; i < ndv; ++i) {
         const cplx B = comp[i] * fac /
                        (double(nmodes[pairs[i].row]) *
@@ -928,8 +979,10 @@ struct Engine {
       // Shot noise (threept.cpp:1974-2140).
       if (p.ell1 == 0 && p.ell2 == 0)
         for (int i = 0; i < ndv; ++i) sn[i] += t.coupling * Sbar;
+      Stats st_prev;
       if (p.ell2 == 0) {
         Stats st = twopt_stats(hb, dn, NLM, Sbar, p.ell1, t.m1);
+        st_prev = st;
         for (int i = 0; i < ndv; ++i) {
           const int b = pairs[i].row;
           const cplx S = t.coupling * (st.pk[b] - st.sn[b]);
@@ -937,16 +990,19 @@ struct Engine {
         }
       }
       if (p.ell1 == 0) {
-        Stats st = twopt_stats(hb, dn, NLM, Sbar, p.ell2, t.m2);
+        // Same statistics as the ell2 = 0 branch when both legs coincide.
+        Stats st = (p.ell2 == 0 && t.m1 == t.m2)
+                       ? st_prev
+                       : twopt_stats(hb, dn, NLM, Sbar, p.ell2, t.m2);
         for (int i = 0; i < ndv; ++i) {
           const int b = pairs[i].col;
           const cplx S = t.coupling * (st.pk[b] - st.sn[b]);
           sn[i] += S + mirror * std::conj(S);
         }
       }
-      if (survey) twopt_xi(dnLM, nf, Sbar, xi_re, xi_im);
-      const vector<cplx> Sij = shotnoise_pairs(
-          xi_re, xi_im, p.ell1, t.m1, p.ell2, t.m2, sja, sjb, ka, kbv);
+      if (survey) xi = twopt_xi(dnLM, nf, Sbar);
+      const vector<cplx> Sij = shotnoise_pairs(xi, p.ell1, t.m1, p.ell2, t.m2,
+                                               sja, sjb, ka, kbv);
       for (int i = 0; i < ndv; ++i) {
         const cplx S = t.coupling * Sij[i];
         sn[i] += phase * (S + mirror_w3j * std::conj(S));
@@ -1035,30 +1091,26 @@ struct Engine {
     vector<long long> npairs(hb.nb, 0);
     vector<double> reff(hb.nb, 0.);
 
-    C* G = nullptr;
-    double *xi_re = nullptr, *xi_im = nullptr;
-    if (!survey) {
-      G = build_G(dn, M, K);
-      twopt_xi(dn, nf, cplx(double(dd.n), 0.), xi_re, xi_im);
-    }
+    Xi xi;
+    if (!survey) xi = twopt_xi(dn, nf, cplx(double(dd.n), 0.));
 
     bool first = true;
     for (const Term& t : terms) {
       const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
       const double mirror = zero_t ? 0. : ((p.ELL & 1) ? -1. : 1.);
       const double mirror_w3j = zero_t ? 0. : 1.;
+      FieldSpec<Real> dnLM = dn;
       if (survey) {
         const bool cplxM = (t.M != 0);
         Field fdn = make_field("dnLM",
                                {{dd, ylm_ws(1., 1, p.ELL, t.M, false)},
                                 {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
                                cplxM);
-        FieldSpec<Real> dnLM = k0_view(fdn, 0.);
+        dnLM = k0_view(fdn, 0.);
         const cplx Sbar = weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false)) +
                           alpha * alpha * alpha *
                               weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
-        twopt_xi(dnLM, nf, Sbar, xi_re, xi_im);
-        G = build_G(dnLM, M, K);
+        xi = twopt_xi(dnLM, nf, Sbar);
       }
 
       // Shot noise (field.cpp:3090-3196; threept.cpp:2307-2345).
@@ -1068,8 +1120,16 @@ struct Engine {
       zero(dnp, hb.nb * sizeof(long long));
       zero(drs, hb.nb * sizeof(double));
       zero(dxi, 2 * hb.nb * sizeof(double));
-      launch_shotnoise_3pcf_bins<double>(ctx, g, xi_re, xi_im, p.ell1, t.m1,
-                                       p.ell2, t.m2, bd, dnp, drs, dxi);
+      if (xi.dbl)
+        launch_shotnoise_3pcf_bins<double>(
+            ctx, g, static_cast<const double*>(xi.re),
+            static_cast<const double*>(xi.im), p.ell1, t.m1, p.ell2, t.m2, bd,
+            dnp, drs, dxi);
+      else
+        launch_shotnoise_3pcf_bins<float>(
+            ctx, g, static_cast<const float*>(xi.re),
+            static_cast<const float*>(xi.im), p.ell1, t.m1, p.ell2, t.m2, bd,
+            dnp, drs, dxi);
       vector<long long> np = download(dnp, hb.nb);
       vector<double> rs = download(drs, hb.nb), xs = download(dxi, 2 * hb.nb);
       vector<cplx> xib(hb.nb);
@@ -1097,7 +1157,7 @@ struct Engine {
       // Raw 3PCF with j_l(k r)-weighted transforms (field.cpp:1908-2010).
       Leg la{p.ell1, t.m1, true, sja}, lb{p.ell2, t.m2, true, sjb};
       const vector<cplx> comp =
-          pair_sums(dn, G, la, lb, pairs, hb, reff, M, K);
+          pair_sums(dn, dnLM, la, lb, pairs, hb, reff, M, K, K);
       for (int i = 0; i < ndv; ++i)
         zeta[i] += t.coupling * g.vol_cell * phase *
                    (comp[i] + mirror * std::conj(comp[i]));

@@ -115,6 +115,9 @@ struct Context {
   int pruned_grid[3] = {0, 0, 0};
   // Options.
   bool full_mesh_shells = false;  // evaluate shell fields on the full mesh
+  // FP32-mixed precision choices: shot-noise field / shell fields in FP64.
+  bool shotnoise_fp64 = false;
+  bool shell_fields_fp64 = false;
   // Profiling: per-launch events of the current call, per-name totals of
   // the last call.
   bool profiling = false;

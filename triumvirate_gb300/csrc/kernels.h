@@ -106,24 +106,26 @@ void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
                         const BinsDev& bins, long long* nmodes,
                         double* ksum);
 
-template <class Real>
+// Field builders read spectra of precision Real and write evaluation-grid
+// fields of precision FR.
+template <class Real, class FR>
 void launch_build_G(Context& ctx, const Geom& g, const int M[3],
                     const int Kg[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax,
-                    typename CplxOf<Real>::type* out);
+                    typename CplxOf<FR>::type* out);
 
-template <class Real>
+template <class Real, class FR>
 void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const int K[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
-                    double hi_max, typename CplxOf<Real>::type* out);
+                    double hi_max, typename CplxOf<FR>::type* out);
 
-template <class Real>
+template <class Real, class FR>
 void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const AxisTablesDev& ax, int ell, int m,
                         const SplineTable& sj, const double* radii, int nb,
-                        typename CplxOf<Real>::type* out);
+                        typename CplxOf<FR>::type* out);
 
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
@@ -132,13 +134,13 @@ void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const BinsDev& bins, long long* nmodes, double* ksum,
                         double* pk, double* sn);
 
-// The shot-noise field spectrum is formed and transformed in FP64 at every
-// precision (it is a difference of nearly equal quantities).
-template <class Real>
+// The shot-noise field spectrum, written in precision XR for its C2R.
+template <class Real, class XR>
 void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         const FieldSpec<Real>& fb, cd shot,
-                        const AxisTablesDev& ax, double2* out_re,
-                        double2* out_im);
+                        const AxisTablesDev& ax,
+                        typename CplxOf<XR>::type* out_re,
+                        typename CplxOf<XR>::type* out_im);
 
 // ---- reduce.cu -----------------------------------------------------------
 template <class Real>

@@ -146,12 +146,24 @@ SplineHost::SplineHost(int ell_) : ell(ell_) {
     c[m] = dp[m - 1];
     for (int q = m - 2; q >= 0; --q) c[q + 1] = dp[q] - cp[q] * c[q + 2];
   }
+  // Interval polynomials: b_i = (y_{i+1} - y_i)/h - h (c_{i+1} + 2 c_i)/3,
+  // d_i = (c_{i+1} - c_i) / (3 h), with h the node spacing of interval i.
+  b.assign(n, 0.);
+  d.assign(n, 0.);
+  for (int i = 0; i + 1 < n; ++i) {
+    const double hh = (xmin + dx * (i + 1)) - (xmin + dx * i);
+    b[i] = (y[i + 1] - y[i]) / hh - hh * (c[i + 1] + 2.0 * c[i]) / 3.0;
+    d[i] = (c[i + 1] - c[i]) / (3.0 * hh);
+  }
 }
 
-SplineTable SplineHost::table(const double* dy, const double* dc) const {
+SplineTable SplineHost::table(const double* dy, const double* db,
+                              const double* dc, const double* dd) const {
   SplineTable t;
   t.y = dy;
+  t.b = db;
   t.c = dc;
+  t.d = dd;
   t.n = int(y.size());
   t.ell = ell;
   t.split = split;

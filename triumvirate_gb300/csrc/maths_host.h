@@ -19,10 +19,11 @@ constexpr double kEpsCoupling = 1.e-9;   // maths.cpp:165
 struct SplineHost {
   int ell;
   double split;
-  std::vector<double> y, c;
+  std::vector<double> y, b, c, d;
   explicit SplineHost(int ell);
-  // Table view over device (or host) copies of y and c.
-  SplineTable table(const double* dy, const double* dc) const;
+  // Table view over device (or host) copies of y, b, c and d.
+  SplineTable table(const double* dy, const double* db, const double* dc,
+                    const double* dd) const;
 };
 
 }  // namespace trvg

@@ -126,29 +126,103 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
   }
 }
 
+// The same sums with every cell of a mirror orbit handled by one thread:
+// for even mesh numbers the cells (+-s_x, +-s_y, +-s_z) -- and, when
+// n_x = n_y, their x <-> y swaps -- share one key, so one thread adds up
+// to 16 cells and issues one atomic.  Reads stay coalesced along z.
+template <class Real>
+__global__ void __launch_bounds__(256)
+radial_hist_orbit_kernel(Geom g, const Real* xi_re, const Real* xi_im,
+                         int ell_a, int m_a, int ell_b, int m_b, bool swap,
+                         double* hist) {
+  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+  const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
+  const int64_t nzc = hz + 1;
+  const int64_t count = int64_t(hx + 1) * (hy + 1) * nzc;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(t % nzc);
+    const int b = int((t / nzc) % (hy + 1));
+    const int a = int(t / (nzc * (hy + 1)));
+    if (swap && b > a) continue;
+    const int xs[2] = {a, (g.n[0] - a) % g.n[0]};
+    const int ys[2] = {b, (g.n[1] - b) % g.n[1]};
+    const int zs[2] = {c, (g.n[2] - c) % g.n[2]};
+    const int nxs = (xs[1] == xs[0]) ? 1 : 2;
+    const int nys = (ys[1] == ys[0]) ? 1 : 2;
+    const int nzs = (zs[1] == zs[0]) ? 1 : 2;
+    cd acc = {0., 0.};
+    const int nsw = (swap && a != b) ? 2 : 1;
+    for (int w = 0; w < nsw; ++w) {
+      for (int p = 0; p < nxs; ++p) {
+        for (int q = 0; q < nys; ++q) {
+          const int i = (w == 0) ? xs[p] : ys[q];
+          const int j = (w == 0) ? ys[q] : xs[p];
+          const int64_t row = (int64_t(i) * g.n[1] + j) * g.n[2];
+          for (int r = 0; r < nzs; ++r) {
+            const int k = zs[r];
+            cd v = {double(xi_re[row + k]),
+                    xi_im != nullptr ? double(xi_im[row + k]) : 0.};
+            if (!trivial) {
+              const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
+              const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
+              const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
+              v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
+                       reduced_ylm(ell_b, m_b, rx, ry, rz));
+            }
+            acc = acc + v;
+          }
+        }
+      }
+    }
+    const int64_t key = int64_t(a) * a + int64_t(b) * b + int64_t(c) * c;
+    atomicAdd(hist + 2 * key, acc.re);
+    if (acc.im != 0.) atomicAdd(hist + 2 * key + 1, acc.im);
+  }
+}
+
 struct PairBesselArgs {
   SplineTable ja, jb;
   const double* ka;
   const double* kb;
 };
 
+constexpr int kKeyPairChunk = 8;
+
+// One thread per key: r = dr sqrt(key) once, then the Bessel weights of a
+// chunk of pairs (one spline evaluation when both legs coincide).
 __global__ void __launch_bounds__(256)
 pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* hist,
-                        PairBesselArgs a, double* out) {
-  __shared__ double red[2 * 32];
-  const int p = blockIdx.y;
-  const double ka = a.ka[p], kb = a.kb[p];
-  double acc[2] = {0., 0.};
+                        PairBesselArgs a, int npairs, bool same_leg,
+                        double* out) {
+  __shared__ double red[2 * kKeyPairChunk * 32];
+  const int p0 = blockIdx.y * kKeyPairChunk;
+  double ka[kKeyPairChunk], kb[kKeyPairChunk];
+#pragma unroll
+  for (int q = 0; q < kKeyPairChunk; ++q) {
+    const int pi = min(p0 + q, npairs - 1);
+    ka[q] = a.ka[pi];
+    kb[q] = a.kb[pi];
+  }
+  double acc[2 * kKeyPairChunk];
+#pragma unroll
+  for (int q = 0; q < 2 * kKeyPairChunk; ++q) acc[q] = 0.;
   for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
     const double hr = hist[2 * key], hi = hist[2 * key + 1];
     if (hr == 0. && hi == 0.) continue;
     const double r = dr * sqrt(double(key));
-    const double w = spline_eval(a.ja, ka * r) * spline_eval(a.jb, kb * r);
-    acc[0] += w * hr;
-    acc[1] += w * hi;
+#pragma unroll
+    for (int q = 0; q < kKeyPairChunk; ++q) {
+      const double ja = spline_eval(a.ja, ka[q] * r);
+      const double jb = (same_leg && ka[q] == kb[q])
+                            ? ja : spline_eval(a.jb, kb[q] * r);
+      const double w = ja * jb;
+      acc[2 * q] += w * hr;
+      acc[2 * q + 1] += w * hi;
+    }
   }
-  block_add<2>(acc, out + 2 * p, red);
+  block_add<2 * kKeyPairChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
 }
 
 constexpr int kBesselChunk = 4;
@@ -263,6 +337,19 @@ template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                         const Real* xi_im, int ell_a, int m_a, int ell_b,
                         int m_b, double* hist) {
+  const bool even = (g.n[0] % 2 == 0) && (g.n[1] % 2 == 0) &&
+                    (g.n[2] % 2 == 0);
+  if (even) {
+    const bool swap = g.n[0] == g.n[1];
+    const int64_t count =
+        int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) * (g.n[2] / 2 + 1);
+    TRVG_KBEGIN(ctx, "radial_hist_kernel");
+    radial_hist_orbit_kernel<Real><<<grid_for(count, 256), 256, 0,
+                                     ctx.stream>>>(
+        g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
+    TRVG_LAUNCHED(ctx);
+    return;
+  }
   TRVG_KBEGIN(ctx, "radial_hist_kernel");
   radial_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
       g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, hist);
@@ -275,10 +362,12 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* kb, int npairs, double* out) {
   if (npairs <= 0) return;
   PairBesselArgs a{sja, sjb, ka, kb};
-  dim3 grid(grid_for(nkeys, 256, 64), npairs);
+  const bool same_leg = sja.ell == sjb.ell;
+  const int chunks = (npairs + kKeyPairChunk - 1) / kKeyPairChunk;
+  dim3 grid(grid_for(nkeys, 256, 152 * 2), chunks);
   TRVG_KBEGIN(ctx, "pair_bessel_sums_kernel");
-  pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(nkeys, g.dr[0], hist,
-                                                        a, out);
+  pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(
+      nkeys, g.dr[0], hist, a, npairs, same_leg, out);
   TRVG_LAUNCHED(ctx);
 }
 

@@ -152,12 +152,12 @@ __global__ void count_modes_kernel(Geom g, Cube cube, BinsDev bins,
 
 // G on the evaluation grid: dn(k) / W(k) / V for |s| <= Kg on pruned axes,
 // every mode on dense axes (G_LM: threept.cpp:1665-1670, field.cpp:1657-1785).
-template <class Real>
+template <class Real, class FR>
 __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
                                int Kg1, int Kg2, FieldSpec<Real> f,
                                AxisTablesDev ax,
-                               typename CplxOf<Real>::type* out) {
-  using C = typename CplxOf<Real>::type;
+                               typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
   const int64_t count = int64_t(M0) * M1 * M2;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
        t += int64_t(gridDim.x) * blockDim.x) {
@@ -178,8 +178,8 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
       const cd v = field_value(f, g, i, j, k);
       const double w = window_pow(ax, i, j, k);
       const cd r = cdivr(cdivr(v, w), g.vol);
-      o.x = Real(r.re);
-      o.y = Real(r.im);
+      o.x = FR(r.re);
+      o.y = FR(r.im);
     }
     out[t] = o;
   }
@@ -188,13 +188,13 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
 // Shell-filtered spectra y_lm(k) f(k) / W(k), one per bin, on the
 // evaluation grid (field.cpp:1812-1847).  The 1/nmodes of the reference is
 // applied to the reduced sums instead of the fields.
-template <class Real>
+template <class Real, class FR>
 __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
                                int K2, FieldSpec<Real> f, AxisTablesDev ax,
                                int ell, int m, const double* lo,
                                const double* hi, int nb, double hi_max,
-                               typename CplxOf<Real>::type* out) {
-  using C = typename CplxOf<Real>::type;
+                               typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
   const int64_t count = int64_t(M0) * M1 * M2;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
        t += int64_t(gridDim.x) * blockDim.x) {
@@ -225,8 +225,8 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
     for (int q = 0; q < nb; ++q) {
       C o;
       const bool sel = in && (lo[q] <= k) && (k < hi[q]);
-      o.x = sel ? Real(val.re) : Real(0);
-      o.y = sel ? Real(val.im) : Real(0);
+      o.x = sel ? FR(val.re) : FR(0);
+      o.y = sel ? FR(val.im) : FR(0);
       out[int64_t(q) * count + t] = o;
     }
   }
@@ -240,12 +240,12 @@ struct SjlArgs {
 
 // j_l(k r) y_lm(k) f(k) / W(k) / V on the full mesh, one per radius
 // (field.cpp:1908-2010).
-template <class Real>
+template <class Real, class FR>
 __global__ void build_F_sjl_kernel(Geom g, FieldSpec<Real> f,
                                    AxisTablesDev ax, int ell, int m,
                                    SjlArgs sa,
-                                   typename CplxOf<Real>::type* out) {
-  using C = typename CplxOf<Real>::type;
+                                   typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
   const int64_t count = g.nmesh;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
        t += int64_t(gridDim.x) * blockDim.x) {
@@ -263,8 +263,8 @@ __global__ void build_F_sjl_kernel(Geom g, FieldSpec<Real> f,
     for (int q = 0; q < sa.nb; ++q) {
       const double jl = spline_eval(sa.sj, k * sa.radii[q]);
       C o;
-      o.x = Real(jl * val.re / g.vol);
-      o.y = Real(jl * val.im / g.vol);
+      o.x = FR(jl * val.re / g.vol);
+      o.y = FR(jl * val.im / g.vol);
       out[int64_t(q) * count + t] = o;
     }
   }
@@ -353,9 +353,11 @@ __global__ void twopt_stats_kernel(Geom g, Cube cube, FieldSpec<Real> fa,
 }
 
 // Shot-noise two-point field spectrum (fa fb^* / win_pk - S C_1 / win_sn) / V
-// (field.cpp:3273-3298) on the half-spectrum grid.  When `out_im` is given
-// the spectrum is split into its Hermitian parts so that both halves
-// transform with C2R: P = H_re + i H_im.
+// (field.cpp:3273-3298) on the half-spectrum grid.  Without interlacing
+// win_pk = win_sn = C_1, so the mode is fa fb^* / C_1 - S, formed with the
+// reciprocal tables (no division).  When `out_im` is given the spectrum is
+// split into its Hermitian parts so that both halves transform with C2R:
+// P = H_re + i H_im.
 template <class Real>
 __device__ __forceinline__ cd twopt_mode(const Geom& g, const FieldSpec<Real>& fa,
                                          const FieldSpec<Real>& fb, cd shot,
@@ -363,26 +365,26 @@ __device__ __forceinline__ cd twopt_mode(const Geom& g, const FieldSpec<Real>& f
                                          int j, int k) {
   const cd va = field_value(fa, g, i, j, k);
   const cd vb = field_value(fb, g, i, j, k);
-  const double al = alias_sn(ax, i, j, k);
-  double win_pk, win_sn;
-  if (ax.interlace) {
-    const double w = window_pow(ax, i, j, k);
-    win_pk = w * w;
-    win_sn = win_pk;
-  } else {
-    win_pk = al;
-    win_sn = al;
+  const cd pr = va * conjg(vb);
+  if (!ax.interlace) {
+    const double inv = ax.t.inv_alias[0][i] * ax.t.inv_alias[1][j] *
+                       ax.t.inv_alias[2][k];
+    return cd{pr.re * inv - shot.re, pr.im * inv - shot.im};
   }
-  const cd p = cdivr(va * conjg(vb), win_pk) - cdivr(al * shot, win_sn);
-  return cdivr(p, g.vol);
+  const double al = alias_sn(ax, i, j, k);
+  const double w = window_pow(ax, i, j, k);
+  const double win = w * w;
+  return cdivr(pr, win) - cdivr(al * shot, win);
 }
 
-template <class Real>
+template <class Real, class XR>
 __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
                                    FieldSpec<Real> fb, cd shot,
-                                   AxisTablesDev ax, double2* out_re,
-                                   double2* out_im) {
-  using C = double2;
+                                   AxisTablesDev ax,
+                                   typename CplxOf<XR>::type* out_re,
+                                   typename CplxOf<XR>::type* out_im) {
+  using C = typename CplxOf<XR>::type;
+  const double inv_vol = 1. / g.vol;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        t < g.nhalf; t += int64_t(gridDim.x) * blockDim.x) {
     const int k = int(t % g.nzh);
@@ -391,8 +393,8 @@ __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
     const cd p = twopt_mode(g, fa, fb, shot, ax, i, j, k);
     C o;
     if (out_im == nullptr) {
-      o.x = p.re;
-      o.y = p.im;
+      o.x = XR(p.re * inv_vol);
+      o.y = XR(p.im * inv_vol);
       out_re[t] = o;
     } else {
       const int ii = (i == 0) ? 0 : g.n[0] - i;
@@ -400,12 +402,13 @@ __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
       const int kk = (k == 0) ? 0 : g.n[2] - k;
       const cd q = conjg(twopt_mode(g, fa, fb, shot, ax, ii, jj, kk));
       const cd s = p + q, d = p - q;
-      o.x = s.re / 2.;
-      o.y = s.im / 2.;
+      const double h = 0.5 * inv_vol;
+      o.x = XR(s.re * h);
+      o.y = XR(s.im * h);
       out_re[t] = o;
       C oi;
-      oi.x = d.im / 2.;
-      oi.y = -d.re / 2.;
+      oi.x = XR(d.im * h);
+      oi.y = XR(-d.re * h);
       out_im[t] = oi;
     }
   }
@@ -423,40 +426,40 @@ void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
   TRVG_LAUNCHED(ctx);
 }
 
-template <class Real>
+template <class Real, class FR>
 void launch_build_G(Context& ctx, const Geom& g, const int M[3],
                     const int Kg[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax,
-                    typename CplxOf<Real>::type* out) {
+                    typename CplxOf<FR>::type* out) {
   const int64_t count = int64_t(M[0]) * M[1] * M[2];
   TRVG_KBEGIN(ctx, "build_G_kernel");
-  build_G_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+  build_G_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, ax, out);
   TRVG_LAUNCHED(ctx);
 }
 
-template <class Real>
+template <class Real, class FR>
 void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const int K[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
-                    double hi_max, typename CplxOf<Real>::type* out) {
+                    double hi_max, typename CplxOf<FR>::type* out) {
   const int64_t count = int64_t(M[0]) * M[1] * M[2];
   TRVG_KBEGIN(ctx, "build_F_kernel");
-  build_F_kernel<Real><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+  build_F_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
       hi_max, out);
   TRVG_LAUNCHED(ctx);
 }
 
-template <class Real>
+template <class Real, class FR>
 void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const AxisTablesDev& ax, int ell, int m,
                         const SplineTable& sj, const double* radii, int nb,
-                        typename CplxOf<Real>::type* out) {
+                        typename CplxOf<FR>::type* out) {
   SjlArgs sa{sj, radii, nb};
   TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
-  build_F_sjl_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+  build_F_sjl_kernel<Real, FR><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
       g, f, ax, ell, m, sa, out);
   TRVG_LAUNCHED(ctx);
 }
@@ -475,40 +478,42 @@ void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
   TRVG_LAUNCHED(ctx);
 }
 
-template <class Real>
+template <class Real, class XR>
 void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         const FieldSpec<Real>& fb, cd shot,
-                        const AxisTablesDev& ax, double2* out_re,
-                        double2* out_im) {
+                        const AxisTablesDev& ax,
+                        typename CplxOf<XR>::type* out_re,
+                        typename CplxOf<XR>::type* out_im) {
   TRVG_KBEGIN(ctx, "twopt_field_kernel");
-  twopt_field_kernel<Real><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+  twopt_field_kernel<Real, XR><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
       g, fa, fb, shot, ax, out_re, out_im);
   TRVG_LAUNCHED(ctx);
 }
 
+#define TRVG_INST2(R, F)                                                     \
+  template void launch_build_G<R, F>(Context&, const Geom&, const int*,      \
+                                     const int*, const FieldSpec<R>&,        \
+                                     const AxisTablesDev&, CplxOf<F>::type*);\
+  template void launch_build_F<R, F>(                                        \
+      Context&, const Geom&, const int*, const int*, const FieldSpec<R>&,    \
+      const AxisTablesDev&, int, int, const double*, const double*, int,     \
+      double, CplxOf<F>::type*);                                             \
+  template void launch_build_F_sjl<R, F>(                                    \
+      Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
+      int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
+  template void launch_twopt_field<R, F>(                                    \
+      Context&, const Geom&, const FieldSpec<R>&, const FieldSpec<R>&, cd,   \
+      const AxisTablesDev&, CplxOf<F>::type*, CplxOf<F>::type*);
+TRVG_INST2(float, float)
+TRVG_INST2(float, double)
+TRVG_INST2(double, double)
+#undef TRVG_INST2
+
 #define TRVG_INST(R)                                                         \
-  template void launch_build_G<R>(Context&, const Geom&, const int*,         \
-                                  const int*, const FieldSpec<R>&,           \
-                                  const AxisTablesDev&, CplxOf<R>::type*);   \
-  template void launch_build_F<R>(Context&, const Geom&, const int*,         \
-                                  const int*, const FieldSpec<R>&,           \
-                                  const AxisTablesDev&, int, int,            \
-                                  const double*, const double*, int, double, \
-                                  CplxOf<R>::type*);                         \
-  template void launch_build_F_sjl<R>(Context&, const Geom&,                 \
-                                      const FieldSpec<R>&,                   \
-                                      const AxisTablesDev&, int, int,        \
-                                      const SplineTable&, const double*,     \
-                                      int, CplxOf<R>::type*);                \
   template void launch_twopt_stats<R>(                                       \
       Context&, const Geom&, const Cube&, const FieldSpec<R>&,               \
       const FieldSpec<R>&, cd, int, int, const AxisTablesDev&,               \
-      const BinsDev&, long long*, double*, double*, double*);                \
-  template void launch_twopt_field<R>(Context&, const Geom&,                 \
-                                      const FieldSpec<R>&,                   \
-                                      const FieldSpec<R>&, cd,               \
-                                      const AxisTablesDev&, double2*,        \
-                                      double2*);
+      const BinsDev&, long long*, double*, double*, double*);
 TRVG_INST(float)
 TRVG_INST(double)
 #undef TRVG_INST
