@@ -177,22 +177,26 @@ def ncu_traffic(kernel):
 
 
 def algorithmic_bytes(kernel, args, real_bytes):
-    """Compulsory HBM bytes of one launch of `kernel` on the workload."""
+    """Compulsory HBM bytes of one launch of `kernel` on the FP32-mixed
+    workload (every input read once, every output written once)."""
     nm = args.ngrid ** 3
     nh = args.ngrid * args.ngrid * (args.ngrid // 2 + 1)
-    if kernel == 'assign_kernel':
-        # x, y, z read once; every mesh cell written once.
-        return 24 * args.npart + real_bytes * nm
-    if kernel == 'twopt_field_kernel':
-        # FP32 half spectrum read, FP64 half spectrum written.
-        return 2 * real_bytes * nh + 16 * nh
-    if kernel == 'radial_hist_kernel':
-        return 8 * nm          # FP64 shot-noise field read once
-    if kernel == 'cufft.r2c.mesh':
-        return real_bytes * nm + 2 * real_bytes * nh
-    if kernel == 'cufft.c2r.xi':
-        return 16 * nh + 8 * nm
-    return None
+    c = 2 * real_bytes          # complex value
+    table = {
+        # x, y, z read; every mesh cell written once.
+        'assign_kernel': 24 * args.npart + real_bytes * nm,
+        # x, y, z read; tile key and rank written.
+        'tile_key_kernel': 32 * args.npart,
+        # x, y, z, key, rank read; sorted x, y, z written.
+        'scatter_kernel': 56 * args.npart,
+        # half spectrum read, shot-noise half spectrum written.
+        'twopt_field_kernel': 2 * c * nh,
+        # shot-noise field read once.
+        'radial_hist_kernel': real_bytes * nm,
+        'cufft.r2c.mesh': real_bytes * nm + c * nh,
+        'cufft.c2r.xi': c * nh + real_bytes * nm,
+    }
+    return table.get(kernel)
 
 
 def run_gb300(args):

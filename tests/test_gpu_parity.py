@@ -481,3 +481,33 @@ def test_fp32mixed_precision_options(shell64, shot64):
         ctx.set_option('shell_fields_fp64', 0)
         ctx.set_option('shotnoise_fp64', 0)
     assert_close_threept(res, ref, 'bispec', 'fp32mixed')
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_oracle_gpp_sorted_catalogue(precision):
+    """Catalogues of >= 65536 particles are tile-sorted on the device before
+    assignment; the result must not change."""
+    box, n, ngrid = 900., 100000, 32
+    pos = _uniform(n, box, seed=77)
+    bins = (0.01, 0.1, 4)
+    ref = _oracle_gpp('bispec', pos, box, ngrid, 'pcs', (0, 0, 0), 'diag',
+                      None, bins)
+    res = compute_bispec_in_gpp_box(
+        ParticleCatalogue(*pos.T, nz=n / box ** 3), degrees=(0, 0, 0),
+        binning=Binning('fourier', 'lin', *bins), form='diag',
+        sampling_params=_sampling(precision, ngrid, 'pcs', box=box))
+    assert_close_threept(res, ref, 'bispec', precision)
+
+
+def test_oracle_lpp_sorted_randoms():
+    d, r, wd, wr = _survey_inputs(2000, 80000, seed=78)
+    bins = (0.01, 0.1, 3)
+    ref = _oracle_survey('bispec', d, r, wd, wr, 1000., 32, 'tsc', (2, 0, 2),
+                         'diag', None, bins)
+    res = compute_bispec(ParticleCatalogue(*d.T, nz=1e-4, wc=wd),
+                         ParticleCatalogue(*r.T, nz=1e-4, wc=wr),
+                         degrees=(2, 0, 2),
+                         binning=Binning('fourier', 'lin', *bins), form='diag',
+                         sampling_params=_sampling('fp64', 32, 'tsc',
+                                                   box=1000.))
+    assert_close_threept(res, ref, 'bispec', 'fp64')

@@ -298,6 +298,7 @@ struct Engine {
   trvg_params p;
   Geom g;
   AxisTablesDev ax;
+  const float* inv_alias_f[3] = {nullptr, nullptr, nullptr};
   bool interlace;
 
   Engine(Context& c, const trvg_params& prm, bool allow_interlace)
@@ -369,6 +370,12 @@ struct Engine {
         host[size_t(4 * a + 3) * nmax + i] = 1. / al;
       }
     }
+    vector<float> hf(size_t(3) * nmax, 0.f);
+    for (int a = 0; a < 3; ++a)
+      for (int i = 0; i < g.n[a]; ++i)
+        hf[size_t(a) * nmax + i] = float(host[size_t(4 * a + 3) * nmax + i]);
+    const float* df = upload("axis_tables_f", hf);
+    for (int a = 0; a < 3; ++a) inv_alias_f[a] = df + size_t(a) * nmax;
     double* d = upload("axis_tables", host);
     for (int a = 0; a < 3; ++a) {
       ax.t.sinc[a] = d + size_t(4 * a + 0) * nmax;
@@ -399,10 +406,12 @@ struct Engine {
       d.y = c->y;
       d.z = c->z;
       d.w = c->w;
-      d.lx = c->los_x;
-      d.ly = c->los_y;
-      d.lz = c->los_z;
-      return d;
+      if (need_los) {
+        d.lx = c->los_x;
+        d.ly = c->los_y;
+        d.lz = c->los_z;
+      }
+      return spatially_sorted(d, tag);
     }
     if (c->memory != TRVG_MEM_HOST)
       throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown memory kind %d.",
@@ -424,7 +433,13 @@ struct Engine {
       d.ly = put(c->los_y, ".ly");
       d.lz = put(c->los_z, ".lz");
     }
-    return d;
+    return spatially_sorted(d, tag);
+  }
+
+  // Large catalogues are reordered by mesh tile before assignment.
+  DevCatalogue spatially_sorted(const DevCatalogue& d, const std::string& tag) {
+    if (d.n < (int64_t(1) << 16)) return d;
+    return sort_catalogue(ctx, g, d, tag);
   }
 
   // Assign all parts into one (complex if `cplx`) mesh, with the shadow when
@@ -589,8 +604,25 @@ struct Engine {
                            shot.imag() == 0.;
     XC* hre = ctx.buf<XC>("xi.h.re", size_t(g.nhalf));
     XC* him = hermitian ? nullptr : ctx.buf<XC>("xi.h.im", size_t(g.nhalf));
-    launch_twopt_field<Real, XR>(ctx, g, fa, fb, cd{shot.real(), shot.imag()},
-                                 ax, hre, him);
+    const bool fast = sizeof(Real) == 4 && sizeof(XR) == 4 && hermitian &&
+                      !interlace && fa.re_s == nullptr && fb.re_s == nullptr &&
+                      fa.k0_set && fb.k0_set;
+    if (fast) {
+      // k = 0 mode in FP64: (fa fb^* / C_1(0) - S) / V with C_1(0) = 1.
+      const cplx a0(fa.k0.re, fa.k0.im), b0(fb.k0.re, fb.k0.im);
+      const cplx p0 = (a0 * std::conj(b0) - shot) / g.vol;
+      float2 p0f;
+      p0f.x = float(p0.real());
+      p0f.y = float(p0.imag());
+      launch_twopt_field_real_f32(
+          ctx, g, reinterpret_cast<const float2*>(fa.re),
+          reinterpret_cast<const float2*>(fb.re), inv_alias_f,
+          float(shot.real()), p0f, reinterpret_cast<float2*>(hre));
+    } else {
+      launch_twopt_field<Real, XR>(ctx, g, fa, fb,
+                                   cd{shot.real(), shot.imag()}, ax, hre,
+                                   him);
+    }
     cufftHandle h = ctx.plan(FFT<XR>::kC2R, g.n, 1);
     Xi xi;
     xi.dbl = sizeof(XR) == 8;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -92,6 +93,11 @@ template <class Real>
 void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
                            double scale, double* out);
 
+// ---- sort.cu -------------------------------------------------------------
+// Copy of `in` ordered by 8^3-cell mesh tile (device buffers named by tag).
+DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
+                            const std::string& tag);
+
 // ---- spectral.cu ---------------------------------------------------------
 // Mode cube: frequencies s in [-K, K] per axis, or the whole axis when
 // dense[ax].
@@ -141,6 +147,13 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         const AxisTablesDev& ax,
                         typename CplxOf<XR>::type* out_re,
                         typename CplxOf<XR>::type* out_im);
+
+// FP32 fast path of the shot-noise field spectrum for two real-mesh spectra
+// without interlacing; `p0` is the exact k = 0 mode (already / V).
+void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
+                                 const float2* fa, const float2* fb,
+                                 const float* const inv_alias[3], float shot,
+                                 float2 p0, float2* out);
 
 // ---- reduce.cu -----------------------------------------------------------
 template <class Real>

@@ -11,6 +11,8 @@
 //  * pair_bessel_direct: the same sum evaluated cell by cell (any cells).
 //  * shotnoise_3pcf_bins: r-binned sums of the 3PCF shot noise
 //    (field.cpp:3090-3196) with exact per-cell separations.
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace trvg {
@@ -129,53 +131,65 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
 // The same sums with every cell of a mirror orbit handled by one thread:
 // for even mesh numbers the cells (+-s_x, +-s_y, +-s_z) -- and, when
 // n_x = n_y, their x <-> y swaps -- share one key, so one thread adds up
-// to 16 cells and issues one atomic.  Reads stay coalesced along z.
+// to 16 cells and issues one atomic.  One block per (|s_x|, |s_y|) pair
+// (|s_y| <= |s_x| with the swap), threads along z; reads stay coalesced.
 template <class Real>
 __global__ void __launch_bounds__(256)
 radial_hist_orbit_kernel(Geom g, const Real* xi_re, const Real* xi_im,
                          int ell_a, int m_a, int ell_b, int m_b, bool swap,
                          double* hist) {
   const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
-  const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
-  const int64_t nzc = hz + 1;
-  const int64_t count = int64_t(hx + 1) * (hy + 1) * nzc;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int c = int(t % nzc);
-    const int b = int((t / nzc) % (hy + 1));
-    const int a = int(t / (nzc * (hy + 1)));
-    if (swap && b > a) continue;
-    const int xs[2] = {a, (g.n[0] - a) % g.n[0]};
-    const int ys[2] = {b, (g.n[1] - b) % g.n[1]};
+  const int hy = g.n[1] / 2, hz = g.n[2] / 2;
+  int a, b;
+  const int q = blockIdx.x;
+  if (swap) {
+    // Triangular index q = a (a + 1) / 2 + b, 0 <= b <= a.
+    a = int((sqrtf(8.f * float(q) + 1.f) - 1.f) * 0.5f);
+    while ((a + 1) * (a + 2) / 2 <= q) ++a;
+    while (a * (a + 1) / 2 > q) --a;
+    b = q - a * (a + 1) / 2;
+  } else {
+    a = q / (hy + 1);
+    b = q - a * (hy + 1);
+  }
+  const int xs[2] = {a, (g.n[0] - a) % g.n[0]};
+  const int ys[2] = {b, (g.n[1] - b) % g.n[1]};
+  const int nxs = (xs[1] == xs[0]) ? 1 : 2;
+  const int nys = (ys[1] == ys[0]) ? 1 : 2;
+  const int nsw = (swap && a != b) ? 2 : 1;
+  const int64_t key0 = int64_t(a) * a + int64_t(b) * b;
+  for (int c = threadIdx.x; c <= hz; c += blockDim.x) {
     const int zs[2] = {c, (g.n[2] - c) % g.n[2]};
-    const int nxs = (xs[1] == xs[0]) ? 1 : 2;
-    const int nys = (ys[1] == ys[0]) ? 1 : 2;
     const int nzs = (zs[1] == zs[0]) ? 1 : 2;
+    Real sr = Real(0), si = Real(0);
     cd acc = {0., 0.};
-    const int nsw = (swap && a != b) ? 2 : 1;
     for (int w = 0; w < nsw; ++w) {
       for (int p = 0; p < nxs; ++p) {
-        for (int q = 0; q < nys; ++q) {
-          const int i = (w == 0) ? xs[p] : ys[q];
-          const int j = (w == 0) ? ys[q] : xs[p];
+        for (int qq = 0; qq < nys; ++qq) {
+          const int i = (w == 0) ? xs[p] : ys[qq];
+          const int j = (w == 0) ? ys[qq] : xs[p];
           const int64_t row = (int64_t(i) * g.n[1] + j) * g.n[2];
           for (int r = 0; r < nzs; ++r) {
             const int k = zs[r];
-            cd v = {double(xi_re[row + k]),
-                    xi_im != nullptr ? double(xi_im[row + k]) : 0.};
-            if (!trivial) {
+            if (trivial) {
+              sr += xi_re[row + k];
+              if (xi_im != nullptr) si += xi_im[row + k];
+            } else {
+              cd v = {double(xi_re[row + k]),
+                      xi_im != nullptr ? double(xi_im[row + k]) : 0.};
               const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
               const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
               const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
               v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
                        reduced_ylm(ell_b, m_b, rx, ry, rz));
+              acc = acc + v;
             }
-            acc = acc + v;
           }
         }
       }
     }
-    const int64_t key = int64_t(a) * a + int64_t(b) * b + int64_t(c) * c;
+    if (trivial) acc = cd{double(sr), double(si)};
+    const int64_t key = key0 + int64_t(c) * c;
     atomicAdd(hist + 2 * key, acc.re);
     if (acc.im != 0.) atomicAdd(hist + 2 * key + 1, acc.im);
   }
@@ -341,11 +355,12 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                     (g.n[2] % 2 == 0);
   if (even) {
     const bool swap = g.n[0] == g.n[1];
-    const int64_t count =
-        int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) * (g.n[2] / 2 + 1);
+    const int hx = g.n[0] / 2, hy = g.n[1] / 2;
+    const int nblocks =
+        swap ? (hx + 1) * (hx + 2) / 2 : (hx + 1) * (hy + 1);
+    const int threads = std::min(256, ((g.n[2] / 2 + 1 + 31) / 32) * 32);
     TRVG_KBEGIN(ctx, "radial_hist_kernel");
-    radial_hist_orbit_kernel<Real><<<grid_for(count, 256), 256, 0,
-                                     ctx.stream>>>(
+    radial_hist_orbit_kernel<Real><<<nblocks, threads, 0, ctx.stream>>>(
         g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
     TRVG_LAUNCHED(ctx);
     return;

@@ -158,12 +158,10 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
                                AxisTablesDev ax,
                                typename CplxOf<FR>::type* out) {
   using C = typename CplxOf<FR>::type;
-  const int64_t count = int64_t(M0) * M1 * M2;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int c = int(t % M2);
-    const int b = int((t / M2) % M1);
-    const int a = int(t / (int64_t(M2) * M1));
+  const int row = blockIdx.x;
+  const int a = row / M1, b = row - (row / M1) * M1;
+  for (int c = threadIdx.x; c < M2; c += blockDim.x) {
+    const int64_t t = int64_t(row) * M2 + c;
     const int sx = shift_index(a, M0), sy = shift_index(b, M1),
               sz = shift_index(c, M2);
     const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
@@ -196,11 +194,10 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
                                typename CplxOf<FR>::type* out) {
   using C = typename CplxOf<FR>::type;
   const int64_t count = int64_t(M0) * M1 * M2;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int c = int(t % M2);
-    const int b = int((t / M2) % M1);
-    const int a = int(t / (int64_t(M2) * M1));
+  const int row = blockIdx.x;
+  const int a = row / M1, b = row - (row / M1) * M1;
+  for (int c = threadIdx.x; c < M2; c += blockDim.x) {
+    const int64_t t = int64_t(row) * M2 + c;
     const int sx = shift_index(a, M0), sy = shift_index(b, M1),
               sz = shift_index(c, M2);
     const bool in = (M0 == g.n[0] || abs(sx) <= K0) &&
@@ -377,19 +374,18 @@ __device__ __forceinline__ cd twopt_mode(const Geom& g, const FieldSpec<Real>& f
   return cdivr(pr, win) - cdivr(al * shot, win);
 }
 
+// One block per (i, j) row of the half spectrum; threads run along k.
 template <class Real, class XR>
-__global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
-                                   FieldSpec<Real> fb, cd shot,
-                                   AxisTablesDev ax,
-                                   typename CplxOf<XR>::type* out_re,
-                                   typename CplxOf<XR>::type* out_im) {
+__global__ void __launch_bounds__(256)
+twopt_field_kernel(Geom g, FieldSpec<Real> fa, FieldSpec<Real> fb, cd shot,
+                   AxisTablesDev ax, typename CplxOf<XR>::type* out_re,
+                   typename CplxOf<XR>::type* out_im) {
   using C = typename CplxOf<XR>::type;
   const double inv_vol = 1. / g.vol;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-       t < g.nhalf; t += int64_t(gridDim.x) * blockDim.x) {
-    const int k = int(t % g.nzh);
-    const int j = int((t / g.nzh) % g.n[1]);
-    const int i = int(t / (int64_t(g.nzh) * g.n[1]));
+  const int row = blockIdx.x;
+  const int i = row / g.n[1], j = row - (row / g.n[1]) * g.n[1];
+  for (int k = threadIdx.x; k < g.nzh; k += blockDim.x) {
+    const int64_t t = int64_t(row) * g.nzh + k;
     const cd p = twopt_mode(g, fa, fb, shot, ax, i, j, k);
     C o;
     if (out_im == nullptr) {
@@ -414,6 +410,29 @@ __global__ void twopt_field_kernel(Geom g, FieldSpec<Real> fa,
   }
 }
 
+// FP32 fast path for two real-mesh spectra without interlacing:
+// P = (fa fb^* / C_1 - S) / V in float, the k = 0 mode given exactly.
+__global__ void __launch_bounds__(256)
+twopt_field_real_f32_kernel(int n1, int nzh, const float2* fa,
+                            const float2* fb, const float* inv_alias_x,
+                            const float* inv_alias_y,
+                            const float* inv_alias_z, float shot,
+                            float inv_vol, float2 p0, float2* out) {
+  const int row = blockIdx.x;
+  const int i = row / n1, j = row - (row / n1) * n1;
+  const float axy = inv_alias_x[i] * inv_alias_y[j];
+  for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
+    const int64_t t = int64_t(row) * nzh + k;
+    const float2 a = fa[t], b = fb[t];
+    const float inv = axy * inv_alias_z[k];
+    float2 o;
+    o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
+    o.y = ((a.y * b.x - a.x * b.y) * inv) * inv_vol;
+    if (row == 0 && k == 0) o = p0;
+    out[t] = o;
+  }
+}
+
 }  // namespace
 
 void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
@@ -431,9 +450,8 @@ void launch_build_G(Context& ctx, const Geom& g, const int M[3],
                     const int Kg[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax,
                     typename CplxOf<FR>::type* out) {
-  const int64_t count = int64_t(M[0]) * M[1] * M[2];
   TRVG_KBEGIN(ctx, "build_G_kernel");
-  build_G_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+  build_G_kernel<Real, FR><<<M[0] * M[1], 128, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, ax, out);
   TRVG_LAUNCHED(ctx);
 }
@@ -444,9 +462,8 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
                     double hi_max, typename CplxOf<FR>::type* out) {
-  const int64_t count = int64_t(M[0]) * M[1] * M[2];
   TRVG_KBEGIN(ctx, "build_F_kernel");
-  build_F_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+  build_F_kernel<Real, FR><<<M[0] * M[1], 128, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
       hi_max, out);
   TRVG_LAUNCHED(ctx);
@@ -485,8 +502,19 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
                         typename CplxOf<XR>::type* out_re,
                         typename CplxOf<XR>::type* out_im) {
   TRVG_KBEGIN(ctx, "twopt_field_kernel");
-  twopt_field_kernel<Real, XR><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+  twopt_field_kernel<Real, XR><<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
       g, fa, fb, shot, ax, out_re, out_im);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
+                                 const float2* fa, const float2* fb,
+                                 const float* const inv_alias[3], float shot,
+                                 float2 p0, float2* out) {
+  TRVG_KBEGIN(ctx, "twopt_field_kernel");
+  twopt_field_real_f32_kernel<<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
+      g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1], inv_alias[2], shot,
+      float(1. / g.vol), p0, out);
   TRVG_LAUNCHED(ctx);
 }
 
