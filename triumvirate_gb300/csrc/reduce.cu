@@ -12,6 +12,9 @@
 //  * shotnoise_3pcf_bins: r-binned sums of the 3PCF shot noise
 //    (field.cpp:3090-3196) with exact per-cell separations.
 #include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
 
 #include "kernels.h"
 
@@ -128,22 +131,18 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
   }
 }
 
-// The same sums with every cell of a mirror orbit handled by one thread:
-// for even mesh numbers the cells (+-s_x, +-s_y, +-s_z) -- and, when
-// n_x = n_y, their x <-> y swaps -- share one key, so one thread adds up
-// to 16 cells and issues one atomic.  One block per (|s_x|, |s_y|) pair
-// (|s_y| <= |s_x| with the swap), threads along z; reads stay coalesced.
-template <class Real>
-__global__ void __launch_bounds__(256)
-radial_hist_orbit_kernel(Geom g, const Real* xi_re, const Real* xi_im,
-                         int ell_a, int m_a, int ell_b, int m_b, bool swap,
-                         double* hist) {
-  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
-  const int hy = g.n[1] / 2, hz = g.n[2] / 2;
-  int a, b;
-  const int q = blockIdx.x;
+// The same sums without atomics, for even mesh numbers.  The cells
+// (+-s_x, +-s_y, +-s_z) -- and, when n_x = n_y, their x <-> y swaps -- share
+// one key.
+//   (1) orbit_rows: one block per (a, b) = (|s_x|, |s_y|) (b <= a with the
+//       swap), threads along c = |s_z|; each thread sums its <= 16 mirror
+//       cells and stores V[(a, b)][c] (coalesced, no atomics);
+//   (2) key_gather: one thread per key gathers H[key] = sum of V[(a, b)][c]
+//       over a^2 + b^2 + c^2 = key, walking c and a host-built list of the
+//       (a, b) pairs of each u = a^2 + b^2.  Every (a, b, c) is read once.
+__device__ __forceinline__ void orbit_ab(int q, bool swap, int hy, int& a,
+                                         int& b) {
   if (swap) {
-    // Triangular index q = a (a + 1) / 2 + b, 0 <= b <= a.
     a = int((sqrtf(8.f * float(q) + 1.f) - 1.f) * 0.5f);
     while ((a + 1) * (a + 2) / 2 <= q) ++a;
     while (a * (a + 1) / 2 > q) --a;
@@ -152,46 +151,90 @@ radial_hist_orbit_kernel(Geom g, const Real* xi_re, const Real* xi_im,
     a = q / (hy + 1);
     b = q - a * (hy + 1);
   }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256)
+orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
+                  int m_a, int ell_b, int m_b, bool swap, double* v_re,
+                  double* v_im) {
+  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+  const int hy = g.n[1] / 2, hz = g.n[2] / 2;
+  const int q = blockIdx.x;
+  int a, b;
+  orbit_ab(q, swap, hy, a, b);
   const int xs[2] = {a, (g.n[0] - a) % g.n[0]};
   const int ys[2] = {b, (g.n[1] - b) % g.n[1]};
   const int nxs = (xs[1] == xs[0]) ? 1 : 2;
   const int nys = (ys[1] == ys[0]) ? 1 : 2;
   const int nsw = (swap && a != b) ? 2 : 1;
-  const int64_t key0 = int64_t(a) * a + int64_t(b) * b;
+  // The up-to-8 rows of the orbit.
+  int64_t rows[8];
+  int nrows = 0;
+  for (int w = 0; w < nsw; ++w)
+    for (int p = 0; p < nxs; ++p)
+      for (int qq = 0; qq < nys; ++qq) {
+        const int i = (w == 0) ? xs[p] : ys[qq];
+        const int j = (w == 0) ? ys[qq] : xs[p];
+        rows[nrows++] = (int64_t(i) * g.n[1] + j) * g.n[2];
+      }
   for (int c = threadIdx.x; c <= hz; c += blockDim.x) {
-    const int zs[2] = {c, (g.n[2] - c) % g.n[2]};
-    const int nzs = (zs[1] == zs[0]) ? 1 : 2;
-    Real sr = Real(0), si = Real(0);
+    const int c2 = (g.n[2] - c) % g.n[2];
+    const bool two = (c2 != c);
     cd acc = {0., 0.};
-    for (int w = 0; w < nsw; ++w) {
-      for (int p = 0; p < nxs; ++p) {
-        for (int qq = 0; qq < nys; ++qq) {
-          const int i = (w == 0) ? xs[p] : ys[qq];
-          const int j = (w == 0) ? ys[qq] : xs[p];
-          const int64_t row = (int64_t(i) * g.n[1] + j) * g.n[2];
-          for (int r = 0; r < nzs; ++r) {
-            const int k = zs[r];
-            if (trivial) {
-              sr += xi_re[row + k];
-              if (xi_im != nullptr) si += xi_im[row + k];
-            } else {
-              cd v = {double(xi_re[row + k]),
-                      xi_im != nullptr ? double(xi_im[row + k]) : 0.};
-              const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
-              const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
-              const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
-              v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
-                       reduced_ylm(ell_b, m_b, rx, ry, rz));
-              acc = acc + v;
-            }
-          }
+    if (trivial) {
+      Real sr = Real(0), si = Real(0);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        if (r >= nrows) break;
+        sr += xi_re[rows[r] + c] + (two ? xi_re[rows[r] + c2] : Real(0));
+        if (xi_im != nullptr)
+          si += xi_im[rows[r] + c] + (two ? xi_im[rows[r] + c2] : Real(0));
+      }
+      acc = cd{double(sr), double(si)};
+    } else {
+      for (int r = 0; r < nrows; ++r) {
+        const int64_t row = rows[r];
+        const int i = int(row / (int64_t(g.n[1]) * g.n[2]));
+        const int j = int((row / g.n[2]) % g.n[1]);
+        for (int z = 0; z < (two ? 2 : 1); ++z) {
+          const int k = (z == 0) ? c : c2;
+          cd v = {double(xi_re[row + k]),
+                  xi_im != nullptr ? double(xi_im[row + k]) : 0.};
+          const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
+          const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
+          const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
+          v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
+                   reduced_ylm(ell_b, m_b, rx, ry, rz));
+          acc = acc + v;
         }
       }
     }
-    if (trivial) acc = cd{double(sr), double(si)};
-    const int64_t key = key0 + int64_t(c) * c;
-    atomicAdd(hist + 2 * key, acc.re);
-    if (acc.im != 0.) atomicAdd(hist + 2 * key + 1, acc.im);
+    const int64_t o = int64_t(q) * (hz + 1) + c;
+    v_re[o] = acc.re;
+    if (v_im != nullptr) v_im[o] = acc.im;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+key_gather_kernel(int64_t nkeys, int hz, int umax, const int* u_off,
+                  const int* u_list, const double* v_re, const double* v_im,
+                  double* hist) {
+  for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
+    double hr = 0., hi = 0.;
+    for (int c = 0; c <= hz; ++c) {
+      const int64_t u = key - int64_t(c) * c;
+      if (u < 0) break;
+      if (u > umax) continue;
+      for (int e = u_off[u]; e < u_off[u + 1]; ++e) {
+        const int64_t o = int64_t(u_list[e]) * (hz + 1) + c;
+        hr += v_re[o];
+        if (v_im != nullptr) hi += v_im[o];
+      }
+    }
+    hist[2 * key] = hr;
+    hist[2 * key + 1] = hi;
   }
 }
 
@@ -355,13 +398,72 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                     (g.n[2] % 2 == 0);
   if (even) {
     const bool swap = g.n[0] == g.n[1];
-    const int hx = g.n[0] / 2, hy = g.n[1] / 2;
+    const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
     const int nblocks =
         swap ? (hx + 1) * (hx + 2) / 2 : (hx + 1) * (hy + 1);
-    const int threads = std::min(256, ((g.n[2] / 2 + 1 + 31) / 32) * 32);
-    TRVG_KBEGIN(ctx, "radial_hist_kernel");
-    radial_hist_orbit_kernel<Real><<<nblocks, threads, 0, ctx.stream>>>(
-        g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
+    // (a, b) pairs grouped by u = a^2 + b^2 (cached per mesh shape).
+    const int umax = hx * hx + hy * hy;
+    const std::string tag = "orbit." + std::to_string(g.n[0]) + "." +
+                            std::to_string(g.n[1]) + "." +
+                            std::to_string(g.n[2]);
+    auto it = ctx.buffers.find(tag + ".off");
+    int* u_off;
+    int* u_list;
+    if (it == ctx.buffers.end()) {
+      std::vector<int> cnt(size_t(umax) + 2, 0);
+      for (int q = 0; q < nblocks; ++q) {
+        int a, b;
+        if (swap) {
+          a = int((std::sqrt(8. * q + 1.) - 1.) * 0.5);
+          while ((a + 1) * (a + 2) / 2 <= q) ++a;
+          while (a * (a + 1) / 2 > q) --a;
+          b = q - a * (a + 1) / 2;
+        } else {
+          a = q / (hy + 1);
+          b = q - a * (hy + 1);
+        }
+        cnt[size_t(a) * a + size_t(b) * b + 1]++;
+      }
+      for (size_t u = 1; u < cnt.size(); ++u) cnt[u] += cnt[u - 1];
+      std::vector<int> list(nblocks), fill(cnt.begin(), cnt.end() - 1);
+      for (int q = 0; q < nblocks; ++q) {
+        int a, b;
+        if (swap) {
+          a = int((std::sqrt(8. * q + 1.) - 1.) * 0.5);
+          while ((a + 1) * (a + 2) / 2 <= q) ++a;
+          while (a * (a + 1) / 2 > q) --a;
+          b = q - a * (a + 1) / 2;
+        } else {
+          a = q / (hy + 1);
+          b = q - a * (hy + 1);
+        }
+        list[fill[size_t(a) * a + size_t(b) * b]++] = q;
+      }
+      u_off = ctx.buf<int>(tag + ".off", cnt.size());
+      u_list = ctx.buf<int>(tag + ".list", list.size());
+      TRVG_CUDA(cudaMemcpyAsync(u_off, cnt.data(), cnt.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx.stream));
+      TRVG_CUDA(cudaMemcpyAsync(u_list, list.data(),
+                                list.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx.stream));
+      TRVG_CUDA(cudaStreamSynchronize(ctx.stream));
+    } else {
+      u_off = static_cast<int*>(it->second.ptr);
+      u_list = static_cast<int*>(ctx.buffers[tag + ".list"].ptr);
+    }
+    const size_t nv = size_t(nblocks) * (hz + 1);
+    double* v_re = ctx.buf<double>("orbit.v.re", nv);
+    double* v_im = xi_im ? ctx.buf<double>("orbit.v.im", nv) : nullptr;
+    const int threads = std::min(256, ((hz + 1 + 31) / 32) * 32);
+    TRVG_KBEGIN(ctx, "orbit_rows_kernel");
+    orbit_rows_kernel<Real><<<nblocks, threads, 0, ctx.stream>>>(
+        g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, v_re, v_im);
+    TRVG_LAUNCHED(ctx);
+    const int64_t nkeys = int64_t(hx) * hx + int64_t(hy) * hy +
+                          int64_t(hz) * hz + 1;
+    TRVG_KBEGIN(ctx, "key_gather_kernel");
+    key_gather_kernel<<<grid_for(nkeys, 256), 256, 0, ctx.stream>>>(
+        nkeys, hz, umax, u_off, u_list, v_re, v_im, hist);
     TRVG_LAUNCHED(ctx);
     return;
   }

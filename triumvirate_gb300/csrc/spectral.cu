@@ -158,10 +158,13 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
                                AxisTablesDev ax,
                                typename CplxOf<FR>::type* out) {
   using C = typename CplxOf<FR>::type;
-  const int row = blockIdx.x;
-  const int a = row / M1, b = row - (row / M1) * M1;
-  for (int c = threadIdx.x; c < M2; c += blockDim.x) {
-    const int64_t t = int64_t(row) * M2 + c;
+  const uint32_t count = uint32_t(M0) * M1 * M2;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(M2));
+    const uint32_t row = t / uint32_t(M2);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
     const int sx = shift_index(a, M0), sy = shift_index(b, M1),
               sz = shift_index(c, M2);
     const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
@@ -193,11 +196,13 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
                                const double* hi, int nb, double hi_max,
                                typename CplxOf<FR>::type* out) {
   using C = typename CplxOf<FR>::type;
-  const int64_t count = int64_t(M0) * M1 * M2;
-  const int row = blockIdx.x;
-  const int a = row / M1, b = row - (row / M1) * M1;
-  for (int c = threadIdx.x; c < M2; c += blockDim.x) {
-    const int64_t t = int64_t(row) * M2 + c;
+  const uint32_t count = uint32_t(M0) * M1 * M2;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(M2));
+    const uint32_t row = t / uint32_t(M2);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
     const int sx = shift_index(a, M0), sy = shift_index(b, M1),
               sz = shift_index(c, M2);
     const bool in = (M0 == g.n[0] || abs(sx) <= K0) &&
@@ -450,8 +455,11 @@ void launch_build_G(Context& ctx, const Geom& g, const int M[3],
                     const int Kg[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax,
                     typename CplxOf<FR>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
   TRVG_KBEGIN(ctx, "build_G_kernel");
-  build_G_kernel<Real, FR><<<M[0] * M[1], 128, 0, ctx.stream>>>(
+  build_G_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, ax, out);
   TRVG_LAUNCHED(ctx);
 }
@@ -462,8 +470,11 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
                     double hi_max, typename CplxOf<FR>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
   TRVG_KBEGIN(ctx, "build_F_kernel");
-  build_F_kernel<Real, FR><<<M[0] * M[1], 128, 0, ctx.stream>>>(
+  build_F_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
       g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
       hi_max, out);
   TRVG_LAUNCHED(ctx);
