@@ -79,8 +79,8 @@ __device__ __forceinline__ Stencil<ORDER> axis_stencil(double pos, int n,
   return st;
 }
 
-__device__ __forceinline__ void atomic_add_real(float* p, double v) {
-  atomicAdd(p, float(v));
+__device__ __forceinline__ void atomic_add_real(float* p, float v) {
+  atomicAdd(p, v);
 }
 __device__ __forceinline__ void atomic_add_real(double* p, double v) {
   atomicAdd(p, v);
@@ -100,6 +100,10 @@ struct AssignArgs {
 };
 
 // Deposit one stencil; returns the weight that landed inside the mesh.
+// Stencil indices and window values are FP64 (they decide the cells); the
+// products deposited into an FP32 mesh are formed in FP32.  The landed
+// weight is w * (sum_i wx_i)(sum_j wy_j)(sum_k wz_k) in FP64 when every
+// cell is inside the mesh, and accumulated cell by cell otherwise.
 template <int ORDER, class Real>
 __device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
                                       bool shadow, cd wgt, Real* re,
@@ -107,28 +111,74 @@ __device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
   Stencil<ORDER> sx = axis_stencil<ORDER>(pos[0], a.n[0], a.L[0], shadow);
   Stencil<ORDER> sy = axis_stencil<ORDER>(pos[1], a.n[1], a.L[1], shadow);
   Stencil<ORDER> sz = axis_stencil<ORDER>(pos[2], a.n[2], a.L[2], shadow);
+  Real wx[ORDER], wy[ORDER], wz[ORDER];
+  double tx = 0., ty = 0., tz = 0.;
+#pragma unroll
+  for (int i = 0; i < ORDER; ++i) {
+    tx += sx.win[i];
+    ty += sy.win[i];
+    tz += sz.win[i];
+  }
+  const Real wre = Real(wgt.re), wim = Real(wgt.im);
+#pragma unroll
+  for (int i = 0; i < ORDER; ++i) {
+    wx[i] = Real(sx.win[i]) * wre;
+    wy[i] = Real(sy.win[i]);
+    wz[i] = Real(sz.win[i]);
+  }
+  bool all_in = true;
   cd landed = {0., 0.};
 #pragma unroll
   for (int i = 0; i < ORDER; ++i) {
 #pragma unroll
     for (int j = 0; j < ORDER; ++j) {
       const int64_t row = (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
-      const double wij = sx.win[i] * sy.win[j];
+      const Real wij = wx[i] * wy[j];
 #pragma unroll
       for (int k = 0; k < ORDER; ++k) {
         const int64_t gid = row + sz.idx[k];
-        if (gid < 0 || gid >= a.nmesh) continue;
-        const double wv = wij * sz.win[k];
-        const double vre = wgt.re * wv;
-        atomic_add_real(re + gid, vre);
-        landed.re += vre;
-        if (im != nullptr) {
-          const double vim = wgt.im * wv;
-          atomic_add_real(im + gid, vim);
-          landed.im += vim;
+        if (gid < 0 || gid >= a.nmesh) {
+          all_in = false;
+          continue;
+        }
+        atomic_add_real(re + gid, wij * wz[k]);
+      }
+    }
+  }
+  if (im != nullptr) {
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i) {
+#pragma unroll
+      for (int j = 0; j < ORDER; ++j) {
+        const int64_t row =
+            (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
+        const Real wij = Real(sx.win[i]) * wim * wy[j];
+#pragma unroll
+        for (int k = 0; k < ORDER; ++k) {
+          const int64_t gid = row + sz.idx[k];
+          if (gid < 0 || gid >= a.nmesh) continue;
+          atomic_add_real(im + gid, wij * wz[k]);
         }
       }
     }
+  }
+  if (all_in) {
+    const double t = tx * ty * tz;
+    landed = cd{wgt.re * t, wgt.im * t};
+  } else {
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i)
+#pragma unroll
+      for (int j = 0; j < ORDER; ++j)
+#pragma unroll
+        for (int k = 0; k < ORDER; ++k) {
+          const int64_t gid =
+              (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2] + sz.idx[k];
+          if (gid < 0 || gid >= a.nmesh) continue;
+          const double wv = sx.win[i] * sy.win[j] * sz.win[k];
+          landed.re += wgt.re * wv;
+          landed.im += wgt.im * wv;
+        }
   }
   return landed;
 }

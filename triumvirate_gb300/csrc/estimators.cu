@@ -783,6 +783,68 @@ struct Engine {
     ctx.fft_launches++;
   }
 
+  // Real-field variants: half spectra on the evaluation grid, then C2R.
+  template <class FR>
+  const FR* build_G_real(const FieldSpec<Real>& f, const int M[3],
+                         const int Kg[3]) {
+    using FC = typename CplxOf<FR>::type;
+    const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+    const size_t Mc = size_t(M[0]) * M[1] * M[2];
+    FC* H = ctx.buf<FC>("G.h", Mh);
+    launch_build_G_half<Real, FR>(ctx, g, M, Kg, f, ax, H);
+    FR* G = ctx.buf<FR>("G.r", Mc);
+    cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, 1);
+    ctx.kbegin("cufft.c2r.G");
+    FFT<FR>::c2r(h, H, G);
+    ctx.kend();
+    ctx.fft_launches++;
+    return G;
+  }
+
+  template <class FR>
+  void build_leg_real(const FieldSpec<Real>& src, const Leg& leg,
+                      const vector<int>& bins, const HostBins& hb,
+                      const vector<double>& radii, const int M[3],
+                      const int K[3], const std::string& tag, FR* out) {
+    using FC = typename CplxOf<FR>::type;
+    const int nb = int(bins.size());
+    const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+    FC* H = ctx.buf<FC>(tag + ".h", size_t(nb) * Mh);
+    if (leg.sjl) {
+      vector<double> r(nb);
+      for (int i = 0; i < nb; ++i) r[i] = radii[bins[i]];
+      const double* dr = upload(tag + ".r", r);
+      launch_build_F_sjl_half<Real, FR>(ctx, g, src, ax, leg.ell, leg.m,
+                                        leg.sj, dr, nb, H);
+    } else {
+      vector<double> lo(nb), hi(nb);
+      double hmax = 0.;
+      for (int i = 0; i < nb; ++i) {
+        lo[i] = hb.lo[bins[i]];
+        hi[i] = hb.hi[bins[i]];
+        hmax = std::max(hmax, hi[i]);
+      }
+      const double* dlo = upload(tag + ".lo", lo);
+      const double* dhi = upload(tag + ".hi", hi);
+      launch_build_F_half<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m,
+                                    dlo, dhi, nb, hmax, H);
+    }
+    cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, nb);
+    ctx.kbegin("cufft.c2r.F");
+    FFT<FR>::c2r(h, H, out);
+    ctx.kend();
+    ctx.fft_launches++;
+  }
+
+  // Shell fields and G are real when both legs have m = 0 and even ell and
+  // both source fields are real meshes without interlacing.
+  bool real_fields(const FieldSpec<Real>& src, const FieldSpec<Real>& gsrc,
+                   const Leg& la, const Leg& lb) const {
+    return la.m == 0 && lb.m == 0 && la.ell % 2 == 0 && lb.ell % 2 == 0 &&
+           src.im == nullptr && src.re_s == nullptr && gsrc.im == nullptr &&
+           gsrc.re_s == nullptr;
+  }
+
   // sum over the evaluation grid of F_a(row) F_b(col) G for every pair, G
   // being the compensated field of `gsrc`; evaluation-grid fields in FP64
   // for the FP64 path or with the "shell_fields_fp64" option.
@@ -806,7 +868,9 @@ struct Engine {
     using FC = typename CplxOf<FR>::type;
     const int np = int(pairs.size());
     vector<cplx> res(np, cplx(0., 0.));
-    const FC* G = build_G<FR>(gsrc, M, Kg);
+    const bool real = real_fields(src, gsrc, la, lb);
+    const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
+    const FR* Gr = real ? build_G_real<FR>(gsrc, M, Kg) : nullptr;
     const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;
     vector<int> A, B;
     for (const Pair& q : pairs) {
@@ -824,11 +888,13 @@ struct Engine {
     uniq(A);
     uniq(B);
     const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
-    const size_t perF = size_t(Mc) * sizeof(FC);
+    const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+    const size_t perF = real ? size_t(Mc) * sizeof(FR) + Mh * sizeof(FC)
+                             : size_t(Mc) * sizeof(FC);
     size_t free_b = 0, total_b = 0;
     TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     size_t have = 0;
-    for (const char* nm : {"F.A", "F.B"}) {
+    for (const char* nm : {"F.A", "F.B", "legA.h", "legB.h"}) {
       auto it = ctx.buffers.find(nm);
       if (it != ctx.buffers.end()) have += it->second.bytes;
     }
@@ -859,8 +925,15 @@ struct Engine {
     const auto blocksB = shared ? blocksA : chunk(B, SB);
     for (size_t I = 0; I < blocksA.size(); ++I) {
       const vector<int>& bA = blocksA[I];
-      FC* FA = ctx.buf<FC>("F.A", bA.size() * size_t(Mc));
-      build_leg<FR>(src, la, bA, hb, radii, M, K, "legA", FA);
+      FC* FA = nullptr;
+      FR* FAr = nullptr;
+      if (real) {
+        FAr = ctx.buf<FR>("F.A", bA.size() * size_t(Mc));
+        build_leg_real<FR>(src, la, bA, hb, radii, M, K, "legA", FAr);
+      } else {
+        FA = ctx.buf<FC>("F.A", bA.size() * size_t(Mc));
+        build_leg<FR>(src, la, bA, hb, radii, M, K, "legA", FA);
+      }
       for (size_t J = 0; J < blocksB.size(); ++J) {
         const vector<int>& bB = blocksB[J];
         vector<int> pa, pb, idx;
@@ -875,17 +948,28 @@ struct Engine {
         }
         if (idx.empty()) continue;
         const FC* FB = FA;
+        const FR* FBr = FAr;
         if (!(shared && I == J)) {
-          FC* fb = ctx.buf<FC>("F.B", bB.size() * size_t(Mc));
-          build_leg<FR>(src, lb, bB, hb, radii, M, K, "legB", fb);
-          FB = fb;
+          if (real) {
+            FR* fb = ctx.buf<FR>("F.B", bB.size() * size_t(Mc));
+            build_leg_real<FR>(src, lb, bB, hb, radii, M, K, "legB", fb);
+            FBr = fb;
+          } else {
+            FC* fb = ctx.buf<FC>("F.B", bB.size() * size_t(Mc));
+            build_leg<FR>(src, lb, bB, hb, radii, M, K, "legB", fb);
+            FB = fb;
+          }
         }
         const int* dpa = upload("pairs.a", pa);
         const int* dpb = upload("pairs.b", pb);
         double* dout = ctx.buf<double>("pairs.out", 2 * idx.size());
         zero(dout, 2 * idx.size() * sizeof(double));
-        launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb, int(idx.size()),
-                                dout);
+        if (real)
+          launch_reduce_pairs_real<FR>(ctx, Mc, Gr, FAr, FBr, dpa, dpb,
+                                       int(idx.size()), dout);
+        else
+          launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb,
+                                  int(idx.size()), dout);
         vector<double> h = download(dout, 2 * idx.size());
         for (size_t q = 0; q < idx.size(); ++q)
           res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);

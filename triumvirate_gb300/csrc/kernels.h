@@ -133,6 +133,25 @@ void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const SplineTable& sj, const double* radii, int nb,
                         typename CplxOf<FR>::type* out);
 
+// Half-spectrum builders for real fields (C2R on the evaluation grid).
+template <class Real, class FR>
+void launch_build_G_half(Context& ctx, const Geom& g, const int M[3],
+                         const int Kg[3], const FieldSpec<Real>& f,
+                         const AxisTablesDev& ax,
+                         typename CplxOf<FR>::type* out);
+template <class Real, class FR>
+void launch_build_F_half(Context& ctx, const Geom& g, const int M[3],
+                         const int K[3], const FieldSpec<Real>& f,
+                         const AxisTablesDev& ax, int ell, int m,
+                         const double* lo, const double* hi, int nb,
+                         double hi_max, typename CplxOf<FR>::type* out);
+template <class Real, class FR>
+void launch_build_F_sjl_half(Context& ctx, const Geom& g,
+                             const FieldSpec<Real>& f, const AxisTablesDev& ax,
+                             int ell, int m, const SplineTable& sj,
+                             const double* radii, int nb,
+                             typename CplxOf<FR>::type* out);
+
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
@@ -163,6 +182,12 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
                          const typename CplxOf<Real>::type* Fb,
                          const int* pa, const int* pb, int npairs,
                          double* out /* 2 * npairs */);
+
+template <class Real>
+void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
+                              const Real* Fa, const Real* Fb, const int* pa,
+                              const int* pb, int npairs,
+                              double* out /* 2 * npairs, imaginary 0 */);
 
 template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,

@@ -103,6 +103,55 @@ reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
   block_add<2 * kPairChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
 }
 
+// Real fields: sum_x F_a F_b G with FP64 accumulation; the imaginary part
+// of the output is left at zero.
+template <class Real>
+__global__ void __launch_bounds__(256)
+reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
+                         const Real* Fb, const int* pa, const int* pb,
+                         int npairs, double* out) {
+  __shared__ double red[kPairChunk * 32];
+  const int p0 = blockIdx.y * kPairChunk;
+  int ia[kPairChunk], ib[kPairChunk];
+  bool ok[kPairChunk];
+#pragma unroll
+  for (int q = 0; q < kPairChunk; ++q) {
+    ok[q] = (p0 + q) < npairs;
+    ia[q] = ok[q] ? pa[p0 + q] : 0;
+    ib[q] = ok[q] ? pb[p0 + q] : 0;
+  }
+  double acc[kPairChunk];
+#pragma unroll
+  for (int q = 0; q < kPairChunk; ++q) acc[q] = 0.;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const Real g = G[t];
+#pragma unroll
+    for (int q = 0; q < kPairChunk; ++q) {
+      if (!ok[q]) continue;
+      const Real a = Fa[int64_t(ia[q]) * ncell + t];
+      const Real b = (ia[q] == ib[q] && Fa == Fb)
+                         ? a : Fb[int64_t(ib[q]) * ncell + t];
+      acc[q] += double(a * b * g);
+    }
+  }
+  // Reduce and write the real parts at out[2 * (p0 + q)].
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kPairChunk; ++q) {
+    const double s = warp_sum(acc[q]);
+    if (lane == 0) red[q * 32 + wid] = s;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < kPairChunk; q += blockDim.x) {
+    if (!ok[q]) continue;
+    double s = 0.;
+    for (int w = 0; w < nw; ++w) s += red[q * 32 + w];
+    atomicAdd(out + 2 * (p0 + q), s);
+  }
+}
+
 // Sum of xi * y_a * y_b per integer key s_x^2 + s_y^2 + s_z^2 (cubic cells).
 template <class Real>
 __global__ void __launch_bounds__(256)
@@ -391,6 +440,19 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
 }
 
 template <class Real>
+void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
+                              const Real* Fa, const Real* Fb, const int* pa,
+                              const int* pb, int npairs, double* out) {
+  if (npairs <= 0) return;
+  const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
+  dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
+  TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
+  reduce_pairs_real_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
+      ncell, G, Fa, Fb, pa, pb, npairs, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                         const Real* xi_im, int ell_a, int m_a, int ell_b,
                         int m_b, double* hist) {
@@ -524,6 +586,9 @@ void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
                                        const CplxOf<R>::type*,                \
                                        const CplxOf<R>::type*, const int*,    \
                                        const int*, int, double*);             \
+  template void launch_reduce_pairs_real<R>(Context&, int64_t, const R*,     \
+                                            const R*, const R*, const int*,   \
+                                            const int*, int, double*);        \
   template void launch_radial_hist<R>(Context&, const Geom&, const R*,        \
                                       const R*, int, int, int, int, double*); \
   template void launch_pair_bessel_direct<R>(                                 \

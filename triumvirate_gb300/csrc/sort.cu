@@ -36,30 +36,61 @@ __global__ void tile_key_kernel(DevCatalogue cat, int n0, int n1, int n2,
   }
 }
 
-// Exclusive scan of `count[0..n)` in place, one block of 1024 threads.
-__global__ void __launch_bounds__(1024)
-scan_kernel(int* count, int n) {
-  __shared__ int part[1024];
-  const int chunk = (n + blockDim.x - 1) / blockDim.x;
-  const int lo = min(n, int(threadIdx.x) * chunk);
-  const int hi = min(n, lo + chunk);
-  int s = 0;
-  for (int i = lo; i < hi; ++i) s += count[i];
-  part[threadIdx.x] = s;
+// Exclusive scan of count[0..n) in place: per-block scans of 2048
+// elements, a scan of the block totals, then the block offsets added.
+constexpr int kScanBlock = 1024;
+constexpr int kScanTile = 2 * kScanBlock;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* sh) {
+  // Inclusive Hillis-Steele scan in shared memory, returned exclusive.
+  sh[threadIdx.x] = v;
   __syncthreads();
-  // Hillis-Steele inclusive scan of the partial sums.
   for (int off = 1; off < int(blockDim.x); off <<= 1) {
-    const int v = (int(threadIdx.x) >= off) ? part[threadIdx.x - off] : 0;
+    const int t = (int(threadIdx.x) >= off) ? sh[threadIdx.x - off] : 0;
     __syncthreads();
-    part[threadIdx.x] += v;
+    sh[threadIdx.x] += t;
     __syncthreads();
   }
-  int run = (threadIdx.x == 0) ? 0 : part[threadIdx.x - 1];
-  for (int i = lo; i < hi; ++i) {
-    const int c = count[i];
-    count[i] = run;
-    run += c;
+  const int incl = sh[threadIdx.x];
+  __syncthreads();
+  return incl - v;
+}
+
+__global__ void __launch_bounds__(kScanBlock)
+scan_tiles_kernel(int* count, int n, int* tile_sum) {
+  __shared__ int sh[kScanBlock];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile;
+  const int64_t i0 = base + 2 * threadIdx.x, i1 = i0 + 1;
+  const int a = (i0 < n) ? count[i0] : 0;
+  const int b = (i1 < n) ? count[i1] : 0;
+  const int ex = block_exclusive_scan(a + b, sh);
+  if (i0 < n) count[i0] = ex;
+  if (i1 < n) count[i1] = ex + a;
+  if (threadIdx.x == blockDim.x - 1) tile_sum[blockIdx.x] = ex + a + b;
+}
+
+// Exclusive scan of the tile totals (at most 1024 * 2048 tiles handled by
+// looping one block over them).
+__global__ void __launch_bounds__(kScanBlock)
+scan_sums_kernel(int* tile_sum, int ntiles) {
+  __shared__ int sh[kScanBlock];
+  int carry = 0;
+  for (int base = 0; base < ntiles; base += kScanBlock) {
+    const int i = base + threadIdx.x;
+    const int v = (i < ntiles) ? tile_sum[i] : 0;
+    const int ex = block_exclusive_scan(v, sh);
+    if (i < ntiles) tile_sum[i] = carry + ex;
+    __shared__ int total;
+    if (threadIdx.x == blockDim.x - 1) total = ex + v;
+    __syncthreads();
+    carry += total;
+    __syncthreads();
   }
+}
+
+__global__ void add_offsets_kernel(int* count, int n, const int* tile_sum) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) count[i] += tile_sum[i / kScanTile];
 }
 
 struct SortedOut {
@@ -120,8 +151,18 @@ DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
       in, g.n[0], g.n[1], g.n[2], g.L[0], g.L[1], g.L[2], t1, t2, key, rank,
       count);
   TRVG_LAUNCHED(ctx);
+  const int nscan = int((ntiles + kScanTile - 1) / kScanTile);
+  int* tile_sum = ctx.buf<int>(tag + ".sort.tiles", size_t(nscan));
   TRVG_KBEGIN(ctx, "scan_kernel");
-  scan_kernel<<<1, 1024, 0, ctx.stream>>>(count, int(ntiles));
+  scan_tiles_kernel<<<nscan, kScanBlock, 0, ctx.stream>>>(count, int(ntiles),
+                                                          tile_sum);
+  TRVG_LAUNCHED(ctx);
+  TRVG_KBEGIN(ctx, "scan_kernel");
+  scan_sums_kernel<<<1, kScanBlock, 0, ctx.stream>>>(tile_sum, nscan);
+  TRVG_LAUNCHED(ctx);
+  TRVG_KBEGIN(ctx, "scan_kernel");
+  add_offsets_kernel<<<int((ntiles + 255) / 256), 256, 0, ctx.stream>>>(
+      count, int(ntiles), tile_sum);
   TRVG_LAUNCHED(ctx);
   SortedOut o;
   const size_t n = size_t(in.n);

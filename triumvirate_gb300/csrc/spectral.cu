@@ -234,6 +234,91 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
   }
 }
 
+// Half-spectrum variants (M0 x M1 x (M2/2 + 1)) of the builders for fields
+// that are real: y_lm real with even ell and a real source field make the
+// spectrum Hermitian, so the field is the C2R transform of its half.
+template <class Real, class FR>
+__global__ void build_G_half_kernel(Geom g, int M0, int M1, int M2, int Kg0,
+                                    int Kg1, int Kg2, FieldSpec<Real> f,
+                                    AxisTablesDev ax,
+                                    typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * Mh;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(Mh));
+    const uint32_t row = t / uint32_t(Mh);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
+                    (M1 == g.n[1] || abs(sy) <= Kg1) &&
+                    (M2 == g.n[2] || abs(sz) <= Kg2);
+    C o;
+    o.x = 0;
+    o.y = 0;
+    if (in) {
+      const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                k = wrap(sz, g.n[2]);
+      const cd v = field_value(f, g, i, j, k);
+      const double w = window_pow(ax, i, j, k);
+      const cd r = cdivr(cdivr(v, w), g.vol);
+      o.x = FR(r.re);
+      o.y = FR(r.im);
+    }
+    out[t] = o;
+  }
+}
+
+template <class Real, class FR>
+__global__ void build_F_half_kernel(Geom g, int M0, int M1, int M2, int K0,
+                                    int K1, int K2, FieldSpec<Real> f,
+                                    AxisTablesDev ax, int ell, int m,
+                                    const double* lo, const double* hi,
+                                    int nb, double hi_max,
+                                    typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * Mh;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(Mh));
+    const uint32_t row = t / uint32_t(Mh);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= K0) &&
+                    (M1 == g.n[1] || abs(sy) <= K1) &&
+                    (M2 == g.n[2] || abs(sz) <= K2);
+    double k = -1.;
+    cd val = {0., 0.};
+    if (in) {
+      const double kx = dmul(double(sx), g.dk[0]);
+      const double ky = dmul(double(sy), g.dk[1]);
+      const double kz = dmul(double(sz), g.dk[2]);
+      k = vec3_mag(kx, ky, kz);
+      if (k < hi_max) {
+        const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                  kk = wrap(sz, g.n[2]);
+        const cd v = field_value(f, g, i, j, kk);
+        const double w = window_pow(ax, i, j, kk);
+        const cd y = reduced_ylm(ell, m, kx, ky, kz);
+        val = y * cdivr(v, w);
+      }
+    }
+    for (int q = 0; q < nb; ++q) {
+      C o;
+      const bool sel = in && (lo[q] <= k) && (k < hi[q]);
+      o.x = sel ? FR(val.re) : FR(0);
+      o.y = sel ? FR(val.im) : FR(0);
+      out[int64_t(q) * count + t] = o;
+    }
+  }
+}
+
 struct SjlArgs {
   SplineTable sj;
   const double* radii;
@@ -254,6 +339,36 @@ __global__ void build_F_sjl_kernel(Geom g, FieldSpec<Real> f,
     const int kk = int(t % g.n[2]);
     const int j = int((t / g.n[2]) % g.n[1]);
     const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const double kx = dmul(double(shift_index(i, g.n[0])), g.dk[0]);
+    const double ky = dmul(double(shift_index(j, g.n[1])), g.dk[1]);
+    const double kz = dmul(double(shift_index(kk, g.n[2])), g.dk[2]);
+    const double k = vec3_mag(kx, ky, kz);
+    const cd v = field_value(f, g, i, j, kk);
+    const double w = window_pow(ax, i, j, kk);
+    const cd y = reduced_ylm(ell, m, kx, ky, kz);
+    const cd val = y * cdivr(v, w);
+    for (int q = 0; q < sa.nb; ++q) {
+      const double jl = spline_eval(sa.sj, k * sa.radii[q]);
+      C o;
+      o.x = FR(jl * val.re / g.vol);
+      o.y = FR(jl * val.im / g.vol);
+      out[int64_t(q) * count + t] = o;
+    }
+  }
+}
+
+template <class Real, class FR>
+__global__ void build_F_sjl_half_kernel(Geom g, FieldSpec<Real> f,
+                                        AxisTablesDev ax, int ell, int m,
+                                        SjlArgs sa,
+                                        typename CplxOf<FR>::type* out) {
+  using C = typename CplxOf<FR>::type;
+  const int64_t count = g.nhalf;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int kk = int(t % g.nzh);
+    const int j = int((t / g.nzh) % g.n[1]);
+    const int i = int(t / (int64_t(g.nzh) * g.n[1]));
     const double kx = dmul(double(shift_index(i, g.n[0])), g.dk[0]);
     const double ky = dmul(double(shift_index(j, g.n[1])), g.dk[1]);
     const double kz = dmul(double(shift_index(kk, g.n[2])), g.dk[2]);
@@ -529,6 +644,51 @@ void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
   TRVG_LAUNCHED(ctx);
 }
 
+template <class Real, class FR>
+void launch_build_G_half(Context& ctx, const Geom& g, const int M[3],
+                         const int Kg[3], const FieldSpec<Real>& f,
+                         const AxisTablesDev& ax,
+                         typename CplxOf<FR>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  TRVG_KBEGIN(ctx, "build_G_kernel");
+  build_G_half_kernel<Real, FR><<<grid_for(count, 256), 256, 0,
+                                  ctx.stream>>>(g, M[0], M[1], M[2], Kg[0],
+                                                Kg[1], Kg[2], f, ax, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real, class FR>
+void launch_build_F_half(Context& ctx, const Geom& g, const int M[3],
+                         const int K[3], const FieldSpec<Real>& f,
+                         const AxisTablesDev& ax, int ell, int m,
+                         const double* lo, const double* hi, int nb,
+                         double hi_max, typename CplxOf<FR>::type* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  TRVG_KBEGIN(ctx, "build_F_kernel");
+  build_F_half_kernel<Real, FR><<<grid_for(count, 256), 256, 0,
+                                  ctx.stream>>>(g, M[0], M[1], M[2], K[0],
+                                                K[1], K[2], f, ax, ell, m, lo,
+                                                hi, nb, hi_max, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real, class FR>
+void launch_build_F_sjl_half(Context& ctx, const Geom& g,
+                             const FieldSpec<Real>& f, const AxisTablesDev& ax,
+                             int ell, int m, const SplineTable& sj,
+                             const double* radii, int nb,
+                             typename CplxOf<FR>::type* out) {
+  SjlArgs sa{sj, radii, nb};
+  TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
+  build_F_sjl_half_kernel<Real, FR><<<grid_for(g.nhalf, 256), 256, 0,
+                                      ctx.stream>>>(g, f, ax, ell, m, sa, out);
+  TRVG_LAUNCHED(ctx);
+}
+
 #define TRVG_INST2(R, F)                                                     \
   template void launch_build_G<R, F>(Context&, const Geom&, const int*,      \
                                      const int*, const FieldSpec<R>&,        \
@@ -538,6 +698,16 @@ void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
       const AxisTablesDev&, int, int, const double*, const double*, int,     \
       double, CplxOf<F>::type*);                                             \
   template void launch_build_F_sjl<R, F>(                                    \
+      Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
+      int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
+  template void launch_build_G_half<R, F>(                                   \
+      Context&, const Geom&, const int*, const int*, const FieldSpec<R>&,    \
+      const AxisTablesDev&, CplxOf<F>::type*);                               \
+  template void launch_build_F_half<R, F>(                                   \
+      Context&, const Geom&, const int*, const int*, const FieldSpec<R>&,    \
+      const AxisTablesDev&, int, int, const double*, const double*, int,     \
+      double, CplxOf<F>::type*);                                             \
+  template void launch_build_F_sjl_half<R, F>(                               \
       Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
       int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
   template void launch_twopt_field<R, F>(                                    \
