@@ -245,6 +245,27 @@ int trvg_calc_grid_based_powlaw_norm(
   trvg_context* ctx, const trvg_params* params,
   const trvg_catalogue* particles, int order, double* norm_factor);
 
+/* Allocation-free variant of trvg_calc_grid_based_powlaw_norm; it has no
+ * counterpart in the reference.  It allocates no device memory and creates
+ * no context: the mesh and reduction slots live in one static device array
+ * of 2^21 cells (128^3, 16 MiB), so meshes with more cells are rejected
+ * (TRVG_ERR_INVALID_PARAMETER).  It serves callers whose device memory is
+ * held by another allocator, or that must not call cudaMalloc / cudaFree
+ * (both synchronise the device) once running.
+ *  - `particles` must be device-resident (TRVG_MEM_DEVICE);
+ *  - runs on the calling thread's current device, on `stream` (a
+ *    cudaStream_t; NULL for the legacy default stream), always in FP64,
+ *    and waits for `stream` before writing *norm_factor (host);
+ *  - the call zeroes the scratch it uses itself; nothing must be zero on
+ *    entry;
+ *  - the scratch is one per device: overlapping calls on one device race
+ *    and must be serialised by the caller;
+ *  - the first call on a device looks up the scratch address on that
+ *    device; make it before any stream capture. */
+int trvg_calc_grid_based_powlaw_norm_noalloc(
+  const trvg_params* params, const trvg_catalogue* particles, int order,
+  void* stream, double* norm_factor);
+
 /* The weighted mesh n(x) = sum_i w_i W(x - x_i) / dV (real weights) or its
  * interlacing shadow (`shadow` = 1), written to `mesh_out` (host, ngrid[0]
  * * ngrid[1] * ngrid[2] doubles, row-major, z fastest). */

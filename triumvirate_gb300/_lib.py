@@ -39,6 +39,7 @@ EXPORTED = [
     "trvg_wigner_3j", "trvg_sph_bessel", "trvg_sph_bessel_spline",
     "trvg_reduced_ylm", "trvg_context_set_stream", "trvg_set_option",
     "trvg_kernel_time_count", "trvg_kernel_time_get",
+    "trvg_calc_grid_based_powlaw_norm_noalloc",
 ]
 
 
@@ -184,6 +185,8 @@ def _declare(lib):
         vp, P(Params), P(Catalogue), ip, P(dp)]
     lib.trvg_assign_weighted_field_to_mesh.argtypes = [
         vp, P(Params), P(Catalogue), ip, P(dp)]
+    lib.trvg_calc_grid_based_powlaw_norm_noalloc.argtypes = [
+        P(Params), P(Catalogue), ip, vp, P(dp)]
     lib.trvg_wigner_3j.argtypes = [ip] * 6
     lib.trvg_wigner_3j.restype = dp
     lib.trvg_sph_bessel.argtypes = [ip, dp]
