@@ -253,6 +253,17 @@ __global__ void to_double_kernel(const Real* mesh, int64_t n, double scale,
     out[i] = double(mesh[i]) * scale;
 }
 
+// Every cell set to -(sum / n): the mesh starts at minus the mean of the
+// deposit to come.  `sum` is read from device memory when `dsum` is given.
+template <class Real>
+__global__ void fill_offset_kernel(Real* mesh, int64_t n, const double* dsum,
+                                   double hsum) {
+  const Real v = Real(-((dsum != nullptr) ? *dsum : hsum) / double(n));
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    mesh[i] = v;
+}
+
 // sum_p scale * w_p^power * [conj] y_lm(los_p) in FP64
 // (calc_ylm_wgtd_shotnoise_amp_for_bispec, threept.cpp:156-208, and its
 // power-spectrum twin, twopt.cpp:298-350).
@@ -360,6 +371,15 @@ void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
   TRVG_LAUNCHED(ctx);
 }
 
+template <class Real>
+void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
+                        const double* dsum, double hsum) {
+  TRVG_KBEGIN(ctx, "fill_offset_kernel");
+  fill_offset_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(
+      mesh, n, dsum, hsum);
+  TRVG_LAUNCHED(ctx);
+}
+
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
                        const WeightSpec& ws, double* out) {
   if (cat.n == 0) return;
@@ -376,7 +396,9 @@ void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
   template void launch_mesh_sum_pow<R>(Context&, const R*, int64_t, int,    \
                                        double*);                            \
   template void launch_mesh_to_double<R>(Context&, const R*, int64_t,       \
-                                         double, double*);
+                                         double, double*);                  \
+  template void launch_fill_offset<R>(Context&, R*, int64_t, const double*, \
+                                      double);
 TRVG_INST(float)
 TRVG_INST(double)
 #undef TRVG_INST

@@ -452,11 +452,29 @@ struct Engine {
     Real* sre = interlace ? ctx.buf<Real>("mesh.sre", g.nmesh) : nullptr;
     Real* sim = (interlace && cplx) ? ctx.buf<Real>("mesh.sim", g.nmesh)
                                     : nullptr;
-    const size_t mb = size_t(g.nmesh) * sizeof(Real);
-    zero(mre, mb);
-    if (mim) zero(mim, mb);
-    if (sre) zero(sre, mb);
-    if (sim) zero(sim, mb);
+    // Each mesh starts at minus the mean of its deposit instead of zero.
+    // Only the k = 0 mode changes, and every reader replaces that mode by
+    // the exact FP64 sum (k0_view); the other modes come out of an FP32
+    // transform with far less rounding, because the mean no longer builds
+    // large partial sums on the k = 0 planes and axes inside the FFT.
+    double hsum = 0.;
+    bool on_host = true;
+    for (const Part& part : parts) {
+      if (part.cat.w != nullptr || part.ws.use_ylm) on_host = false;
+      hsum += part.ws.scale * double(part.cat.n);
+    }
+    double* wsum = nullptr;
+    if (!on_host) {
+      wsum = ctx.buf<double>("mesh.mean", 2);
+      zero(wsum, 2 * sizeof(double));
+      for (const Part& part : parts)
+        launch_weight_sum(ctx, part.cat, part.ws, wsum);
+    }
+    const double* wsum_im = (wsum != nullptr) ? wsum + 1 : nullptr;
+    launch_fill_offset<Real>(ctx, mre, g.nmesh, wsum, hsum);
+    if (mim) launch_fill_offset<Real>(ctx, mim, g.nmesh, wsum_im, 0.);
+    if (sre) launch_fill_offset<Real>(ctx, sre, g.nmesh, wsum, hsum);
+    if (sim) launch_fill_offset<Real>(ctx, sim, g.nmesh, wsum_im, 0.);
     double* sums = ctx.buf<double>("assign.sums", 4);
     zero(sums, 4 * sizeof(double));
     for (const Part& part : parts)
@@ -837,9 +855,15 @@ struct Engine {
   }
 
   // Shell fields and G are real when both legs have m = 0 and even ell and
-  // both source fields are real meshes without interlacing.
+  // both source fields are real meshes without interlacing, and the
+  // evaluated modes are closed under k -> -k.  On an odd axis the library's
+  // frequency of index n/2 is -(n/2 + 1) (field.cpp:540-564), whose mirror
+  // index carries -n/2: the compensation window then differs between the
+  // two, and G is complex whenever that axis is evaluated whole (M = n).
   bool real_fields(const FieldSpec<Real>& src, const FieldSpec<Real>& gsrc,
-                   const Leg& la, const Leg& lb) const {
+                   const Leg& la, const Leg& lb, const int M[3]) const {
+    for (int a = 0; a < 3; ++a)
+      if (g.n[a] % 2 != 0 && M[a] == g.n[a]) return false;
     return la.m == 0 && lb.m == 0 && la.ell % 2 == 0 && lb.ell % 2 == 0 &&
            src.im == nullptr && src.re_s == nullptr && gsrc.im == nullptr &&
            gsrc.re_s == nullptr;
@@ -868,7 +892,7 @@ struct Engine {
     using FC = typename CplxOf<FR>::type;
     const int np = int(pairs.size());
     vector<cplx> res(np, cplx(0., 0.));
-    const bool real = real_fields(src, gsrc, la, lb);
+    const bool real = real_fields(src, gsrc, la, lb, M);
     const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
     const FR* Gr = real ? build_G_real<FR>(gsrc, M, Kg) : nullptr;
     const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;

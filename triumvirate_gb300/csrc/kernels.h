@@ -92,6 +92,10 @@ void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
 template <class Real>
 void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
                            double scale, double* out);
+// Fill a mesh with -(sum / n), sum from device memory (`dsum`) or `hsum`.
+template <class Real>
+void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
+                        const double* dsum, double hsum);
 
 // ---- sort.cu -------------------------------------------------------------
 // Copy of `in` ordered by 8^3-cell mesh tile (device buffers named by tag).
