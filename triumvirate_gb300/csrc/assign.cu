@@ -94,10 +94,157 @@ __device__ __forceinline__ double warp_sum(double v) {
 struct AssignArgs {
   int n[3];
   double L[3];
+  double ratio[3];  // n / L
   int64_t nmesh;
   DevCatalogue cat;
   WeightSpec ws;
+  bool vec4;        // z rows 16-byte aligned in every target mesh
 };
+
+// ---- FP32-mesh fast stencil ------------------------------------------------
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so for FP32 meshes
+// FP64 enters only in loc = x * (n / L) and its split into cell index and
+// offset; windows and products are FP32.  The multiply by the ratio differs
+// from the library's (n x) / L by a few ulps of loc (< 1e-12 here), which
+// can change a cell choice only when the offset lies that close to 0, 1/2
+// or 1 (the cell edge, the TSC / NGP split and the interlacing shadow's
+// half-cell shift).  Particles whose offset lies within kTieMargin of those
+// values, or outside [0, L), take the exact FP64 stencil instead.
+
+constexpr float kTieMargin = 1e-6f;
+
+template <int ORDER>
+struct StencilF {
+  int idx[ORDER];
+  float win[ORDER];
+};
+
+// Cell indices (the same branches as axis_stencil) and FP32 windows for the
+// offset s of cell idx.
+template <int ORDER>
+__device__ __forceinline__ void fill_stencil_f(int idx, float s, int n,
+                                               bool shadow,
+                                               StencilF<ORDER>& st) {
+  if (ORDER == 1) {
+    int i0 = idx;
+    if (s >= 0.5f) i0 = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[0] = i0;
+    st.win[0] = 1.f;
+  } else if (ORDER == 2) {
+    st.idx[0] = idx;
+    st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+    st.win[0] = 1.f - s;
+    st.win[1] = s;
+  } else if (ORDER == 3) {
+    if (s < 0.5f) {
+      st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+      st.idx[1] = idx;
+      st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+      st.win[0] = 0.5f * (0.5f - s) * (0.5f - s);
+      st.win[1] = 0.75f - s * s;
+      st.win[2] = 0.5f * (0.5f + s) * (0.5f + s);
+    } else {
+      st.idx[0] = idx;
+      st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+      if (shadow) {
+        st.idx[2] = (idx == n - 1) ? 0 : st.idx[1] + 1;
+      } else {
+        st.idx[2] = (st.idx[1] == n - 1) ? 0 : st.idx[1] + 1;
+      }
+      const float t = 1.f - s;
+      st.win[0] = 0.5f * (0.5f + t) * (0.5f + t);
+      st.win[1] = 0.75f - t * t;
+      st.win[2] = 0.5f * (0.5f - t) * (0.5f - t);
+    }
+  } else {
+    st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+    st.idx[1] = idx;
+    st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[3] = (st.idx[2] == n - 1) ? 0 : st.idx[2] + 1;
+    const float t = 1.f - s;
+    const float c = 1.f / 6.f;
+    st.win[0] = c * t * t * t;
+    st.win[1] = c * (4.f - 6.f * s * s + 3.f * s * s * s);
+    st.win[2] = c * (4.f - 6.f * t * t + 3.f * t * t * t);
+    st.win[3] = c * s * s * s;
+  }
+}
+
+// Main (and, if `shadow` is given, shadow) stencil of one axis; false when
+// the particle must take the exact path.  The shadow cell follows from the
+// main one: loc + 1/2 stays in cell idx when s < 1/2 and moves to the next
+// cell (wrapping to 0 past the last, as the library's loc -= n does)
+// otherwise.
+template <int ORDER>
+__device__ __forceinline__ bool axis_stencil_f(double pos, int n, double ratio,
+                                               StencilF<ORDER>& main,
+                                               StencilF<ORDER>* shadow) {
+  const double loc = pos * ratio;
+  const int idx = int(loc);
+  const float s = float(loc - double(idx));
+  if (idx < 0 || idx >= n || !(s >= kTieMargin) || s > 1.f - kTieMargin ||
+      fabsf(s - 0.5f) < kTieMargin)
+    return false;
+  fill_stencil_f<ORDER>(idx, s, n, false, main);
+  if (shadow != nullptr) {
+    if (s < 0.5f)
+      fill_stencil_f<ORDER>(idx, s + 0.5f, n, true, *shadow);
+    else
+      fill_stencil_f<ORDER>((idx == n - 1) ? 0 : idx + 1, s - 0.5f, n, true,
+                            *shadow);
+  }
+  return true;
+}
+
+// Adds v[0..ORDER) to the z run starting at cell `z0` of a row beginning at
+// `row` (16-byte aligned): one or two float4 atomics, zeros in the lanes
+// outside the run (adding 0 leaves a cell unchanged).
+template <int ORDER>
+__device__ __forceinline__ void red_run4(float* row, int z0, const float* v) {
+  const int off = z0 & 3;
+  float q[8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    float x = 0.f;
+#pragma unroll
+    for (int k = 0; k < ORDER; ++k) x = (l == off + k) ? v[k] : x;
+    q[l] = x;
+  }
+  float4* p = reinterpret_cast<float4*>(row + (z0 - off));
+  atomicAdd(p, make_float4(q[0], q[1], q[2], q[3]));
+  if (off + ORDER > 4) atomicAdd(p + 1, make_float4(q[4], q[5], q[6], q[7]));
+}
+
+template <int ORDER>
+__device__ __forceinline__ void deposit_f(const AssignArgs& a,
+                                          const StencilF<ORDER>& sx,
+                                          const StencilF<ORDER>& sy,
+                                          const StencilF<ORDER>& sz, float wgt,
+                                          float* mesh) {
+  bool run = a.vec4;
+#pragma unroll
+  for (int k = 1; k < ORDER; ++k) run = run && (sz.idx[k] == sz.idx[0] + k);
+#pragma unroll
+  for (int i = 0; i < ORDER; ++i) {
+    const float wi = sx.win[i] * wgt;
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) {
+      float* row =
+          mesh + (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
+      const float wij = wi * sy.win[j];
+      float v[ORDER];
+#pragma unroll
+      for (int k = 0; k < ORDER; ++k) v[k] = wij * sz.win[k];
+      if (run) {
+        red_run4<ORDER>(row, sz.idx[0], v);
+      } else {
+#pragma unroll
+        for (int k = 0; k < ORDER; ++k) atomicAdd(row + sz.idx[k], v[k]);
+      }
+    }
+  }
+}
 
 // Deposit one stencil; returns the weight that landed inside the mesh.
 // Stencil indices and window values are FP64 (they decide the cells); the
@@ -183,7 +330,20 @@ __device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
   return landed;
 }
 
+// Exact deposit of one particle (main and shadow); out of line in the FP32
+// kernel, where only the rare particles near a tie take it.
 template <int ORDER, class Real>
+__device__ __noinline__ void exact_particle(const AssignArgs& a,
+                                            const double* pos, cd wgt,
+                                            Real* re, Real* im, Real* sre,
+                                            Real* sim, cd* landed) {
+  landed[0] = deposit<ORDER, Real>(a, pos, false, wgt, re, im);
+  if (sre != nullptr)
+    landed[1] = deposit<ORDER, Real>(a, pos, true, wgt, sre, sim);
+}
+
+// SH: the interlacing shadow is deposited too (sre != nullptr).
+template <int ORDER, class Real, bool SH>
 __global__ void __launch_bounds__(256)
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
@@ -201,11 +361,38 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
       if (a.ws.conj_ylm) y = conjg(y);
       wgt = (a.ws.scale * wp) * y;
     }
-    cd l = deposit<ORDER, Real>(a, pos, false, wgt, re, im);
-    acc = acc + l;
-    if (sre != nullptr) {
-      cd ls = deposit<ORDER, Real>(a, pos, true, wgt, sre, sim);
-      acc_s = acc_s + ls;
+    if constexpr (sizeof(Real) == 4) {
+      StencilF<ORDER> sx, sy, sz, hx, hy, hz;
+      if (axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                                SH ? &hx : nullptr) &&
+          axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                                SH ? &hy : nullptr) &&
+          axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                                SH ? &hz : nullptr)) {
+        // Every cell is inside the mesh and the windows sum to one: the
+        // landed weight is the weight itself.
+        deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), re);
+        if (im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), im);
+        acc = acc + wgt;
+        if constexpr (SH) {
+          deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), sre);
+          if (sim != nullptr)
+            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), sim);
+          acc_s = acc_s + wgt;
+        }
+        continue;
+      }
+      cd landed[2] = {{0., 0.}, {0., 0.}};
+      exact_particle<ORDER, Real>(a, pos, wgt, re, im, sre, sim, landed);
+      acc = acc + landed[0];
+      acc_s = acc_s + landed[1];
+    } else {
+      cd l = deposit<ORDER, Real>(a, pos, false, wgt, re, im);
+      acc = acc + l;
+      if constexpr (SH) {
+        cd ls = deposit<ORDER, Real>(a, pos, true, wgt, sre, sim);
+        acc_s = acc_s + ls;
+      }
     }
   }
   // Block-wide FP64 sums of the deposited weight (k = 0 modes).
@@ -317,34 +504,38 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
   for (int i = 0; i < 3; ++i) {
     a.n[i] = g.n[i];
     a.L[i] = g.L[i];
+    a.ratio[i] = double(g.n[i]) / g.L[i];
   }
   a.nmesh = g.nmesh;
   a.cat = cat;
   a.ws = ws;
   Real* sre = interlace ? shadow_re : nullptr;
   Real* sim = interlace ? shadow_im : nullptr;
+  auto aligned16 = [](const Real* p) {
+    return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0;
+  };
+  a.vec4 = g.n[2] % 4 == 0 && aligned16(mesh_re) && aligned16(mesh_im) &&
+           aligned16(sre) && aligned16(sim);
   const int block = 256;
   const int grid = grid_for(cat.n, block);
+  auto go = [&](auto kernel) {
+    TRVG_KBEGIN(ctx, "assign_kernel");
+    kernel<<<grid, block, 0, ctx.stream>>>(a, mesh_re, mesh_im, sre, sim,
+                                           sums);
+  };
+  const bool sh = sre != nullptr;
   switch (order) {
     case 1:
-      TRVG_KBEGIN(ctx, "assign_kernel");
-      assign_kernel<1, Real><<<grid, block, 0, ctx.stream>>>(
-          a, mesh_re, mesh_im, sre, sim, sums);
+      sh ? go(assign_kernel<1, Real, true>) : go(assign_kernel<1, Real, false>);
       break;
     case 2:
-      TRVG_KBEGIN(ctx, "assign_kernel");
-      assign_kernel<2, Real><<<grid, block, 0, ctx.stream>>>(
-          a, mesh_re, mesh_im, sre, sim, sums);
+      sh ? go(assign_kernel<2, Real, true>) : go(assign_kernel<2, Real, false>);
       break;
     case 3:
-      TRVG_KBEGIN(ctx, "assign_kernel");
-      assign_kernel<3, Real><<<grid, block, 0, ctx.stream>>>(
-          a, mesh_re, mesh_im, sre, sim, sums);
+      sh ? go(assign_kernel<3, Real, true>) : go(assign_kernel<3, Real, false>);
       break;
     case 4:
-      TRVG_KBEGIN(ctx, "assign_kernel");
-      assign_kernel<4, Real><<<grid, block, 0, ctx.stream>>>(
-          a, mesh_re, mesh_im, sre, sim, sums);
+      sh ? go(assign_kernel<4, Real, true>) : go(assign_kernel<4, Real, false>);
       break;
     default:
       throw_error(TRVG_ERR_INVALID_PARAMETER,

@@ -209,4 +209,53 @@ struct AxisTables {
   const double* inv_alias[3];  // 1 / alias
 };
 
+// ---------------------------------------------------------------------------
+// Float-float accumulation.  GB300 issues FP64 (adds, and even conversions
+// from FP32) at a small fraction of its FP32 rate, so long FP32 sums are
+// carried as an unevaluated pair hi + lo updated with Knuth's TwoSum (the
+// rounding error of each addition is recovered exactly and kept in lo).
+// The pair holds a sum to about 2^-44 relative using FP32 operations only;
+// it becomes a double once, at the end.
+// ---------------------------------------------------------------------------
+
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_zero() { return FF{0.f, 0.f}; }
+
+// a += x.
+__device__ __forceinline__ void ff_add(FF& a, float x) {
+  const float s = a.hi + x;
+  const float bv = s - a.hi;
+  const float err = (a.hi - (s - bv)) + (x - bv);
+  a.hi = s;
+  a.lo += err;
+}
+
+// a += b.
+__device__ __forceinline__ void ff_merge(FF& a, const FF& b) {
+  const float s = a.hi + b.hi;
+  const float bv = s - a.hi;
+  const float err = (a.hi - (s - bv)) + (b.hi - bv) + (a.lo + b.lo);
+  const float t = s + err;
+  a.lo = err - (t - s);
+  a.hi = t;
+}
+
+__device__ __forceinline__ double ff_value(const FF& a) {
+  return double(a.hi) + double(a.lo);
+}
+
+// Warp-wide float-float sum; the total is valid in lane 0.
+__device__ __forceinline__ FF ff_warp_sum(FF a) {
+  for (int o = 16; o > 0; o >>= 1) {
+    FF b;
+    b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+    b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+    ff_merge(a, b);
+  }
+  return a;
+}
+
 }  // namespace trvg

@@ -152,6 +152,7 @@ void Context::release() {
   for (auto& kv : buffers)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   buffers.clear();
+  splines.clear();
 }
 
 void destroy_events(Context& c) {

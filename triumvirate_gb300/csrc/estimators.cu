@@ -672,14 +672,19 @@ struct Engine {
     SplineTable t;
   };
 
+  // The table of j_ell, built and uploaded once per context.
   SplineTable spline(int ell) {
+    auto it = ctx.splines.find(ell);
+    if (it != ctx.splines.end()) return it->second;
     SplineHost s(ell);
     const std::string tag = "spline." + std::to_string(ell);
     const double* y = upload(tag + ".y", s.y);
     const double* b = upload(tag + ".b", s.b);
     const double* c = upload(tag + ".c", s.c);
     const double* d = upload(tag + ".d", s.d);
-    return s.table(y, b, c, d);
+    const SplineTable t = s.table(y, b, c, d);
+    ctx.splines[ell] = t;
+    return t;
   }
 
   // Uncoupled shot noise per pair (field.cpp:3349-3396):

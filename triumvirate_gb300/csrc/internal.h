@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include "common.cuh"
 #include "trvg.h"
 
 namespace trvg {
@@ -127,6 +128,8 @@ struct Context {
   const char* pending = nullptr;
   cudaEvent_t pending_begin = nullptr;
   std::vector<std::pair<std::string, std::pair<double, int64_t>>> ktimes;
+  // j_ell spline tables by ell (device arrays are named buffers).
+  std::map<int, SplineTable> splines;
 
   void kbegin(const char* name);
   void kend();

@@ -2,7 +2,8 @@
 //
 //  * reduce_pairs: sum_x F_a(x) F_b(x) G(x) for many bin pairs in one launch
 //    (the triple-product loops of threept.cpp:1703-1723 and its copies),
-//    accumulated in FP64.
+//    accumulated in FP64 for FP64 fields and as float-float pairs (FP32
+//    operations only) for FP32 fields.
 //  * radial_hist + pair_bessel_sums: the uncoupled shot noise of the
 //    bispectrum, vol_cell sum_x j_la(k_a r) j_lb(k_b r) y_a(r) y_b(r) xi(x)
 //    (field.cpp:3349-3396).  With cubic cells r depends on x only through
@@ -67,6 +68,46 @@ __device__ __forceinline__ C cmulc(C a, C b) {
 
 constexpr int kPairChunk = 8;
 
+// Per-thread sum: float-float for FP32 fields, FP64 for FP64 fields.
+template <class Real>
+struct Acc;
+template <>
+struct Acc<float> {
+  FF v = {0.f, 0.f};
+  __device__ __forceinline__ void add(float x) { ff_add(v, x); }
+  __device__ __forceinline__ double warp_total() {
+    return ff_value(ff_warp_sum(v));
+  }
+};
+template <>
+struct Acc<double> {
+  double v = 0.;
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ double warp_total() { return warp_sum(v); }
+};
+
+// Block-wide sums of N accumulators, atomically added to out[q * stride]
+// for q < limit.  Warps sum in the accumulators' own arithmetic; the
+// (at most 32) warp totals are added in FP64.
+template <int N, class Real>
+__device__ __forceinline__ void block_add_acc(Acc<Real> (&a)[N], double* out,
+                                              int stride, int limit,
+                                              double* red /* [N][32] */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double s = a[q].warp_total();
+    if (lane == 0) red[q * 32 + wid] = s;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < N && q < limit; q += blockDim.x) {
+    double s = 0.;
+    for (int w = 0; w < nw; ++w) s += red[q * 32 + w];
+    atomicAdd(out + int64_t(q) * stride, s);
+  }
+}
+
 template <class Real>
 __global__ void __launch_bounds__(256)
 reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
@@ -84,9 +125,7 @@ reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
     ia[q] = ok[q] ? pa[p0 + q] : 0;
     ib[q] = ok[q] ? pb[p0 + q] : 0;
   }
-  double acc[2 * kPairChunk];
-#pragma unroll
-  for (int q = 0; q < 2 * kPairChunk; ++q) acc[q] = 0.;
+  Acc<Real> acc[2 * kPairChunk];
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
        t += int64_t(gridDim.x) * blockDim.x) {
     const C g = G[t];
@@ -96,15 +135,16 @@ reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
       const C a = Fa[int64_t(ia[q]) * ncell + t];
       const C b = Fb[int64_t(ib[q]) * ncell + t];
       const C p = cmulc(cmulc(a, b), g);
-      acc[2 * q] += double(p.x);
-      acc[2 * q + 1] += double(p.y);
+      acc[2 * q].add(p.x);
+      acc[2 * q + 1].add(p.y);
     }
   }
-  block_add<2 * kPairChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
+  block_add_acc<2 * kPairChunk, Real>(acc, out + 2 * p0, 1, 2 * (npairs - p0),
+                                      red);
 }
 
-// Real fields: sum_x F_a F_b G with FP64 accumulation; the imaginary part
-// of the output is left at zero.
+// Real fields: sum_x F_a F_b G; the imaginary part of the output is left
+// at zero.
 template <class Real>
 __global__ void __launch_bounds__(256)
 reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
@@ -120,9 +160,7 @@ reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
     ia[q] = ok[q] ? pa[p0 + q] : 0;
     ib[q] = ok[q] ? pb[p0 + q] : 0;
   }
-  double acc[kPairChunk];
-#pragma unroll
-  for (int q = 0; q < kPairChunk; ++q) acc[q] = 0.;
+  Acc<Real> acc[kPairChunk];
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
        t += int64_t(gridDim.x) * blockDim.x) {
     const Real g = G[t];
@@ -132,24 +170,10 @@ reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
       const Real a = Fa[int64_t(ia[q]) * ncell + t];
       const Real b = (ia[q] == ib[q] && Fa == Fb)
                          ? a : Fb[int64_t(ib[q]) * ncell + t];
-      acc[q] += double(a * b * g);
+      acc[q].add(a * b * g);
     }
   }
-  // Reduce and write the real parts at out[2 * (p0 + q)].
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
-#pragma unroll
-  for (int q = 0; q < kPairChunk; ++q) {
-    const double s = warp_sum(acc[q]);
-    if (lane == 0) red[q * 32 + wid] = s;
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < kPairChunk; q += blockDim.x) {
-    if (!ok[q]) continue;
-    double s = 0.;
-    for (int w = 0; w < nw; ++w) s += red[q * 32 + w];
-    atomicAdd(out + 2 * (p0 + q), s);
-  }
+  block_add_acc<kPairChunk, Real>(acc, out + 2 * p0, 2, npairs - p0, red);
 }
 
 // Sum of xi * y_a * y_b per integer key s_x^2 + s_y^2 + s_z^2 (cubic cells).
@@ -180,15 +204,12 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
   }
 }
 
-// The same sums without atomics, for even mesh numbers.  The cells
-// (+-s_x, +-s_y, +-s_z) -- and, when n_x = n_y, their x <-> y swaps -- share
-// one key.
-//   (1) orbit_rows: one block per (a, b) = (|s_x|, |s_y|) (b <= a with the
-//       swap), threads along c = |s_z|; each thread sums its <= 16 mirror
-//       cells and stores V[(a, b)][c] (coalesced, no atomics);
-//   (2) key_gather: one thread per key gathers H[key] = sum of V[(a, b)][c]
-//       over a^2 + b^2 + c^2 = key, walking c and a host-built list of the
-//       (a, b) pairs of each u = a^2 + b^2.  Every (a, b, c) is read once.
+// The same sums for even mesh numbers, with one atomic per orbit row
+// instead of one per cell.  The cells (+-s_x, +-s_y, +-s_z) -- and, when
+// n_x = n_y, their x <-> y swaps -- share the key a^2 + b^2 + c^2 with
+// (a, b, c) = (|s_x|, |s_y|, |s_z|).  One block per (a, b) (b <= a with the
+// swap), threads along c: each thread sums its <= 16 mirror cells and adds
+// the sum to the key's FP64 bin.
 __device__ __forceinline__ void orbit_ab(int q, bool swap, int hy, int& a,
                                          int& b) {
   if (swap) {
@@ -202,54 +223,61 @@ __device__ __forceinline__ void orbit_ab(int q, bool swap, int hy, int& a,
   }
 }
 
-template <class Real>
+// TRIVIAL: both degrees are (0, 0), so y_a y_b = 1.
+template <class Real, bool TRIVIAL>
 __global__ void __launch_bounds__(256)
 orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
-                  int m_a, int ell_b, int m_b, bool swap, double* v_re,
-                  double* v_im) {
-  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+                  int m_a, int ell_b, int m_b, bool swap, double* hist) {
   const int hy = g.n[1] / 2, hz = g.n[2] / 2;
-  const int q = blockIdx.x;
   int a, b;
-  orbit_ab(q, swap, hy, a, b);
-  const int xs[2] = {a, (g.n[0] - a) % g.n[0]};
-  const int ys[2] = {b, (g.n[1] - b) % g.n[1]};
-  const int nxs = (xs[1] == xs[0]) ? 1 : 2;
-  const int nys = (ys[1] == ys[0]) ? 1 : 2;
-  const int nsw = (swap && a != b) ? 2 : 1;
-  // The up-to-8 rows of the orbit.
-  int64_t rows[8];
-  int nrows = 0;
-  for (int w = 0; w < nsw; ++w)
-    for (int p = 0; p < nxs; ++p)
-      for (int qq = 0; qq < nys; ++qq) {
-        const int i = (w == 0) ? xs[p] : ys[qq];
-        const int j = (w == 0) ? ys[qq] : xs[p];
-        rows[nrows++] = (int64_t(i) * g.n[1] + j) * g.n[2];
+  orbit_ab(blockIdx.x, swap, hy, a, b);
+  const int xs[2] = {a, (a == 0) ? 0 : g.n[0] - a};
+  const int ys[2] = {b, (b == 0) ? 0 : g.n[1] - b};
+  const bool x2 = xs[1] != xs[0], y2 = ys[1] != ys[0];
+  const bool sw = swap && a != b;
+  // Row i * n_y + j of each of the up-to-8 rows of the orbit (-1: absent),
+  // held in registers so that every load of a thread is issued at once.
+  int rowi[8];
+#pragma unroll
+  for (int w = 0; w < 2; ++w)
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const bool use = (w == 0 || sw) && (p == 0 || x2) && (q == 0 || y2);
+        const int i = (w == 0) ? xs[p] : ys[q];
+        const int j = (w == 0) ? ys[q] : xs[p];
+        rowi[w * 4 + p * 2 + q] = use ? i * g.n[1] + j : -1;
       }
+  const int64_t key_ab = int64_t(a) * a + int64_t(b) * b;
   for (int c = threadIdx.x; c <= hz; c += blockDim.x) {
-    const int c2 = (g.n[2] - c) % g.n[2];
+    const int c2 = (c == 0) ? 0 : g.n[2] - c;
     const bool two = (c2 != c);
     cd acc = {0., 0.};
-    if (trivial) {
+    if constexpr (TRIVIAL) {
       Real sr = Real(0), si = Real(0);
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
-        if (r >= nrows) break;
-        sr += xi_re[rows[r] + c] + (two ? xi_re[rows[r] + c2] : Real(0));
-        if (xi_im != nullptr)
-          si += xi_im[rows[r] + c] + (two ? xi_im[rows[r] + c2] : Real(0));
+        if (rowi[r] < 0) continue;
+        const int64_t base = int64_t(rowi[r]) * g.n[2];
+        sr += xi_re[base + c];
+        if (two) sr += xi_re[base + c2];
+        if (xi_im != nullptr) {
+          si += xi_im[base + c];
+          if (two) si += xi_im[base + c2];
+        }
       }
       acc = cd{double(sr), double(si)};
     } else {
-      for (int r = 0; r < nrows; ++r) {
-        const int64_t row = rows[r];
-        const int i = int(row / (int64_t(g.n[1]) * g.n[2]));
-        const int j = int((row / g.n[2]) % g.n[1]);
+#pragma unroll 1
+      for (int r = 0; r < 8; ++r) {
+        if (rowi[r] < 0) continue;
+        const int i = rowi[r] / g.n[1], j = rowi[r] - i * g.n[1];
+        const int64_t base = int64_t(rowi[r]) * g.n[2];
         for (int z = 0; z < (two ? 2 : 1); ++z) {
           const int k = (z == 0) ? c : c2;
-          cd v = {double(xi_re[row + k]),
-                  xi_im != nullptr ? double(xi_im[row + k]) : 0.};
+          cd v = {double(xi_re[base + k]),
+                  xi_im != nullptr ? double(xi_im[base + k]) : 0.};
           const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
           const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
           const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
@@ -259,31 +287,9 @@ orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
         }
       }
     }
-    const int64_t o = int64_t(q) * (hz + 1) + c;
-    v_re[o] = acc.re;
-    if (v_im != nullptr) v_im[o] = acc.im;
-  }
-}
-
-__global__ void __launch_bounds__(256)
-key_gather_kernel(int64_t nkeys, int hz, int umax, const int* u_off,
-                  const int* u_list, const double* v_re, const double* v_im,
-                  double* hist) {
-  for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-       key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
-    double hr = 0., hi = 0.;
-    for (int c = 0; c <= hz; ++c) {
-      const int64_t u = key - int64_t(c) * c;
-      if (u < 0) break;
-      if (u > umax) continue;
-      for (int e = u_off[u]; e < u_off[u + 1]; ++e) {
-        const int64_t o = int64_t(u_list[e]) * (hz + 1) + c;
-        hr += v_re[o];
-        if (v_im != nullptr) hi += v_im[o];
-      }
-    }
-    hist[2 * key] = hr;
-    hist[2 * key + 1] = hi;
+    const int64_t key = key_ab + int64_t(c) * c;
+    atomicAdd(hist + 2 * key, acc.re);
+    if (xi_im != nullptr || !TRIVIAL) atomicAdd(hist + 2 * key + 1, acc.im);
   }
 }
 
@@ -463,69 +469,15 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
     const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
     const int nblocks =
         swap ? (hx + 1) * (hx + 2) / 2 : (hx + 1) * (hy + 1);
-    // (a, b) pairs grouped by u = a^2 + b^2 (cached per mesh shape).
-    const int umax = hx * hx + hy * hy;
-    const std::string tag = "orbit." + std::to_string(g.n[0]) + "." +
-                            std::to_string(g.n[1]) + "." +
-                            std::to_string(g.n[2]);
-    auto it = ctx.buffers.find(tag + ".off");
-    int* u_off;
-    int* u_list;
-    if (it == ctx.buffers.end()) {
-      std::vector<int> cnt(size_t(umax) + 2, 0);
-      for (int q = 0; q < nblocks; ++q) {
-        int a, b;
-        if (swap) {
-          a = int((std::sqrt(8. * q + 1.) - 1.) * 0.5);
-          while ((a + 1) * (a + 2) / 2 <= q) ++a;
-          while (a * (a + 1) / 2 > q) --a;
-          b = q - a * (a + 1) / 2;
-        } else {
-          a = q / (hy + 1);
-          b = q - a * (hy + 1);
-        }
-        cnt[size_t(a) * a + size_t(b) * b + 1]++;
-      }
-      for (size_t u = 1; u < cnt.size(); ++u) cnt[u] += cnt[u - 1];
-      std::vector<int> list(nblocks), fill(cnt.begin(), cnt.end() - 1);
-      for (int q = 0; q < nblocks; ++q) {
-        int a, b;
-        if (swap) {
-          a = int((std::sqrt(8. * q + 1.) - 1.) * 0.5);
-          while ((a + 1) * (a + 2) / 2 <= q) ++a;
-          while (a * (a + 1) / 2 > q) --a;
-          b = q - a * (a + 1) / 2;
-        } else {
-          a = q / (hy + 1);
-          b = q - a * (hy + 1);
-        }
-        list[fill[size_t(a) * a + size_t(b) * b]++] = q;
-      }
-      u_off = ctx.buf<int>(tag + ".off", cnt.size());
-      u_list = ctx.buf<int>(tag + ".list", list.size());
-      TRVG_CUDA(cudaMemcpyAsync(u_off, cnt.data(), cnt.size() * sizeof(int),
-                                cudaMemcpyHostToDevice, ctx.stream));
-      TRVG_CUDA(cudaMemcpyAsync(u_list, list.data(),
-                                list.size() * sizeof(int),
-                                cudaMemcpyHostToDevice, ctx.stream));
-      TRVG_CUDA(cudaStreamSynchronize(ctx.stream));
-    } else {
-      u_off = static_cast<int*>(it->second.ptr);
-      u_list = static_cast<int*>(ctx.buffers[tag + ".list"].ptr);
-    }
-    const size_t nv = size_t(nblocks) * (hz + 1);
-    double* v_re = ctx.buf<double>("orbit.v.re", nv);
-    double* v_im = xi_im ? ctx.buf<double>("orbit.v.im", nv) : nullptr;
     const int threads = std::min(256, ((hz + 1 + 31) / 32) * 32);
+    const bool trivial = ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0;
     TRVG_KBEGIN(ctx, "orbit_rows_kernel");
-    orbit_rows_kernel<Real><<<nblocks, threads, 0, ctx.stream>>>(
-        g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, v_re, v_im);
-    TRVG_LAUNCHED(ctx);
-    const int64_t nkeys = int64_t(hx) * hx + int64_t(hy) * hy +
-                          int64_t(hz) * hz + 1;
-    TRVG_KBEGIN(ctx, "key_gather_kernel");
-    key_gather_kernel<<<grid_for(nkeys, 256), 256, 0, ctx.stream>>>(
-        nkeys, hz, umax, u_off, u_list, v_re, v_im, hist);
+    if (trivial)
+      orbit_rows_kernel<Real, true><<<nblocks, threads, 0, ctx.stream>>>(
+          g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
+    else
+      orbit_rows_kernel<Real, false><<<nblocks, threads, 0, ctx.stream>>>(
+          g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
     TRVG_LAUNCHED(ctx);
     return;
   }

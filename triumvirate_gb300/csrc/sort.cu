@@ -17,19 +17,21 @@ namespace {
 
 constexpr int kTileShift = 3;  // 8 cells per tile side
 
-__device__ __forceinline__ int cell_of(double x, int n, double L) {
-  int i = int(double(n) * x / L);
+// Approximate cell (the tile only orders the deposits): one multiply by
+// n / L, no division.
+__device__ __forceinline__ int cell_of(double x, int n, double ratio) {
+  int i = int(x * ratio);
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
 
 __global__ void tile_key_kernel(DevCatalogue cat, int n0, int n1, int n2,
-                                double L0, double L1, double L2, int t1,
+                                double r0, double r1, double r2, int t1,
                                 int t2, int* key, int* rank, int* count) {
   for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < cat.n;
        p += int64_t(gridDim.x) * blockDim.x) {
-    const int tx = cell_of(cat.x[p], n0, L0) >> kTileShift;
-    const int ty = cell_of(cat.y[p], n1, L1) >> kTileShift;
-    const int tz = cell_of(cat.z[p], n2, L2) >> kTileShift;
+    const int tx = cell_of(cat.x[p], n0, r0) >> kTileShift;
+    const int ty = cell_of(cat.y[p], n1, r1) >> kTileShift;
+    const int tz = cell_of(cat.z[p], n2, r2) >> kTileShift;
     const int k = (tx * t1 + ty) * t2 + tz;
     key[p] = k;
     rank[p] = atomicAdd(count + k, 1);
@@ -148,8 +150,8 @@ DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
                             ctx.stream));
   TRVG_KBEGIN(ctx, "tile_key_kernel");
   tile_key_kernel<<<grid_for(in.n, 256), 256, 0, ctx.stream>>>(
-      in, g.n[0], g.n[1], g.n[2], g.L[0], g.L[1], g.L[2], t1, t2, key, rank,
-      count);
+      in, g.n[0], g.n[1], g.n[2], g.n[0] / g.L[0], g.n[1] / g.L[1],
+      g.n[2] / g.L[2], t1, t2, key, rank, count);
   TRVG_LAUNCHED(ctx);
   const int nscan = int((ntiles + kScanTile - 1) / kScanTile);
   int* tile_sum = ctx.buf<int>(tag + ".sort.tiles", size_t(nscan));

@@ -541,9 +541,11 @@ twopt_field_real_f32_kernel(int n1, int nzh, const float2* fa,
   const int row = blockIdx.x;
   const int i = row / n1, j = row - (row / n1) * n1;
   const float axy = inv_alias_x[i] * inv_alias_y[j];
+  const bool same = fa == fb;  // |f|^2: one read of the spectrum
   for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
     const int64_t t = int64_t(row) * nzh + k;
-    const float2 a = fa[t], b = fb[t];
+    const float2 a = fa[t];
+    const float2 b = same ? a : fb[t];
     const float inv = axy * inv_alias_z[k];
     float2 o;
     o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
