@@ -511,3 +511,39 @@ def test_oracle_lpp_sorted_randoms():
                          sampling_params=_sampling('fp64', 32, 'tsc',
                                                    box=1000.))
     assert_close_threept(res, ref, 'bispec', 'fp64')
+
+
+# ---------------------------------------------------------------------------
+# Measurement files written by the estimators
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("stat", ['bispec', 'powspec'])
+def test_save_writes_readable_measurements(stat, tmp_path):
+    from triumvirate_gb300 import io
+    from triumvirate_gb300.twopt import compute_powspec_in_gpp_box
+    from triumvirate_gb300.parameters import (ParameterSet,
+                                              fetch_paramset_template)
+    pos = _uniform(3000, 800., 13)
+    cat = ParticleCatalogue(*pos.T, nz=3000 / 800. ** 3)
+    d = fetch_paramset_template('dict')
+    d.update(boxsize={ax: 800. for ax in 'xyz'},
+             ngrid={ax: 32 for ax in 'xyz'}, assignment='tsc',
+             interlace=False, precision='fp64')
+    d['directories']['measurements'] = str(tmp_path)
+    binning = Binning('fourier', 'lin', 0.01, 0.1, 4)
+    if stat == 'bispec':
+        res = compute_bispec_in_gpp_box(
+            cat, degrees=(0, 0, 0), binning=binning, form='diag',
+            paramset=ParameterSet(param_dict=d), save='.txt')
+        path, raw = tmp_path / 'bk000_diag.txt', 'bk_raw'
+    else:
+        res = compute_powspec_in_gpp_box(
+            cat, degree=0, binning=binning,
+            paramset=ParameterSet(param_dict=d), save='.txt')
+        path, raw = tmp_path / 'pk0.txt', 'pk_raw'
+    back = io.read_measurements(path)
+    assert np.allclose(back[raw], res[raw], rtol=1e-9, atol=0.)
+    alt = next(h for h in back['header']
+               if h.startswith('Normalisation factor alternatives'))
+    mesh = float(alt.split(', ')[1].split(' (')[0])
+    assert np.isfinite(mesh) and mesh > 0.

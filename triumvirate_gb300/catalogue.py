@@ -164,21 +164,24 @@ class ParticleCatalogue:
         self._calc_bounds()
 
     def write_attrs_as_header(self, catalogue_ref=None):
-        """Catalogue attributes as a measurement-file header."""
-        def one(cat, label=''):
+        """Catalogue attributes as a measurement-file header
+        (catalogue.py:803-858 of the library)."""
+        def one(cat, name, extents):
             b = cat.bounds
             return "\n".join([
-                f"{label}atalogue source: {cat._source}",
-                f"{label}atalogue size: ntotal = {cat.ntotal}, "
+                f"{name} source: {cat._source}",
+                f"{name} size: ntotal = {cat.ntotal:d}, "
                 f"wtotal = {cat.wtotal:.3f}, wstotal = {cat.wstotal:.3f}",
-                f"{label.replace('C', 'Catalogue').strip() or 'Catalogue'}"
-                f" particle extents: ([{b['x'][0]:.3f}, {b['x'][1]:.3f}], "
+                f"{extents} particle extents: "
+                f"([{b['x'][0]:.3f}, {b['x'][1]:.3f}], "
                 f"[{b['y'][0]:.3f}, {b['y'][1]:.3f}], "
                 f"[{b['z'][0]:.3f}, {b['z'][1]:.3f}])",
             ])
         if catalogue_ref is None:
-            return one(self, 'C')
-        return "\n".join([one(self, 'Data c'), one(catalogue_ref, 'Random c')])
+            return one(self, "Catalogue", "Catalogue")
+        return "\n".join([one(self, "Data catalogue", "Data-source"),
+                          one(catalogue_ref, "Random catalogue",
+                              "Random-source")])
 
     # Arrays handed to the C ABI.
     def _columns(self):

@@ -4,11 +4,10 @@ survey-type catalogues, computed on the GPU through ``libtrvg.so``."""
 from __future__ import annotations
 
 import warnings
-from pathlib import Path
 
 import numpy as np
 
-from . import _engine, _lib
+from . import _engine, _lib, io
 from .dataobjs import Binning
 from .parameters import (ParameterSet, _as_dict,
                          _modify_measurement_parameters,
@@ -68,26 +67,51 @@ def _boxsize(paramset):
     return [float(paramset['boxsize'][ax]) for ax in ['x', 'y', 'z']]
 
 
+def _norm_particle(nz, ws, wc, alpha, order, strict=True):
+    """1 / (alpha sum ws nz^(order-1) wc^order) (threept.cpp:96-136,
+    twopt.cpp:56-99)."""
+    if order == 3:
+        norm = float(np.sum(ws * nz ** 2 * wc ** 3))
+    else:
+        norm = float(np.sum(ws * nz * wc ** 2))
+    if norm == 0.:
+        if not strict:
+            return float('inf')
+        raise _lib.InvalidDataError(
+            "Particle 'nz' values appear to be all zeros. Check the "
+            "input catalogue contains valid 'nz' field.")
+    return 1. / (alpha * norm)
+
+
+def _norm_mesh(ctx, params_c, cat_c, alpha, order):
+    """Grid-based normalisation (threept.cpp:138-149, twopt.cpp:101-130)."""
+    return _engine.grid_powlaw_norm(ctx, params_c, cat_c, order) \
+        / alpha ** order
+
+
 def _norm_factor(paramset, ctx, params_c, cat_c, nz, ws, wc, alpha, order):
-    """Particle / mesh normalisation (threept.cpp:96-149,
-    twopt.cpp:56-130)."""
+    """Particle / mesh normalisation of the chosen convention."""
     conv = paramset['norm_convention']
     if conv == 'none':
         return 1.
     if conv == 'particle':
-        if order == 3:
-            norm = float(np.sum(ws * nz ** 2 * wc ** 3))
-        else:
-            norm = float(np.sum(ws * nz * wc ** 2))
-        if norm == 0.:
-            raise _lib.InvalidDataError(
-                "Particle 'nz' values appear to be all zeros. Check the "
-                "input catalogue contains valid 'nz' field.")
-        return 1. / (alpha * norm)
+        return _norm_particle(nz, ws, wc, alpha, order)
     if conv == 'mesh':
-        return _engine.grid_powlaw_norm(ctx, params_c, cat_c, order) \
-            / alpha ** order
+        return _norm_mesh(ctx, params_c, cat_c, alpha, order)
     raise ValueError(f"Unsupported normalisation convention: {conv}.")
+
+
+def _save(results, paramset, save, ctx, params_c, cat_c, nz, ws, wc, alpha,
+          order, catalogue_data, catalogue_rand=None):
+    """Write the measurements with the library's header: catalogue
+    attributes, sampling parameters and every normalisation alternative
+    (threept.py:707-735, twopt.py:633-663)."""
+    part = _norm_particle(nz, ws, wc, alpha, order, strict=False)
+    mesh = _norm_mesh(ctx, params_c, cat_c, alpha, order)
+    header = "\n".join([
+        catalogue_data.write_attrs_as_header(catalogue_ref=catalogue_rand),
+        io.measurement_header(paramset, part, mesh, 0.)])
+    return io.save_measurements(results, paramset, save, header)
 
 
 def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
@@ -126,7 +150,9 @@ def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
         fn, ctx, params_c, cat.c, binning, norm, kind,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
     if save:
-        _save(results, paramset, save, kind, norm)
+        _save(results, paramset, save, ctx, params_c, cat.c,
+              catalogue_data['nz'], catalogue_data['ws'], catalogue_data['wc'],
+              1., 3, catalogue_data)
     return results
 
 
@@ -183,32 +209,10 @@ def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
         alpha=alpha, shape=paramset['shape'],
         idx_bin=paramset.get('idx_bin') or 0)
     if save:
-        _save(results, paramset, save, kind, norm)
+        _save(results, paramset, save, ctx, params_c, rcat.c,
+              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+              alpha, 3, catalogue_data, catalogue_rand)
     return results
-
-
-def _save(results, paramset, save, kind, norm):
-    """Measurement file in the reference's layout (threept.py:707-735)."""
-    odir = paramset['directories'].get('measurements') or ""
-    tag = paramset['tags'].get('output') or ""
-    deg = paramset['degrees']
-    name = (f"{'bk' if kind == 'bispec' else 'zeta'}"
-            f"{deg['ell1']}{deg['ell2']}{deg['ELL']}_{paramset['form']}{tag}")
-    path = Path(odir, name)
-    header = f"Normalisation factor: {norm:.9e} " \
-             f"({paramset['norm_convention']})"
-    if str(save).lower() == '.txt':
-        keys = list(results.keys())
-        raw, shot = results[keys[6]], results[keys[7]]
-        tab = np.column_stack([results[k] for k in keys[:6]] +
-                              [raw.real, raw.imag, shot.real, shot.imag])
-        fmt = '\t'.join((['%.9e'] * 2 + ['%10d']) * 2 + ['% .9e'] * 4)
-        np.savetxt(path.with_suffix('.txt'), tab, fmt=fmt, header=header,
-                   delimiter='\t')
-    elif str(save).lower().endswith('.npz'):
-        np.savez(path.with_suffix('.npz'), header=header, **results)
-    else:
-        raise ValueError(f"Unrecognised save format for measurements: {save}.")
 
 
 def compute_bispec(catalogue_data, catalogue_rand, los_data=None,

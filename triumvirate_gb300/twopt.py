@@ -8,7 +8,7 @@ import numpy as np
 from . import _engine, _lib
 from .dataobjs import Binning
 from .parameters import _as_dict, _set_ngrid_from_cutoff
-from .threept import _amalgamate_parameters, _boxsize, _norm_factor
+from .threept import _amalgamate_parameters, _boxsize, _norm_factor, _save
 
 
 def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
@@ -40,8 +40,13 @@ def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
     cat = _engine.HostCatalogue(x, y, z, w)
     norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data['nz'],
                         catalogue_data['ws'], catalogue_data['wc'], 1., 2)
-    return _engine.call_powspec('trvg_compute_powspec_in_gpp_box', ctx,
-                                params_c, cat.c, binning, norm)
+    results = _engine.call_powspec('trvg_compute_powspec_in_gpp_box', ctx,
+                                   params_c, cat.c, binning, norm)
+    if save:
+        _save(results, paramset, save, ctx, params_c, cat.c,
+              catalogue_data['nz'], catalogue_data['ws'], catalogue_data['wc'],
+              1., 2, catalogue_data)
+    return results
 
 
 def compute_powspec(catalogue_data, catalogue_rand, los_data=None,
@@ -88,5 +93,11 @@ def compute_powspec(catalogue_data, catalogue_rand, los_data=None,
     rcat = _engine.HostCatalogue(xr, yr, zr, wr, np.asarray(los_rand))
     norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
                         catalogue_rand['ws'], catalogue_rand['wc'], alpha, 2)
-    return _engine.call_powspec('trvg_compute_powspec', ctx, params_c, dcat.c,
-                                binning, norm, rand_c=rcat.c, alpha=alpha)
+    results = _engine.call_powspec('trvg_compute_powspec', ctx, params_c,
+                                   dcat.c, binning, norm, rand_c=rcat.c,
+                                   alpha=alpha)
+    if save:
+        _save(results, paramset, save, ctx, params_c, rcat.c,
+              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+              alpha, 2, catalogue_data, catalogue_rand)
+    return results
