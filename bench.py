@@ -56,6 +56,11 @@ def parse_args():
                     help='run two estimates (for an ncu launch list)')
     ap.add_argument('--variants', action='store_true',
                     help='also time the FP32-mixed precision options')
+    ap.add_argument('--workload', default='metric',
+                    choices=['metric', 'mocks'],
+                    help="'mocks': the batched lognormal-mock workload "
+                         "(its own JSON line)")
+    ap.add_argument('--mocks', type=int, default=256)
     return ap.parse_args()
 
 
@@ -492,10 +497,122 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Batched mocks: lognormal-Poisson catalogues of uneven sizes in one call.
+# ---------------------------------------------------------------------------
+
+MOCK_BOX, MOCK_NGRID = 1000., 256
+
+
+def lognormal_mock(torch, dev, seed, npart, box=MOCK_BOX, n=MOCK_NGRID):
+    """Poisson sample of exp(delta_G - sigma^2 / 2) - 1, delta_G Gaussian
+    with P(k) = 2e4 (k / 0.02)^-1.5 exp(-(k / 0.5)^2) (Mpc/h)^3; positions
+    uniform within their cell.  Returns x, y, z (float64, device)."""
+    g = torch.Generator(device=dev).manual_seed(seed)
+    k1 = torch.fft.fftfreq(n, d=box / n, device=dev) * 2 * np.pi
+    kz = torch.fft.rfftfreq(n, d=box / n, device=dev) * 2 * np.pi
+    k = torch.sqrt(k1[:, None, None] ** 2 + k1[None, :, None] ** 2 +
+                   kz[None, None, :] ** 2)
+    pk = 2e4 * (k.clamp_min(1e-12) / 0.02) ** -1.5 * torch.exp(-(k / 0.5) ** 2)
+    pk[0, 0, 0] = 0.
+    vcell = (box / n) ** 3
+    white = torch.randn((n, n, n), generator=g, device=dev)
+    dg = torch.fft.irfftn(torch.fft.rfftn(white) * torch.sqrt(pk / vcell),
+                          s=(n, n, n))
+    dln = torch.exp(dg - dg.var() / 2.) - 1.
+    lam = npart * (1. + dln) / (1. + dln).sum()
+    counts = torch.poisson(lam.flatten(), generator=g).to(torch.int64)
+    cell = torch.repeat_interleave(torch.arange(n ** 3, device=dev), counts)
+    i, j, l = cell // (n * n), (cell // n) % n, cell % n
+    u = torch.rand((3, cell.numel()), generator=g, device=dev,
+                   dtype=torch.float64)
+    h = box / n
+    return ((i + u[0]) * h, (j + u[1]) * h, (l + u[2]) * h)
+
+
+def run_mocks(args):
+    """Config: 256 lognormal mocks with N ~ U[2e5, 2e6], 256^3 mesh, CIC,
+    B_000 and B_202 diag, 24 bins 0.005-0.245 h/Mpc, FP32-mixed, one
+    batched library call per multipole."""
+    import torch
+
+    from triumvirate_gb300 import _engine, _lib
+    from triumvirate_gb300.dataobjs import Binning
+    dev = torch.device('cuda', 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(2024)
+    sizes = rng.integers(200_000, 2_000_001, args.mocks)
+    cols, offsets = [[], [], []], [0]
+    for i, npart in enumerate(sizes):
+        for c, a in zip(cols, lognormal_mock(torch, dev, 1000 + i, npart)):
+            c.append(a)
+        offsets.append(offsets[-1] + cols[0][-1].numel())
+    x, y, z = (torch.cat(c).contiguous() for c in cols)
+    del cols
+    ntot = x.numel()
+    counts = np.diff(offsets)
+    nbar = counts / MOCK_BOX ** 3
+    norms = 1. / (counts * nbar ** 2)
+    binning = Binning('fourier', 'lin', 0.005, 0.245, 24)
+    ctx = _lib.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    cat = _engine.device_catalogue(ntot, x.data_ptr(), y.data_ptr(),
+                                   z.data_ptr())
+
+    def params(degrees):
+        pd = {'boxsize': {a: MOCK_BOX for a in 'xyz'},
+              'ngrid': {a: MOCK_NGRID for a in 'xyz'}, 'assignment_order': 2,
+              'interlace': False,
+              'degrees': dict(zip(['ell1', 'ell2', 'ELL'], degrees)),
+              'form': 'diag', 'shape': 'diag', 'precision': 'fp32mixed',
+              'verbose': 0}
+        return _engine.make_params(pd, '3pt')
+
+    p000, p202 = params((0, 0, 0)), params((2, 0, 2))
+
+    def batch():
+        r0 = _engine.call_bispec_batch(ctx, p000, cat, offsets, binning,
+                                       norms, shape='diag')
+        r2 = _engine.call_bispec_batch(ctx, p202, cat, offsets, binning,
+                                       norms, shape='diag')
+        return r0, r2
+
+    for _ in range(max(1, args.warmup)):
+        batch()
+    torch.cuda.synchronize(dev)
+    times, launches = [], 0
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = statistics.median(times)
+    line = {
+        "metric": "batched mock bispectra (B_000 + B_202 per mock)",
+        "value": round(args.mocks / t, 2), "unit": "mocks/s",
+        "higher_is_better": True, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "s_per_batch": round(t, 4),
+        "dtype": "f32 meshes/FFTs, f64 offsets/reductions",
+        "data": "synthetic lognormal-Poisson mocks generated on the GPU",
+        "config": {"workload": (f"{args.mocks} mocks, N ~ U[2e5, 2e6] "
+                                f"(total {ntot}), {MOCK_NGRID}^3 mesh, CIC, "
+                                "L=1000 Mpc/h, B_000 and B_202 diag, 24 lin "
+                                "bins 0.005-0.245 h/Mpc"),
+                   "batching": "one library call per multipole"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.workload == 'mocks':
+        run_mocks(args)
     else:
         run_gb300(args)
 

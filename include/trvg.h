@@ -208,6 +208,37 @@ int trvg_compute_bispec_in_gpp_box(
   const trvg_catalogue* data, const trvg_binning* kbinning,
   double norm_factor, trvg_threept_out* out);
 
+/* Bispectra of n_mocks periodic-box catalogues in one call (the reference
+ * calls trv::compute_bispec_in_gpp_box once per catalogue).  `particles`
+ * holds the catalogues back to back: mock i is the slice
+ * [offsets[i], offsets[i + 1]) of every column (offsets[0] = 0,
+ * offsets[n_mocks] = particles->n); norm_factors[i] and outs[i] belong to
+ * mock i.  Plans, workspace, spline tables and the catalogue-independent
+ * mode counts are shared by the whole batch. */
+/* Adjoint of the raw periodic-box bispectrum of degrees (0, 0, 0); the
+ * reference has no derivatives.  For the cotangent
+ * cotangent[2 i] = dL / d Re(raw_i) of every data-vector entry (raw B_000
+ * is real, so cotangent[2 i + 1] is not used) it writes, each optional and
+ * in the memory kind of `data`:
+ *   grad_mesh  dL/dm of the weighted count mesh m that the assignment
+ *              deposits (ngrid[0] * ngrid[1] * ngrid[2] doubles, z fastest);
+ *   grad_w     dL/dw_i (n doubles);
+ *   grad_pos   dL/dx_i, dL/dy_i, dL/dz_i (3 n doubles: every x, then every
+ *              y, then every z), for positions in [0, L);
+ * and, if `out` is given, the raw values themselves (shot left at 0: shot
+ * noise is not differentiated).  Needs even mesh numbers or a pruned
+ * evaluation grid. */
+int trvg_bispec_gpp_adjoint(
+  trvg_context* ctx, const trvg_params* params, const trvg_catalogue* data,
+  const trvg_binning* kbinning, double norm_factor, const double* cotangent,
+  double* grad_mesh, double* grad_w, double* grad_pos, trvg_threept_out* out);
+
+int trvg_compute_bispec_in_gpp_box_batch(
+  trvg_context* ctx, const trvg_params* params,
+  const trvg_catalogue* particles, int n_mocks, const int64_t* offsets,
+  const trvg_binning* kbinning, const double* norm_factors,
+  trvg_threept_out* outs);
+
 /* Bispectrum, survey-type catalogues, local plane-parallel line of sight.
  * `alpha` = wstotal_data / wstotal_rand (threept.cpp:271). */
 int trvg_compute_bispec(

@@ -547,3 +547,37 @@ def test_save_writes_readable_measurements(stat, tmp_path):
                if h.startswith('Normalisation factor alternatives'))
     mesh = float(alt.split(', ')[1].split(' (')[0])
     assert np.isfinite(mesh) and mesh > 0.
+
+
+# ---------------------------------------------------------------------------
+# Batched catalogues
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("precision", ['fp64', 'fp32mixed'])
+def test_batch_matches_single_calls(precision):
+    """Mocks of uneven sizes in one call give each mock's own result."""
+    from triumvirate_gb300.threept import compute_bispec_in_gpp_box_batch
+    box, sizes = 600., [1500, 4000, 2500]
+    pos = [_uniform(n, box, 30 + i) for i, n in enumerate(sizes)]
+    binning = Binning('fourier', 'lin', 0.01, 0.1, 4)
+    samp = _sampling(precision, 32, box=box)
+
+    def cats():
+        return [ParticleCatalogue(*p.T, nz=len(p) / box ** 3) for p in pos]
+    single = [compute_bispec_in_gpp_box(c, degrees=(0, 0, 0),
+                                        binning=binning, form='diag',
+                                        sampling_params=samp)
+              for c in cats()]
+    batch = compute_bispec_in_gpp_box_batch(cats(), degrees=(0, 0, 0),
+                                            binning=binning, form='diag',
+                                            sampling_params=samp)
+    assert len(batch) == len(single)
+    for b, s in zip(batch, single):
+        assert np.array_equal(b['nmodes_1'], s['nmodes_1'])
+        for k in ('bk_raw', 'bk_shot'):
+            if precision == 'fp64':
+                assert rel_err(b[k], s[k]) < 1e-10, k
+            else:
+                # FP32 atomics deposit in a different order on each call.
+                err = np.max(np.abs(b[k] - s[k])) / np.max(np.abs(s[k]))
+                assert err < 1e-5, k

@@ -153,6 +153,25 @@ def call_threept(fn_name, ctx, params, data_c, binning, norm, kind,
     return res.as_dict(kind)
 
 
+def call_bispec_batch(ctx, params, cat_c, offsets, binning, norms, shape,
+                      idx_bin=0):
+    """trvg_compute_bispec_in_gpp_box_batch over the concatenated catalogue
+    `cat_c`; one result dictionary per mock."""
+    lib = _lib.load()
+    n_mocks = len(norms)
+    dim = dv_dim(shape, binning.num_bins, idx_bin)
+    res = [ThreeptResult(dim) for _ in range(n_mocks)]
+    outs = (_lib.ThreeptOut * n_mocks)(*[r.c for r in res])
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nrm = np.ascontiguousarray(norms, dtype=np.float64)
+    hb = HostBinning(binning)
+    _lib.check(lib.trvg_compute_bispec_in_gpp_box_batch(
+        ctx.handle, C.byref(params), C.byref(cat_c), int(n_mocks),
+        off.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(hb.c),
+        _lib.dptr(nrm), outs))
+    return [r.as_dict('bispec') for r in res]
+
+
 def call_powspec(fn_name, ctx, params, data_c, binning, norm, rand_c=None,
                  alpha=None):
     lib = _lib.load()

@@ -40,6 +40,7 @@ EXPORTED = [
     "trvg_reduced_ylm", "trvg_context_set_stream", "trvg_set_option",
     "trvg_kernel_time_count", "trvg_kernel_time_get",
     "trvg_calc_grid_based_powlaw_norm_noalloc",
+    "trvg_compute_bispec_in_gpp_box_batch", "trvg_bispec_gpp_adjoint",
 ]
 
 
@@ -185,6 +186,12 @@ def _declare(lib):
         vp, P(Params), P(Catalogue), ip, P(dp)]
     lib.trvg_assign_weighted_field_to_mesh.argtypes = [
         vp, P(Params), P(Catalogue), ip, P(dp)]
+    lib.trvg_compute_bispec_in_gpp_box_batch.argtypes = [
+        vp, P(Params), P(Catalogue), ip, P(C.c_int64), P(BinningC), P(dp),
+        P(ThreeptOut)]
+    lib.trvg_bispec_gpp_adjoint.argtypes = [
+        vp, P(Params), P(Catalogue), P(BinningC), dp, P(dp), vp, vp, vp,
+        P(ThreeptOut)]
     lib.trvg_calc_grid_based_powlaw_norm_noalloc.argtypes = [
         P(Params), P(Catalogue), ip, vp, P(dp)]
     lib.trvg_wigner_3j.argtypes = [ip] * 6

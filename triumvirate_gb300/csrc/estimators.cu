@@ -387,8 +387,11 @@ struct Engine {
     ax.interlace = interlace;
   }
 
+  // Particle arrays on the device; `sort` orders a copy by mesh tile for
+  // the deposit (the caller's order is kept with sort = false).
   DevCatalogue upload_catalogue(const trvg_catalogue* c,
-                                const std::string& tag, bool need_los) {
+                                const std::string& tag, bool need_los,
+                                bool sort = true) {
     if (c == nullptr)
       throw_error(TRVG_ERR_INVALID_DATA, "Particle data are uninitialised.");
     if (c->n < 0)
@@ -411,7 +414,7 @@ struct Engine {
         d.ly = c->los_y;
         d.lz = c->los_z;
       }
-      return spatially_sorted(d, tag);
+      return sort ? spatially_sorted(d, tag) : d;
     }
     if (c->memory != TRVG_MEM_HOST)
       throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown memory kind %d.",
@@ -433,7 +436,7 @@ struct Engine {
       d.ly = put(c->los_y, ".ly");
       d.lz = put(c->los_z, ".lz");
     }
-    return spatially_sorted(d, tag);
+    return sort ? spatially_sorted(d, tag) : d;
   }
 
   // Large catalogues are reordered by mesh tile before assignment.
@@ -544,9 +547,20 @@ struct Engine {
     return b;
   }
 
+  // Mode counts of the last binning (they depend on the mesh and the bins
+  // only, so a batch of catalogues counts them once).
+  vector<double> cm_lo, cm_hi;
+  vector<long long> cm_nmodes;
+  vector<double> cm_keff;
+
   // nmodes and k_eff per bin (field.cpp:1812-1847, 1904-1905).
   void count_modes(const HostBins& hb, vector<long long>& nmodes,
                    vector<double>& keff) {
+    if (!cm_nmodes.empty() && cm_lo == hb.lo && cm_hi == hb.hi) {
+      nmodes = cm_nmodes;
+      keff = cm_keff;
+      return;
+    }
     const double kmax = *std::max_element(hb.hi.begin(), hb.hi.end());
     Cube cube = make_cube(kmax);
     BinsDev bd = bins_dev("cm", hb, nullptr, nullptr);
@@ -559,6 +573,10 @@ struct Engine {
     vector<double> ks = download(dk, hb.nb);
     keff.resize(hb.nb);
     for (int b = 0; b < hb.nb; ++b) keff[b] = ks[b] / double(nmodes[b]);
+    cm_lo = hb.lo;
+    cm_hi = hb.hi;
+    cm_nmodes = nmodes;
+    cm_keff = keff;
   }
 
   // Fine-binned two-point statistics (field.cpp:2511-2703).
@@ -1171,6 +1189,189 @@ struct Engine {
   }
 
   // -------------------------------------------------------------------------
+  // Adjoint of the raw periodic-box bispectrum B_000.
+  // -------------------------------------------------------------------------
+  // For a cotangent dL/d(raw B) of every data-vector entry: dL/dm of the
+  // count mesh m (what the assignment deposits), and the gathered
+  // gradients of the particle weights and positions (caller's order).
+  // The shell fields are recomputed, not stored from a forward call.
+  void bispec_adjoint(const trvg_catalogue* data, const trvg_binning* kb,
+                      double norm, const double* cot, double* grad_mesh,
+                      double* grad_w, double* grad_pos,
+                      trvg_threept_out* out) {
+    const HostBins hb = host_bins(kb);
+    validate_threept(&p, hb.nb);
+    if (p.ell1 != 0 || p.ell2 != 0 || p.ELL != 0)
+      throw_error(TRVG_ERR_UNIMPLEMENTED,
+                  "The bispectrum adjoint covers degrees (0, 0, 0) only.");
+    if (cot == nullptr)
+      throw_error(TRVG_ERR_INVALID_PARAMETER, "Null cotangent.");
+    const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
+    const int ndv = int(pairs.size());
+    if (out != nullptr && out->dim != ndv)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Output data vector has dimension %d, expected %d.",
+                  out->dim, ndv);
+    const DevCatalogue raw = upload_catalogue(data, "data", false, false);
+    const DevCatalogue dd = spatially_sorted(raw, "data");
+    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+    Field base = make_field("N", {{dd, WeightSpec()}}, false);
+    const double nbar = double(dd.n) / g.vol;
+    const FieldSpec<Real> dn = k0_view(base, -nbar * g.vol);
+
+    vector<long long> nmodes;
+    vector<double> keff;
+    count_modes(hb, nmodes, keff);
+    int M[3], K[3], Kg[3];
+    eval_grid(*std::max_element(hb.hi.begin(), hb.hi.end()), M, K, Kg);
+    for (int a = 0; a < 3; ++a) ctx.pruned_grid[a] = M[a];
+    const Leg leg{0, 0};
+    if (!real_fields(dn, dn, leg, leg, M))
+      throw_error(TRVG_ERR_UNIMPLEMENTED,
+                  "The bispectrum adjoint needs even mesh numbers or a "
+                  "pruned evaluation grid.");
+    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+    const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+    const double fac = double(g.nmesh) / double(Mc);
+
+    // Every bin of the pairs, in one set of shell fields.
+    vector<int> bins;
+    for (const Pair& q : pairs) {
+      bins.push_back(q.row);
+      bins.push_back(q.col);
+    }
+    std::sort(bins.begin(), bins.end());
+    bins.erase(std::unique(bins.begin(), bins.end()), bins.end());
+    const int nbl = int(bins.size());
+    auto local = [&](int b) {
+      return int(std::lower_bound(bins.begin(), bins.end(), b) -
+                 bins.begin());
+    };
+    const Real* G = build_G_real<Real>(dn, M, Kg);
+    Real* F = ctx.buf<Real>("adj.F", size_t(nbl) * Mc);
+    vector<double> no_radii;
+    build_leg_real<Real>(dn, leg, bins, hb, no_radii, M, K, "adj.leg", F);
+
+    // Forward values and the weights cw_p of raw = cw_p sum F_a F_b G.
+    vector<int> pa(ndv), pb(ndv);
+    vector<double> cw(ndv);
+    for (int i = 0; i < ndv; ++i) {
+      pa[i] = local(pairs[i].row);
+      pb[i] = local(pairs[i].col);
+      cw[i] = norm * g.vol_cell * fac /
+             (double(nmodes[pairs[i].row]) * double(nmodes[pairs[i].col]));
+    }
+    const int* dpa = upload("adj.pa", pa);
+    const int* dpb = upload("adj.pb", pb);
+    double* dout = ctx.buf<double>("adj.out", 2 * size_t(ndv));
+    zero(dout, 2 * ndv * sizeof(double));
+    launch_reduce_pairs_real<Real>(ctx, Mc, G, F, F, dpa, dpb, ndv, dout);
+
+    // Cotangent lists: partners of each local bin, and the pairs.
+    vector<vector<std::pair<int, double>>> part(nbl);
+    vector<double> plam(ndv);
+    for (int i = 0; i < ndv; ++i) {
+      const double lam = cot[2 * i] * cw[i];
+      plam[i] = lam;
+      part[pa[i]].push_back({pb[i], lam});
+      part[pb[i]].push_back({pa[i], lam});
+    }
+    vector<int> off(nbl + 1, 0), partner;
+    vector<double> lam;
+    for (int a = 0; a < nbl; ++a) {
+      for (const auto& e : part[a]) {
+        partner.push_back(e.first);
+        lam.push_back(e.second);
+      }
+      off[a + 1] = int(partner.size());
+    }
+    AdjointLists l;
+    l.off = upload("adj.off", off);
+    l.partner = upload("adj.partner", partner);
+    l.lam = upload("adj.lam", lam);
+    l.prow = dpa;
+    l.pcol = dpb;
+    l.plam = upload("adj.plam", plam);
+    l.npairs = ndv;
+    Real* H = ctx.buf<Real>("adj.H", size_t(nbl) * Mc);
+    Real* Q = ctx.buf<Real>("adj.Q", size_t(Mc));
+    launch_adjoint_fields<Real>(ctx, Mc, G, F, nbl, l, H, Q);
+
+    // Forward FFTs on the evaluation grid, masks and window, one C2R.
+    C* Hh = ctx.buf<C>("adj.Hh", size_t(nbl) * Mh);
+    C* Qh = ctx.buf<C>("adj.Qh", Mh);
+    {
+      cufftHandle h = ctx.plan(FFT<Real>::kR2C, M, nbl);
+      ctx.kbegin("cufft.r2c.adj");
+      FFT<Real>::r2c(h, H, Hh);
+      ctx.kend();
+      cufftHandle h1 = ctx.plan(FFT<Real>::kR2C, M, 1);
+      ctx.kbegin("cufft.r2c.adj");
+      FFT<Real>::r2c(h1, Q, Qh);
+      ctx.kend();
+      ctx.fft_launches += 2;
+    }
+    vector<double> lo(nbl), hi(nbl);
+    for (int a = 0; a < nbl; ++a) {
+      lo[a] = hb.lo[bins[a]];
+      hi[a] = hb.hi[bins[a]];
+    }
+    C* U = ctx.buf<C>("adj.U", size_t(g.nhalf));
+    zero(U, size_t(g.nhalf) * sizeof(C));
+    launch_adjoint_spectrum<Real, Real>(ctx, g, M, K, Kg, Hh, Qh,
+                                        upload("adj.lo", lo),
+                                        upload("adj.hi", hi), nbl, ax, U);
+    Real* gm = ctx.buf<Real>("adj.grad", size_t(g.nmesh));
+    {
+      cufftHandle h = ctx.plan(FFT<Real>::kC2R, g.n, 1);
+      ctx.kbegin("cufft.c2r.adj");
+      FFT<Real>::c2r(h, U, gm);
+      ctx.kend();
+      ctx.fft_launches++;
+    }
+
+    // Outputs, in the memory kind of the particle arrays.
+    const bool on_dev = data->memory == TRVG_MEM_DEVICE;
+    const size_t n = size_t(raw.n);
+    auto deliver = [&](const double* src, double* dst, size_t count) {
+      if (dst == nullptr || count == 0) return;
+      TRVG_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                                on_dev ? cudaMemcpyDeviceToDevice
+                                       : cudaMemcpyDeviceToHost,
+                                ctx.stream));
+    };
+    if (grad_mesh != nullptr) {
+      double* gd = ctx.buf<double>("adj.grad.dbl", size_t(g.nmesh));
+      launch_mesh_to_double<Real>(ctx, gm, g.nmesh, 1., gd);
+      deliver(gd, grad_mesh, size_t(g.nmesh));
+    }
+    if ((grad_w != nullptr || grad_pos != nullptr) && n > 0) {
+      double* gw = ctx.buf<double>("adj.gw", n);
+      double* gp = ctx.buf<double>("adj.gp", 3 * n);
+      launch_gather_grad<Real>(ctx, g, p.assignment_order, raw, gm, gw, gp,
+                               gp + n, gp + 2 * n);
+      deliver(gw, grad_w, n);
+      deliver(gp, grad_pos, 3 * n);
+    }
+    const vector<double> h = download(dout, 2 * size_t(ndv));
+    if (out != nullptr) {
+      for (int i = 0; i < ndv; ++i) {
+        const Pair& q = pairs[i];
+        out->coord1_bin[i] = hb.centre[q.row];
+        out->coord2_bin[i] = hb.centre[q.col];
+        out->coord1_eff[i] = keff[q.row];
+        out->coord2_eff[i] = keff[q.col];
+        out->count_1[i] = int32_t(nmodes[q.row]);
+        out->count_2[i] = int32_t(nmodes[q.col]);
+        out->raw[2 * i] = cw[i] * h[2 * i];
+        out->raw[2 * i + 1] = cw[i] * h[2 * i + 1];
+        out->shot[2 * i] = 0.;
+        out->shot[2 * i + 1] = 0.;
+      }
+    }
+  }
+
+  // -------------------------------------------------------------------------
   // Three-point correlation function.
   // -------------------------------------------------------------------------
   void threepcf(const trvg_catalogue* data, const trvg_catalogue* rand,
@@ -1497,6 +1698,52 @@ int trvg_compute_bispec_in_gpp_box(trvg_context* ctx,
   TRVG_API_BEGIN
   run(ctx, params, false, [&](auto& e) {
     e.bispec(data, nullptr, 1., kbinning, norm_factor, out, false);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_bispec_in_gpp_box_batch(
+    trvg_context* ctx, const trvg_params* params,
+    const trvg_catalogue* particles, int n_mocks, const int64_t* offsets,
+    const trvg_binning* kbinning, const double* norm_factors,
+    trvg_threept_out* outs) {
+  TRVG_API_BEGIN
+  if (particles == nullptr || offsets == nullptr || norm_factors == nullptr ||
+      outs == nullptr || n_mocks < 1)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Invalid batch arguments.");
+  if (offsets[0] != 0 || offsets[n_mocks] != particles->n)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                      "Batch offsets must run from 0 to the particle count.");
+  for (int i = 0; i < n_mocks; ++i)
+    if (offsets[i + 1] < offsets[i])
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "Batch offsets must not decrease.");
+  run(ctx, params, false, [&](auto& e) {
+    for (int i = 0; i < n_mocks; ++i) {
+      // Mock i: the slice [offsets[i], offsets[i + 1]) of every column.
+      trvg_catalogue c = *particles;
+      const int64_t o = offsets[i];
+      c.n = offsets[i + 1] - o;
+      c.x = particles->x + o;
+      c.y = particles->y + o;
+      c.z = particles->z + o;
+      if (particles->w != nullptr) c.w = particles->w + o;
+      e.bispec(&c, nullptr, 1., kbinning, norm_factors[i], &outs[i], false);
+    }
+  });
+  TRVG_API_END
+}
+
+int trvg_bispec_gpp_adjoint(trvg_context* ctx, const trvg_params* params,
+                            const trvg_catalogue* data,
+                            const trvg_binning* kbinning, double norm_factor,
+                            const double* cotangent, double* grad_mesh,
+                            double* grad_w, double* grad_pos,
+                            trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.bispec_adjoint(data, kbinning, norm_factor, cotangent, grad_mesh,
+                     grad_w, grad_pos, out);
   });
   TRVG_API_END
 }

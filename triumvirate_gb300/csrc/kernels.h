@@ -69,6 +69,15 @@ struct AxisTablesDev {
   bool interlace;
 };
 
+// W(k)^order (field.cpp:1114-1146) at full-mesh index (i, j, k).
+__device__ __forceinline__ double window_pow(const AxisTablesDev& ax, int i,
+                                             int j, int k) {
+  const double wk = ax.t.sinc[0][i] * ax.t.sinc[1][j] * ax.t.sinc[2][k];
+  double r = 1.;
+  for (int q = 0; q < ax.order; ++q) r *= wk;
+  return r;
+}
+
 // Bin edges and the fine-sample index ranges of each bin.
 struct BinsDev {
   int nbins = 0;
@@ -192,6 +201,37 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
                               const Real* Fa, const Real* Fb, const int* pa,
                               const int* pb, int npairs,
                               double* out /* 2 * npairs, imaginary 0 */);
+
+// ---- adjoint.cu ----------------------------------------------------------
+// Cotangent bookkeeping of the bispectrum adjoint: the partners of bin a in
+// the pairs, with their weights, are entries [off[a], off[a + 1]) of
+// partner / lam; the pairs themselves are (prow, pcol) with weights plam.
+struct AdjointLists {
+  const int* off;
+  const int* partner;
+  const double* lam;
+  const int* prow;
+  const int* pcol;
+  const double* plam;
+  int npairs;
+};
+
+template <class FR>
+void launch_adjoint_fields(Context& ctx, int64_t ncell, const FR* G,
+                           const FR* F, int nb, const AdjointLists& l, FR* H,
+                           FR* Q);
+template <class FR, class UR>
+void launch_adjoint_spectrum(Context& ctx, const Geom& g, const int M[3],
+                             const int K[3], const int Kg[3],
+                             const typename CplxOf<FR>::type* Hh,
+                             const typename CplxOf<FR>::type* Qh,
+                             const double* lo, const double* hi, int nb,
+                             const AxisTablesDev& ax,
+                             typename CplxOf<UR>::type* U);
+template <class Real>
+void launch_gather_grad(Context& ctx, const Geom& g, int order,
+                        const DevCatalogue& cat, const Real* grad, double* gw,
+                        double* gx, double* gy, double* gz);
 
 template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,

@@ -64,15 +64,6 @@ __device__ __forceinline__ cd field_value(const FieldSpec<Real>& f,
   return v;
 }
 
-// W(k)^order (field.cpp:1114-1146).
-__device__ __forceinline__ double window_pow(const AxisTablesDev& ax, int i,
-                                             int j, int k) {
-  const double wk = ax.t.sinc[0][i] * ax.t.sinc[1][j] * ax.t.sinc[2][k];
-  double r = 1.;
-  for (int q = 0; q < ax.order; ++q) r *= wk;
-  return r;
-}
-
 // Shot-noise aliasing C_1(k) (field.cpp:3463-3509).
 __device__ __forceinline__ double alias_sn(const AxisTablesDev& ax, int i,
                                            int j, int k) {

@@ -252,6 +252,50 @@ def compute_bispec_in_gpp_box(catalogue_data, degrees=None, binning=None,
         form=form, idx_bin=idx_bin, save=save, logger=logger, device=device)
 
 
+def compute_bispec_in_gpp_box_batch(catalogues, degrees=None, binning=None,
+                                    form=None, idx_bin=None,
+                                    sampling_params=None, paramset=None,
+                                    device=None):
+    """Bispectra of several periodic-box catalogues (e.g. mocks of uneven
+    sizes) in one library call; returns one result dictionary per
+    catalogue, each equal to that of `compute_bispec_in_gpp_box`.  The
+    library has no batched counterpart: it is called once per catalogue."""
+    if len(catalogues) == 0:
+        return []
+    paramset = _amalgamate_parameters(
+        paramset=paramset, params_sampling=sampling_params, degrees=degrees,
+        binning=binning, form=form, idx_bin=idx_bin,
+        catalogue_type='sim', statistic_type='bispec')
+    if binning is None:
+        binning = Binning.from_parameter_set(paramset)
+    if None in paramset['boxsize'].values():
+        raise ValueError("A batch needs an explicit box size.")
+    if None in paramset['ngrid'].values():
+        pd = _as_dict(paramset)
+        _set_ngrid_from_cutoff(pd)
+        paramset['ngrid'] = pd['ngrid']
+    cols, norms, offsets = [[], [], [], []], [], [0]
+    ctx = _lib.default_context(device)
+    params_c = _engine.make_params(paramset, '3pt')
+    for cat in catalogues:
+        cat.periodise(_boxsize(paramset))
+        if not cat['nz'].any():
+            cat.compute_mean_density(boxsize=_boxsize(paramset))
+        for c, a in zip(cols, cat._columns()):
+            c.append(a)
+        offsets.append(offsets[-1] + cat.ntotal)
+        if paramset['norm_convention'] == 'mesh':
+            hc = _engine.HostCatalogue(*cat._columns())
+            norms.append(_norm_mesh(ctx, params_c, hc.c, 1., 3))
+        else:
+            norms.append(_norm_factor(paramset, ctx, params_c, None,
+                                      cat['nz'], cat['ws'], cat['wc'], 1., 3))
+    allc = _engine.HostCatalogue(*(np.concatenate(c) for c in cols))
+    return _engine.call_bispec_batch(
+        ctx, params_c, allc.c, offsets, binning, norms,
+        shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
+
+
 def compute_3pcf_in_gpp_box(catalogue_data, degrees=None, binning=None,
                             form=None, idx_bin=None, sampling_params=None,
                             paramset=None, save=False, logger=None,
