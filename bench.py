@@ -591,6 +591,16 @@ def run_mocks(args):
         torch.cuda.synchronize(dev)
         times.append(e0.elapsed_time(e1) / 1e3)
     t = statistics.median(times)
+    # Per-kernel CUDA-event time per mock of each multipole's batch call.
+    per_kernel = {}
+    ctx.set_option('profiling', 1)
+    for name, pp in (('B000', p000), ('B202', p202)):
+        _engine.call_bispec_batch(ctx, pp, cat, offsets, binning, norms,
+                                  shape='diag')
+        kt = ctx.kernel_times()
+        per_kernel[name] = {k: round(v[0] / args.mocks, 4) for k, v in
+                            sorted(kt.items(), key=lambda kv: -kv[1][0])}
+    ctx.set_option('profiling', 0)
     line = {
         "metric": "batched mock bispectra (B_000 + B_202 per mock)",
         "value": round(args.mocks / t, 2), "unit": "mocks/s",
@@ -603,6 +613,7 @@ def run_mocks(args):
                                 "L=1000 Mpc/h, B_000 and B_202 diag, 24 lin "
                                 "bins 0.005-0.245 h/Mpc"),
                    "batching": "one library call per multipole"},
+        "kernel_ms_per_mock": per_kernel,
     }
     print(json.dumps(line), flush=True)
 

@@ -299,6 +299,7 @@ struct Engine {
   Geom g;
   AxisTablesDev ax;
   const float* inv_alias_f[3] = {nullptr, nullptr, nullptr};
+  const float* inv_win_f[3] = {nullptr, nullptr, nullptr};
   bool interlace;
 
   Engine(Context& c, const trvg_params& prm, bool allow_interlace)
@@ -370,12 +371,21 @@ struct Engine {
         host[size_t(4 * a + 3) * nmax + i] = 1. / al;
       }
     }
-    vector<float> hf(size_t(3) * nmax, 0.f);
+    // FP32 tables: 1 / alias, then 1 / sinc^order (the per-axis factors of
+    // 1 / W), for the FP32-mixed kernels.
+    vector<float> hf(size_t(6) * nmax, 0.f);
     for (int a = 0; a < 3; ++a)
-      for (int i = 0; i < g.n[a]; ++i)
+      for (int i = 0; i < g.n[a]; ++i) {
         hf[size_t(a) * nmax + i] = float(host[size_t(4 * a + 3) * nmax + i]);
+        hf[size_t(3 + a) * nmax + i] = float(
+            1. / std::pow(host[size_t(4 * a + 0) * nmax + i],
+                          p.assignment_order));
+      }
     const float* df = upload("axis_tables_f", hf);
-    for (int a = 0; a < 3; ++a) inv_alias_f[a] = df + size_t(a) * nmax;
+    for (int a = 0; a < 3; ++a) {
+      inv_alias_f[a] = df + size_t(a) * nmax;
+      inv_win_f[a] = df + size_t(3 + a) * nmax;
+    }
     double* d = upload("axis_tables", host);
     for (int a = 0; a < 3; ++a) {
       ax.t.sinc[a] = d + size_t(4 * a + 0) * nmax;
@@ -824,6 +834,45 @@ struct Engine {
     ctx.fft_launches++;
   }
 
+  // True when no two bins [lo, hi) overlap.
+  static bool disjoint(const vector<double>& lo, const vector<double>& hi) {
+    vector<std::pair<double, double>> e;
+    for (size_t i = 0; i < lo.size(); ++i) e.push_back({lo[i], hi[i]});
+    std::sort(e.begin(), e.end());
+    for (size_t i = 1; i < e.size(); ++i)
+      if (e[i].first < e[i - 1].second) return false;
+    return true;
+  }
+
+  // Shell index per half-spectrum mode of the evaluation grid for bins
+  // lo / hi, built once per mesh, grid and binning and kept as a named
+  // buffer.
+  const int16_t* shell_table(const int M[3], const int K[3],
+                             const vector<double>& lo,
+                             const vector<double>& hi, const double* dlo,
+                             const double* dhi, double hmax) {
+    std::string key;
+    char buf[64];
+    for (int a = 0; a < 3; ++a) {
+      std::snprintf(buf, sizeof(buf), "%d.%d.%d.%a.", g.n[a], M[a], K[a],
+                    g.dk[a]);
+      key += buf;
+    }
+    for (size_t i = 0; i < lo.size(); ++i) {
+      std::snprintf(buf, sizeof(buf), "%a,%a;", lo[i], hi[i]);
+      key += buf;
+    }
+    const std::string name =
+        "shelltab." + std::to_string(std::hash<std::string>{}(key));
+    const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+    auto it = ctx.buffers.find(name);
+    if (it != ctx.buffers.end() && it->second.bytes >= Mh * sizeof(int16_t))
+      return static_cast<const int16_t*>(it->second.ptr);
+    int16_t* tab = ctx.buf<int16_t>(name, Mh);
+    launch_shell_table(ctx, g, M, K, dlo, dhi, int(lo.size()), hmax, tab);
+    return tab;
+  }
+
   // Real-field variants: half spectra on the evaluation grid, then C2R.
   template <class FR>
   const FR* build_G_real(const FieldSpec<Real>& f, const int M[3],
@@ -832,7 +881,14 @@ struct Engine {
     const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
     const size_t Mc = size_t(M[0]) * M[1] * M[2];
     FC* H = ctx.buf<FC>("G.h", Mh);
-    launch_build_G_half<Real, FR>(ctx, g, M, Kg, f, ax, H);
+    bool done = false;
+    if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
+      if (f.im == nullptr && f.re_s == nullptr && f.k0_set) {
+        launch_build_G_half_f32(ctx, g, M, Kg, f.re, f.k0, inv_win_f, H);
+        done = true;
+      }
+    }
+    if (!done) launch_build_G_half<Real, FR>(ctx, g, M, Kg, f, ax, H);
     FR* G = ctx.buf<FR>("G.r", Mc);
     cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, 1);
     ctx.kbegin("cufft.c2r.G");
@@ -867,8 +923,19 @@ struct Engine {
       }
       const double* dlo = upload(tag + ".lo", lo);
       const double* dhi = upload(tag + ".hi", hi);
-      launch_build_F_half<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m,
-                                    dlo, dhi, nb, hmax, H);
+      bool done = false;
+      if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
+        if (src.im == nullptr && src.re_s == nullptr && src.k0_set &&
+            leg.m == 0 && disjoint(lo, hi)) {
+          const int16_t* tab = shell_table(M, K, lo, hi, dlo, dhi, hmax);
+          launch_build_F_half_f32(ctx, g, M, tab, src.re, src.k0, inv_win_f,
+                                  leg.ell, nb, H);
+          done = true;
+        }
+      }
+      if (!done)
+        launch_build_F_half<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m,
+                                      dlo, dhi, nb, hmax, H);
     }
     cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, nb);
     ctx.kbegin("cufft.c2r.F");

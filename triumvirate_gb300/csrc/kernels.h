@@ -165,6 +165,19 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
                              const double* radii, int nb,
                              typename CplxOf<FR>::type* out);
 
+// FP32-mixed builders of real fields without interlacing (values FP32,
+// shell membership from a table of the exact FP64 test).
+void launch_shell_table(Context& ctx, const Geom& g, const int M[3],
+                        const int K[3], const double* lo, const double* hi,
+                        int nb, double hi_max, int16_t* tab);
+void launch_build_G_half_f32(Context& ctx, const Geom& g, const int M[3],
+                             const int Kg[3], const float2* f, cd k0,
+                             const float* const iw[3], float2* out);
+void launch_build_F_half_f32(Context& ctx, const Geom& g, const int M[3],
+                             const int16_t* tab, const float2* f, cd k0,
+                             const float* const iw[3], int ell, int nb,
+                             float2* out);
+
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,

@@ -75,15 +75,19 @@ template <>
 struct Acc<float> {
   FF v = {0.f, 0.f};
   __device__ __forceinline__ void add(float x) { ff_add(v, x); }
-  __device__ __forceinline__ double warp_total() {
-    return ff_value(ff_warp_sum(v));
+  // The warp's total, valid in lane 0 (the only lane that converts).
+  __device__ __forceinline__ double warp_total(int lane) {
+    const FF t = ff_warp_sum(v);
+    double r = 0.;
+    if (lane == 0) r = ff_value(t);
+    return r;
   }
 };
 template <>
 struct Acc<double> {
   double v = 0.;
   __device__ __forceinline__ void add(double x) { v += x; }
-  __device__ __forceinline__ double warp_total() { return warp_sum(v); }
+  __device__ __forceinline__ double warp_total(int) { return warp_sum(v); }
 };
 
 // Block-wide sums of N accumulators, atomically added to out[q * stride]
@@ -97,7 +101,7 @@ __device__ __forceinline__ void block_add_acc(Acc<Real> (&a)[N], double* out,
   const int nw = blockDim.x >> 5;
 #pragma unroll
   for (int q = 0; q < N; ++q) {
-    const double s = a[q].warp_total();
+    const double s = a[q].warp_total(lane);
     if (lane == 0) red[q * 32 + wid] = s;
   }
   __syncthreads();
@@ -161,8 +165,33 @@ reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
     ib[q] = ok[q] ? pb[p0 + q] : 0;
   }
   Acc<Real> acc[kPairChunk];
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
-       t += int64_t(gridDim.x) * blockDim.x) {
+  int64_t t0 = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if constexpr (sizeof(Real) == 4) {
+    // Four cells per load: more bytes in flight per thread (the scalar loop
+    // is bound by load latency); the four products are summed in FP32
+    // before the float-float add.
+    if (ncell % 4 == 0) {
+      const int64_t n4 = ncell / 4;
+      for (int64_t t = t0; t < n4; t += int64_t(gridDim.x) * blockDim.x) {
+        const float4 g = reinterpret_cast<const float4*>(G)[t];
+#pragma unroll
+        for (int q = 0; q < kPairChunk; ++q) {
+          if (!ok[q]) continue;
+          const float4 a =
+              reinterpret_cast<const float4*>(Fa + int64_t(ia[q]) * ncell)[t];
+          const float4 b =
+              (ia[q] == ib[q] && Fa == Fb)
+                  ? a
+                  : reinterpret_cast<const float4*>(
+                        Fb + int64_t(ib[q]) * ncell)[t];
+          acc[q].add((a.x * b.x * g.x + a.y * b.y * g.y) +
+                     (a.z * b.z * g.z + a.w * b.w * g.w));
+        }
+      }
+      t0 = ncell;  // nothing left for the scalar loop
+    }
+  }
+  for (int64_t t = t0; t < ncell; t += int64_t(gridDim.x) * blockDim.x) {
     const Real g = G[t];
 #pragma unroll
     for (int q = 0; q < kPairChunk; ++q) {
@@ -223,8 +252,13 @@ __device__ __forceinline__ void orbit_ab(int q, bool swap, int hy, int& a,
   }
 }
 
-// TRIVIAL: both degrees are (0, 0), so y_a y_b = 1.
-template <class Real, bool TRIVIAL>
+// KIND 0: both degrees are (0, 0), so y_a y_b = 1.
+// KIND 1: m_a = m_b = 0 and ell_a + ell_b even: y_a y_b is a function of
+//   mu^2 = s_z^2 / s^2 alone (y_l0 is a Legendre polynomial in mu of the
+//   parity of l), the same on the 16 mirror cells of an orbit row, so it
+//   multiplies their sum once.
+// KIND 2: any degrees, y_a y_b per cell.
+template <class Real, int KIND>
 __global__ void __launch_bounds__(256)
 orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
                   int m_a, int ell_b, int m_b, bool swap, double* hist) {
@@ -254,7 +288,7 @@ orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
     const int c2 = (c == 0) ? 0 : g.n[2] - c;
     const bool two = (c2 != c);
     cd acc = {0., 0.};
-    if constexpr (TRIVIAL) {
+    if constexpr (KIND != 2) {
       Real sr = Real(0), si = Real(0);
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
@@ -268,6 +302,14 @@ orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
         }
       }
       acc = cd{double(sr), double(si)};
+      if constexpr (KIND == 1) {
+        const double rx = dmul(double(a), g.dr[0]);
+        const double ry = dmul(double(b), g.dr[1]);
+        const double rz = dmul(double(c), g.dr[2]);
+        const double f = (reduced_ylm(ell_a, 0, rx, ry, rz) *
+                          reduced_ylm(ell_b, 0, rx, ry, rz)).re;
+        acc = cd{acc.re * f, acc.im * f};
+      }
     } else {
 #pragma unroll 1
       for (int r = 0; r < 8; ++r) {
@@ -289,7 +331,7 @@ orbit_rows_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
     }
     const int64_t key = key_ab + int64_t(c) * c;
     atomicAdd(hist + 2 * key, acc.re);
-    if (xi_im != nullptr || !TRIVIAL) atomicAdd(hist + 2 * key + 1, acc.im);
+    if (xi_im != nullptr || KIND == 2) atomicAdd(hist + 2 * key + 1, acc.im);
   }
 }
 
@@ -471,12 +513,16 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
         swap ? (hx + 1) * (hx + 2) / 2 : (hx + 1) * (hy + 1);
     const int threads = std::min(256, ((hz + 1 + 31) / 32) * 32);
     const bool trivial = ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0;
+    const bool axial = m_a == 0 && m_b == 0 && (ell_a + ell_b) % 2 == 0;
     TRVG_KBEGIN(ctx, "orbit_rows_kernel");
     if (trivial)
-      orbit_rows_kernel<Real, true><<<nblocks, threads, 0, ctx.stream>>>(
+      orbit_rows_kernel<Real, 0><<<nblocks, threads, 0, ctx.stream>>>(
+          g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
+    else if (axial)
+      orbit_rows_kernel<Real, 1><<<nblocks, threads, 0, ctx.stream>>>(
           g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
     else
-      orbit_rows_kernel<Real, false><<<nblocks, threads, 0, ctx.stream>>>(
+      orbit_rows_kernel<Real, 2><<<nblocks, threads, 0, ctx.stream>>>(
           g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, swap, hist);
     TRVG_LAUNCHED(ctx);
     return;

@@ -89,11 +89,6 @@ __device__ __forceinline__ double alias_sn(const AxisTablesDev& ax, int i,
 
 __device__ __forceinline__ int wrap(int s, int n) { return s < 0 ? s + n : s; }
 
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
 int grid_for(int64_t work, int block, int64_t cap = 152 * 16) {
   int64_t g = (work + block - 1) / block;
   if (g > cap) g = cap;
@@ -307,6 +302,124 @@ __global__ void build_F_half_kernel(Geom g, int M0, int M1, int M2, int K0,
       o.y = sel ? FR(val.im) : FR(0);
       out[int64_t(q) * count + t] = o;
     }
+  }
+}
+
+// ---- FP32-mixed builders of real fields ---------------------------------
+//
+// For an FP32 real field without interlacing the values stay FP32: the
+// half spectrum is read as float2 (Hermitian reconstruction for k >= nzh,
+// the exact k = 0 value), and 1 / W is a product of per-axis FP32 tables.
+// The shell a mode belongs to -- the exact FP64 |k| test of
+// build_F_half_kernel -- comes from a table built once per mesh, grid and
+// binning.
+
+__device__ __forceinline__ float2 half_value_f(const float2* h, const Geom& g,
+                                               int i, int j, int k) {
+  if (k < g.nzh) return h[(int64_t(i) * g.n[1] + j) * g.nzh + k];
+  const int ii = (i == 0) ? 0 : g.n[0] - i;
+  const int jj = (j == 0) ? 0 : g.n[1] - j;
+  float2 v = h[(int64_t(ii) * g.n[1] + jj) * g.nzh + (g.n[2] - k)];
+  v.y = -v.y;
+  return v;
+}
+
+struct InvWinF {
+  const float* w[3];
+};
+
+// Shell index of every half-spectrum mode of the evaluation grid (-1: in
+// no shell), bins disjoint.
+__global__ void shell_table_kernel(Geom g, int M0, int M1, int M2, int K0,
+                                   int K1, int K2, const double* lo,
+                                   const double* hi, int nb, double hi_max,
+                                   int16_t* tab) {
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * Mh;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(Mh));
+    const uint32_t row = t / uint32_t(Mh);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= K0) &&
+                    (M1 == g.n[1] || abs(sy) <= K1) &&
+                    (M2 == g.n[2] || abs(sz) <= K2);
+    int16_t bin = -1;
+    if (in) {
+      const double kx = dmul(double(sx), g.dk[0]);
+      const double ky = dmul(double(sy), g.dk[1]);
+      const double kz = dmul(double(sz), g.dk[2]);
+      const double k = vec3_mag(kx, ky, kz);
+      if (k < hi_max)
+        for (int q = 0; q < nb; ++q)
+          if (lo[q] <= k && k < hi[q]) bin = int16_t(q);
+    }
+    tab[t] = bin;
+  }
+}
+
+__global__ void build_G_half_f32_kernel(Geom g, int M0, int M1, int M2,
+                                        int Kg0, int Kg1, int Kg2,
+                                        const float2* f, float2 k0, InvWinF iw,
+                                        float inv_vol, float2* out) {
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * Mh;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(Mh));
+    const uint32_t row = t / uint32_t(Mh);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
+                    (M1 == g.n[1] || abs(sy) <= Kg1) &&
+                    (M2 == g.n[2] || abs(sz) <= Kg2);
+    float2 o = make_float2(0.f, 0.f);
+    if (in) {
+      const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                k = wrap(sz, g.n[2]);
+      const float2 v = (i == 0 && j == 0 && k == 0) ? k0
+                                                   : half_value_f(f, g, i, j, k);
+      const float s = iw.w[0][i] * iw.w[1][j] * iw.w[2][k] * inv_vol;
+      o = make_float2(v.x * s, v.y * s);
+    }
+    out[t] = o;
+  }
+}
+
+// Writes only the modes inside a shell: `out` is zeroed beforehand.
+__global__ void build_F_half_f32_kernel(Geom g, int M0, int M1, int M2,
+                                        const int16_t* tab, const float2* f,
+                                        float2 k0, InvWinF iw, int ell,
+                                        float2* out) {
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * Mh;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int q = tab[t];
+    if (q < 0) continue;
+    const int c = int(t % uint32_t(Mh));
+    const uint32_t row = t / uint32_t(Mh);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              k = wrap(sz, g.n[2]);
+    const float2 v = (i == 0 && j == 0 && k == 0) ? k0
+                                                 : half_value_f(f, g, i, j, k);
+    float s = iw.w[0][i] * iw.w[1][j] * iw.w[2][k];
+    if (ell != 0) {
+      const double kx = dmul(double(sx), g.dk[0]);
+      const double ky = dmul(double(sy), g.dk[1]);
+      const double kz = dmul(double(sz), g.dk[2]);
+      s *= float(reduced_ylm(ell, 0, kx, ky, kz).re);
+    }
+    out[int64_t(q) * count + t] = make_float2(v.x * s, v.y * s);
   }
 }
 
@@ -634,6 +747,49 @@ void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
   twopt_field_real_f32_kernel<<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
       g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1], inv_alias[2], shot,
       float(1. / g.vol), p0, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_shell_table(Context& ctx, const Geom& g, const int M[3],
+                        const int K[3], const double* lo, const double* hi,
+                        int nb, double hi_max, int16_t* tab) {
+  const int64_t count = int64_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  TRVG_KBEGIN(ctx, "shell_table_kernel");
+  shell_table_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], K[0], K[1], K[2], lo, hi, nb, hi_max, tab);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_build_G_half_f32(Context& ctx, const Geom& g, const int M[3],
+                             const int Kg[3], const float2* f, cd k0,
+                             const float* const iw[3], float2* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  InvWinF w{{iw[0], iw[1], iw[2]}};
+  TRVG_KBEGIN(ctx, "build_G_kernel");
+  build_G_half_f32_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f,
+      make_float2(float(k0.re), float(k0.im)), w, float(1. / g.vol), out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_build_F_half_f32(Context& ctx, const Geom& g, const int M[3],
+                             const int16_t* tab, const float2* f, cd k0,
+                             const float* const iw[3], int ell, int nb,
+                             float2* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  TRVG_CUDA(cudaMemsetAsync(out, 0, size_t(nb) * count * sizeof(float2),
+                            ctx.stream));
+  InvWinF w{{iw[0], iw[1], iw[2]}};
+  TRVG_KBEGIN(ctx, "build_F_kernel");
+  build_F_half_f32_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], tab, f, make_float2(float(k0.re), float(k0.im)), w,
+      ell, out);
   TRVG_LAUNCHED(ctx);
 }
 
