@@ -388,6 +388,13 @@ def run_gb300(args):
                     "per_bin_rel_err": errs}
         ctx.set_option('shell_fields_fp64', 0)
         ctx.set_option('shotnoise_fp64', 0)
+        ctx.set_option('sort_catalogue', 0)
+        estimate(p32, dcat)
+        msn, _, ktn, _, _ = timed(p32, dcat, 2, profile=True)
+        variants["unsorted_catalogue"] = {
+            "s_per_estimate": sum(msn) / 2e3,
+            "assign_ms": round(ktn.get('assign_kernel', [0., 1])[0] / 2, 4)}
+        ctx.set_option('sort_catalogue', 1)
 
     # Roofline of the dominant kernel of this library.
     peak, peak_kind = hbm_peak()

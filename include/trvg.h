@@ -189,7 +189,12 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *   "shotnoise_fp64"   0/1: FP32-mixed: transform the shot-noise field in
  *                           FP64 (default FP32);
  *   "shell_fields_fp64" 0/1: FP32-mixed: evaluate the shell-filtered and
- *                           compensated fields in FP64 (default FP32). */
+ *                           compensated fields in FP64 (default FP32);
+ *   "sort_catalogue"   0/1: order catalogues of >= 65536 particles by mesh
+ *                           tile before the deposit (default 1);
+ *   "ff_transforms"    0/1: FP32-mixed: compute the spectrum modes of the
+ *                           shell fields and the evaluation-grid transforms
+ *                           in float-float arithmetic (default 1). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
 /* Per-kernel device time of the last call (profiling on). */
 int trvg_kernel_time_count(const trvg_context* ctx, int* count);

@@ -153,6 +153,7 @@ void Context::release() {
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   buffers.clear();
   splines.clear();
+  stats_plans.clear();
 }
 
 void destroy_events(Context& c) {
@@ -262,6 +263,10 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     ctx->impl.shotnoise_fp64 = value != 0;
   } else if (k == "shell_fields_fp64") {
     ctx->impl.shell_fields_fp64 = value != 0;
+  } else if (k == "sort_catalogue") {
+    ctx->impl.sort_catalogue = value != 0;
+  } else if (k == "ff_transforms") {
+    ctx->impl.ff_transforms = value != 0;
   } else {
     trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown option '%s'.",
                       key);

@@ -164,7 +164,7 @@ vector<Term> orders_lpp(int l1, int l2, int L) {
 }
 
 bool fft_friendly(int n) {
-  for (int p : {2, 3, 5, 7})
+  for (int p : {2, 3, 5})
     while (n % p == 0) n /= p;
   return n == 1;
 }
@@ -300,6 +300,7 @@ struct Engine {
   AxisTablesDev ax;
   const float* inv_alias_f[3] = {nullptr, nullptr, nullptr};
   const float* inv_win_f[3] = {nullptr, nullptr, nullptr};
+  const float2* inv_win_ff[3] = {nullptr, nullptr, nullptr};
   bool interlace;
 
   Engine(Context& c, const trvg_params& prm, bool allow_interlace)
@@ -386,6 +387,17 @@ struct Engine {
       inv_alias_f[a] = df + size_t(a) * nmax;
       inv_win_f[a] = df + size_t(3 + a) * nmax;
     }
+    // 1 / sinc^order as float-float (hi, lo) for the float-float builders.
+    vector<float2> hff(size_t(3) * nmax, make_float2(0.f, 0.f));
+    for (int a = 0; a < 3; ++a)
+      for (int i = 0; i < g.n[a]; ++i) {
+        const double v = 1. / std::pow(host[size_t(4 * a + 0) * nmax + i],
+                                       p.assignment_order);
+        const float hv = float(v);
+        hff[size_t(a) * nmax + i] = make_float2(hv, float(v - double(hv)));
+      }
+    const float2* dff = upload("axis_tables_ff", hff);
+    for (int a = 0; a < 3; ++a) inv_win_ff[a] = dff + size_t(a) * nmax;
     double* d = upload("axis_tables", host);
     for (int a = 0; a < 3; ++a) {
       ax.t.sinc[a] = d + size_t(4 * a + 0) * nmax;
@@ -451,7 +463,7 @@ struct Engine {
 
   // Large catalogues are reordered by mesh tile before assignment.
   DevCatalogue spatially_sorted(const DevCatalogue& d, const std::string& tag) {
-    if (d.n < (int64_t(1) << 16)) return d;
+    if (d.n < (int64_t(1) << 16) || !ctx.sort_catalogue) return d;
     return sort_catalogue(ctx, g, d, tag);
   }
 
@@ -503,6 +515,11 @@ struct Engine {
       return o;
     };
     f.spec.re = r2c(mre, ".re");
+    ++ctx.mesh_gen;
+    if (mim == nullptr && sre == nullptr) {
+      f.spec.mesh = mre;
+      f.spec.mesh_gen = ctx.mesh_gen;
+    }
     if (mim) f.spec.im = r2c(mim, ".im");
     if (sre) f.spec.re_s = r2c(sre, ".sre");
     if (sim) f.spec.im_s = r2c(sim, ".sim");
@@ -589,9 +606,128 @@ struct Engine {
     cm_keff = keff;
   }
 
-  // Fine-binned two-point statistics (field.cpp:2511-2703).
+  // Fine-binned two-point statistics (field.cpp:2511-2703): the field
+  // products over a mode list cached per mesh, binning and degrees.
   Stats twopt_stats(const HostBins& hb, const FieldSpec<Real>& fa,
                     const FieldSpec<Real>& fb, cplx shot, int ell, int m) {
+    vector<int> smin, smax;
+    const double dk_sample = 1.e-5;
+    sample_ranges(hb, dk_sample, 1000000, smin, smax);
+    // Each mode must fall in at most one bin.
+    vector<std::pair<int, int>> r;
+    for (int b = 0; b < hb.nb; ++b)
+      if (smax[b] > smin[b]) r.push_back({smin[b], smax[b]});
+    std::sort(r.begin(), r.end());
+    for (size_t i = 1; i < r.size(); ++i)
+      if (r[i].first < r[i - 1].second)
+        return twopt_stats_direct(hb, fa, fb, shot, ell, m);
+    const int smax_all = *std::max_element(smax.begin(), smax.end());
+    const Cube cube = make_cube(double(smax_all + 1) * dk_sample);
+    const StatsPlan& sp = stats_plan(hb, smin, smax, cube, ell, m);
+    double* dpk = ctx.buf<double>("st.pk", 2 * hb.nb);
+    zero(dpk, 2 * hb.nb * sizeof(double));
+    const int* off = static_cast<const int*>(ctx.buffers[sp.tag + ".off"].ptr);
+    const uint32_t* list =
+        static_cast<const uint32_t*>(ctx.buffers[sp.tag + ".list"].ptr);
+    const double2* coef =
+        static_cast<const double2*>(ctx.buffers[sp.tag + ".coef"].ptr);
+    launch_stats_pk<Real>(ctx, g, cube, fa, fb, hb.nb, sp.max_count, off,
+                          list, coef, dpk);
+    const vector<double> pk = download(dpk, 2 * hb.nb);
+    Stats s;
+    s.nmodes = sp.nmodes;
+    s.k.resize(hb.nb);
+    s.pk.resize(hb.nb);
+    s.sn.resize(hb.nb);
+    for (int b = 0; b < hb.nb; ++b) {
+      const double n = double(s.nmodes[b]);
+      if (s.nmodes[b] != 0) {
+        s.k[b] = sp.ksum[b] / n;
+        s.pk[b] = cplx(pk[2 * b], pk[2 * b + 1]) / n;
+        s.sn[b] = shot * cplx(sp.snsum[2 * b], sp.snsum[2 * b + 1]) / n;
+      } else {
+        s.k[b] = hb.centre[b];
+        s.pk[b] = 0.;
+        s.sn[b] = 0.;
+      }
+    }
+    return s;
+  }
+
+  // The cached mode list: membership and coefficients once (exact FP64, as
+  // twopt_stats_kernel), then the member modes listed bin by bin.
+  const StatsPlan& stats_plan(const HostBins& hb, const vector<int>& smin,
+                              const vector<int>& smax, const Cube& cube,
+                              int ell, int m) {
+    std::string key;
+    char buf[96];
+    for (int a = 0; a < 3; ++a) {
+      std::snprintf(buf, sizeof(buf), "%d.%a.", g.n[a], g.dk[a]);
+      key += buf;
+    }
+    std::snprintf(buf, sizeof(buf), "%d.%d.%d.%d.", p.assignment_order,
+                  int(interlace), ell, m);
+    key += buf;
+    for (int b = 0; b < hb.nb; ++b) {
+      std::snprintf(buf, sizeof(buf), "%d,%d;", smin[b], smax[b]);
+      key += buf;
+    }
+    auto it = ctx.stats_plans.find(key);
+    if (it != ctx.stats_plans.end()) return it->second;
+    StatsPlan sp;
+    sp.tag = "stplan." + std::to_string(std::hash<std::string>{}(key));
+    const int nb = hb.nb;
+    BinsDev bd = bins_dev(sp.tag, hb, &smin, &smax);
+    const size_t nc = size_t(cube.count);
+    int16_t* qtab = ctx.buf<int16_t>(sp.tag + ".q", nc);
+    double2* coef = ctx.buf<double2>(sp.tag + ".coef", nc);
+    double* kmode = ctx.buf<double>("stplan.kmode", nc);
+    double2* snmode = ctx.buf<double2>("stplan.snmode", nc);
+    launch_stats_plan(ctx, g, cube, ell, m, ax, bd, qtab, coef, kmode,
+                      snmode);
+    const vector<int16_t> hq = download(qtab, nc);
+    const vector<double> hk = download(kmode, nc);
+    const vector<double2> hs = download(snmode, nc);
+    // Per-bin counts and Neumaier-compensated sums in mode order.
+    sp.nmodes.assign(nb, 0);
+    sp.ksum.assign(nb, 0.);
+    sp.snsum.assign(2 * size_t(nb), 0.);
+    vector<double> ck(nb, 0.), cs(2 * size_t(nb), 0.);
+    auto add = [](double& s, double& c, double x) {
+      const double t = s + x;
+      c += (std::fabs(s) >= std::fabs(x)) ? (s - t) + x : (x - t) + s;
+      s = t;
+    };
+    for (size_t t = 0; t < nc; ++t) {
+      const int q = hq[t];
+      if (q < 0) continue;
+      ++sp.nmodes[q];
+      add(sp.ksum[q], ck[q], hk[t]);
+      add(sp.snsum[2 * q], cs[2 * q], hs[t].x);
+      add(sp.snsum[2 * q + 1], cs[2 * q + 1], hs[t].y);
+    }
+    vector<int> off(nb + 1, 0);
+    for (int b = 0; b < nb; ++b) {
+      sp.ksum[b] += ck[b];
+      sp.snsum[2 * b] += cs[2 * b];
+      sp.snsum[2 * b + 1] += cs[2 * b + 1];
+      off[b + 1] = off[b] + int(sp.nmodes[b]);
+      sp.max_count = std::max(sp.max_count, int(sp.nmodes[b]));
+    }
+    const int* doff = upload(sp.tag + ".off", off);
+    int* cursor = ctx.buf<int>(sp.tag + ".cur", nb);
+    zero(cursor, nb * sizeof(int));
+    uint32_t* list =
+        ctx.buf<uint32_t>(sp.tag + ".list", std::max(1, off[nb]));
+    launch_stats_fill(ctx, cube.count, qtab, doff, cursor, list);
+    return ctx.stats_plans.emplace(key, std::move(sp)).first->second;
+  }
+
+  // The same statistics mode by mode in one pass (bins overlapping in
+  // sample index).
+  Stats twopt_stats_direct(const HostBins& hb, const FieldSpec<Real>& fa,
+                           const FieldSpec<Real>& fb, cplx shot, int ell,
+                           int m) {
     vector<int> smin, smax;
     const int n_sample = 1000000;
     const double dk_sample = 1.e-5;
@@ -959,6 +1095,139 @@ struct Engine {
            gsrc.re_s == nullptr;
   }
 
+  // Float-float shell fields apply to FP32 real fields of one source mesh
+  // (G and both legs), shells (not j_l weights), a pruned cubic evaluation
+  // band and transform lengths of radices 2, 3, 5.
+  bool ff_applicable(const FieldSpec<Real>& src, const FieldSpec<Real>& gsrc,
+                     const Leg& la, const Leg& lb, const vector<Pair>& pairs,
+                     const HostBins& hb, const int M[3], const int K[3]) {
+    if (!ctx.ff_transforms || la.sjl || lb.sjl) return false;
+    if (src.mesh == nullptr || src.mesh_gen != ctx.mesh_gen ||
+        gsrc.re != src.re || !src.k0_set)
+      return false;
+    if (K[0] != K[1] || K[1] != K[2]) return false;
+    for (int a = 0; a < 3; ++a)
+      if (M[a] >= g.n[a] || !ff_length_ok(M[a]) || !ff_length_ok(g.n[a]) ||
+          4 * K[a] + 1 > M[a])
+        return false;
+    if ((int64_t(g.n[0]) * g.n[1]) % 2 != 0) return false;
+    vector<double> lo, hi;
+    for (const Pair& q : pairs)
+      for (int b : {q.row, q.col}) {
+        lo.push_back(hb.lo[b]);
+        hi.push_back(hb.hi[b]);
+      }
+    vector<std::pair<double, double>> e;
+    for (size_t i = 0; i < lo.size(); ++i) e.push_back({lo[i], hi[i]});
+    std::sort(e.begin(), e.end());
+    e.erase(std::unique(e.begin(), e.end()), e.end());
+    for (size_t i = 1; i < e.size(); ++i)
+      if (e[i].first < e[i - 1].second) return false;
+    // Device memory of the transforms (float4 scratch, float fields).
+    const int kg = 2 * K[0];
+    const double mc = double(M[0]) * M[1] * M[2];
+    const double bytes =
+        16. * (double(g.n[0]) * (kg + 1) * g.n[1] +
+               double(2 * kg + 1) * (kg + 1) * g.n[0] +
+               double(2 * kg + 1) * (2 * kg + 1) * (kg + 1)) +
+        16. * 3. * double(hb.nb) * (K[0] + 1) * M[0] * M[1] * 2. +
+        8. * mc * (2. * hb.nb + 1.);
+    size_t free_b = 0, total_b = 0;
+    TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    return bytes < 0.6 * double(free_b);
+  }
+
+  // Pair sums with float-float transforms: the source mesh's spectrum on
+  // the cube |s| <= 2K, G and the shell fields of both legs evaluated from
+  // it, then the same real-field reduction.
+  vector<cplx> pair_sums_ff(const FieldSpec<Real>& src, const Leg& la,
+                            const Leg& lb, const vector<Pair>& pairs,
+                            const HostBins& hb, const int M[3],
+                            const int K[3]) {
+    const int k = K[0], kg = 2 * k;
+    const int np = int(pairs.size());
+    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+    float4* T1 = ctx.buf<float4>(
+        "ff.T1", size_t(g.n[0]) * (kg + 1) * g.n[1]);
+    float4* T2 = ctx.buf<float4>(
+        "ff.T2", size_t(2 * kg + 1) * (kg + 1) * g.n[0]);
+    float4* cube = ctx.buf<float4>(
+        "ff.cube", size_t(2 * kg + 1) * (2 * kg + 1) * (kg + 1));
+    launch_ff_forward_cube(ctx, g, reinterpret_cast<const float*>(src.mesh),
+                           kg, T1, T2, cube);
+
+    const bool shared = la.ell == lb.ell && la.m == lb.m;
+    vector<int> A, B;
+    for (const Pair& q : pairs) {
+      A.push_back(q.row);
+      B.push_back(q.col);
+    }
+    if (shared) {
+      A.insert(A.end(), B.begin(), B.end());
+      B = A;
+    }
+    for (vector<int>* v : {&A, &B}) {
+      std::sort(v->begin(), v->end());
+      v->erase(std::unique(v->begin(), v->end()), v->end());
+    }
+    const size_t plane_g = size_t(kg + 1) * M[1] * M[0];
+    const size_t plane_f = size_t(k + 1) * M[1] * M[0];
+    const size_t yn = std::max(plane_g, std::max(A.size(), B.size()) * plane_f);
+    float4* Y1 = ctx.buf<float4>("ff.Y1", yn);
+    float4* Y2 = ctx.buf<float4>("ff.Y2", yn);
+
+    float4* EG = ctx.buf<float4>("ff.EG", plane_g);
+    launch_ff_build_G(ctx, g, M, cube, kg, inv_win_ff, src.k0, EG);
+    float* G = ctx.buf<float>("ff.G", size_t(Mc));
+    float* Gl = ctx.buf<float>("ff.G.lo", size_t(Mc));
+    launch_ff_inverse(ctx, M, 1, kg, kg, EG, Y1, Y2, G, Gl);
+
+    // Float-float fields of one leg: hi words, lo words after nb * Mc.
+    auto leg_fields = [&](const Leg& leg, const vector<int>& bins,
+                          const std::string& tag) -> float* {
+      const int nb = int(bins.size());
+      vector<double> lo(nb), hi(nb);
+      double hmax = 0.;
+      for (int i = 0; i < nb; ++i) {
+        lo[i] = hb.lo[bins[i]];
+        hi[i] = hb.hi[bins[i]];
+        hmax = std::max(hmax, hi[i]);
+      }
+      const double* dlo = upload(tag + ".lo", lo);
+      const double* dhi = upload(tag + ".hi", hi);
+      const int16_t* tab = shell_table(M, K, lo, hi, dlo, dhi, hmax);
+      float4* E = ctx.buf<float4>(tag + ".E", size_t(nb) * plane_f);
+      launch_ff_build_F(ctx, g, M, cube, kg, k, tab, nb, leg.ell, inv_win_ff,
+                        src.k0, E);
+      float* out = ctx.buf<float>(tag + ".F", 2 * size_t(nb) * Mc);
+      launch_ff_inverse(ctx, M, nb, k, k, E, Y1, Y2, out,
+                        out + size_t(nb) * Mc);
+      return out;
+    };
+    const float* FA = leg_fields(la, A, "ffA");
+    const float* FB = shared ? FA : leg_fields(lb, B, "ffB");
+    const float* FAl = FA + A.size() * size_t(Mc);
+    const float* FBl = FB + B.size() * size_t(Mc);
+
+    vector<int> pa(np), pb(np);
+    for (int i = 0; i < np; ++i) {
+      pa[i] = int(std::lower_bound(A.begin(), A.end(), pairs[i].row) -
+                  A.begin());
+      pb[i] = int(std::lower_bound(B.begin(), B.end(), pairs[i].col) -
+                  B.begin());
+    }
+    const int* dpa = upload("pairs.a", pa);
+    const int* dpb = upload("pairs.b", pb);
+    double* dout = ctx.buf<double>("pairs.out", 2 * size_t(np));
+    zero(dout, 2 * np * sizeof(double));
+    launch_reduce_pairs_ff(ctx, Mc, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
+                           dout);
+    const vector<double> h = download(dout, 2 * size_t(np));
+    vector<cplx> res(np);
+    for (int i = 0; i < np; ++i) res[i] = cplx(h[2 * i], h[2 * i + 1]);
+    return res;
+  }
+
   // sum over the evaluation grid of F_a(row) F_b(col) G for every pair, G
   // being the compensated field of `gsrc`; evaluation-grid fields in FP64
   // for the FP64 path or with the "shell_fields_fp64" option.
@@ -983,6 +1252,10 @@ struct Engine {
     const int np = int(pairs.size());
     vector<cplx> res(np, cplx(0., 0.));
     const bool real = real_fields(src, gsrc, la, lb, M);
+    if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
+      if (real && ff_applicable(src, gsrc, la, lb, pairs, hb, M, K))
+        return pair_sums_ff(src, la, lb, pairs, hb, M, K);
+    }
     const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
     const FR* Gr = real ? build_G_real<FR>(gsrc, M, Kg) : nullptr;
     const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;

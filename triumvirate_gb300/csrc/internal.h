@@ -100,6 +100,16 @@ struct KernelRecord {
   cudaEvent_t begin, end;
 };
 
+// Mode list of the fine-binned two-point statistics for one mesh, binning
+// and degree pair (device arrays are named buffers under `tag`).
+struct StatsPlan {
+  std::string tag;
+  int max_count = 0;
+  std::vector<long long> nmodes;
+  std::vector<double> ksum;
+  std::vector<double> snsum;  // re, im per bin
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;       // stream in use
@@ -119,6 +129,12 @@ struct Context {
   // FP32-mixed precision choices: shot-noise field / shell fields in FP64.
   bool shotnoise_fp64 = false;
   bool shell_fields_fp64 = false;
+  // Order large catalogues by mesh tile before the deposit.
+  bool sort_catalogue = true;
+  // FP32-mixed: float-float transforms of the shell fields.
+  bool ff_transforms = true;
+  // Deposits made so far (FieldSpec::mesh_gen).
+  int64_t mesh_gen = 0;
   // Profiling: per-launch events of the current call, per-name totals of
   // the last call.
   bool profiling = false;
@@ -130,6 +146,8 @@ struct Context {
   std::vector<std::pair<std::string, std::pair<double, int64_t>>> ktimes;
   // j_ell spline tables by ell (device arrays are named buffers).
   std::map<int, SplineTable> splines;
+  // Two-point statistics mode lists by key.
+  std::map<std::string, StatsPlan> stats_plans;
 
   void kbegin(const char* name);
   void kend();

@@ -60,6 +60,10 @@ struct FieldSpec {
   const C* im_s = nullptr;
   cd k0 = {0., 0.};
   bool k0_set = false;
+  // The real FP32 mesh the spectrum came from (real fields without
+  // interlacing), valid while mesh_gen equals the context's counter.
+  const Real* mesh = nullptr;
+  int64_t mesh_gen = -1;
 };
 
 // Device copies of the per-axis Fourier factor tables.
@@ -178,6 +182,22 @@ void launch_build_F_half_f32(Context& ctx, const Geom& g, const int M[3],
                              const float* const iw[3], int ell, int nb,
                              float2* out);
 
+// Cached mode lists of the fine-binned two-point statistics.
+// Per cube mode: bin (or -1), coefficient y / W_pk, |k| and the shot-noise
+// weight C1 y / W_sn (the per-bin sums are formed on the host, in mode
+// order, so that near-cancelling sums do not depend on atomic order).
+void launch_stats_plan(Context& ctx, const Geom& g, const Cube& cube,
+                       int ell, int m, const AxisTablesDev& ax,
+                       const BinsDev& bins, int16_t* qtab, double2* coef,
+                       double* kmode, double2* snmode);
+void launch_stats_fill(Context& ctx, int64_t nmode, const int16_t* qtab,
+                       const int* off, int* cursor, uint32_t* list);
+template <class Real>
+void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
+                     const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                     int nbins, int max_count, const int* off,
+                     const uint32_t* list, const double2* coef, double* pk);
+
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
                         const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
@@ -214,6 +234,45 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
                               const Real* Fa, const Real* Fb, const int* pa,
                               const int* pb, int npairs,
                               double* out /* 2 * npairs, imaginary 0 */);
+
+// ---- ffft.cu -------------------------------------------------------------
+// Float-float transforms of the shell fields: a plan is the radix list of
+// the length and its twiddle table (cos, sin of 2 pi k / n, float-float).
+struct FFPlan {
+  int n;
+  int nstage;
+  int radix[16];
+  const float4* tw;
+};
+bool ff_length_ok(int n);
+FFPlan ff_plan(Context& ctx, int n);
+// Spectrum of the FP32 mesh on the cube |sx|, |sy| <= Kg, 0 <= sz <= Kg:
+// cube[sx + Kg][sy + Kg][sz] (T1, T2: scratch of n0 (Kg+1) n1 and
+// (2Kg+1)(Kg+1) n0 float4).
+void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
+                            int Kg, float4* T1, float4* T2, float4* cube);
+// Evaluation-grid half spectra E[c][b][a] of G (planes c <= Kg) and
+// E[q][c][b][a] of nq shell fields (planes c <= K) from the cube.
+void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
+                       const float4* cube, int Kg, const float2* const iw[3],
+                       cd k0, float4* E);
+void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
+                       const float4* cube, int Kg, int K, const int16_t* tab,
+                       int nq, int ell, const float2* const iw[3], cd k0,
+                       float4* E);
+// Real fields on the M grid of nf half spectra E with planes c <= Kcf and
+// band |sx|, |sy| <= Kf, as float-float words out[f][a][b][z] (hi) and
+// out_lo (Y1, Y2: scratch of nf (Kcf+1) M0 M1 float4 each).
+void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
+                       const float4* E, float4* Y1, float4* Y2, float* out,
+                       float* out_lo);
+// sum_x F_a F_b G of float-float fields (hi, lo words) for every pair
+// (real parts at out[2 p]).
+void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, const float* Gh,
+                            const float* Gl, const float* Fah,
+                            const float* Fal, const float* Fbh,
+                            const float* Fbl, const int* pa, const int* pb,
+                            int npairs, double* out);
 
 // ---- adjoint.cu ----------------------------------------------------------
 // Cotangent bookkeeping of the bispectrum adjoint: the partners of bin a in

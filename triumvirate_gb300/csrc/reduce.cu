@@ -205,6 +205,55 @@ reduce_pairs_real_kernel(int64_t ncell, const Real* G, const Real* Fa,
   block_add_acc<kPairChunk, Real>(acc, out + 2 * p0, 2, npairs - p0, red);
 }
 
+// (ah + al)(bh + bl)(gh + gl) as an unnormalised float-float pair: the
+// leading products by TwoProduct, the cross terms to first order (their
+// neglected products are below 2^-46 of the result).
+__device__ __forceinline__ FF ff_prod3(float ah, float al, float bh, float bl,
+                                       float gh, float gl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  const float q = __fmul_rn(p, gh);
+  float f = __fmaf_rn(p, gh, -q);
+  f = __fmaf_rn(p, gl, f);
+  f = __fmaf_rn(e, gh, f);
+  return FF{q, f};
+}
+
+// sum_x F_a F_b G of float-float fields (hi and lo word arrays).
+__global__ void __launch_bounds__(256)
+reduce_pairs_ff_kernel(int64_t ncell, const float* Gh, const float* Gl,
+                       const float* Fah, const float* Fal, const float* Fbh,
+                       const float* Fbl, const int* pa, const int* pb,
+                       int npairs, double* out) {
+  __shared__ double red[kPairChunk * 32];
+  const int p0 = blockIdx.y * kPairChunk;
+  int ia[kPairChunk], ib[kPairChunk];
+  bool ok[kPairChunk];
+#pragma unroll
+  for (int q = 0; q < kPairChunk; ++q) {
+    ok[q] = (p0 + q) < npairs;
+    ia[q] = ok[q] ? pa[p0 + q] : 0;
+    ib[q] = ok[q] ? pb[p0 + q] : 0;
+  }
+  Acc<float> acc[kPairChunk];
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const float gh = Gh[t], gl = Gl[t];
+#pragma unroll
+    for (int q = 0; q < kPairChunk; ++q) {
+      if (!ok[q]) continue;
+      const int64_t oa = int64_t(ia[q]) * ncell + t;
+      const int64_t ob = int64_t(ib[q]) * ncell + t;
+      const float ah = Fah[oa], al = Fal[oa];
+      const float bh = Fbh[ob], bl = Fbl[ob];
+      ff_merge(acc[q].v, ff_prod3(ah, al, bh, bl, gh, gl));
+    }
+  }
+  block_add_acc<kPairChunk, float>(acc, out + 2 * p0, 2, npairs - p0, red);
+}
+
 // Sum of xi * y_a * y_b per integer key s_x^2 + s_y^2 + s_z^2 (cubic cells).
 template <class Real>
 __global__ void __launch_bounds__(256)
@@ -497,6 +546,20 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
   TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
   reduce_pairs_real_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
       ncell, G, Fa, Fb, pa, pb, npairs, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, const float* Gh,
+                            const float* Gl, const float* Fah,
+                            const float* Fal, const float* Fbh,
+                            const float* Fbl, const int* pa, const int* pb,
+                            int npairs, double* out) {
+  if (npairs <= 0) return;
+  const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
+  dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
+  TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
+  reduce_pairs_ff_kernel<<<grid, 256, 0, ctx.stream>>>(
+      ncell, Gh, Gl, Fah, Fal, Fbh, Fbl, pa, pb, npairs, out);
   TRVG_LAUNCHED(ctx);
 }
 

@@ -7,6 +7,8 @@
 // spectra of its real and imaginary part meshes, read back at any full-grid
 // index through Hermitian symmetry.  Interlacing (field.cpp:1615-1653) is
 // applied on read from the raw main and shadow spectra.
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace trvg {
@@ -302,6 +304,117 @@ __global__ void build_F_half_kernel(Geom g, int M0, int M1, int M2, int K0,
       o.y = sel ? FR(val.im) : FR(0);
       out[int64_t(q) * count + t] = o;
     }
+  }
+}
+
+// ---- Fine-binned two-point statistics from a cached mode list ------------
+//
+// What twopt_stats_kernel computes per mode apart from the field product --
+// sample-rule membership, |k|, y_lm(k) / W_pk and the shot-noise weight
+// C1 y_lm / W_sn -- depends on the mesh, the binning and the degrees only.
+// stats_plan_kernel evaluates it once (same exact FP64 arithmetic),
+// stats_fill_kernel lists the member modes bin by bin, and per call
+// stats_pk_kernel sums fa conj(fb) coef over each bin's list, one block row
+// per bin, with no shared-memory atomics.
+
+__device__ __forceinline__ void cube_mode(const Geom& g, const Cube& cube,
+                                          uint32_t t, int& sx, int& sy,
+                                          int& sz) {
+  const int c = int(t % uint32_t(cube.ext[2]));
+  const uint32_t r = t / uint32_t(cube.ext[2]);
+  const int b = int(r % uint32_t(cube.ext[1]));
+  const int a = int(r / uint32_t(cube.ext[1]));
+  sx = cube.dense[0] ? shift_index(a, g.n[0]) : a - cube.K[0];
+  sy = cube.dense[1] ? shift_index(b, g.n[1]) : b - cube.K[1];
+  sz = cube.dense[2] ? shift_index(c, g.n[2]) : c - cube.K[2];
+}
+
+// Bins must be disjoint in sample index (each mode in at most one bin).
+__global__ void stats_plan_kernel(Geom g, Cube cube, int ell, int m,
+                                  AxisTablesDev ax, BinsDev bins,
+                                  int16_t* qtab, double2* coef, double* kmode,
+                                  double2* snmode) {
+  const int n_sample = 1000000;
+  const double dk_sample = 1.e-5;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+       t < uint32_t(cube.count); t += gridDim.x * blockDim.x) {
+    int sx, sy, sz;
+    cube_mode(g, cube, t, sx, sy, sz);
+    const double kx = dmul(double(sx), g.dk[0]);
+    const double ky = dmul(double(sy), g.dk[1]);
+    const double kz = dmul(double(sz), g.dk[2]);
+    const double k = vec3_mag(kx, ky, kz);
+    const int idx_k = int(ddiv(k, dk_sample));
+    int q = -1;
+    if (idx_k >= 0 && idx_k < n_sample)
+      for (int b = 0; b < bins.nbins; ++b)
+        if (bins.smin[b] <= idx_k && idx_k < bins.smax[b]) q = b;
+    qtab[t] = int16_t(q);
+    if (q < 0) continue;
+    kmode[t] = k;
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              kk = wrap(sz, g.n[2]);
+    const double al = alias_sn(ax, i, j, kk);
+    double win_pk, win_sn;
+    if (ax.interlace) {
+      const double w = window_pow(ax, i, j, kk);
+      win_pk = w * w;
+      win_sn = win_pk;
+    } else {
+      win_pk = al;
+      win_sn = al;
+    }
+    const cd y = reduced_ylm(ell, m, kx, ky, kz);
+    const cd c = cdivr(y, win_pk);
+    coef[t] = make_double2(c.re, c.im);
+    const cd sn = cdivr(al * y, win_sn);
+    snmode[t] = make_double2(sn.re, sn.im);
+  }
+}
+
+__global__ void stats_fill_kernel(uint32_t nmode, const int16_t* qtab,
+                                  const int* off, int* cursor,
+                                  uint32_t* list) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nmode;
+       t += gridDim.x * blockDim.x) {
+    const int q = qtab[t];
+    if (q >= 0) list[off[q] + atomicAdd(cursor + q, 1)] = t;
+  }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256)
+stats_pk_kernel(Geom g, Cube cube, FieldSpec<Real> fa, FieldSpec<Real> fb,
+                const int* off, const uint32_t* list, const double2* coef,
+                double* pk) {
+  const int q = blockIdx.y;
+  const int e0 = off[q], e1 = off[q + 1];
+  cd acc = {0., 0.};
+  for (int e = e0 + blockIdx.x * blockDim.x + threadIdx.x; e < e1;
+       e += gridDim.x * blockDim.x) {
+    const uint32_t t = list[e];
+    int sx, sy, sz;
+    cube_mode(g, cube, t, sx, sy, sz);
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              kk = wrap(sz, g.n[2]);
+    const cd va = field_value(fa, g, i, j, kk);
+    const cd vb = field_value(fb, g, i, j, kk);
+    const double2 c = coef[t];
+    acc = acc + (va * conjg(vb)) * cd{c.x, c.y};
+  }
+  __shared__ double red[2][32];
+  double v[2] = {acc.re, acc.im};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int r = 0; r < 2; ++r) {
+    double x = v[r];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[r][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double x = 0.;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) x += red[threadIdx.x][w];
+    if (e1 > e0) atomicAdd(pk + 2 * q + threadIdx.x, x);
   }
 }
 
@@ -636,26 +749,48 @@ twopt_field_kernel(Geom g, FieldSpec<Real> fa, FieldSpec<Real> fb, cd shot,
 
 // FP32 fast path for two real-mesh spectra without interlacing:
 // P = (fa fb^* / C_1 - S) / V in float, the k = 0 mode given exactly.
+// One element of the FP32 shot-noise field at flat half-spectrum index t.
+__device__ __forceinline__ float2 twopt_elem_f32(uint32_t t, int n1, int nzh,
+                                                 float2 a, float2 b,
+                                                 const float* iax,
+                                                 const float* iay,
+                                                 const float* iaz, float shot,
+                                                 float inv_vol, float2 p0) {
+  if (t == 0) return p0;
+  const uint32_t row = t / uint32_t(nzh);
+  const int k = int(t - row * uint32_t(nzh));
+  const int i = int(row / uint32_t(n1)), j = int(row - uint32_t(i) * n1);
+  const float inv = iax[i] * iay[j] * iaz[k];
+  float2 o;
+  o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
+  o.y = ((a.y * b.x - a.x * b.y) * inv) * inv_vol;
+  return o;
+}
+
+// Flat over the half spectrum, two elements per 16-byte load and store.
 __global__ void __launch_bounds__(256)
-twopt_field_real_f32_kernel(int n1, int nzh, const float2* fa,
-                            const float2* fb, const float* inv_alias_x,
-                            const float* inv_alias_y,
-                            const float* inv_alias_z, float shot,
+twopt_field_real_f32_kernel(uint32_t nhalf, int n1, int nzh, const float2* fa,
+                            const float2* fb, const float* iax,
+                            const float* iay, const float* iaz, float shot,
                             float inv_vol, float2 p0, float2* out) {
-  const int row = blockIdx.x;
-  const int i = row / n1, j = row - (row / n1) * n1;
-  const float axy = inv_alias_x[i] * inv_alias_y[j];
   const bool same = fa == fb;  // |f|^2: one read of the spectrum
-  for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
-    const int64_t t = int64_t(row) * nzh + k;
-    const float2 a = fa[t];
-    const float2 b = same ? a : fb[t];
-    const float inv = axy * inv_alias_z[k];
-    float2 o;
-    o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
-    o.y = ((a.y * b.x - a.x * b.y) * inv) * inv_vol;
-    if (row == 0 && k == 0) o = p0;
-    out[t] = o;
+  const uint32_t npair = nhalf / 2;
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < npair;
+       u += gridDim.x * blockDim.x) {
+    const float4 a = reinterpret_cast<const float4*>(fa)[u];
+    const float4 b = same ? a : reinterpret_cast<const float4*>(fb)[u];
+    const float2 o0 = twopt_elem_f32(2 * u, n1, nzh, make_float2(a.x, a.y),
+                                     make_float2(b.x, b.y), iax, iay, iaz,
+                                     shot, inv_vol, p0);
+    const float2 o1 = twopt_elem_f32(2 * u + 1, n1, nzh, make_float2(a.z, a.w),
+                                     make_float2(b.z, b.w), iax, iay, iaz,
+                                     shot, inv_vol, p0);
+    reinterpret_cast<float4*>(out)[u] = make_float4(o0.x, o0.y, o1.x, o1.y);
+  }
+  if ((nhalf & 1u) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t t = nhalf - 1;
+    out[t] = twopt_elem_f32(t, n1, nzh, fa[t], fb[t], iax, iay, iaz, shot,
+                            inv_vol, p0);
   }
 }
 
@@ -743,10 +878,46 @@ void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
                                  const float2* fa, const float2* fb,
                                  const float* const inv_alias[3], float shot,
                                  float2 p0, float2* out) {
+  if (g.nhalf >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Mesh too large.");
   TRVG_KBEGIN(ctx, "twopt_field_kernel");
-  twopt_field_real_f32_kernel<<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
-      g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1], inv_alias[2], shot,
-      float(1. / g.vol), p0, out);
+  twopt_field_real_f32_kernel<<<grid_for(g.nhalf / 2, 256), 256, 0,
+                                ctx.stream>>>(
+      uint32_t(g.nhalf), g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1],
+      inv_alias[2], shot, float(1. / g.vol), p0, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_stats_plan(Context& ctx, const Geom& g, const Cube& cube,
+                       int ell, int m, const AxisTablesDev& ax,
+                       const BinsDev& bins, int16_t* qtab, double2* coef,
+                       double* kmode, double2* snmode) {
+  if (cube.count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Mode cube too large.");
+  TRVG_KBEGIN(ctx, "stats_plan_kernel");
+  stats_plan_kernel<<<grid_for(cube.count, 256), 256, 0, ctx.stream>>>(
+      g, cube, ell, m, ax, bins, qtab, coef, kmode, snmode);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_stats_fill(Context& ctx, int64_t nmode, const int16_t* qtab,
+                       const int* off, int* cursor, uint32_t* list) {
+  TRVG_KBEGIN(ctx, "stats_fill_kernel");
+  stats_fill_kernel<<<grid_for(nmode, 256), 256, 0, ctx.stream>>>(
+      uint32_t(nmode), qtab, off, cursor, list);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
+                     const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                     int nbins, int max_count, const int* off,
+                     const uint32_t* list, const double2* coef, double* pk) {
+  if (nbins <= 0 || max_count <= 0) return;
+  const int bx = int(std::min<int64_t>((max_count + 1023) / 1024, 64));
+  TRVG_KBEGIN(ctx, "twopt_stats_kernel");
+  stats_pk_kernel<Real><<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
+      g, cube, fa, fb, off, list, coef, pk);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -868,6 +1039,10 @@ TRVG_INST2(double, double)
 #undef TRVG_INST2
 
 #define TRVG_INST(R)                                                         \
+  template void launch_stats_pk<R>(Context&, const Geom&, const Cube&,       \
+                                   const FieldSpec<R>&, const FieldSpec<R>&, \
+                                   int, int, const int*, const uint32_t*,    \
+                                   const double2*, double*);                 \
   template void launch_twopt_stats<R>(                                       \
       Context&, const Geom&, const Cube&, const FieldSpec<R>&,               \
       const FieldSpec<R>&, cd, int, int, const AxisTablesDev&,               \
