@@ -1,8 +1,12 @@
 // Float-float ("double-single") arithmetic for the accurate transforms.
 //
-// A value is the unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2),
-// about 48 significant bits, computed on the FP32 pipe only.  Sums use
-// Knuth's TwoSum, products the FMA form of Dekker's TwoProduct.  Every
+// A value is the unevaluated sum hi + lo of two floats, about 48
+// significant bits, computed on the FP32 pipe only.  Sums use Knuth's
+// TwoSum on the leading words, products the FMA form of Dekker's
+// TwoProduct.  The results are left unnormalised (lo may exceed half an ulp
+// of hi by a few ulps): the next operation splits the leading words exactly
+// again, so skipping the renormalisation costs no accuracy, and ffnorm
+// restores the canonical form where a value leaves the transforms.  Every
 // operation goes through the _rn intrinsics, which the compiler never
 // contracts into FMAs: a contracted product or sum would lose the exactly
 // recovered rounding errors these formulas depend on.
@@ -15,10 +19,17 @@ namespace trvg {
 __device__ __forceinline__ FF ffadd(FF a, FF b) {
   const float s = __fadd_rn(a.hi, b.hi);
   const float v = __fsub_rn(s, a.hi);
-  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  const float t = __fadd_rn(s, e);
-  return FF{t, __fsub_rn(e, __fsub_rn(t, s))};
+  const float e =
+      __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  return FF{s, __fadd_rn(e, __fadd_rn(a.lo, b.lo))};
+}
+
+// Canonical form (|lo| <= ulp(hi) / 2) by TwoSum of the two words.
+__device__ __forceinline__ FF ffnorm(FF a) {
+  const float s = __fadd_rn(a.hi, a.lo);
+  const float v = __fsub_rn(s, a.hi);
+  return FF{s, __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)),
+                         __fsub_rn(a.lo, v))};
 }
 
 __device__ __forceinline__ FF ffneg(FF a) { return FF{-a.hi, -a.lo}; }
@@ -30,8 +41,7 @@ __device__ __forceinline__ FF ffmul(FF a, FF b) {
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  const float t = __fadd_rn(p, e);
-  return FF{t, __fsub_rn(e, __fsub_rn(t, p))};
+  return FF{p, e};
 }
 
 // Multiplication by a power of two (exact).
@@ -55,9 +65,29 @@ __device__ __forceinline__ FFC ffc_add(FFC a, FFC b) {
 __device__ __forceinline__ FFC ffc_sub(FFC a, FFC b) {
   return FFC{ffsub(a.re, b.re), ffsub(a.im, b.im)};
 }
+// a b + c d: both leading products and their sum are split exactly
+// (TwoProduct, TwoSum); the cross terms go into the error word by FMA, and
+// only lo * lo is dropped (about 2^-48 relative).
+__device__ __forceinline__ FF ffdot2(FF a, FF b, FF c, FF d) {
+  const float p1 = __fmul_rn(a.hi, b.hi);
+  const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+  const float p2 = __fmul_rn(c.hi, d.hi);
+  const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+  const float s = __fadd_rn(p1, p2);
+  const float v = __fsub_rn(s, p1);
+  const float es =
+      __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+  float e = __fadd_rn(__fadd_rn(e1, e2), es);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  e = __fmaf_rn(c.hi, d.lo, e);
+  e = __fmaf_rn(c.lo, d.hi, e);
+  return FF{s, e};
+}
+
 __device__ __forceinline__ FFC ffc_mul(FFC a, FFC b) {
-  return FFC{ffsub(ffmul(a.re, b.re), ffmul(a.im, b.im)),
-             ffadd(ffmul(a.re, b.im), ffmul(a.im, b.re))};
+  return FFC{ffdot2(a.re, b.re, ffneg(a.im), b.im),
+             ffdot2(a.re, b.im, a.im, b.re)};
 }
 // a * s for a real float-float s.
 __device__ __forceinline__ FFC ffc_mulr(FFC a, FF s) {
@@ -73,6 +103,10 @@ __device__ __forceinline__ FFC ffc_scale2(FFC a, float p2) {
 }
 __device__ __forceinline__ FFC ffc_zero() {
   return FFC{FF{0.f, 0.f}, FF{0.f, 0.f}};
+}
+
+__device__ __forceinline__ FFC ffc_norm(FFC a) {
+  return FFC{ffnorm(a.re), ffnorm(a.im)};
 }
 
 // Storage: float4 (re.hi, re.lo, im.hi, im.lo).

@@ -14,6 +14,7 @@
 // rounded to FP32 once, at the end.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "ff.cuh"
@@ -53,43 +54,40 @@ __device__ __forceinline__ FF k_c2_5() { return FF{-0x1.9e377ap-1f, 0x1.1a02d6p-
 __device__ __forceinline__ FF k_s1_5() { return FF{0x1.e6f0e2p-1f, -0x1.97756p-26f}; }
 __device__ __forceinline__ FF k_s2_5() { return FF{0x1.2cf23p-1f, 0x1.1d5698p-27f}; }
 
-// In-place DFT of size R with root exp(d 2 pi i / R).
-template <int R>
-__device__ __forceinline__ void small_dft(FFC* v, int d);
-
-template <>
-__device__ __forceinline__ void small_dft<2>(FFC* v, int) {
+// In-place DFTs of size R with root exp(D 2 pi i / R), D = +-1.
+template <int D>
+__device__ __forceinline__ void small_dft2(FFC* v) {
   const FFC a = v[0], b = v[1];
   v[0] = ffc_add(a, b);
   v[1] = ffc_sub(a, b);
 }
 
-template <>
-__device__ __forceinline__ void small_dft<4>(FFC* v, int d) {
+template <int D>
+__device__ __forceinline__ void small_dft4(FFC* v) {
   const FFC t0 = ffc_add(v[0], v[2]), t1 = ffc_sub(v[0], v[2]);
   const FFC t2 = ffc_add(v[1], v[3]);
-  const FFC t3 = ffc_muli(ffc_sub(v[1], v[3]), d);
+  const FFC t3 = ffc_muli(ffc_sub(v[1], v[3]), D);
   v[0] = ffc_add(t0, t2);
   v[2] = ffc_sub(t0, t2);
   v[1] = ffc_add(t1, t3);
   v[3] = ffc_sub(t1, t3);
 }
 
-template <>
-__device__ __forceinline__ void small_dft<8>(FFC* v, int d) {
+template <int D>
+__device__ __forceinline__ void small_dft8(FFC* v) {
   FFC e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
-  small_dft<4>(e, d);
-  small_dft<4>(o, d);
-  // o_k *= exp(d 2 pi i k / 8)
+  small_dft4<D>(e);
+  small_dft4<D>(o);
+  // o_k *= exp(D 2 pi i k / 8)
   const FF c = k_rsqrt2();
   auto w1 = [&](FFC x) {
-    const FF re = (d > 0) ? ffsub(x.re, x.im) : ffadd(x.re, x.im);
-    const FF im = (d > 0) ? ffadd(x.im, x.re) : ffsub(x.im, x.re);
+    const FF re = (D > 0) ? ffsub(x.re, x.im) : ffadd(x.re, x.im);
+    const FF im = (D > 0) ? ffadd(x.im, x.re) : ffsub(x.im, x.re);
     return FFC{ffmul(re, c), ffmul(im, c)};
   };
   o[1] = w1(o[1]);
-  o[2] = ffc_muli(o[2], d);
-  o[3] = ffc_muli(w1(o[3]), d);
+  o[2] = ffc_muli(o[2], D);
+  o[3] = ffc_muli(w1(o[3]), D);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     v[k] = ffc_add(e[k], o[k]);
@@ -97,32 +95,41 @@ __device__ __forceinline__ void small_dft<8>(FFC* v, int d) {
   }
 }
 
-template <>
-__device__ __forceinline__ void small_dft<3>(FFC* v, int d) {
+template <int D>
+__device__ __forceinline__ void small_dft3(FFC* v) {
   const FFC t = ffc_add(v[1], v[2]);
   const FFC m = ffc_sub(v[0], ffc_scale2(t, 0.5f));
-  const FFC u = ffc_mulr(ffc_muli(ffc_sub(v[1], v[2]), d), k_sqrt3_2());
+  const FFC u = ffc_mulr(ffc_muli(ffc_sub(v[1], v[2]), D), k_sqrt3_2());
   v[0] = ffc_add(v[0], t);
   v[1] = ffc_add(m, u);
   v[2] = ffc_sub(m, u);
 }
 
-template <>
-__device__ __forceinline__ void small_dft<5>(FFC* v, int d) {
+template <int D>
+__device__ __forceinline__ void small_dft5(FFC* v) {
   const FFC t1 = ffc_add(v[1], v[4]), t2 = ffc_add(v[2], v[3]);
   const FFC t3 = ffc_sub(v[1], v[4]), t4 = ffc_sub(v[2], v[3]);
   const FF c1 = k_c1_5(), c2 = k_c2_5(), s1 = k_s1_5(), s2 = k_s2_5();
   const FFC b1 = ffc_add(v[0], ffc_add(ffc_mulr(t1, c1), ffc_mulr(t2, c2)));
   const FFC b2 = ffc_add(v[0], ffc_add(ffc_mulr(t1, c2), ffc_mulr(t2, c1)));
   const FFC b3 =
-      ffc_muli(ffc_add(ffc_mulr(t3, s1), ffc_mulr(t4, s2)), d);
+      ffc_muli(ffc_add(ffc_mulr(t3, s1), ffc_mulr(t4, s2)), D);
   const FFC b4 =
-      ffc_muli(ffc_sub(ffc_mulr(t3, s2), ffc_mulr(t4, s1)), d);
+      ffc_muli(ffc_sub(ffc_mulr(t3, s2), ffc_mulr(t4, s1)), D);
   v[0] = ffc_add(v[0], ffc_add(t1, t2));
   v[1] = ffc_add(b1, b3);
   v[4] = ffc_sub(b1, b3);
   v[2] = ffc_add(b2, b4);
   v[3] = ffc_sub(b2, b4);
+}
+
+template <int R, int D>
+__device__ __forceinline__ void small_dft(FFC* v) {
+  if constexpr (R == 2) small_dft2<D>(v);
+  else if constexpr (R == 4) small_dft4<D>(v);
+  else if constexpr (R == 8) small_dft8<D>(v);
+  else if constexpr (R == 3) small_dft3<D>(v);
+  else small_dft5<D>(v);
 }
 
 // Shared-memory slot of element i of a line: one pad slot per 8 elements,
@@ -132,6 +139,13 @@ __host__ __device__ __forceinline__ int pidx(int i) { return i + (i >> 3); }
 __host__ __device__ __forceinline__ int padded_len(int n) {
   return pidx(n - 1) + 1;
 }
+// Distance between the lines of a block: odd, so that the same element of
+// consecutive lines falls in different bank groups.
+__host__ __device__ __forceinline__ int line_stride(int n) {
+  return padded_len(n) | 1;
+}
+// Lines per block at most (per-line offsets are kept in shared memory).
+constexpr int kMaxLines = 16;
 
 // Butterflies one thread keeps in registers per stage.
 template <int R>
@@ -139,156 +153,317 @@ struct StageItems {
   static constexpr int value = R == 8 || R == 5 ? 1 : 2;
 };
 
-// One Stockham stage of radix R over the nl lines of A (padded line length
-// ln), in place: every thread loads and transforms its butterflies, the
-// block synchronises, then every thread writes its results.
-template <int R>
-__device__ __noinline__ void ff_stage(float4* A, int nl, int n, int ln,
-                                         int Ns, const float4* tw, int d) {
+// Quotient of w by d through the plan's multiplier (w, d small: see FFPlan).
+__device__ __forceinline__ int fdiv(int w, int d, unsigned m) {
+  return d == 1 ? w : int(__umulhi(unsigned(w), m));
+}
+
+// One Stockham stage of radix R (stage s of the plan) over the nl lines of
+// A (padded line length ln), in place: every thread loads and transforms
+// its butterflies, the block synchronises, then every thread writes its
+// results.
+template <int R, int D>
+__device__ __forceinline__ void ff_stage_body(float4* A, int nl, int ln,
+                                      const FFPlan& P, int s,
+                                      const float4* tw) {
   constexpr int IMAX = StageItems<R>::value;
-  const int nb = n / R;
+  const int nb = P.nb[s], Ns = P.ns[s], tstep = P.tstep[s];
+  const unsigned mnb = P.mnb[s], mns = P.mns[s];
   const int items = nl * nb;
   FFC v[IMAX][R];
 #pragma unroll
   for (int it = 0; it < IMAX; ++it) {
     const int w = threadIdx.x + it * blockDim.x;
     if (w >= items) break;
-    const int l = w / nb, j = w - l * nb;
+    const int l = fdiv(w, nb, mnb), j = w - l * nb;
+    const int q = fdiv(j, Ns, mns), k = j - q * Ns;
     const float4* in = A + l * ln;
-    const int k = j % Ns;
-    const int step = (n / (Ns * R)) * k;  // r * step < n
+    const int step = tstep * k;  // r * step < n
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       v[it][r] = ffc_load(in + pidx(j + r * nb));
       if (r > 0 && k > 0) {
         const float4 t = tw[r * step];
         FFC wv{FF{t.x, t.y}, FF{t.z, t.w}};
-        if (d < 0) wv.im = ffneg(wv.im);
+        if (D < 0) wv.im = ffneg(wv.im);
         v[it][r] = ffc_mul(v[it][r], wv);
       }
     }
-    small_dft<R>(v[it], d);
+    small_dft<R, D>(v[it]);
   }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < IMAX; ++it) {
     const int w = threadIdx.x + it * blockDim.x;
     if (w >= items) break;
-    const int l = w / nb, j = w - l * nb;
+    const int l = fdiv(w, nb, mnb), j = w - l * nb;
+    const int q = fdiv(j, Ns, mns), k = j - q * Ns;
     float4* out = A + l * ln;
-    const int k = j % Ns;
-    const int idx = (j / Ns) * Ns * R + k;
+    const int idx = q * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) ffc_store(out + pidx(idx + r * Ns), v[it][r]);
   }
   __syncthreads();
 }
 
-// Transforms the nl lines of A (padded line length ln) in place.
-__device__ void ff_fft_lines(float4* A, int nl, int ln, const FFPlan& P,
-                             int d) {
-  __syncthreads();
-  int Ns = 1;
-  for (int s = 0; s < P.nstage; ++s) {
-    switch (P.radix[s]) {
-      case 8: ff_stage<8>(A, nl, P.n, ln, Ns, P.tw, d); break;
-      case 4: ff_stage<4>(A, nl, P.n, ln, Ns, P.tw, d); break;
-      case 2: ff_stage<2>(A, nl, P.n, ln, Ns, P.tw, d); break;
-      case 3: ff_stage<3>(A, nl, P.n, ln, Ns, P.tw, d); break;
-      default: ff_stage<5>(A, nl, P.n, ln, Ns, P.tw, d); break;
+// Butterflies per lane when one warp transforms a line.
+template <int R>
+struct WarpItems {
+  static constexpr int value = (R == 8 || R == 5) ? 1 : (R == 2 ? 3 : 2);
+};
+
+// One stage of radix R over the line L of this warp (same indexing as
+// ff_stage, butterfly j = lane + 32 it), synchronised within the warp only.
+template <int R, int D>
+__device__ __forceinline__ void ff_stage_warp_body(float4* L, const FFPlan& P,
+                                                   int s, const float4* tw) {
+  constexpr int IMAX = WarpItems<R>::value;
+  const int nb = P.nb[s], Ns = P.ns[s], tstep = P.tstep[s];
+  const unsigned mns = P.mns[s];
+  const int lane = threadIdx.x & 31;
+  FFC v[IMAX][R];
+#pragma unroll
+  for (int it = 0; it < IMAX; ++it) {
+    const int j = lane + 32 * it;
+    if (j >= nb) break;
+    const int k = j - fdiv(j, Ns, mns) * Ns;
+    const int step = tstep * k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      v[it][r] = ffc_load(L + pidx(j + r * nb));
+      if (r > 0 && k > 0) {
+        const float4 t = tw[r * step];
+        FFC wv{FF{t.x, t.y}, FF{t.z, t.w}};
+        if (D < 0) wv.im = ffneg(wv.im);
+        v[it][r] = ffc_mul(v[it][r], wv);
+      }
     }
-    Ns *= P.radix[s];
+    small_dft<R, D>(v[it]);
   }
+  __syncwarp();
+#pragma unroll
+  for (int it = 0; it < IMAX; ++it) {
+    const int j = lane + 32 * it;
+    if (j >= nb) break;
+    const int q = fdiv(j, Ns, mns), k = j - q * Ns;
+    const int idx = q * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) ffc_store(L + pidx(idx + r * Ns), v[it][r]);
+  }
+  __syncwarp();
 }
 
+// Transforms the nl lines of A (line stride ln) in place, direction D,
+// with the twiddle table tw (n entries, usually a shared-memory copy).
+// Radix sets of a plan (bit per radix); kernels specialised for a set
+// inline its stages, the generic ones (kRadixAll) call them out of line, so
+// that each stage keeps its own register allocation.
+constexpr int kRadix8 = 1, kRadix4 = 2, kRadix2 = 4, kRadix3 = 8,
+              kRadix5 = 16, kRadixAll = 31;
+
+template <int R, int D>
+__device__ __noinline__ void ff_stage_call(float4* A, int nl, int ln,
+                                           const FFPlan& P, int s,
+                                           const float4* tw) {
+  ff_stage_body<R, D>(A, nl, ln, P, s, tw);
+}
+template <int R, int D>
+__device__ __noinline__ void ff_stage_warp_call(float4* L, const FFPlan& P,
+                                                int s, const float4* tw) {
+  ff_stage_warp_body<R, D>(L, P, s, tw);
+}
+
+template <int R, int D, int MASK>
+__device__ __forceinline__ void ff_stage(float4* A, int nl, int ln,
+                                         const FFPlan& P, int s,
+                                         const float4* tw) {
+  if constexpr (MASK == kRadixAll) ff_stage_call<R, D>(A, nl, ln, P, s, tw);
+  else ff_stage_body<R, D>(A, nl, ln, P, s, tw);
+}
+template <int R, int D, int MASK>
+__device__ __forceinline__ void ff_stage_warp(float4* L, const FFPlan& P,
+                                              int s, const float4* tw) {
+  if constexpr (MASK == kRadixAll) ff_stage_warp_call<R, D>(L, P, s, tw);
+  else ff_stage_warp_body<R, D>(L, P, s, tw);
+}
+
+// Transforms the nl lines of A (line stride ln) in place, direction D,
+// with the twiddle table tw (n entries, a shared-memory copy).  The plan
+// orders its stages by radix (8, 4, 2, 3, 5); MASK holds every radix of
+// the plan.
+template <int D, int MASK>
+__device__ void ff_fft_lines(float4* A, int nl, int ln, const FFPlan& P,
+                             const float4* tw) {
+  __syncthreads();
+  if (P.warp_lines) {
+    for (int l = threadIdx.x >> 5; l < nl; l += blockDim.x >> 5) {
+      float4* L = A + l * ln;
+      int s = 0;
+      if constexpr ((MASK & kRadix8) != 0)
+        for (; s < P.nstage && P.radix[s] == 8; ++s)
+          ff_stage_warp<8, D, MASK>(L, P, s, tw);
+      if constexpr ((MASK & kRadix4) != 0)
+        for (; s < P.nstage && P.radix[s] == 4; ++s)
+          ff_stage_warp<4, D, MASK>(L, P, s, tw);
+      if constexpr ((MASK & kRadix2) != 0)
+        for (; s < P.nstage && P.radix[s] == 2; ++s)
+          ff_stage_warp<2, D, MASK>(L, P, s, tw);
+      if constexpr ((MASK & kRadix3) != 0)
+        for (; s < P.nstage && P.radix[s] == 3; ++s)
+          ff_stage_warp<3, D, MASK>(L, P, s, tw);
+      if constexpr ((MASK & kRadix5) != 0)
+        for (; s < P.nstage; ++s) ff_stage_warp<5, D, MASK>(L, P, s, tw);
+    }
+    __syncthreads();
+    return;
+  }
+  int s = 0;
+  if constexpr ((MASK & kRadix8) != 0)
+    for (; s < P.nstage && P.radix[s] == 8; ++s)
+      ff_stage<8, D, MASK>(A, nl, ln, P, s, tw);
+  if constexpr ((MASK & kRadix4) != 0)
+    for (; s < P.nstage && P.radix[s] == 4; ++s)
+      ff_stage<4, D, MASK>(A, nl, ln, P, s, tw);
+  if constexpr ((MASK & kRadix2) != 0)
+    for (; s < P.nstage && P.radix[s] == 2; ++s)
+      ff_stage<2, D, MASK>(A, nl, ln, P, s, tw);
+  if constexpr ((MASK & kRadix3) != 0)
+    for (; s < P.nstage && P.radix[s] == 3; ++s)
+      ff_stage<3, D, MASK>(A, nl, ln, P, s, tw);
+  if constexpr ((MASK & kRadix5) != 0)
+    for (; s < P.nstage; ++s) ff_stage<5, D, MASK>(A, nl, ln, P, s, tw);
+}
+
+// Shared-memory copy of the plan's twiddles after the nl lines of a block.
+__device__ __forceinline__ const float4* stage_twiddles(float4* smem,
+                                                        int LB, int ls,
+                                                        const FFPlan& P) {
+  float4* tw = smem + LB * ls;
+  for (int i = threadIdx.x; i < P.n; i += blockDim.x) tw[i] = P.tw[i];
+  return tw;
+}
+
+// Global-memory form: canonical float-float words.
 __device__ __forceinline__ float4 ffc_pack(FFC a) {
+  a = ffc_norm(a);
   return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo);
 }
 
 // ---- Forward cube ----------------------------------------------------------
 
+// Element loops of the passes: loads run one warp per line along the
+// contiguous axis; stores that transpose run with the line index fastest
+// (the lines of a block are consecutive in the output), over the next power
+// of two of the line count.  Per-line offsets are computed once per block.
+__device__ __forceinline__ int lines_shift(int nl) {
+  return nl <= 1 ? 0 : 32 - __clz(nl - 1);
+}
+
 // z lines of the real mesh, two rows per complex line; keeps kz in [0, Kz]
 // into T1[x][kz][y].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
-ff_fwd_z_kernel(Geom g, const float* mesh, FFPlan P, int LB, int Kz,
-                float4* T1) {
+ff_fwd_z_kernel(Geom g, const float* mesh, __grid_constant__ const FFPlan P,
+                int LB, int Kz, float4* T1) {
   extern __shared__ float4 smem[];
-  const int n2 = g.n[2], ln = padded_len(n2);
+  __shared__ int64_t obase[2 * kMaxLines];
+  const int n2 = g.n[2], ls = line_stride(n2);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int64_t npair = int64_t(g.n[0]) * g.n[1] / 2;
   const int64_t p0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, npair - p0);
-  for (int w = threadIdx.x; w < nl * n2; w += blockDim.x) {
-    const int l = w / n2, i = w - l * n2;
-    const int64_t r0 = 2 * (p0 + l);
-    A[l * ln + pidx(i)] =
-        make_float4(mesh[r0 * n2 + i], 0.f, mesh[(r0 + 1) * n2 + i], 0.f);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  if (threadIdx.x < 2 * nl) {
+    const int64_t r = 2 * p0 + threadIdx.x;  // row = x n1 + y
+    const int64_t x = r / g.n[1], y = r - x * g.n[1];
+    obase[threadIdx.x] = x * (Kz + 1) * g.n[1] + y;
   }
-  ff_fft_lines(A, nl, ln, P, -1);
-  for (int w = threadIdx.x; w < nl * (Kz + 1); w += blockDim.x) {
-    const int l = w / (Kz + 1), kz = w - l * (Kz + 1);
-    const FFC z = ffc_load(A + l * ln + pidx(kz));
+  for (int l = warp; l < nl; l += nw) {
+    const float* row = mesh + 2 * (p0 + l) * n2;
+    for (int i = lane; i < n2; i += 32)
+      A[l * ls + pidx(i)] = make_float4(row[i], 0.f, row[n2 + i], 0.f);
+  }
+  ff_fft_lines<-1, MASK>(A, nl, ls, P, tw);
+  const int sh = lines_shift(2 * nl);
+  for (int w = threadIdx.x; w < (Kz + 1) << sh; w += blockDim.x) {
+    const int t = w & ((1 << sh) - 1), kz = w >> sh;
+    if (t >= 2 * nl) continue;
+    const int l = t >> 1;
+    const FFC z = ffc_load(A + l * ls + pidx(kz));
     const FFC zm = ffc_conj(
-        ffc_load(A + l * ln + pidx(kz == 0 ? 0 : n2 - kz)));
-    const FFC x0 = ffc_scale2(ffc_add(z, zm), 0.5f);
-    const FFC x1 = ffc_scale2(ffc_muli(ffc_sub(z, zm), -1), 0.5f);
-    const int64_t r0 = 2 * (p0 + l);
-    for (int h = 0; h < 2; ++h) {
-      const int64_t r = r0 + h;
-      const int x = int(r / g.n[1]), y = int(r - int64_t(x) * g.n[1]);
-      T1[(int64_t(x) * (Kz + 1) + kz) * g.n[1] + y] = ffc_pack(h ? x1 : x0);
-    }
+        ffc_load(A + l * ls + pidx(kz == 0 ? 0 : n2 - kz)));
+    // rows 2l and 2l + 1: (Z(k) + conj Z(-k)) / 2 and (Z(k) - conj Z(-k)) / 2i
+    const FFC v = (t & 1) ? ffc_scale2(ffc_muli(ffc_sub(z, zm), -1), 0.5f)
+                          : ffc_scale2(ffc_add(z, zm), 0.5f);
+    T1[obase[t] + int64_t(kz) * g.n[1]] = ffc_pack(v);
   }
 }
 
-// y lines (x, kz) of T1; keeps sy in [-Ky, Ky] into T2[sy + Ky][kz][x].
+// y lines of T1, ordered kz * n0 + x; keeps sy in [-Ky, Ky] into
+// T2[sy + Ky][kz][x].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
-ff_fwd_y_kernel(Geom g, const float4* T1, FFPlan P, int LB, int Ky, int Kz,
-                float4* T2) {
+ff_fwd_y_kernel(Geom g, const float4* T1, __grid_constant__ const FFPlan P,
+                int LB, int Ky, int Kz, float4* T2) {
   extern __shared__ float4 smem[];
-  const int n1 = g.n[1], ln = padded_len(n1);
+  __shared__ int64_t ibase[kMaxLines], obase[kMaxLines];
+  const int n1 = g.n[1], ls = line_stride(n1);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int64_t nlines = int64_t(g.n[0]) * (Kz + 1);
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
-  for (int w = threadIdx.x; w < nl * n1; w += blockDim.x) {
-    const int l = w / n1, i = w - l * n1;
-    A[l * ln + pidx(i)] = T1[l0 * n1 + w];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  if (threadIdx.x < nl) {
+    const int64_t line = l0 + threadIdx.x;
+    const int64_t kz = line / g.n[0], x = line - kz * g.n[0];
+    ibase[threadIdx.x] = (x * (Kz + 1) + kz) * n1;
+    obase[threadIdx.x] = line;  // kz * n0 + x
   }
-  ff_fft_lines(A, nl, ln, P, -1);
-  const int ny = 2 * Ky + 1;
-  for (int w = threadIdx.x; w < nl * ny; w += blockDim.x) {
-    const int l = w / ny, b = w - l * ny;
-    const int64_t line = l0 + l;
-    const int x = int(line / (Kz + 1)), kz = int(line - int64_t(x) * (Kz + 1));
-    T2[(int64_t(b) * (Kz + 1) + kz) * g.n[0] + x] =
-        A[l * ln + pidx(wrapi(b - Ky, n1))];
+  __syncthreads();
+  for (int l = warp; l < nl; l += nw) {
+    const float4* src = T1 + ibase[l];
+    for (int i = lane; i < n1; i += 32) A[l * ls + pidx(i)] = src[i];
+  }
+  ff_fft_lines<-1, MASK>(A, nl, ls, P, tw);
+  const int sh = lines_shift(nl);
+  const int64_t plane = int64_t(Kz + 1) * g.n[0];
+  for (int w = threadIdx.x; w < (2 * Ky + 1) << sh; w += blockDim.x) {
+    const int l = w & ((1 << sh) - 1), b = w >> sh;
+    if (l >= nl) continue;
+    T2[obase[l] + b * plane] = A[l * ls + pidx(wrapi(b - Ky, n1))];
   }
 }
 
 // x lines (sy, kz) of T2; keeps sx in [-Kx, Kx] into
 // cube[sx + Kx][sy + Ky][kz].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
-ff_fwd_x_kernel(Geom g, const float4* T2, FFPlan P, int LB, int Kx, int Ky,
-                int Kz, float4* cube) {
+ff_fwd_x_kernel(Geom g, const float4* T2, __grid_constant__ const FFPlan P,
+                int LB, int Kx, int Ky, int Kz, float4* cube) {
   extern __shared__ float4 smem[];
-  const int n0 = g.n[0], ln = padded_len(n0);
+  const int n0 = g.n[0], ls = line_stride(n0);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int64_t nlines = int64_t(2 * Ky + 1) * (Kz + 1);
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
-  for (int w = threadIdx.x; w < nl * n0; w += blockDim.x) {
-    const int l = w / n0, i = w - l * n0;
-    A[l * ln + pidx(i)] = T2[l0 * n0 + w];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int l = warp; l < nl; l += nw) {
+    const float4* src = T2 + (l0 + l) * n0;
+    for (int i = lane; i < n0; i += 32) A[l * ls + pidx(i)] = src[i];
   }
-  ff_fft_lines(A, nl, ln, P, -1);
-  const int nx = 2 * Kx + 1;
-  for (int w = threadIdx.x; w < nl * nx; w += blockDim.x) {
-    const int l = w / nx, a = w - l * nx;
-    const int64_t line = l0 + l;  // = b * (Kz + 1) + kz
-    const int b = int(line / (Kz + 1)), kz = int(line - int64_t(b) * (Kz + 1));
-    cube[(int64_t(a) * (2 * Ky + 1) + b) * (Kz + 1) + kz] =
-        A[l * ln + pidx(wrapi(a - Kx, n0))];
+  ff_fft_lines<-1, MASK>(A, nl, ls, P, tw);
+  const int sh = lines_shift(nl);
+  for (int w = threadIdx.x; w < (2 * Kx + 1) << sh; w += blockDim.x) {
+    const int l = w & ((1 << sh) - 1), a = w >> sh;
+    if (l >= nl) continue;
+    // line = (sy + Ky) (Kz + 1) + kz
+    cube[int64_t(a) * nlines + l0 + l] = A[l * ls + pidx(wrapi(a - Kx, n0))];
   }
 }
 
@@ -368,102 +543,137 @@ __global__ void ff_build_F_kernel(Geom g, FFBuild bd, int M2, const float4* cube
 // nf fields, each with planes c in [0, Kcf] and band |sx|, |sy| <= Kf.
 
 // x lines (f, c, b in band) of E[f][c][b][a]; writes Y1[f][c][a][b].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_x_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* E,
-                FFPlan P, int LB, float4* Y1) {
+                __grid_constant__ const FFPlan P, int LB, float4* Y1) {
   extern __shared__ float4 smem[];
-  const int ln = padded_len(M0);
+  __shared__ int64_t ibase[kMaxLines], obase[kMaxLines];
+  const int ls = line_stride(M0);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int nb = 2 * Kf + 1;
   const int64_t nlines = int64_t(nf) * (Kcf + 1) * nb;
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
-  for (int w = threadIdx.x; w < nl * M0; w += blockDim.x) {
-    const int l = w / M0, a = w - l * M0;
-    const int64_t line = l0 + l;
-    const int bb = int(line % nb);
-    const int64_t fc = line / nb;  // f * (Kcf + 1) + c
-    const int b = wrapi(bb - Kf, M1);
-    A[l * ln + pidx(a)] = E[(fc * M1 + b) * M0 + a];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  if (threadIdx.x < nl) {
+    const int64_t line = l0 + threadIdx.x;
+    const int64_t fc = line / nb;  // f (Kcf + 1) + c
+    const int b = wrapi(int(line - fc * nb) - Kf, M1);
+    ibase[threadIdx.x] = (fc * M1 + b) * M0;
+    obase[threadIdx.x] = fc * M0 * M1 + b;
   }
-  ff_fft_lines(A, nl, ln, P, +1);
-  for (int w = threadIdx.x; w < nl * M0; w += blockDim.x) {
-    const int l = w / M0, a = w - l * M0;
-    const int64_t line = l0 + l;
-    const int bb = int(line % nb);
-    const int64_t fc = line / nb;
-    const int b = wrapi(bb - Kf, M1);
-    Y1[(fc * M0 + a) * M1 + b] = A[l * ln + pidx(a)];
+  __syncthreads();
+  for (int l = warp; l < nl; l += nw) {
+    const float4* src = E + ibase[l];
+    for (int a = lane; a < M0; a += 32) A[l * ls + pidx(a)] = src[a];
+  }
+  ff_fft_lines<+1, MASK>(A, nl, ls, P, tw);
+  const int sh = lines_shift(nl);
+  for (int w = threadIdx.x; w < M0 << sh; w += blockDim.x) {
+    const int l = w & ((1 << sh) - 1), a = w >> sh;
+    if (l >= nl) continue;
+    Y1[obase[l] + int64_t(a) * M1] = A[l * ls + pidx(a)];
   }
 }
 
-// y lines (f, c, a) of Y1 (entries outside the band are zero); writes
-// Y2[f][a][b][c].
+// y lines of Y1 (entries outside the band are zero), ordered
+// (f M0 + a) (Kcf + 1) + c; writes Y2[f][a][b][c].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_y_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* Y1,
-                FFPlan P, int LB, float4* Y2) {
+                __grid_constant__ const FFPlan P, int LB, float4* Y2) {
   extern __shared__ float4 smem[];
-  const int ln = padded_len(M1);
+  __shared__ int64_t ibase[kMaxLines], obase[kMaxLines];
+  const int ls = line_stride(M1);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int64_t nlines = int64_t(nf) * (Kcf + 1) * M0;
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
-  for (int w = threadIdx.x; w < nl * M1; w += blockDim.x) {
-    const int l = w / M1, b = w - l * M1;
-    const int sb = sym_shift(b, M1);
-    A[l * ln + pidx(b)] =
-        (abs(sb) <= Kf) ? Y1[(l0 + l) * M1 + b] : make_float4(0, 0, 0, 0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  if (threadIdx.x < nl) {
+    const int64_t line = l0 + threadIdx.x;
+    const int64_t fa = line / (Kcf + 1);
+    const int64_t c = line - fa * (Kcf + 1);
+    const int64_t f = fa / M0, a = fa - f * M0;
+    ibase[threadIdx.x] = ((f * (Kcf + 1) + c) * M0 + a) * M1;
+    obase[threadIdx.x] = fa * M1 * (Kcf + 1) + c;
   }
-  ff_fft_lines(A, nl, ln, P, +1);
-  for (int w = threadIdx.x; w < nl * M1; w += blockDim.x) {
-    const int l = w / M1, b = w - l * M1;
-    const int64_t line = l0 + l;  // (f * (Kcf + 1) + c) * M0 + a
-    const int a = int(line % M0);
-    const int64_t fc = line / M0;
-    const int c = int(fc % (Kcf + 1));
-    const int64_t f = fc / (Kcf + 1);
-    Y2[((f * M0 + a) * M1 + b) * (Kcf + 1) + c] = A[l * ln + pidx(b)];
+  __syncthreads();
+  for (int l = warp; l < nl; l += nw) {
+    const float4* src = Y1 + ibase[l];
+    for (int b = lane; b < M1; b += 32)
+      A[l * ls + pidx(b)] = (abs(sym_shift(b, M1)) <= Kf)
+                                ? src[b]
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  ff_fft_lines<+1, MASK>(A, nl, ls, P, tw);
+  const int sh = lines_shift(nl);
+  for (int w = threadIdx.x; w < M1 << sh; w += blockDim.x) {
+    const int l = w & ((1 << sh) - 1), b = w >> sh;
+    if (l >= nl) continue;
+    Y2[obase[l] + int64_t(b) * (Kcf + 1)] = A[l * ls + pidx(b)];
   }
 }
 
 // C2R along z of the half lines Y2[f][a][b][0..Kcf] (zero above), two
 // lines per complex transform; writes the real fields out[f][a][b][z].
+template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
-                FFPlan P, int LB, float* out, float* out_lo) {
+                __grid_constant__ const FFPlan P, int LB, float* out,
+                float* out_lo) {
   extern __shared__ float4 smem[];
-  const int ln = padded_len(M2);
+  const int ls = line_stride(M2);
   float4* A = smem;
+  const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int64_t nlines = int64_t(nf) * M0 * M1;
   const int64_t npair = (nlines + 1) / 2;
   const int64_t p0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, npair - p0);
-  auto half = [&](int64_t line, int k) -> FFC {
-    // Hermitian extension of the half line.
-    if (line >= nlines) return ffc_zero();
-    const int kk = (k <= M2 / 2) ? k : M2 - k;
-    if (kk > Kcf) return ffc_zero();
-    const FFC v = ffc_load(Y2 + line * (Kcf + 1) + kk);
-    return (k <= M2 / 2) ? v : ffc_conj(v);
-  };
-  for (int w = threadIdx.x; w < nl * M2; w += blockDim.x) {
-    const int l = w / M2, k = w - l * M2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int l = warp; l < nl; l += nw) {
     const int64_t line0 = 2 * (p0 + l);
-    const FFC h1 = half(line0, k), h2 = half(line0 + 1, k);
-    // Z = H1 + i H2
-    A[l * ln + pidx(k)] =
-        ffc_pack(FFC{ffsub(h1.re, h2.im), ffadd(h1.im, h2.re)});
+    const bool two = line0 + 1 < nlines;
+    const float4* h1 = Y2 + line0 * (Kcf + 1);
+    const float4* h2 = h1 + (Kcf + 1);
+    for (int k = lane; k < M2; k += 32) {
+      // Hermitian extension of the half lines; Z = H1 + i H2.
+      const bool up = k <= M2 / 2;
+      const int kk = up ? k : M2 - k;
+      FFC a = ffc_zero(), b = ffc_zero();
+      if (kk <= Kcf) {
+        a = ffc_load(h1 + kk);
+        if (two) b = ffc_load(h2 + kk);
+        if (!up) {
+          a = ffc_conj(a);
+          b = ffc_conj(b);
+        }
+      }
+      A[l * ls + pidx(k)] =
+          ffc_pack(FFC{ffsub(a.re, b.im), ffadd(a.im, b.re)});
+    }
   }
-  ff_fft_lines(A, nl, ln, P, +1);
-  for (int w = threadIdx.x; w < nl * M2; w += blockDim.x) {
-    const int l = w / M2, z = w - l * M2;
+  ff_fft_lines<+1, MASK>(A, nl, ls, P, tw);
+  for (int l = warp; l < nl; l += nw) {
     const int64_t line0 = 2 * (p0 + l);
-    const float4 v = A[l * ln + pidx(z)];
-    out[line0 * M2 + z] = v.x;
-    out_lo[line0 * M2 + z] = v.y;
-    if (line0 + 1 < nlines) {
-      out[(line0 + 1) * M2 + z] = v.z;
-      out_lo[(line0 + 1) * M2 + z] = v.w;
+    const bool two = line0 + 1 < nlines;
+    float* o = out + line0 * M2;
+    float* ol = out_lo + line0 * M2;
+    for (int z = lane; z < M2; z += 32) {
+      const float4 v = A[l * ls + pidx(z)];
+      const FF re = ffnorm(FF{v.x, v.y}), im = ffnorm(FF{v.z, v.w});
+      o[z] = re.hi;
+      ol[z] = re.lo;
+      if (two) {
+        o[M2 + z] = im.hi;
+        ol[M2 + z] = im.lo;
+      }
     }
   }
 }
@@ -471,7 +681,8 @@ ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
 // Lines per block: every butterfly of a stage must fit the registers the
 // stage keeps per thread (StageItems, 256 threads).
 int lines_per_block(const FFPlan& P) {
-  int lb = 16;
+  if (P.warp_lines) return 8;  // one line per warp of the 256 threads
+  int lb = kMaxLines;
   for (int s = 0; s < P.nstage; ++s) {
     const int R = P.radix[s];
     const int items = (R == 8 || R == 5) ? 1 : 2;
@@ -481,7 +692,7 @@ int lines_per_block(const FFPlan& P) {
 }
 
 size_t smem_bytes(int n, int lb) {
-  return size_t(lb) * padded_len(n) * sizeof(float4);
+  return (size_t(lb) * line_stride(n) + n) * sizeof(float4);
 }
 
 // Opt in to more than 48 KB of dynamic shared memory (per launch: the
@@ -515,6 +726,22 @@ FFPlan ff_plan(Context& ctx, int n) {
   if (m != 1 || P.nstage > 16)
     throw_error(TRVG_ERR_INVALID_PARAMETER,
                 "Float-float transform length %d unsupported.", n);
+  auto magic = [](int dv) {
+    return dv <= 1 ? 0u : unsigned((uint64_t(1) << 32) / uint64_t(dv) + 1);
+  };
+  for (int s = 0, ns = 1; s < P.nstage; ns *= P.radix[s], ++s) {
+    P.nb[s] = n / P.radix[s];
+    P.ns[s] = ns;
+    P.tstep[s] = n / (ns * P.radix[s]);
+    P.mnb[s] = magic(P.nb[s]);
+    P.mns[s] = magic(ns);
+  }
+  P.warp_lines = true;
+  for (int s = 0; s < P.nstage; ++s) {
+    const int R = P.radix[s];
+    const int items = (R == 8 || R == 5) ? 1 : (R == 2 ? 3 : 2);  // WarpItems
+    if (P.nb[s] > 32 * items) P.warp_lines = false;
+  }
   const std::string name = "fftw." + std::to_string(n);
   auto it = ctx.buffers.find(name);
   if (it != ctx.buffers.end() && it->second.bytes >= size_t(n) * sizeof(float4)) {
@@ -536,38 +763,77 @@ FFPlan ff_plan(Context& ctx, int n) {
   return P;
 }
 
+namespace {
+
+int radix_mask(const FFPlan& P) {
+  int m = 0;
+  for (int s = 0; s < P.nstage; ++s)
+    switch (P.radix[s]) {
+      case 8: m |= kRadix8; break;
+      case 4: m |= kRadix4; break;
+      case 2: m |= kRadix2; break;
+      case 3: m |= kRadix3; break;
+      default: m |= kRadix5; break;
+    }
+  return m;
+}
+
+template <int M>
+using RadixSet = std::integral_constant<int, M>;
+
+// Calls f with the specialised radix set that holds all radices of P:
+// powers of two for the mesh passes, {3, 5} and {2, 3} for the usual
+// evaluation grids, the generic kernels otherwise.
+template <class F>
+void with_radix_set(const FFPlan& P, F&& f) {
+  const int m = radix_mask(P);
+  if ((m & ~kRadix8) == 0) f(RadixSet<kRadix8>{});
+  else if ((m & ~(kRadix8 | kRadix4)) == 0) f(RadixSet<kRadix8 | kRadix4>{});
+  else if ((m & ~(kRadix3 | kRadix5)) == 0) f(RadixSet<kRadix3 | kRadix5>{});
+  else if ((m & ~(kRadix2 | kRadix3)) == 0) f(RadixSet<kRadix2 | kRadix3>{});
+  else f(RadixSet<kRadixAll>{});
+}
+
+}  // namespace
+
 void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
                             int Kg, float4* T1, float4* T2, float4* cube) {
   const FFPlan Pz = ff_plan(ctx, g.n[2]);
   const FFPlan Py = ff_plan(ctx, g.n[1]);
   const FFPlan Px = ff_plan(ctx, g.n[0]);
-  {
+  with_radix_set(Pz, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Pz);
     const int64_t npair = int64_t(g.n[0]) * g.n[1] / 2;
-    allow_smem(ff_fwd_z_kernel);
+    allow_smem(ff_fwd_z_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_forward_kernel");
-    ff_fwd_z_kernel<<<int((npair + lb - 1) / lb), 256, smem_bytes(g.n[2], lb),
-                      ctx.stream>>>(g, mesh, Pz, lb, Kg, T1);
+    ff_fwd_z_kernel<MASK><<<int((npair + lb - 1) / lb), 256,
+                            smem_bytes(g.n[2], lb), ctx.stream>>>(
+        g, mesh, Pz, lb, Kg, T1);
     TRVG_LAUNCHED(ctx);
-  }
-  {
+  });
+  with_radix_set(Py, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(g.n[0]) * (Kg + 1);
-    allow_smem(ff_fwd_y_kernel);
+    allow_smem(ff_fwd_y_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_forward_kernel");
-    ff_fwd_y_kernel<<<int((nl + lb - 1) / lb), 256, smem_bytes(g.n[1], lb),
-                      ctx.stream>>>(g, T1, Py, lb, Kg, Kg, T2);
+    ff_fwd_y_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
+                            smem_bytes(g.n[1], lb), ctx.stream>>>(
+        g, T1, Py, lb, Kg, Kg, T2);
     TRVG_LAUNCHED(ctx);
-  }
-  {
+  });
+  with_radix_set(Px, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(2 * Kg + 1) * (Kg + 1);
-    allow_smem(ff_fwd_x_kernel);
+    allow_smem(ff_fwd_x_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_forward_kernel");
-    ff_fwd_x_kernel<<<int((nl + lb - 1) / lb), 256, smem_bytes(g.n[0], lb),
-                      ctx.stream>>>(g, T2, Px, lb, Kg, Kg, Kg, cube);
+    ff_fwd_x_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
+                            smem_bytes(g.n[0], lb), ctx.stream>>>(
+        g, T2, Px, lb, Kg, Kg, Kg, cube);
     TRVG_LAUNCHED(ctx);
-  }
+  });
 }
 
 void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
@@ -606,34 +872,39 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
   const FFPlan Px = ff_plan(ctx, M[0]);
   const FFPlan Py = ff_plan(ctx, M[1]);
   const FFPlan Pz = ff_plan(ctx, M[2]);
-  {
+  with_radix_set(Px, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * (2 * Kf + 1);
-    allow_smem(ff_inv_x_kernel);
+    allow_smem(ff_inv_x_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_inverse_kernel");
-    ff_inv_x_kernel<<<int((nl + lb - 1) / lb), 256, smem_bytes(M[0], lb),
-                      ctx.stream>>>(M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1);
+    ff_inv_x_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
+                            smem_bytes(M[0], lb), ctx.stream>>>(
+        M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1);
     TRVG_LAUNCHED(ctx);
-  }
-  {
+  });
+  with_radix_set(Py, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * M[0];
-    allow_smem(ff_inv_y_kernel);
+    allow_smem(ff_inv_y_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_inverse_kernel");
-    ff_inv_y_kernel<<<int((nl + lb - 1) / lb), 256, smem_bytes(M[1], lb),
-                      ctx.stream>>>(M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2);
+    ff_inv_y_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
+                            smem_bytes(M[1], lb), ctx.stream>>>(
+        M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2);
     TRVG_LAUNCHED(ctx);
-  }
-  {
+  });
+  with_radix_set(Pz, [&](auto set) {
+    constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Pz);
     const int64_t np = (int64_t(nf) * M[0] * M[1] + 1) / 2;
-    allow_smem(ff_inv_z_kernel);
+    allow_smem(ff_inv_z_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_inverse_kernel");
-    ff_inv_z_kernel<<<int((np + lb - 1) / lb), 256, smem_bytes(M[2], lb),
-                      ctx.stream>>>(M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb,
-                                    out, out_lo);
+    ff_inv_z_kernel<MASK><<<int((np + lb - 1) / lb), 256,
+                            smem_bytes(M[2], lb), ctx.stream>>>(
+        M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb, out, out_lo);
     TRVG_LAUNCHED(ctx);
-  }
+  });
 }
 
 }  // namespace trvg

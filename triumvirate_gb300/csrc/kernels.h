@@ -242,6 +242,14 @@ struct FFPlan {
   int n;
   int nstage;
   int radix[16];
+  // Per stage: butterflies per line (n / radix), span of the finished
+  // sub-transforms (Ns), twiddle stride n / (Ns radix), and the multipliers
+  // floor(2^32 / d) + 1 that divide by n / radix and Ns exactly through a
+  // multiply-high (valid for dividends below 2^32 / d).
+  int nb[16], ns[16], tstep[16];
+  unsigned mnb[16], mns[16];
+  // Every stage fits one warp per line (WarpItems butterflies per lane).
+  bool warp_lines;
   const float4* tw;
 };
 bool ff_length_ok(int n);
