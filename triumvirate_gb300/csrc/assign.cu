@@ -112,13 +112,42 @@ __device__ __forceinline__ void fill_stencil_f(int idx, float s, int n,
 // main one: loc + 1/2 stays in cell idx when s < 1/2 and moves to the next
 // cell (wrapping to 0 past the last, as the library's loc -= n does)
 // otherwise.
+// Cell index (the truncation of loc) and the leading 24 bits of the
+// fraction of loc >= 0, read from the bits of the double with integer
+// operations (GB300 converts FP64 on its slow FP64 pipe).  idx is -1 for
+// negative offsets and INT_MAX at or above 2^30; both fail the range test.
+__device__ __forceinline__ void split_offset(double loc, int& idx, float& s) {
+  const long long bits = __double_as_longlong(loc);
+  const int e = int((bits >> 52) & 0x7ff) - 1023;
+  if (bits < 0) {
+    idx = -1;
+    s = 0.f;
+  } else if (e < 0) {  // 0 <= loc < 1 (zero and subnormals included)
+    idx = 0;
+    s = float(loc);
+  } else if (e >= 30) {
+    idx = 0x7fffffff;
+    s = 0.f;
+  } else {
+    const unsigned long long m =
+        (static_cast<unsigned long long>(bits) & ((1ull << 52) - 1)) |
+        (1ull << 52);
+    const int sh = 52 - e;  // fraction bits, 23..52
+    idx = int(m >> sh);
+    const unsigned long long f = m & ((1ull << sh) - 1);
+    s = sh > 24 ? float(unsigned(f >> (sh - 24))) * 0x1p-24f
+                : ldexpf(float(unsigned(f)), -sh);
+  }
+}
+
 template <int ORDER>
 __device__ __forceinline__ bool axis_stencil_f(double pos, int n, double ratio,
                                                StencilF<ORDER>& main,
                                                StencilF<ORDER>* shadow) {
   const double loc = pos * ratio;
-  const int idx = int(loc);
-  const float s = float(loc - double(idx));
+  int idx;
+  float s;
+  split_offset(loc, idx, s);
   if (idx < 0 || idx >= n || !(s >= kTieMargin) || s > 1.f - kTieMargin ||
       fabsf(s - 0.5f) < kTieMargin)
     return false;
@@ -284,6 +313,9 @@ __global__ void __launch_bounds__(256)
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
   cd acc = {0., 0.}, acc_s = {0., 0.};
+  // Equal weights: fully landed particles are counted, not summed in FP64.
+  const bool uniform = a.cat.w == nullptr && !a.ws.use_ylm;
+  long long nland = 0;
   for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        p < a.cat.n; p += int64_t(gridDim.x) * blockDim.x) {
     const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
@@ -309,12 +341,16 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
         // landed weight is the weight itself.
         deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), re);
         if (im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), im);
-        acc = acc + wgt;
         if constexpr (SH) {
           deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), sre);
           if (sim != nullptr)
             deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), sim);
-          acc_s = acc_s + wgt;
+        }
+        if (uniform) {
+          ++nland;
+        } else {
+          acc = acc + wgt;
+          if constexpr (SH) acc_s = acc_s + wgt;
         }
         continue;
       }
@@ -330,6 +366,11 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
         acc_s = acc_s + ls;
       }
     }
+  }
+  if (uniform && nland > 0) {
+    const double land = double(nland) * a.ws.scale;
+    acc.re += land;
+    if constexpr (SH) acc_s.re += land;
   }
   // Block-wide FP64 sums of the deposited weight (k = 0 modes).
   __shared__ double red[4][8];

@@ -172,6 +172,10 @@ struct SplineTable {
   int n;
   int ell;
   double split;
+  // FP32 copy for the FP32-mixed kernels: per interval (y hi, y lo, b, c)
+  // and d (null when not uploaded).
+  const float4* q = nullptr;
+  const float* dq = nullptr;
 };
 
 constexpr double kSplineStep = 0.05;

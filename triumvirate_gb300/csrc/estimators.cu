@@ -846,7 +846,17 @@ struct Engine {
     const double* b = upload(tag + ".b", s.b);
     const double* c = upload(tag + ".c", s.c);
     const double* d = upload(tag + ".d", s.d);
-    const SplineTable t = s.table(y, b, c, d);
+    SplineTable t = s.table(y, b, c, d);
+    vector<float4> q(s.y.size());
+    vector<float> dq(s.y.size());
+    for (size_t i = 0; i < s.y.size(); ++i) {
+      const float yh = float(s.y[i]);
+      q[i] = make_float4(yh, float(s.y[i] - double(yh)), float(s.b[i]),
+                         float(s.c[i]));
+      dq[i] = float(s.d[i]);
+    }
+    t.q = upload(tag + ".q", q);
+    t.dq = upload(tag + ".dq", dq);
     ctx.splines[ell] = t;
     return t;
   }
@@ -881,7 +891,7 @@ struct Engine {
                                   static_cast<const float*>(xi.im), la, ma, lb,
                                   mb, hist);
       launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
-                              out);
+                              !xi.dbl, out);
     } else {
       if (xi.dbl)
         launch_pair_bessel_direct<double>(
@@ -1178,9 +1188,10 @@ struct Engine {
 
     float4* EG = ctx.buf<float4>("ff.EG", plane_g);
     launch_ff_build_G(ctx, g, M, cube, kg, inv_win_ff, src.k0, EG);
-    float* G = ctx.buf<float>("ff.G", size_t(Mc));
-    float* Gl = ctx.buf<float>("ff.G.lo", size_t(Mc));
-    launch_ff_inverse(ctx, M, 1, kg, kg, EG, Y1, Y2, G, Gl);
+    const int64_t ld = ff_field_stride(Mc);
+    float* G = ctx.buf<float>("ff.G", size_t(ld));
+    float* Gl = ctx.buf<float>("ff.G.lo", size_t(ld));
+    launch_ff_inverse(ctx, M, 1, kg, kg, EG, Y1, Y2, G, Gl, ld);
 
     // Float-float fields of one leg: hi words, lo words after nb * Mc.
     auto leg_fields = [&](const Leg& leg, const vector<int>& bins,
@@ -1199,15 +1210,15 @@ struct Engine {
       float4* E = ctx.buf<float4>(tag + ".E", size_t(nb) * plane_f);
       launch_ff_build_F(ctx, g, M, cube, kg, k, tab, nb, leg.ell, inv_win_ff,
                         src.k0, E);
-      float* out = ctx.buf<float>(tag + ".F", 2 * size_t(nb) * Mc);
+      float* out = ctx.buf<float>(tag + ".F", 2 * size_t(nb) * ld);
       launch_ff_inverse(ctx, M, nb, k, k, E, Y1, Y2, out,
-                        out + size_t(nb) * Mc);
+                        out + size_t(nb) * ld, ld);
       return out;
     };
     const float* FA = leg_fields(la, A, "ffA");
     const float* FB = shared ? FA : leg_fields(lb, B, "ffB");
-    const float* FAl = FA + A.size() * size_t(Mc);
-    const float* FBl = FB + B.size() * size_t(Mc);
+    const float* FAl = FA + A.size() * size_t(ld);
+    const float* FBl = FB + B.size() * size_t(ld);
 
     vector<int> pa(np), pb(np);
     for (int i = 0; i < np; ++i) {
@@ -1220,7 +1231,7 @@ struct Engine {
     const int* dpb = upload("pairs.b", pb);
     double* dout = ctx.buf<double>("pairs.out", 2 * size_t(np));
     zero(dout, 2 * np * sizeof(double));
-    launch_reduce_pairs_ff(ctx, Mc, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
+    launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
                            dout);
     const vector<double> h = download(dout, 2 * size_t(np));
     vector<cplx> res(np);

@@ -626,7 +626,7 @@ template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
                 __grid_constant__ const FFPlan P, int LB, float* out,
-                float* out_lo) {
+                float* out_lo, int64_t ld) {
   extern __shared__ float4 smem[];
   const int ls = line_stride(M2);
   float4* A = smem;
@@ -660,19 +660,23 @@ ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
     }
   }
   ff_fft_lines<+1, MASK>(A, nl, ls, P, tw);
+  const int64_t plane = int64_t(M0) * M1;  // lines per field
+  auto offset = [&](int64_t line) {
+    const int64_t f = line / plane;
+    return f * ld + (line - f * plane) * M2;
+  };
   for (int l = warp; l < nl; l += nw) {
     const int64_t line0 = 2 * (p0 + l);
     const bool two = line0 + 1 < nlines;
-    float* o = out + line0 * M2;
-    float* ol = out_lo + line0 * M2;
+    const int64_t o0 = offset(line0), o1 = two ? offset(line0 + 1) : 0;
     for (int z = lane; z < M2; z += 32) {
       const float4 v = A[l * ls + pidx(z)];
       const FF re = ffnorm(FF{v.x, v.y}), im = ffnorm(FF{v.z, v.w});
-      o[z] = re.hi;
-      ol[z] = re.lo;
+      out[o0 + z] = re.hi;
+      out_lo[o0 + z] = re.lo;
       if (two) {
-        o[M2 + z] = im.hi;
-        ol[M2 + z] = im.lo;
+        out[o1 + z] = im.hi;
+        out_lo[o1 + z] = im.lo;
       }
     }
   }
@@ -806,7 +810,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
     const int lb = lines_per_block(Pz);
     const int64_t npair = int64_t(g.n[0]) * g.n[1] / 2;
     allow_smem(ff_fwd_z_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_forward_kernel");
+    TRVG_KBEGIN(ctx, "ff_fwd_z_kernel");
     ff_fwd_z_kernel<MASK><<<int((npair + lb - 1) / lb), 256,
                             smem_bytes(g.n[2], lb), ctx.stream>>>(
         g, mesh, Pz, lb, Kg, T1);
@@ -817,7 +821,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(g.n[0]) * (Kg + 1);
     allow_smem(ff_fwd_y_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_forward_kernel");
+    TRVG_KBEGIN(ctx, "ff_fwd_y_kernel");
     ff_fwd_y_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(g.n[1], lb), ctx.stream>>>(
         g, T1, Py, lb, Kg, Kg, T2);
@@ -828,7 +832,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(2 * Kg + 1) * (Kg + 1);
     allow_smem(ff_fwd_x_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_forward_kernel");
+    TRVG_KBEGIN(ctx, "ff_fwd_x_kernel");
     ff_fwd_x_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(g.n[0], lb), ctx.stream>>>(
         g, T2, Px, lb, Kg, Kg, Kg, cube);
@@ -868,7 +872,7 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
 
 void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
                        const float4* E, float4* Y1, float4* Y2, float* out,
-                       float* out_lo) {
+                       float* out_lo, int64_t ld) {
   const FFPlan Px = ff_plan(ctx, M[0]);
   const FFPlan Py = ff_plan(ctx, M[1]);
   const FFPlan Pz = ff_plan(ctx, M[2]);
@@ -877,7 +881,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * (2 * Kf + 1);
     allow_smem(ff_inv_x_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_inverse_kernel");
+    TRVG_KBEGIN(ctx, "ff_inv_x_kernel");
     ff_inv_x_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(M[0], lb), ctx.stream>>>(
         M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1);
@@ -888,7 +892,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * M[0];
     allow_smem(ff_inv_y_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_inverse_kernel");
+    TRVG_KBEGIN(ctx, "ff_inv_y_kernel");
     ff_inv_y_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(M[1], lb), ctx.stream>>>(
         M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2);
@@ -899,10 +903,10 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
     const int lb = lines_per_block(Pz);
     const int64_t np = (int64_t(nf) * M[0] * M[1] + 1) / 2;
     allow_smem(ff_inv_z_kernel<MASK>);
-    TRVG_KBEGIN(ctx, "ff_inverse_kernel");
+    TRVG_KBEGIN(ctx, "ff_inv_z_kernel");
     ff_inv_z_kernel<MASK><<<int((np + lb - 1) / lb), 256,
                             smem_bytes(M[2], lb), ctx.stream>>>(
-        M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb, out, out_lo);
+        M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb, out, out_lo, ld);
     TRVG_LAUNCHED(ctx);
   });
 }

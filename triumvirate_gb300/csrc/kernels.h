@@ -269,18 +269,22 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                        int nq, int ell, const float2* const iw[3], cd k0,
                        float4* E);
 // Real fields on the M grid of nf half spectra E with planes c <= Kcf and
-// band |sx|, |sy| <= Kf, as float-float words out[f][a][b][z] (hi) and
-// out_lo (Y1, Y2: scratch of nf (Kcf+1) M0 M1 float4 each).
+// band |sx|, |sy| <= Kf, as float-float words: field f at out + f ld (hi)
+// and out_lo + f ld, cells [a][b][z] (Y1, Y2: scratch of
+// nf (Kcf+1) M0 M1 float4 each).
 void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
                        const float4* E, float4* Y1, float4* Y2, float* out,
-                       float* out_lo);
-// sum_x F_a F_b G of float-float fields (hi, lo words) for every pair
-// (real parts at out[2 p]).
-void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, const float* Gh,
-                            const float* Gl, const float* Fah,
-                            const float* Fal, const float* Fbh,
-                            const float* Fbl, const int* pa, const int* pb,
-                            int npairs, double* out);
+                       float* out_lo, int64_t ld);
+// Field stride of the reductions: cells rounded up to whole float4 quads.
+inline int64_t ff_field_stride(int64_t ncell) { return (ncell + 3) / 4 * 4; }
+// sum_x F_a F_b G of float-float fields (hi, lo words; field q of a leg at
+// q ld, ld a multiple of 4, 16-byte aligned bases) for every pair (real
+// parts at out[2 p]).
+void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,
+                            const float* Gh, const float* Gl,
+                            const float* Fah, const float* Fal,
+                            const float* Fbh, const float* Fbl, const int* pa,
+                            const int* pb, int npairs, double* out);
 
 // ---- adjoint.cu ----------------------------------------------------------
 // Cotangent bookkeeping of the bispectrum adjoint: the partners of bin a in
@@ -318,10 +322,13 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
                         const Real* xi_im, int ell_a, int m_a, int ell_b,
                         int m_b, double* hist /* 2 * nkeys */);
 
+// With `ff` (and the tables' FP32 copies) the Bessel weights come from the
+// float-float evaluation on the FP32 pipe, else from the FP64 spline.
 void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* hist, const SplineTable& sja,
                              const SplineTable& sjb, const double* ka,
-                             const double* kb, int npairs, double* out);
+                             const double* kb, int npairs, bool ff,
+                             double* out);
 
 template <class Real>
 void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,

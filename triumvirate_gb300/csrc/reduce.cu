@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "ff.cuh"
 #include "kernels.h"
 
 namespace trvg {
@@ -221,34 +222,67 @@ __device__ __forceinline__ FF ff_prod3(float ah, float al, float bh, float bl,
   return FF{q, f};
 }
 
-// sum_x F_a F_b G of float-float fields (hi and lo word arrays).
+// sum_x F_a F_b G of float-float fields (hi and lo word arrays, field q at
+// q ld): four cells per float4 load, the cells past the last whole quad by
+// the first block; a pair whose legs are the same field loads it once.
+__device__ __forceinline__ void ff_quad(FF& acc, float4 ah, float4 al,
+                                        float4 bh, float4 bl, float4 gh,
+                                        float4 gl) {
+  ff_merge(acc, ff_prod3(ah.x, al.x, bh.x, bl.x, gh.x, gl.x));
+  ff_merge(acc, ff_prod3(ah.y, al.y, bh.y, bl.y, gh.y, gl.y));
+  ff_merge(acc, ff_prod3(ah.z, al.z, bh.z, bl.z, gh.z, gl.z));
+  ff_merge(acc, ff_prod3(ah.w, al.w, bh.w, bl.w, gh.w, gl.w));
+}
+
 __global__ void __launch_bounds__(256)
-reduce_pairs_ff_kernel(int64_t ncell, const float* Gh, const float* Gl,
-                       const float* Fah, const float* Fal, const float* Fbh,
-                       const float* Fbl, const int* pa, const int* pb,
-                       int npairs, double* out) {
+reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
+                       const float* __restrict__ Gh,
+                       const float* __restrict__ Gl,
+                       const float* __restrict__ Fah,
+                       const float* __restrict__ Fal,
+                       const float* __restrict__ Fbh,
+                       const float* __restrict__ Fbl, const int* pa,
+                       const int* pb, int npairs, double* out) {
   __shared__ double red[kPairChunk * 32];
   const int p0 = blockIdx.y * kPairChunk;
-  int ia[kPairChunk], ib[kPairChunk];
-  bool ok[kPairChunk];
+  int64_t oa[kPairChunk], ob[kPairChunk];
+  bool ok[kPairChunk], same[kPairChunk];
 #pragma unroll
   for (int q = 0; q < kPairChunk; ++q) {
     ok[q] = (p0 + q) < npairs;
-    ia[q] = ok[q] ? pa[p0 + q] : 0;
-    ib[q] = ok[q] ? pb[p0 + q] : 0;
+    oa[q] = ok[q] ? int64_t(pa[p0 + q]) * ld : 0;
+    ob[q] = ok[q] ? int64_t(pb[p0 + q]) * ld : 0;
+    same[q] = Fah == Fbh && oa[q] == ob[q];
   }
   Acc<float> acc[kPairChunk];
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < ncell;
+  const int64_t nquad = ncell / 4;
+  auto q4 = [](const float* p, int64_t off, int64_t t) {
+    return reinterpret_cast<const float4*>(p + off)[t];
+  };
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nquad;
        t += int64_t(gridDim.x) * blockDim.x) {
-    const float gh = Gh[t], gl = Gl[t];
+    const float4 gh = q4(Gh, 0, t), gl = q4(Gl, 0, t);
 #pragma unroll
     for (int q = 0; q < kPairChunk; ++q) {
       if (!ok[q]) continue;
-      const int64_t oa = int64_t(ia[q]) * ncell + t;
-      const int64_t ob = int64_t(ib[q]) * ncell + t;
-      const float ah = Fah[oa], al = Fal[oa];
-      const float bh = Fbh[ob], bl = Fbl[ob];
-      ff_merge(acc[q].v, ff_prod3(ah, al, bh, bl, gh, gl));
+      const float4 ah = q4(Fah, oa[q], t), al = q4(Fal, oa[q], t);
+      if (same[q]) {
+        ff_quad(acc[q].v, ah, al, ah, al, gh, gl);
+      } else {
+        const float4 bh = q4(Fbh, ob[q], t), bl = q4(Fbl, ob[q], t);
+        ff_quad(acc[q].v, ah, al, bh, bl, gh, gl);
+      }
+    }
+  }
+  if (blockIdx.x == 0) {
+    for (int64_t c = nquad * 4 + threadIdx.x; c < ncell; c += blockDim.x) {
+#pragma unroll
+      for (int q = 0; q < kPairChunk; ++q) {
+        if (!ok[q]) continue;
+        ff_merge(acc[q].v, ff_prod3(Fah[oa[q] + c], Fal[oa[q] + c],
+                                    Fbh[ob[q] + c], Fbl[ob[q] + c], Gh[c],
+                                    Gl[c]));
+      }
     }
   }
   block_add_acc<kPairChunk, float>(acc, out + 2 * p0, 2, npairs - p0, red);
@@ -428,6 +462,86 @@ pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* hist,
   block_add<2 * kKeyPairChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
 }
 
+// j_ell(x) at x = x.hi + x.lo >= 0 from the FP32 copy of the spline: the
+// knot value in float-float, the cubic terms (dx < 0.05) in FP32, which
+// keeps about 1e-8 absolute error; the same interval rule as spline_eval.
+__device__ __forceinline__ FF spline_eval_ff(const SplineTable& t, FF x) {
+  if (x.hi >= float(t.split)) {
+    const double v = sph_bessel_upward(t.ell, double(x.hi) + double(x.lo));
+    return FF{float(v), float(v - double(float(v)))};
+  }
+  const float hh = 0x1.99999ap-5f, hl = -0x1.99999ap-31f;  // 0.05
+  auto offset = [&](int i) {  // x - 0.05 i in FP32 (float-float knot)
+    const float fi = float(i);
+    const float p = __fmul_rn(hh, fi);
+    const float e = __fmaf_rn(hl, fi, __fmaf_rn(hh, fi, -p));
+    return __fadd_rn(__fsub_rn(x.hi, p), __fsub_rn(x.lo, e));
+  };
+  int i = int(__fmul_rn(x.hi, 20.f));
+  i = max(0, min(i, t.n - 2));
+  float dx = offset(i);
+  if (dx < 0.f && i > 0) {
+    --i;
+    dx = offset(i);
+  } else if (dx >= hh && i < t.n - 2) {
+    ++i;
+    dx = offset(i);
+  }
+  const float4 q = t.q[i];
+  const float poly =
+      __fmul_rn(dx, __fmaf_rn(dx, __fmaf_rn(dx, t.dq[i], q.w), q.z));
+  return ffadd(FF{q.x, q.y}, FF{poly, 0.f});
+}
+
+// pair_bessel_sums_kernel on the FP32 pipe: r = dr sqrt(key) and k r in
+// float-float, Bessel weights from spline_eval_ff, products and sums in
+// float-float; FP64 only per key (the histogram words) and at the end.
+__global__ void __launch_bounds__(256)
+pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* hist,
+                           PairBesselArgs a, int npairs, bool same_leg,
+                           double* out) {
+  __shared__ double red[2 * kKeyPairChunk * 32];
+  const int p0 = blockIdx.y * kKeyPairChunk;
+  FF ka[kKeyPairChunk], kb[kKeyPairChunk];
+  bool same[kKeyPairChunk];
+#pragma unroll
+  for (int q = 0; q < kKeyPairChunk; ++q) {
+    const int pi = min(p0 + q, npairs - 1);
+    ka[q] = ff_from_double(a.ka[pi]);
+    kb[q] = ff_from_double(a.kb[pi]);
+    same[q] = same_leg && a.ka[pi] == a.kb[pi];
+  }
+  const FF drf = ff_from_double(dr);
+  FF acc[2 * kKeyPairChunk];
+#pragma unroll
+  for (int q = 0; q < 2 * kKeyPairChunk; ++q) acc[q] = FF{0.f, 0.f};
+  for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
+    const double2 h = reinterpret_cast<const double2*>(hist)[key];
+    if (h.x == 0. && h.y == 0.) continue;
+    const FF hr = ff_from_double(h.x), hi = ff_from_double(h.y);
+    // sqrt(key) in float-float (key < 2^24 is exact in FP32).
+    const float kf = float(key);
+    const float sh = __fsqrt_rn(kf);
+    const float sl = sh > 0.f
+                         ? __fdiv_rn(__fmaf_rn(-sh, sh, kf), __fmul_rn(2.f, sh))
+                         : 0.f;
+    const FF r = ffmul(drf, FF{sh, sl});
+#pragma unroll
+    for (int q = 0; q < kKeyPairChunk; ++q) {
+      const FF ja = spline_eval_ff(a.ja, ffmul(ka[q], r));
+      const FF jb = same[q] ? ja : spline_eval_ff(a.jb, ffmul(kb[q], r));
+      const FF w = ffmul(ja, jb);
+      ff_merge(acc[2 * q], ffnorm(ffmul(w, hr)));
+      ff_merge(acc[2 * q + 1], ffnorm(ffmul(w, hi)));
+    }
+  }
+  double v[2 * kKeyPairChunk];
+#pragma unroll
+  for (int q = 0; q < 2 * kKeyPairChunk; ++q) v[q] = ff_value(acc[q]);
+  block_add<2 * kKeyPairChunk>(v, out + 2 * p0, red, 2 * (npairs - p0));
+}
+
 constexpr int kBesselChunk = 4;
 
 template <class Real>
@@ -549,17 +663,21 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
   TRVG_LAUNCHED(ctx);
 }
 
-void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, const float* Gh,
-                            const float* Gl, const float* Fah,
-                            const float* Fal, const float* Fbh,
-                            const float* Fbl, const int* pa, const int* pb,
-                            int npairs, double* out) {
+void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,
+                            const float* Gh, const float* Gl,
+                            const float* Fah, const float* Fal,
+                            const float* Fbh, const float* Fbl, const int* pa,
+                            const int* pb, int npairs, double* out) {
   if (npairs <= 0) return;
+  if (ld % 4 != 0 || ld < ncell)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Field stride %lld is not a multiple of 4 cells >= %lld.",
+                (long long)ld, (long long)ncell);
   const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
-  dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
+  dim3 grid(grid_for((ncell + 3) / 4, 256, 152 * 4), chunks);
   TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
   reduce_pairs_ff_kernel<<<grid, 256, 0, ctx.stream>>>(
-      ncell, Gh, Gl, Fah, Fal, Fbh, Fbl, pa, pb, npairs, out);
+      ncell, ld, Gh, Gl, Fah, Fal, Fbh, Fbl, pa, pb, npairs, out);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -599,15 +717,20 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
 void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* hist, const SplineTable& sja,
                              const SplineTable& sjb, const double* ka,
-                             const double* kb, int npairs, double* out) {
+                             const double* kb, int npairs, bool ff,
+                             double* out) {
   if (npairs <= 0) return;
   PairBesselArgs a{sja, sjb, ka, kb};
   const bool same_leg = sja.ell == sjb.ell;
   const int chunks = (npairs + kKeyPairChunk - 1) / kKeyPairChunk;
   dim3 grid(grid_for(nkeys, 256, 152 * 2), chunks);
   TRVG_KBEGIN(ctx, "pair_bessel_sums_kernel");
-  pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(
-      nkeys, g.dr[0], hist, a, npairs, same_leg, out);
+  if (ff && sja.q != nullptr && sjb.q != nullptr)
+    pair_bessel_sums_ff_kernel<<<grid, 256, 0, ctx.stream>>>(
+        nkeys, g.dr[0], hist, a, npairs, same_leg, out);
+  else
+    pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(
+        nkeys, g.dr[0], hist, a, npairs, same_leg, out);
   TRVG_LAUNCHED(ctx);
 }
 
