@@ -237,8 +237,9 @@ def algorithmic_bytes(kernel, args, real_bytes):
         'ff_inv_z_kernel': (ig[2] + i_f[2]) / 2,
         # shot-noise field xi read once; the key histogram written once.
         'orbit_rows_kernel': real_bytes * nm + 16 * nkeys,
-        # G and the nbins shell fields (real, on M^3) read once.
-        'reduce_pairs_kernel': real_bytes * mc * (1 + args.nbins),
+        # G and the nbins shell fields (real, on M^3, float-float hi and lo
+        # words) read once.
+        'reduce_pairs_kernel': 2 * real_bytes * mc * (1 + args.nbins),
         # key histogram read once.
         'pair_bessel_sums_kernel': 16 * nkeys,
         # nbins half-spectrum shell fields on the evaluation grid written.
@@ -597,12 +598,12 @@ def run_mocks(args):
     cat = _engine.device_catalogue(ntot, x.data_ptr(), y.data_ptr(),
                                    z.data_ptr())
 
-    def params(degrees):
+    def params(degrees, precision='fp32mixed'):
         pd = {'boxsize': {a: MOCK_BOX for a in 'xyz'},
               'ngrid': {a: MOCK_NGRID for a in 'xyz'}, 'assignment_order': 2,
               'interlace': False,
               'degrees': dict(zip(['ell1', 'ell2', 'ELL'], degrees)),
-              'form': 'diag', 'shape': 'diag', 'precision': 'fp32mixed',
+              'form': 'diag', 'shape': 'diag', 'precision': precision,
               'verbose': 0}
         return _engine.make_params(pd, '3pt')
 
@@ -615,19 +616,53 @@ def run_mocks(args):
                                        norms, shape='diag')
         return r0, r2
 
-    for _ in range(max(1, args.warmup)):
-        batch()
-    torch.cuda.synchronize(dev)
-    times, launches = [], 0
-    for _ in range(args.steps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        batch()
-        e1.record(stream)
+    def timed_batches(steps):
+        for _ in range(max(1, args.warmup)):
+            batch()
         torch.cuda.synchronize(dev)
-        times.append(e0.elapsed_time(e1) / 1e3)
-    t = statistics.median(times)
+        times = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return statistics.median(times)
+
+    t = timed_batches(args.steps)
+
+    # Accuracy against FP64 on the first mocks, and the same workload with
+    # the FP32 cuFFT transforms instead of the float-float ones.
+    nchk = min(4, args.mocks)
+    sub = _engine.device_catalogue(int(offsets[nchk]), x.data_ptr(),
+                                   y.data_ptr(), z.data_ptr())
+
+    def max_err():
+        e = {}
+        for name, deg in (('B000', (0, 0, 0)), ('B202', (2, 0, 2))):
+            r64 = _engine.call_bispec_batch(ctx, params(deg, 'fp64'), sub,
+                                            offsets[:nchk + 1], binning,
+                                            norms[:nchk], shape='diag')
+            r32 = _engine.call_bispec_batch(ctx, params(deg), sub,
+                                            offsets[:nchk + 1], binning,
+                                            norms[:nchk], shape='diag')
+            e[name] = {k: float(max(np.max(np.abs(a[k] - b[k]) / np.abs(b[k]))
+                                    for a, b in zip(r32, r64)))
+                       for k in ('bk_raw', 'bk_shot')}
+            # Normwise: max |error| over max |B| of the mock.
+            e[name]['normwise'] = {
+                k: float(max(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k]))
+                             for a, b in zip(r32, r64)))
+                for k in ('bk_raw', 'bk_shot')}
+        return e
+
+    err_ff = max_err()
+    ctx.set_option('ff_transforms', 0)
+    t_fp32fft = timed_batches(max(1, min(args.steps, 2)))
+    err_fp32fft = max_err()
+    ctx.set_option('ff_transforms', 1)
     # Per-kernel CUDA-event time per mock of each multipole's batch call.
     per_kernel = {}
     ctx.set_option('profiling', 1)
@@ -651,6 +686,9 @@ def run_mocks(args):
                                 "bins 0.005-0.245 h/Mpc"),
                    "batching": "one library call per multipole"},
         "kernel_ms_per_mock": per_kernel,
+        "max_rel_err_vs_fp64": {"mocks": nchk, **err_ff},
+        "fp32_cufft_variant": {"mocks_per_s": round(args.mocks / t_fp32fft, 2),
+                               "max_rel_err_vs_fp64": err_fp32fft},
     }
     print(json.dumps(line), flush=True)
 

@@ -367,16 +367,32 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
       }
     }
   }
-  if (uniform && nland > 0) {
-    const double land = double(nland) * a.ws.scale;
-    acc.re += land;
-    if constexpr (SH) acc_s.re += land;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (uniform) {
+    // Landed count: integer block sum, one FP64 product per block (the FP64
+    // warp sums below would cost more than the particles themselves when a
+    // thread handles few particles).
+    __shared__ long long cnt[8];
+    for (int o = 16; o > 0; o >>= 1)
+      nland += __shfl_down_sync(0xffffffffu, nland, o);
+    if (lane == 0) cnt[wid] = nland;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long t = 0;
+      for (int q = 0; q < int(blockDim.x >> 5); ++q) t += cnt[q];
+      const double land = double(t) * a.ws.scale;
+      if (t != 0) {
+        atomicAdd(sums + 0, land);
+        if constexpr (SH) atomicAdd(sums + 2, land);
+      }
+    }
+    // Particles of the exact path landed their weights in acc / acc_s.
+    if (__syncthreads_or(acc.re != 0. || acc_s.re != 0.) == 0) return;
   }
   // Block-wide FP64 sums of the deposited weight (k = 0 modes).
   __shared__ double red[4][8];
   double v[4] = {warp_sum(acc.re), warp_sum(acc.im), warp_sum(acc_s.re),
                  warp_sum(acc_s.im)};
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0)
     for (int q = 0; q < 4; ++q) red[q][wid] = v[q];
   __syncthreads();
@@ -494,7 +510,8 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
   a.vec4 = g.n[2] % 4 == 0 && aligned16(mesh_re) && aligned16(mesh_im) &&
            aligned16(sre) && aligned16(sim);
   const int block = 256;
-  const int grid = grid_for(cat.n, block);
+  // Several particles per thread: the per-block k = 0 sums are amortised.
+  const int grid = std::min(grid_for(cat.n, block), 152 * 8);
   auto go = [&](auto kernel) {
     TRVG_KBEGIN(ctx, "assign_kernel");
     kernel<<<grid, block, 0, ctx.stream>>>(a, mesh_re, mesh_im, sre, sim,

@@ -154,6 +154,7 @@ void Context::release() {
   buffers.clear();
   splines.clear();
   stats_plans.clear();
+  mode_counts.clear();
 }
 
 void destroy_events(Context& c) {

@@ -574,18 +574,25 @@ struct Engine {
     return b;
   }
 
-  // Mode counts of the last binning (they depend on the mesh and the bins
-  // only, so a batch of catalogues counts them once).
-  vector<double> cm_lo, cm_hi;
-  vector<long long> cm_nmodes;
-  vector<double> cm_keff;
-
-  // nmodes and k_eff per bin (field.cpp:1812-1847, 1904-1905).
+  // nmodes and k_eff per bin (field.cpp:1812-1847, 1904-1905).  They
+  // depend on the mesh and the bin edges only, so the context keeps them
+  // for later calls and catalogues.
   void count_modes(const HostBins& hb, vector<long long>& nmodes,
                    vector<double>& keff) {
-    if (!cm_nmodes.empty() && cm_lo == hb.lo && cm_hi == hb.hi) {
-      nmodes = cm_nmodes;
-      keff = cm_keff;
+    std::string key;
+    char buf[96];
+    for (int a = 0; a < 3; ++a) {
+      std::snprintf(buf, sizeof(buf), "%d.%a.", g.n[a], g.dk[a]);
+      key += buf;
+    }
+    for (int b = 0; b < hb.nb; ++b) {
+      std::snprintf(buf, sizeof(buf), "%a,%a;", hb.lo[b], hb.hi[b]);
+      key += buf;
+    }
+    auto it = ctx.mode_counts.find(key);
+    if (it != ctx.mode_counts.end()) {
+      nmodes = it->second.first;
+      keff = it->second.second;
       return;
     }
     const double kmax = *std::max_element(hb.hi.begin(), hb.hi.end());
@@ -600,10 +607,22 @@ struct Engine {
     vector<double> ks = download(dk, hb.nb);
     keff.resize(hb.nb);
     for (int b = 0; b < hb.nb; ++b) keff[b] = ks[b] / double(nmodes[b]);
-    cm_lo = hb.lo;
-    cm_hi = hb.hi;
-    cm_nmodes = nmodes;
-    cm_keff = keff;
+    ctx.mode_counts[key] = {nmodes, keff};
+  }
+
+  // Whether the float-float cube of the last pair_sums_ff holds both legs
+  // (one real FP32 field, same deposit, exact k = 0) on the modes of `cube`.
+  bool cube_covers(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                   const Cube& cube) const {
+    if (sizeof(Real) != 4 || ff_cube.cube == nullptr) return false;
+    for (const FieldSpec<Real>* f : {&fa, &fb})
+      if (f->re != ff_cube.spec || f->mesh_gen != ff_cube.gen ||
+          f->mesh_gen != ctx.mesh_gen || f->im != nullptr ||
+          f->re_s != nullptr || !f->k0_set)
+        return false;
+    for (int a = 0; a < 3; ++a)
+      if (cube.dense[a] || cube.K[a] > ff_cube.half) return false;
+    return true;
   }
 
   // Fine-binned two-point statistics (field.cpp:2511-2703): the field
@@ -631,8 +650,12 @@ struct Engine {
         static_cast<const uint32_t*>(ctx.buffers[sp.tag + ".list"].ptr);
     const double2* coef =
         static_cast<const double2*>(ctx.buffers[sp.tag + ".coef"].ptr);
-    launch_stats_pk<Real>(ctx, g, cube, fa, fb, hb.nb, sp.max_count, off,
-                          list, coef, dpk);
+    if (cube_covers(fa, fb, cube))
+      launch_stats_pk_cube(ctx, g, cube, ff_cube.cube, ff_cube.half, fa.k0,
+                           fb.k0, hb.nb, sp.max_count, off, list, coef, dpk);
+    else
+      launch_stats_pk<Real>(ctx, g, cube, fa, fb, hb.nb, sp.max_count, off,
+                            list, coef, dpk);
     const vector<double> pk = download(dpk, 2 * hb.nb);
     Stats s;
     s.nmodes = sp.nmodes;
@@ -1147,6 +1170,15 @@ struct Engine {
     return bytes < 0.6 * double(free_b);
   }
 
+  // The float-float spectrum cube of the last source mesh transformed by
+  // pair_sums_ff (the two-point statistics of that field read it too).
+  struct FFCube {
+    const float4* cube = nullptr;
+    int half = -1;
+    const void* spec = nullptr;  // the FieldSpec::re it belongs to
+    int64_t gen = -1;
+  } ff_cube;
+
   // Pair sums with float-float transforms: the source mesh's spectrum on
   // the cube |s| <= 2K, G and the shell fields of both legs evaluated from
   // it, then the same real-field reduction.
@@ -1165,6 +1197,7 @@ struct Engine {
         "ff.cube", size_t(2 * kg + 1) * (2 * kg + 1) * (kg + 1));
     launch_ff_forward_cube(ctx, g, reinterpret_cast<const float*>(src.mesh),
                            kg, T1, T2, cube);
+    ff_cube = {cube, kg, src.re, src.mesh_gen};
 
     const bool shared = la.ell == lb.ell && la.m == lb.m;
     vector<int> A, B;

@@ -148,6 +148,9 @@ struct Context {
   std::map<int, SplineTable> splines;
   // Two-point statistics mode lists by key.
   std::map<std::string, StatsPlan> stats_plans;
+  // Shell mode counts and k sums (nmodes, k_eff) by mesh and bin edges.
+  std::map<std::string, std::pair<std::vector<long long>,
+                                  std::vector<double>>> mode_counts;
 
   void kbegin(const char* name);
   void kend();

@@ -197,6 +197,13 @@ void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
                      const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
                      int nbins, int max_count, const int* off,
                      const uint32_t* list, const double2* coef, double* pk);
+// The same sums for one real source mesh (both legs) from its float-float
+// spectrum cube |s| <= Kc (launch_ff_forward_cube), k = 0 from k0a / k0b.
+void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
+                          const float4* ffcube, int Kc, cd k0a, cd k0b,
+                          int nbins, int max_count, const int* off,
+                          const uint32_t* list, const double2* coef,
+                          double* pk);
 
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,

@@ -382,11 +382,47 @@ __global__ void stats_fill_kernel(uint32_t nmode, const int16_t* qtab,
   }
 }
 
+// Mode values of the two legs: the (FP32 or FP64) spectra of the fields.
 template <class Real>
+struct SpectrumModes {
+  FieldSpec<Real> fa, fb;
+  __device__ __forceinline__ void values(const Geom& g, int sx, int sy,
+                                         int sz, cd& va, cd& vb) const {
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              kk = wrap(sz, g.n[2]);
+    va = field_value(fa, g, i, j, kk);
+    vb = field_value(fb, g, i, j, kk);
+  }
+};
+
+// Mode values from the float-float spectrum cube |s| <= Kc of one real
+// source mesh (both legs), cube[sx + Kc][sy + Kc][sz] for sz >= 0 and the
+// conjugate mirror below; k = 0 from each leg's exact sum.
+struct CubeModes {
+  const float4* cube;
+  int Kc;
+  cd k0a, k0b;
+  __device__ __forceinline__ void values(const Geom&, int sx, int sy, int sz,
+                                         cd& va, cd& vb) const {
+    if (sx == 0 && sy == 0 && sz == 0) {
+      va = k0a;
+      vb = k0b;
+      return;
+    }
+    const bool neg = sz < 0;
+    const int ax = neg ? -sx : sx, ay = neg ? -sy : sy, az = neg ? -sz : sz;
+    const float4 c =
+        cube[(int64_t(ax + Kc) * (2 * Kc + 1) + (ay + Kc)) * (Kc + 1) + az];
+    const double im = double(c.z) + double(c.w);
+    va = cd{double(c.x) + double(c.y), neg ? -im : im};
+    vb = va;
+  }
+};
+
+template <class Modes>
 __global__ void __launch_bounds__(256)
-stats_pk_kernel(Geom g, Cube cube, FieldSpec<Real> fa, FieldSpec<Real> fb,
-                const int* off, const uint32_t* list, const double2* coef,
-                double* pk) {
+stats_pk_kernel(Geom g, Cube cube, Modes modes, const int* off,
+                const uint32_t* list, const double2* coef, double* pk) {
   const int q = blockIdx.y;
   const int e0 = off[q], e1 = off[q + 1];
   cd acc = {0., 0.};
@@ -395,10 +431,8 @@ stats_pk_kernel(Geom g, Cube cube, FieldSpec<Real> fa, FieldSpec<Real> fb,
     const uint32_t t = list[e];
     int sx, sy, sz;
     cube_mode(g, cube, t, sx, sy, sz);
-    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
-              kk = wrap(sz, g.n[2]);
-    const cd va = field_value(fa, g, i, j, kk);
-    const cd vb = field_value(fb, g, i, j, kk);
+    cd va, vb;
+    modes.values(g, sx, sy, sz, va, vb);
     const double2 c = coef[t];
     acc = acc + (va * conjg(vb)) * cd{c.x, c.y};
   }
@@ -916,8 +950,21 @@ void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
   if (nbins <= 0 || max_count <= 0) return;
   const int bx = int(std::min<int64_t>((max_count + 1023) / 1024, 64));
   TRVG_KBEGIN(ctx, "twopt_stats_kernel");
-  stats_pk_kernel<Real><<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
-      g, cube, fa, fb, off, list, coef, pk);
+  stats_pk_kernel<<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
+      g, cube, SpectrumModes<Real>{fa, fb}, off, list, coef, pk);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
+                          const float4* ffcube, int Kc, cd k0a, cd k0b,
+                          int nbins, int max_count, const int* off,
+                          const uint32_t* list, const double2* coef,
+                          double* pk) {
+  if (nbins <= 0 || max_count <= 0) return;
+  const int bx = int(std::min<int64_t>((max_count + 1023) / 1024, 64));
+  TRVG_KBEGIN(ctx, "twopt_stats_kernel");
+  stats_pk_kernel<<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
+      g, cube, CubeModes{ffcube, Kc, k0a, k0b}, off, list, coef, pk);
   TRVG_LAUNCHED(ctx);
 }
 
