@@ -13,6 +13,8 @@
  *                                      (include/threept.hpp:290)
  *   trvg_compute_3pcf               <- trv::compute_3pcf
  *                                      (include/threept.hpp:257)
+ *   trvg_compute_3pcf_window        <- trv::compute_3pcf_window
+ *                                      (include/threept.hpp:310)
  *   trvg_compute_powspec_in_gpp_box <- trv::compute_powspec_in_gpp_box
  *                                      (include/twopt.hpp:283)
  *   trvg_compute_powspec            <- trv::compute_powspec
@@ -98,6 +100,7 @@ typedef struct trvg_params {
   int idx_bin;            /* row / off-diagonal index */
   int precision;          /* TRVG_PREC_* */
   int verbose;            /* 0 silent; >= 20 stage log on stderr */
+  int i_wa, j_wa;         /* wide-angle orders (3PCF window only) */
 } trvg_params;
 
 /* trv::Binning (include/dataobjs.hpp:58): edges and centres, host memory. */
@@ -262,6 +265,15 @@ int trvg_compute_3pcf(
   trvg_context* ctx, const trvg_params* params,
   const trvg_catalogue* data, const trvg_catalogue* rand, double alpha,
   const trvg_binning* rbinning, double norm_factor, trvg_threept_out* out);
+
+/* Three-point correlation function window from a random catalogue: the
+ * survey estimator on alpha * (random field) alone, the shot-noise
+ * amplitude alpha^3 sum y w^3, and with `wide_angle` the power-law kernel
+ * r^-(i_wa + j_wa) applied to G in configuration space. */
+int trvg_compute_3pcf_window(
+  trvg_context* ctx, const trvg_params* params, const trvg_catalogue* rand,
+  double alpha, const trvg_binning* rbinning, double norm_factor,
+  int wide_angle, trvg_threept_out* out);
 
 /* Power spectrum multipole (ELL = params->ELL), periodic box. */
 int trvg_compute_powspec_in_gpp_box(

@@ -989,6 +989,85 @@ def compute_3pcf(data, rand, params, edges, centres, norm_factor):
     return _finish_3pcf(out, norm_factor)
 
 
+def _rand_field(rand, alpha_pow, ell, m, params, power=1, conj=False):
+    """Single-catalogue ``compute_ylm_wgtd_field`` / ``_quad_field``
+    (field.cpp:1325-1362, 1449-1489): the random field times alpha (linear)
+    or alpha^2 (quadratic, conjugate Y_lm and w^2)."""
+    mr = mesh_weighted(rand['pos'],
+                       _ylm_weights(ell, m, rand['los'], rand['w'], power,
+                                    conj), params)
+    s = alpha_pow * mr.shadow if params.interlace else None
+    return Mesh(alpha_pow * mr.field, s)
+
+
+def wide_angle_pow_law(field, rmag, i_wa, j_wa):
+    """``apply_wide_angle_pow_law_kernel`` (field.cpp:1727-1760): times
+    r^-(i_wa + j_wa) away from the origin (r >= 1e-6)."""
+    far = rmag >= 1.e-6
+    out = field.copy()
+    out[far] = field[far] * rmag[far] ** (-(i_wa + j_wa))
+    return out
+
+
+def compute_3pcf_window(rand, params, edges, centres, norm_factor,
+                        alpha=1., wide_angle=False, i_wa=0, j_wa=0):
+    """``trv::compute_3pcf_window`` (threept.cpp:2621-3077): the survey
+    3PCF with alpha * (random field) in place of data - alpha * randoms,
+    S-bar from the randoms alone (threept.cpp:210-236), and the wide-angle
+    kernel on G when requested."""
+    _validate_coupling(params)
+    pairs = dv_pairs(params.shape, len(centres), params.idx_bin)
+    ndv = len(pairs)
+    factor_phase = (1j) ** (params.ell1 + params.ell2)
+    factor_parity = (-1.) ** (params.ell1 + params.ell2)
+    n_00 = fourier_transform(_rand_field(rand, alpha, 0, 0, params), params)
+    N_00 = fourier_transform(
+        _rand_field(rand, alpha ** 2, 0, 0, params, power=2, conj=True),
+        params)
+    win = assignment_window(params)
+    alias = shotnoise_aliasing(params)
+    win_pk = (win * win) if params.interlace else alias
+    kvec = grid_wavevectors(params)
+    kmag = vec3_mag(*kvec)
+    rvec = grid_positions(params)
+    rmag = vec3_mag(*rvec)
+    sj_a = SphericalBessel(params.ell1)
+    sj_b = SphericalBessel(params.ell2)
+    out = _empty_3pcf(ndv)
+    for term_idx, (m1, m2, M, coupling) in enumerate(_sph_orders_lpp(params)):
+        zero = (m1 == 0 and m2 == 0 and M == 0)
+        factor_mirror = 0. if zero else (-1.) ** params.ELL
+        factor_mirror_w3j = 0. if zero else 1.
+        ylm_r_a = ylm_grid(params.ell1, m1, rvec)
+        ylm_r_b = ylm_grid(params.ell2, m2, rvec)
+        ylm_k_a = ylm_grid(params.ell1, m1, kvec)
+        ylm_k_b = ylm_grid(params.ell2, m2, kvec)
+        n_LM = fourier_transform(
+            _rand_field(rand, alpha, params.ELL, M, params), params)
+        Sbar = complex(alpha ** 3 * np.sum(
+            reduced_ylm(params.ELL, M, rand['los']) * rand['w'] ** 3))
+        xi = twopt_field(n_LM, N_00, Sbar, params, win_pk, alias)
+        npairs, r_eff, xi_b = shotnoise_3pcf(xi, ylm_r_a, ylm_r_b, rmag,
+                                             edges, centres, params)
+        for i, b in _sn_3pcf_diag_entries(params.shape, pairs, len(centres),
+                                          params.idx_bin):
+            out['sn'][i] += coupling * factor_parity * (
+                xi_b[b] + factor_mirror_w3j * np.conj(xi_b[b]))
+        _zeta_pairs(out, pairs, centres, npairs, r_eff, term_idx == 0)
+        G = inv_fourier_transform(n_LM / win, params)
+        if wide_angle:
+            G = wide_angle_pow_law(G, rmag, i_wa, j_wa)
+        for i in range(ndv):
+            Fa = sjl_ylm_ifft(n_00, ylm_k_a, win, kmag, sj_a,
+                              out['r1_eff'][i], params)
+            Fb = sjl_ylm_ifft(n_00, ylm_k_b, win, kmag, sj_b,
+                              out['r2_eff'][i], params)
+            comp = complex(np.sum(Fa * Fb * G))
+            out['zeta'][i] += coupling * params.vol_cell * factor_phase * (
+                comp + factor_mirror * np.conj(comp))
+    return _finish_3pcf(out, norm_factor)
+
+
 def compute_powspec_in_gpp_box(pos, params, edges, centres, norm_factor):
     """``trv::compute_powspec_in_gpp_box`` (twopt.cpp:609-701)."""
     npart = pos.shape[0]

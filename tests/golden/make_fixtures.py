@@ -31,6 +31,8 @@ FILES = [
     "stats/zeta202_diag_gpp.txt",
     "stats/zeta000_diag_lpp.txt", "stats/zeta000_row0_lpp.txt",
     "stats/zeta202_diag_lpp.txt",
+    "stats/zetaw000_diag.txt", "stats/zetaw000_row0.txt",
+    "stats/zetaw202_diag.txt",
     "stats/pk0_gpp.txt", "stats/pk2_gpp.txt",
     "stats/pk0_lpp.txt", "stats/pk2_lpp.txt",
     "ctlgs/test_data_catalogue.txt",

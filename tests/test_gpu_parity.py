@@ -13,12 +13,13 @@ import pytest
 
 from conftest import BOX, KBINS, NMESH, RBINS, THREEPT_CASES, load_golden
 from oracle import trv_oracle as O
-from test_oracle import check_powspec, check_threept
+from test_oracle import (WINDOW_CASES, _window_rand, check_powspec,
+                         check_threept)
 from triumvirate_gb300 import _engine, _lib
 from triumvirate_gb300.catalogue import ParticleCatalogue
 from triumvirate_gb300.dataobjs import Binning
 from triumvirate_gb300.threept import (compute_3pcf, compute_3pcf_in_gpp_box,
-                                       compute_bispec,
+                                       compute_3pcf_window, compute_bispec,
                                        compute_bispec_in_gpp_box)
 from triumvirate_gb300.twopt import (compute_powspec,
                                      compute_powspec_in_gpp_box)
@@ -120,6 +121,40 @@ def _check_golden(res, ext, kind, precision):
         ref = ext[a] + 1j * ext[b]
         assert np.allclose(res[k], ref,
                            atol=1e-5 * np.max(np.abs(ref)) + 1e-6), k
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("degrees, form, idx_bin, golden", WINDOW_CASES)
+def test_golden_3pcf_window(precision, degrees, form, idx_bin, golden,
+                            rand_catalogue_array):
+    """Reference tests/test_threept.py:265-332 (3PCF window)."""
+    r = rand_catalogue_array
+    rc = ParticleCatalogue(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3])
+    res = compute_3pcf_window(rc, degrees=degrees,
+                              binning=Binning('config', 'lin', *RBINS),
+                              form=form, idx_bin=idx_bin,
+                              sampling_params=_sampling(precision))
+    _check_golden(res, load_golden(golden), '3pcf', precision)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("degrees, wa", [((0, 0, 0), (1, 1)),
+                                         ((2, 0, 2), (0, 1))])
+def test_3pcf_window_wide_angle_matches_oracle(precision, degrees, wa,
+                                               rand_catalogue_array):
+    """The wide-angle kernel r^-(i_wa + j_wa) on G (field.cpp:1727-1760)
+    has no golden file; the oracle is the reference."""
+    r = rand_catalogue_array
+    rc = ParticleCatalogue(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3])
+    res = compute_3pcf_window(rc, degrees=degrees, wa_orders=wa,
+                              binning=Binning('config', 'lin', *RBINS),
+                              form='diag', sampling_params=_sampling(precision))
+    p = O.Params(BOX, NMESH, 'tsc', False, *degrees, form='diag')
+    edges, centres = O.lin_binning(*RBINS)
+    norm = O.bispec_norm_from_particles(r[:, 3], 1., 1.)
+    ref = O.compute_3pcf_window(_window_rand(r), p, edges, centres, norm,
+                                wide_angle=True, i_wa=wa[0], j_wa=wa[1])
+    assert_close_threept(res, ref, '3pcf', precision)
 
 
 @pytest.mark.parametrize("precision", PRECISIONS)

@@ -118,3 +118,47 @@ def test_wigner_3j_exact():
                  (1, 1, 2, 1, -1, 0), (3, 2, 1, -2, 1, 1),
                  (4, 4, 4, 2, -1, -1), (2, 2, 2, 0, 0, 0)]:
         assert abs(O.wigner_3j(*args) - float(wigner_3j(*args))) < 1e-15
+
+
+WINDOW_CASES = [
+    ((0, 0, 0), 'diag', None, 'zetaw000_diag.txt'),
+    ((2, 0, 2), 'diag', None, 'zetaw202_diag.txt'),
+    ((0, 0, 0), 'row', 0, 'zetaw000_row0.txt'),
+]
+
+
+def _window_rand(r):
+    """The random catalogue as the reference's compute_3pcf_window prepares
+    it (threept.py:1976-1987): lines of sight before centring, then
+    centred and periodised in the box."""
+    los = O.compute_los(r[:, 0], r[:, 1], r[:, 2])
+    (x, y, z), _ = O.centre(r[:, 0], r[:, 1], r[:, 2], [BOX] * 3)
+    x, y, z = O.periodise(x, y, z, [BOX] * 3)
+    n = r.shape[0]
+    return dict(pos=np.stack([x, y, z], -1), los=los, w=np.ones(n),
+                ws=np.ones(n))
+
+
+@pytest.mark.parametrize("degrees, form, idx_bin, golden", WINDOW_CASES)
+def test_oracle_3pcf_window(degrees, form, idx_bin, golden,
+                            rand_catalogue_array):
+    rand = _window_rand(rand_catalogue_array)
+    p = O.Params(BOX, NMESH, 'tsc', False, *degrees, form=form,
+                 idx_bin=idx_bin)
+    edges, centres = O.lin_binning(*RBINS)
+    norm = O.bispec_norm_from_particles(rand_catalogue_array[:, 3], 1., 1.)
+    res = O.compute_3pcf_window(rand, p, edges, centres, norm)
+    check_threept(res, load_golden(golden), '3pcf')
+
+
+def test_oracle_wide_angle_kernel():
+    """r^-(i + j) away from the origin; orders (0, 0) leave G unchanged."""
+    rng = np.random.default_rng(3)
+    g = rng.normal(size=(4, 4, 4)) + 1j * rng.normal(size=(4, 4, 4))
+    r = rng.uniform(1., 3., size=(4, 4, 4))
+    r[0, 0, 0] = 0.
+    out = O.wide_angle_pow_law(g, r, 1, 1)
+    assert out[0, 0, 0] == g[0, 0, 0]
+    far = r > 0
+    assert np.allclose(out[far], g[far] / r[far] ** 2)
+    assert np.array_equal(O.wide_angle_pow_law(g, r, 0, 0), g)

@@ -29,6 +29,9 @@ def make_params(paramset, npoint):
     p.precision = _lib.PRECISIONS[paramset.get('precision', 'fp64')]
     verbose = paramset.get('verbose', 0)
     p.verbose = int(verbose) if verbose is not None else 0
+    wa = paramset.get('wa_orders') or {}
+    p.i_wa = int(wa.get('i') or 0)
+    p.j_wa = int(wa.get('j') or 0)
     return p
 
 
@@ -151,6 +154,18 @@ def call_threept(fn_name, ctx, params, data_c, binning, norm, kind,
                 C.byref(res.c))
     _lib.check(st)
     return res.as_dict(kind)
+
+
+def call_3pcf_window(ctx, params, rand_c, binning, norm, alpha, wide_angle,
+                     shape=None, idx_bin=0):
+    """trvg_compute_3pcf_window; the 3PCF result dictionary."""
+    lib = _lib.load()
+    res = ThreeptResult(dv_dim(shape, binning.num_bins, idx_bin))
+    hb = HostBinning(binning)
+    _lib.check(lib.trvg_compute_3pcf_window(
+        ctx.handle, C.byref(params), C.byref(rand_c), float(alpha),
+        C.byref(hb.c), float(norm), int(bool(wide_angle)), C.byref(res.c)))
+    return res.as_dict('3pcf')
 
 
 def call_bispec_batch(ctx, params, cat_c, offsets, binning, norms, shape,

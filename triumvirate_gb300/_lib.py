@@ -41,6 +41,7 @@ EXPORTED = [
     "trvg_kernel_time_count", "trvg_kernel_time_get",
     "trvg_calc_grid_based_powlaw_norm_noalloc",
     "trvg_compute_bispec_in_gpp_box_batch", "trvg_bispec_gpp_adjoint",
+    "trvg_compute_3pcf_window",
 ]
 
 
@@ -81,6 +82,7 @@ class Params(C.Structure):
         ("idx_bin", C.c_int),
         ("precision", C.c_int),
         ("verbose", C.c_int),
+        ("i_wa", C.c_int), ("j_wa", C.c_int),
     ]
 
 
@@ -177,6 +179,8 @@ def _declare(lib):
         getattr(lib, nm).argtypes = [vp, P(Params), P(Catalogue),
                                      P(Catalogue), dp, P(BinningC), dp,
                                      P(ThreeptOut)]
+    lib.trvg_compute_3pcf_window.argtypes = [
+        vp, P(Params), P(Catalogue), dp, P(BinningC), dp, ip, P(ThreeptOut)]
     lib.trvg_compute_powspec_in_gpp_box.argtypes = [
         vp, P(Params), P(Catalogue), P(BinningC), dp, P(PowspecOut)]
     lib.trvg_compute_powspec.argtypes = [

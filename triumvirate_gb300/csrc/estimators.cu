@@ -1170,6 +1170,10 @@ struct Engine {
     return bytes < 0.6 * double(free_b);
   }
 
+  // 3PCF window with wide-angle corrections: G(x) *= r^-wide_angle_power.
+  bool wide_angle = false;
+  double wide_angle_power = 0.;
+
   // The float-float spectrum cube of the last source mesh transformed by
   // pair_sums_ff (the two-point statistics of that field read it too).
   struct FFCube {
@@ -1302,6 +1306,15 @@ struct Engine {
     }
     const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
     const FR* Gr = real ? build_G_real<FR>(gsrc, M, Kg) : nullptr;
+    if (wide_angle) {  // 3PCF window: G is on the full mesh
+      if (M[0] != g.n[0] || M[1] != g.n[1] || M[2] != g.n[2])
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Wide-angle kernel needs G on the full mesh.");
+      if (real)
+        launch_wide_angle(ctx, g, const_cast<FR*>(Gr), wide_angle_power);
+      else
+        launch_wide_angle(ctx, g, const_cast<FC*>(G), wide_angle_power);
+    }
     const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;
     vector<int> A, B;
     for (const Pair& q : pairs) {
@@ -1758,9 +1771,12 @@ struct Engine {
   // -------------------------------------------------------------------------
   // Three-point correlation function.
   // -------------------------------------------------------------------------
+  // survey = false: periodic box; survey = true: data and randoms, or
+  // with `window` the randoms alone (data == nullptr; threept.cpp:2621-3077).
   void threepcf(const trvg_catalogue* data, const trvg_catalogue* rand,
                 double alpha, const trvg_binning* rbin, double norm,
-                trvg_threept_out* out, bool survey) {
+                trvg_threept_out* out, bool survey, bool window = false,
+                bool wa = false) {
     const HostBins hb = host_bins(rbin);
     validate_threept(&p, hb.nb);
     const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
@@ -1771,10 +1787,31 @@ struct Engine {
                   out ? out->dim : -1, ndv);
     const vector<Term> terms = survey ? orders_lpp(p.ell1, p.ell2, p.ELL)
                                       : orders_gpp(p.ell1, p.ell2, p.ELL);
-    const DevCatalogue dd = upload_catalogue(data, "data", survey);
-    DevCatalogue dr;
+    DevCatalogue dd, dr;
+    if (!window) dd = upload_catalogue(data, "data", survey);
     if (survey) dr = upload_catalogue(rand, "rand", true);
     TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+    wide_angle = window && wa;
+    wide_angle_power = double(p.i_wa + p.j_wa);
+    // Parts of a field: the data (weight 1) and the randoms (weight
+    // `rand_scale`); the window has the randoms alone.
+    auto parts = [&](double rand_scale, int power, int ell, int m,
+                     bool conj) {
+      WeightSpec wd, wr;
+      for (WeightSpec* w : {&wd, &wr}) {
+        w->power = power;
+        w->use_ylm = !(ell == 0 && m == 0);
+        w->ell = ell;
+        w->m = m;
+        w->conj_ylm = conj;
+      }
+      wd.scale = 1.;
+      wr.scale = rand_scale;
+      vector<Part> v;
+      if (!window) v.push_back({dd, wd});
+      v.push_back({dr, wr});
+      return v;
+    };
 
     auto ylm_ws = [](double scale, int power, int ell, int m, bool conj) {
       WeightSpec w;
@@ -1794,13 +1831,12 @@ struct Engine {
       dn = k0_view(base, -nbar * g.vol);
       nf = k0_view(base, 0.);
     } else {
-      Field f0 = make_field("dn00", {{dd, ylm_ws(1., 1, 0, 0, false)},
-                                     {dr, ylm_ws(-alpha, 1, 0, 0, false)}},
-                            false);
+      // Window: n_00 = alpha * (random field) (field.cpp:1325-1362).
+      const double s1 = window ? alpha : -alpha;
+      Field f0 = make_field("dn00", parts(s1, 1, 0, 0, false), false);
       dn = k0_view(f0, 0.);
-      Field n0 = make_field("N00", {{dd, ylm_ws(1., 2, 0, 0, true)},
-                                    {dr, ylm_ws(alpha * alpha, 2, 0, 0, true)}},
-                            false);
+      Field n0 =
+          make_field("N00", parts(alpha * alpha, 2, 0, 0, true), false);
       nf = k0_view(n0, 0.);
     }
 
@@ -1832,14 +1868,14 @@ struct Engine {
       FieldSpec<Real> dnLM = dn;
       if (survey) {
         const bool cplxM = (t.M != 0);
-        Field fdn = make_field("dnLM",
-                               {{dd, ylm_ws(1., 1, p.ELL, t.M, false)},
-                                {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
-                               cplxM);
+        Field fdn = make_field(
+            "dnLM", parts(window ? alpha : -alpha, 1, p.ELL, t.M, false),
+            cplxM);
         dnLM = k0_view(fdn, 0.);
-        const cplx Sbar = weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false)) +
-                          alpha * alpha * alpha *
-                              weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
+        // S-bar_LM (threept.cpp:156-236; randoms alone for the window).
+        cplx Sbar = alpha * alpha * alpha *
+                    weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
+        if (!window) Sbar += weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false));
         xi = twopt_xi(dnLM, nf, Sbar);
       }
 
@@ -2162,6 +2198,18 @@ int trvg_compute_3pcf(trvg_context* ctx, const trvg_params* params,
   TRVG_API_BEGIN
   run(ctx, params, false, [&](auto& e) {
     e.threepcf(data, rand, alpha, rbinning, norm_factor, out, true);
+  });
+  TRVG_API_END
+}
+
+int trvg_compute_3pcf_window(trvg_context* ctx, const trvg_params* params,
+                             const trvg_catalogue* rand, double alpha,
+                             const trvg_binning* rbinning, double norm_factor,
+                             int wide_angle, trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.threepcf(nullptr, rand, alpha, rbinning, norm_factor, out, true, true,
+               wide_angle != 0);
   });
   TRVG_API_END
 }

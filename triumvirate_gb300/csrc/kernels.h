@@ -197,6 +197,11 @@ void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
                      const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
                      int nbins, int max_count, const int* off,
                      const uint32_t* list, const double2* coef, double* pk);
+// f(x) *= r^-p on the full mesh (r < 1e-6 unchanged): the 3PCF window's
+// wide-angle kernel; T is float, double, float2 or double2.
+template <class T>
+void launch_wide_angle(Context& ctx, const Geom& g, T* f, double p);
+
 // The same sums for one real source mesh (both legs) from its float-float
 // spectrum cube |s| <= Kc (launch_ff_forward_cube), k = 0 from k0a / k0b.
 void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,

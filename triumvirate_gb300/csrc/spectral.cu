@@ -8,6 +8,7 @@
 // index through Hermitian symmetry.  Interlacing (field.cpp:1615-1653) is
 // applied on read from the raw main and shadow spectra.
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.h"
 
@@ -954,6 +955,47 @@ void launch_stats_pk(Context& ctx, const Geom& g, const Cube& cube,
       g, cube, SpectrumModes<Real>{fa, fb}, off, list, coef, pk);
   TRVG_LAUNCHED(ctx);
 }
+
+// Wide-angle power-law kernel (field.cpp:1727-1760): every cell of a
+// configuration-space field on the mesh times r^-p, r = |grid position|
+// (the library's shifted cell coordinates), cells with r < 1e-6 unchanged.
+template <class T>
+__global__ void wide_angle_kernel(Geom g, T* f, double p) {
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const double rx = double(shift_index(i, g.n[0])) * g.dr[0];
+    const double ry = double(shift_index(j, g.n[1])) * g.dr[1];
+    const double rz = double(shift_index(k, g.n[2])) * g.dr[2];
+    const double r = vec3_mag(rx, ry, rz);
+    if (r < 1.e-6) continue;
+    const double s = pow(r, -p);
+    if constexpr (std::is_same_v<T, float2> || std::is_same_v<T, double2>) {
+      using E = decltype(f[t].x);
+      f[t].x = E(double(f[t].x) * s);
+      f[t].y = E(double(f[t].y) * s);
+    } else {
+      f[t] = T(double(f[t]) * s);
+    }
+  }
+}
+
+template <class T>
+void launch_wide_angle(Context& ctx, const Geom& g, T* f, double p) {
+  TRVG_KBEGIN(ctx, "wide_angle_kernel");
+  wide_angle_kernel<T><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+      g, f, p);
+  TRVG_LAUNCHED(ctx);
+}
+template void launch_wide_angle<float>(Context&, const Geom&, float*, double);
+template void launch_wide_angle<double>(Context&, const Geom&, double*,
+                                        double);
+template void launch_wide_angle<float2>(Context&, const Geom&, float2*,
+                                        double);
+template void launch_wide_angle<double2>(Context&, const Geom&, double2*,
+                                         double);
 
 void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
                           const float4* ffcube, int Kc, cd k0a, cd k0b,

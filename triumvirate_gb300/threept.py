@@ -240,6 +240,46 @@ def compute_3pcf(catalogue_data, catalogue_rand, los_data=None,
         save=save, logger=logger, device=device)
 
 
+def compute_3pcf_window(catalogue_rand, los_rand=None, degrees=None,
+                        wa_orders=None, binning=None, form=None,
+                        idx_bin=None, sampling_params=None, paramset=None,
+                        save=False, logger=None, device=None):
+    """3PCF window from a random catalogue, with wide-angle corrections of
+    orders `wa_orders` (i_wa, j_wa) when given (threept.py:1832-2080).
+
+    The random field alone, scaled by alpha = 1, takes the place of the
+    data-minus-randoms field of :func:`compute_3pcf`; the normalisation is
+    the randoms' own (alpha = 1).  Returns the keys of
+    :func:`compute_3pcf` ('r1_bin', 'r1_eff', 'npairs_1', 'r2_*',
+    'zeta_raw', 'zeta_shot')."""
+    wide_angle = wa_orders is not None
+    paramset = _amalgamate_parameters(
+        paramset=paramset, params_sampling=sampling_params, degrees=degrees,
+        wa_orders=wa_orders, binning=binning, form=form, idx_bin=idx_bin,
+        catalogue_type='random', statistic_type='3pcf-win')
+    if binning is None:
+        binning = Binning.from_parameter_set(paramset)
+    if los_rand is None:
+        los_rand = catalogue_rand.compute_los()
+    los_rand = np.ascontiguousarray(los_rand)
+    catalogue_rand.centre(_boxsize(paramset))
+    catalogue_rand.periodise(_boxsize(paramset))
+    ctx = _lib.default_context(device)
+    params_c = _engine.make_params(paramset, '3pt')
+    xr, yr, zr, wr = catalogue_rand._columns()
+    rcat = _engine.HostCatalogue(xr, yr, zr, wr, los_rand)
+    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
+                        catalogue_rand['ws'], catalogue_rand['wc'], 1., 3)
+    results = _engine.call_3pcf_window(
+        ctx, params_c, rcat.c, binning, norm, 1., wide_angle,
+        shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
+    if save:
+        _save(results, paramset, save, ctx, params_c, rcat.c,
+              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+              1., 3, catalogue_rand)
+    return results
+
+
 def compute_bispec_in_gpp_box(catalogue_data, degrees=None, binning=None,
                               form=None, idx_bin=None, sampling_params=None,
                               paramset=None, save=False, logger=None,
