@@ -164,6 +164,8 @@ typedef struct trvg_stats {
   int64_t fft_launches;   /* cuFFT executions */
   int pruned_grid[3];     /* evaluation grid of the shell fields (== ngrid
                              when the full mesh is used) */
+  int64_t graph_replays;  /* mocks of the last batch replayed from its
+                             captured CUDA graph */
 } trvg_stats;
 
 /* ---- Context -------------------------------------------------------- */
@@ -197,7 +199,10 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           tile before the deposit (default 1);
  *   "ff_transforms"    0/1: FP32-mixed: compute the spectrum modes of the
  *                           shell fields and the evaluation-grid transforms
- *                           in float-float arithmetic (default 1). */
+ *                           in float-float arithmetic (default 1);
+ *   "graph_batch"      0/1: FP32-mixed batches: capture one mock as a CUDA
+ *                           graph and replay it for the others (default 1;
+ *                           off while profiling). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
 /* Per-kernel device time of the last call (profiling on). */
 int trvg_kernel_time_count(const trvg_context* ctx, int* count);

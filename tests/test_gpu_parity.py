@@ -618,6 +618,37 @@ def test_batch_matches_single_calls(precision):
                 assert err < 1e-5, k
 
 
+@pytest.mark.parametrize("degrees", [(0, 0, 0), (2, 0, 2)])
+def test_batch_graph_replay_matches_single_calls(degrees):
+    """FP32-mixed batch on the float-float path (64^3, pruned grid M = 36):
+    the largest mock runs as a warm-up, the others replay one captured CUDA
+    graph with per-mock counts and offsets read on the device (sorted and
+    unsorted sizes), and every mock matches its own single call and FP64."""
+    from triumvirate_gb300.threept import compute_bispec_in_gpp_box_batch
+    box, sizes = 1000., [70000, 30000, 90000, 50000]
+    pos = [_uniform(n, box, 50 + i) for i, n in enumerate(sizes)]
+    binning = Binning('fourier', 'lin', 0.005, 0.045, 4)
+
+    def cats():
+        return [ParticleCatalogue(*q.T, nz=len(q) / box ** 3) for q in pos]
+    kw = dict(degrees=degrees, binning=binning, form='diag')
+    batch = compute_bispec_in_gpp_box_batch(
+        cats(), sampling_params=_sampling('fp32mixed', 64, box=box), **kw)
+    assert _lib.default_context(None).stats()['graph_replays'] == 3
+    for i, c in enumerate(cats()):
+        s32 = compute_bispec_in_gpp_box(
+            c, sampling_params=_sampling('fp32mixed', 64, box=box), **kw)
+        s64 = compute_bispec_in_gpp_box(
+            c, sampling_params=_sampling('fp64', 64, box=box), **kw)
+        b = batch[i]
+        assert np.array_equal(b['nmodes_1'], s64['nmodes_1'])
+        assert np.allclose(b['k1_eff'], s64['k1_eff'], rtol=1e-12, atol=0)
+        for k in ('bk_raw', 'bk_shot'):
+            scale = np.max(np.abs(s64[k]))
+            assert np.max(np.abs(b[k] - s32[k])) / scale < 1e-6, (i, k)
+            assert np.max(np.abs(b[k] - s64[k])) / scale < 1e-5, (i, k)
+
+
 # ---------------------------------------------------------------------------
 # Float-float shell-field transforms (FP32-mixed default)
 # ---------------------------------------------------------------------------

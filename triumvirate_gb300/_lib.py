@@ -137,6 +137,7 @@ class Stats(C.Structure):
         ("kernel_launches", C.c_int64),
         ("fft_launches", C.c_int64),
         ("pruned_grid", C.c_int * 3),
+        ("graph_replays", C.c_int64),
     ]
 
 
@@ -247,7 +248,8 @@ class Context:
         return dict(ms_total=s.ms_total, ms_h2d=s.ms_h2d,
                     h2d_bytes=s.h2d_bytes, kernel_launches=s.kernel_launches,
                     fft_launches=s.fft_launches,
-                    pruned_grid=tuple(s.pruned_grid))
+                    pruned_grid=tuple(s.pruned_grid),
+                    graph_replays=s.graph_replays)
 
     def set_stream(self, stream_ptr):
         """Run on a caller's cudaStream_t (None: the context's own)."""

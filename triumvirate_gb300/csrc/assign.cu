@@ -316,8 +316,9 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
   // Equal weights: fully landed particles are counted, not summed in FP64.
   const bool uniform = a.cat.w == nullptr && !a.ws.use_ylm;
   long long nland = 0;
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-       p < a.cat.n; p += int64_t(gridDim.x) * blockDim.x) {
+  const int64_t np = a.cat.count(), p0 = a.cat.first();
+  for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
     const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
     double w = (a.cat.w != nullptr) ? a.cat.w[p] : 1.0;
     double wp = w;
@@ -450,8 +451,9 @@ __global__ void fill_offset_kernel(Real* mesh, int64_t n, const double* dsum,
 __global__ void weight_sum_kernel(DevCatalogue cat, WeightSpec ws,
                                   double* out) {
   cd acc = {0., 0.};
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < cat.n;
-       p += int64_t(gridDim.x) * blockDim.x) {
+  const int64_t np = cat.count(), p0 = cat.first();
+  for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
     const double w = (cat.w != nullptr) ? cat.w[p] : 1.0;
     double wp = 1.;
     for (int i = 0; i < ws.power; ++i) wp *= w;

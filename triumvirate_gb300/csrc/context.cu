@@ -116,6 +116,7 @@ void Context::begin_call() {
   kernel_launches = 0;
   fft_launches = 0;
   h2d_bytes = 0;
+  graph_replays = 0;
   records.clear();
   events_used = 0;
   pending = nullptr;
@@ -238,6 +239,7 @@ int trvg_get_stats(const trvg_context* ctx, trvg_stats* out) {
   out->kernel_launches = c.kernel_launches;
   out->fft_launches = c.fft_launches;
   for (int i = 0; i < 3; ++i) out->pruned_grid[i] = c.pruned_grid[i];
+  out->graph_replays = c.graph_replays;
   TRVG_API_END
 }
 
@@ -268,6 +270,8 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     ctx->impl.sort_catalogue = value != 0;
   } else if (k == "ff_transforms") {
     ctx->impl.ff_transforms = value != 0;
+  } else if (k == "graph_batch") {
+    ctx->impl.graph_batch = value != 0;
   } else {
     trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown option '%s'.",
                       key);

@@ -292,7 +292,30 @@ struct Engine {
     vector<long long> nmodes;
     vector<double> k;
     vector<cplx> pk, sn;
+    // Replayed batch: the unnormalised sums stay on the device.
+    const double* dev_pk = nullptr;
+    const double* dev_nmodes = nullptr;
+    const double* dev_snsum = nullptr;
   };
+
+  // Replayed batch (batch.cu): while set, nothing is uploaded or read
+  // back; the per-mock scalars come from `state`, and each term's sums are
+  // combined on the device into `acc`.
+  struct Replay {
+    MockState* state = nullptr;
+    double* acc = nullptr;
+    double* raw = nullptr;
+    double* shot = nullptr;
+    const int* prow = nullptr;
+    const int* pcol = nullptr;
+    const double* nmodes = nullptr;
+  };
+  const Replay* replay = nullptr;
+  // Device results of the last pair sums and shot-noise pair sums.
+  const double* dev_pairs = nullptr;
+  const double* dev_sij = nullptr;
+  // Whether the last pair sums took the float-float path.
+  bool ff_taken = false;
 
   Context& ctx;
   trvg_params p;
@@ -324,6 +347,15 @@ struct Engine {
 
   template <class T>
   T* upload(const std::string& name, const vector<T>& v) {
+    if (replay != nullptr) {
+      // Captured replay: the warm-up estimate uploaded the same values.
+      auto it = ctx.buffers.find(name);
+      if (it == ctx.buffers.end() || it->second.bytes < v.size() * sizeof(T))
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Batch replay needs buffer '%s' from the warm-up.",
+                    name.c_str());
+      return static_cast<T*>(it->second.ptr);
+    }
     T* d = ctx.buf<T>(name, v.size());
     if (!v.empty())
       TRVG_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T),
@@ -333,6 +365,9 @@ struct Engine {
 
   template <class T>
   vector<T> download(const T* d, size_t n) {
+    if (replay != nullptr)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "No read-back is possible in a captured batch replay.");
     vector<T> v(n);
     if (n > 0) {
       TRVG_CUDA(cudaMemcpyAsync(v.data(), d, n * sizeof(T),
@@ -436,6 +471,10 @@ struct Engine {
         d.ly = c->los_y;
         d.lz = c->los_z;
       }
+      if (replay != nullptr) {  // the current mock of the batch columns
+        d.dev_n = &replay->state->count;
+        d.dev_first = &replay->state->first;
+      }
       return sort ? spatially_sorted(d, tag) : d;
     }
     if (c->memory != TRVG_MEM_HOST)
@@ -483,7 +522,7 @@ struct Engine {
     // transform with far less rounding, because the mean no longer builds
     // large partial sums on the k = 0 planes and axes inside the FFT.
     double hsum = 0.;
-    bool on_host = true;
+    bool on_host = replay == nullptr;  // replay: counts are on the device
     for (const Part& part : parts) {
       if (part.cat.w != nullptr || part.ws.use_ylm) on_host = false;
       hsum += part.ws.scale * double(part.cat.n);
@@ -523,6 +562,10 @@ struct Engine {
     if (mim) f.spec.im = r2c(mim, ".im");
     if (sre) f.spec.re_s = r2c(sre, ".sre");
     if (sim) f.spec.im_s = r2c(sim, ".sim");
+    if (replay != nullptr) {  // k = 0 modes formed on the device
+      launch_mock_k0(ctx, replay->state, sums);
+      return f;
+    }
     vector<double> hs = download(sums, 4);
     for (int i = 0; i < 4; ++i) f.sums[i] = hs[i];
     return f;
@@ -643,7 +686,8 @@ struct Engine {
     const int smax_all = *std::max_element(smax.begin(), smax.end());
     const Cube cube = make_cube(double(smax_all + 1) * dk_sample);
     const StatsPlan& sp = stats_plan(hb, smin, smax, cube, ell, m);
-    double* dpk = ctx.buf<double>("st.pk", 2 * hb.nb);
+    // One sum buffer per degree: a replayed term reads both legs' sums.
+    double* dpk = ctx.buf<double>("st.pk." + std::to_string(ell), 2 * hb.nb);
     zero(dpk, 2 * hb.nb * sizeof(double));
     const int* off = static_cast<const int*>(ctx.buffers[sp.tag + ".off"].ptr);
     const uint32_t* list =
@@ -652,10 +696,21 @@ struct Engine {
         static_cast<const double2*>(ctx.buffers[sp.tag + ".coef"].ptr);
     if (cube_covers(fa, fb, cube))
       launch_stats_pk_cube(ctx, g, cube, ff_cube.cube, ff_cube.half, fa.k0,
-                           fb.k0, hb.nb, sp.max_count, off, list, coef, dpk);
+                           fb.k0, hb.nb, sp.max_count, off, list, coef, dpk,
+                           fa.k0_dev, fb.k0_dev);
+    else if (replay != nullptr)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Batch replay needs the float-float statistics path.");
     else
       launch_stats_pk<Real>(ctx, g, cube, fa, fb, hb.nb, sp.max_count, off,
                             list, coef, dpk);
+    if (replay != nullptr) {
+      Stats s;
+      s.dev_pk = dpk;
+      s.dev_nmodes = sp.dev_nmodes;
+      s.dev_snsum = sp.dev_snsum;
+      return s;
+    }
     const vector<double> pk = download(dpk, 2 * hb.nb);
     Stats s;
     s.nmodes = sp.nmodes;
@@ -737,6 +792,10 @@ struct Engine {
       off[b + 1] = off[b] + int(sp.nmodes[b]);
       sp.max_count = std::max(sp.max_count, int(sp.nmodes[b]));
     }
+    vector<double> nm_d(nb);
+    for (int b = 0; b < nb; ++b) nm_d[b] = double(sp.nmodes[b]);
+    sp.dev_nmodes = upload(sp.tag + ".nmodes_d", nm_d);
+    sp.dev_snsum = upload(sp.tag + ".snsum", sp.snsum);
     const int* doff = upload(sp.tag + ".off", off);
     int* cursor = ctx.buf<int>(sp.tag + ".cur", nb);
     zero(cursor, nb * sizeof(int));
@@ -822,8 +881,12 @@ struct Engine {
       launch_twopt_field_real_f32(
           ctx, g, reinterpret_cast<const float2*>(fa.re),
           reinterpret_cast<const float2*>(fb.re), inv_alias_f,
-          float(shot.real()), p0f, reinterpret_cast<float2*>(hre));
+          float(shot.real()), p0f, reinterpret_cast<float2*>(hre), fa.k0_dev,
+          fb.k0_dev, replay ? replay->state->count_d : nullptr);
     } else {
+      if (replay != nullptr)
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Batch replay covers the FP32 real shot-noise field only.");
       launch_twopt_field<Real, XR>(ctx, g, fa, fb,
                                    cd{shot.real(), shot.imag()}, ax, hre,
                                    him);
@@ -927,6 +990,8 @@ struct Engine {
             static_cast<const float*>(xi.im), la, ma, lb, mb, sja, sjb, dka,
             dkb, np, out);
     }
+    dev_sij = out;
+    if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));
     vector<double> h = download(out, 2 * size_t(np));
     vector<cplx> res(np);
     for (int i = 0; i < np; ++i)
@@ -1165,6 +1230,7 @@ struct Engine {
                double(2 * kg + 1) * (2 * kg + 1) * (kg + 1)) +
         16. * 3. * double(hb.nb) * (K[0] + 1) * M[0] * M[1] * 2. +
         8. * mc * (2. * hb.nb + 1.);
+    if (replay != nullptr) return ff_taken;  // as in the warm-up estimate
     size_t free_b = 0, total_b = 0;
     TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     return bytes < 0.6 * double(free_b);
@@ -1224,7 +1290,8 @@ struct Engine {
     float4* Y2 = ctx.buf<float4>("ff.Y2", yn);
 
     float4* EG = ctx.buf<float4>("ff.EG", plane_g);
-    launch_ff_build_G(ctx, g, M, cube, kg, inv_win_ff, src.k0, EG);
+    launch_ff_build_G(ctx, g, M, cube, kg, inv_win_ff, src.k0, EG,
+                      src.k0_dev);
     const int64_t ld = ff_field_stride(Mc);
     float* G = ctx.buf<float>("ff.G", size_t(ld));
     float* Gl = ctx.buf<float>("ff.G.lo", size_t(ld));
@@ -1246,7 +1313,7 @@ struct Engine {
       const int16_t* tab = shell_table(M, K, lo, hi, dlo, dhi, hmax);
       float4* E = ctx.buf<float4>(tag + ".E", size_t(nb) * plane_f);
       launch_ff_build_F(ctx, g, M, cube, kg, k, tab, nb, leg.ell, inv_win_ff,
-                        src.k0, E);
+                        src.k0, E, src.k0_dev);
       float* out = ctx.buf<float>(tag + ".F", 2 * size_t(nb) * ld);
       launch_ff_inverse(ctx, M, nb, k, k, E, Y1, Y2, out,
                         out + size_t(nb) * ld, ld);
@@ -1270,6 +1337,9 @@ struct Engine {
     zero(dout, 2 * np * sizeof(double));
     launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
                            dout);
+    ff_taken = true;
+    dev_pairs = dout;
+    if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));
     const vector<double> h = download(dout, 2 * size_t(np));
     vector<cplx> res(np);
     for (int i = 0; i < np; ++i) res[i] = cplx(h[2 * i], h[2 * i + 1]);
@@ -1304,6 +1374,7 @@ struct Engine {
       if (real && ff_applicable(src, gsrc, la, lb, pairs, hb, M, K))
         return pair_sums_ff(src, la, lb, pairs, hb, M, K);
     }
+    if (replay == nullptr) ff_taken = false;
     const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
     const FR* Gr = real ? build_G_real<FR>(gsrc, M, Kg) : nullptr;
     if (wide_angle) {  // 3PCF window: G is on the full mesh
@@ -1438,10 +1509,14 @@ struct Engine {
                   out ? out->dim : -1, ndv);
     const vector<Term> terms = survey ? orders_lpp(p.ell1, p.ell2, p.ELL)
                                       : orders_gpp(p.ell1, p.ell2, p.ELL);
+    if (replay != nullptr && survey)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Batch replay covers periodic-box bispectra only.");
     const DevCatalogue dd = upload_catalogue(data, "data", survey);
     DevCatalogue dr;
     if (survey) dr = upload_catalogue(rand, "rand", true);
-    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+    if (replay == nullptr)
+      TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
 
     auto ylm_ws = [](double scale, int power, int ell, int m, bool conj) {
       WeightSpec w;
@@ -1456,7 +1531,15 @@ struct Engine {
 
     // delta n_00 and N_00 (gpp: one unit-weight assignment serves both).
     FieldSpec<Real> dn, nf;
-    if (!survey) {
+    if (!survey && replay != nullptr) {
+      // The mock's k = 0 modes are formed on the device (batch.cu).
+      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      dn = base.spec;
+      nf = base.spec;
+      dn.k0_set = nf.k0_set = true;
+      dn.k0_dev = replay->state->k0_dn;
+      nf.k0_dev = replay->state->k0_nf;
+    } else if (!survey) {
       Field base = make_field("N", {{dd, WeightSpec()}}, false);
       const double nbar = double(dd.n) / g.vol;
       dn = k0_view(base, -nbar * g.vol);
@@ -1529,6 +1612,39 @@ struct Engine {
       Leg la{p.ell1, t.m1}, lb{p.ell2, t.m2};
       const vector<cplx> comp =
           pair_sums(dn, dnLM, la, lb, pairs, hb, no_radii, M, K, Kg);
+      if (replay != nullptr) {
+        // The same combinations on the device (batch.cu).
+        MockTermArgs a{};
+        a.ndv = ndv;
+        a.prow = replay->prow;
+        a.pcol = replay->pcol;
+        a.nmodes = replay->nmodes;
+        a.comp = dev_pairs;
+        a.fac = fac;
+        a.coupling = t.coupling;
+        a.vol_cell = g.vol_cell;
+        a.mirror = mirror;
+        a.mirror_w3j = mirror_w3j;
+        a.phase_re = phase.real();
+        a.phase_im = phase.imag();
+        a.sn_const = p.ell1 == 0 && p.ell2 == 0;
+        Stats st_row, st_col;
+        if (p.ell2 == 0) st_row = twopt_stats(hb, dn, NLM, Sbar, p.ell1, t.m1);
+        if (p.ell1 == 0)
+          st_col = (p.ell2 == 0 && t.m1 == t.m2)
+                       ? st_row
+                       : twopt_stats(hb, dn, NLM, Sbar, p.ell2, t.m2);
+        a.pk_row = st_row.dev_pk;
+        a.nst_row = st_row.dev_nmodes;
+        a.snsum_row = st_row.dev_snsum;
+        a.pk_col = st_col.dev_pk;
+        a.nst_col = st_col.dev_nmodes;
+        a.snsum_col = st_col.dev_snsum;
+        shotnoise_pairs(xi, p.ell1, t.m1, p.ell2, t.m2, sja, sjb, ka, kbv);
+        a.sij = dev_sij;
+        launch_mock_term(ctx, replay->state, a, replay->acc);
+        continue;
+      }
       for (int i = 0; i < ndv; ++i) {
         const cplx B = comp[i] * fac /
                        (double(nmodes[pairs[i].row]) *
@@ -1569,6 +1685,11 @@ struct Engine {
       }
     }
 
+    if (replay != nullptr) {
+      launch_mock_store(ctx, replay->state, replay->acc, ndv, replay->raw,
+                        replay->shot);
+      return;
+    }
     for (int i = 0; i < ndv; ++i) {
       const Pair& q = pairs[i];
       out->coord1_bin[i] = hb.centre[q.row];
@@ -1582,6 +1703,164 @@ struct Engine {
       out->raw[2 * i + 1] = r.imag();
       out->shot[2 * i] = s.real();
       out->shot[2 * i + 1] = s.imag();
+    }
+  }
+
+  // -------------------------------------------------------------------------
+  // A batch of periodic-box bispectra: columns concatenated, mock i at
+  // [offsets[i], offsets[i + 1]).  FP32-mixed batches of three or more mocks
+  // on the float-float path run their largest mock as an ordinary estimate
+  // (building every cached table and sizing every buffer), capture one more
+  // mock into a CUDA graph whose kernels read the mock's count, offset and
+  // k = 0 modes from device memory (batch.cu), and replay it for the rest;
+  // the results are read back once.  Other batches run mock by mock.
+  // -------------------------------------------------------------------------
+  void bispec_batch(const trvg_catalogue* cat, int n_mocks,
+                    const int64_t* offsets, const trvg_binning* kb,
+                    const double* norms, trvg_threept_out* outs) {
+    auto slice = [&](const trvg_catalogue& all, int i) {
+      trvg_catalogue c = all;
+      const int64_t o = offsets[i];
+      c.n = offsets[i + 1] - o;
+      c.x = all.x + o;
+      c.y = all.y + o;
+      c.z = all.z + o;
+      if (all.w != nullptr) c.w = all.w + o;
+      return c;
+    };
+    auto eager = [&](const trvg_catalogue& all, int i) {
+      const trvg_catalogue c = slice(all, i);
+      bispec(&c, nullptr, 1., kb, norms[i], &outs[i], false);
+    };
+    const bool use_graph = sizeof(Real) == 4 && n_mocks >= 3 &&
+                           ctx.graph_batch && !ctx.profiling;
+    if (!use_graph) {
+      for (int i = 0; i < n_mocks; ++i) eager(*cat, i);
+      return;
+    }
+    // Device columns for the whole batch.
+    trvg_catalogue all = *cat;
+    if (cat->memory == TRVG_MEM_HOST && cat->n > 0) {
+      auto put = [&](const double* h, const char* nm) -> const double* {
+        if (h == nullptr) return nullptr;
+        double* d = ctx.buf<double>(std::string("batch.") + nm,
+                                    size_t(cat->n));
+        TRVG_CUDA(cudaMemcpyAsync(d, h, size_t(cat->n) * sizeof(double),
+                                  cudaMemcpyHostToDevice, ctx.stream));
+        ctx.h2d_bytes += cat->n * int64_t(sizeof(double));
+        return d;
+      };
+      all.x = put(cat->x, "x");
+      all.y = put(cat->y, "y");
+      all.z = put(cat->z, "z");
+      all.w = put(cat->w, "w");
+      all.memory = TRVG_MEM_DEVICE;
+    }
+    int imax = 0;
+    for (int i = 1; i < n_mocks; ++i)
+      if (offsets[i + 1] - offsets[i] > offsets[imax + 1] - offsets[imax])
+        imax = i;
+    eager(all, imax);
+    if (!ff_taken) {
+      for (int i = 0; i < n_mocks; ++i)
+        if (i != imax) eager(all, i);
+      return;
+    }
+    const HostBins hb = host_bins(kb);
+    const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
+    const int ndv = int(pairs.size());
+    vector<long long> nmodes;
+    vector<double> keff;
+    count_modes(hb, nmodes, keff);
+    vector<int64_t> order;
+    for (int i = 0; i < n_mocks; ++i)
+      if (i != imax) order.push_back(i);
+    vector<int> prow(ndv), pcol(ndv);
+    for (int i = 0; i < ndv; ++i) {
+      prow[i] = pairs[i].row;
+      pcol[i] = pairs[i].col;
+    }
+    vector<double> nm_d(nmodes.begin(), nmodes.end());
+    Replay r;
+    const int64_t* d_order = upload("batch.order", order);
+    const int64_t* d_off = upload(
+        "batch.offsets", vector<int64_t>(offsets, offsets + n_mocks + 1));
+    const double* d_norm =
+        upload("batch.norms", vector<double>(norms, norms + n_mocks));
+    r.prow = upload("batch.prow", prow);
+    r.pcol = upload("batch.pcol", pcol);
+    r.nmodes = upload("batch.nmodes", nm_d);
+    r.state = static_cast<MockState*>(
+        ctx.buffer("batch.state", sizeof(MockState)));
+    zero(r.state, sizeof(MockState));
+    r.acc = ctx.buf<double>("batch.acc", 4 * size_t(ndv));
+    r.raw = ctx.buf<double>("batch.raw", 2 * size_t(ndv) * n_mocks);
+    r.shot = ctx.buf<double>("batch.shot", 2 * size_t(ndv) * n_mocks);
+    sync();
+
+    // Capture one mock.  The catalogue handed to the capture is the whole
+    // batch with the largest count (grid sizes); the kernels read the
+    // current mock from r.state.
+    trvg_catalogue capt = all;
+    capt.n = offsets[imax + 1] - offsets[imax];
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int64_t launches0 = ctx.kernel_launches, ffts0 = ctx.fft_launches;
+    replay = &r;
+    TRVG_CUDA(cudaStreamBeginCapture(ctx.stream,
+                                     cudaStreamCaptureModeRelaxed));
+    bool captured = true;
+    try {
+      launch_mock_begin(ctx, r.state, d_order, d_off, d_norm, r.acc, 4 * ndv);
+      bispec(&capt, nullptr, 1., kb, 1., &outs[imax], false);
+    } catch (const Error& err) {
+      captured = false;
+      ctx.log(10, "batch capture abandoned (%s); mock by mock instead",
+              err.what());
+    }
+    replay = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx.stream, &graph);
+    if (captured && ce == cudaSuccess && graph != nullptr &&
+        cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+      const int64_t per_mock = ctx.kernel_launches - launches0;
+      const int64_t ffts = ctx.fft_launches - ffts0;
+      for (size_t k = 0; k < order.size(); ++k)
+        TRVG_CUDA(cudaGraphLaunch(exec, ctx.stream));
+      ctx.kernel_launches += per_mock * int64_t(order.size() - 1);
+      ctx.fft_launches += ffts * int64_t(order.size() - 1);
+      ctx.graph_replays = int64_t(order.size());
+    } else {
+      captured = false;
+    }
+    (void)cudaGetLastError();
+    if (exec != nullptr) cudaGraphExecDestroy(exec);
+    if (graph != nullptr) cudaGraphDestroy(graph);
+    if (!captured) {
+      for (int64_t i : order) eager(all, int(i));
+      return;
+    }
+    const vector<double> raw = download(r.raw, 2 * size_t(ndv) * n_mocks);
+    const vector<double> shot = download(r.shot, 2 * size_t(ndv) * n_mocks);
+    const trvg_threept_out& ref = outs[imax];
+    for (int64_t m : order) {
+      trvg_threept_out& o = outs[m];
+      if (o.dim != ndv)
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Output data vector has dimension %d, expected %d.",
+                    o.dim, ndv);
+      for (int i = 0; i < ndv; ++i) {
+        o.coord1_bin[i] = ref.coord1_bin[i];
+        o.coord2_bin[i] = ref.coord2_bin[i];
+        o.coord1_eff[i] = ref.coord1_eff[i];
+        o.coord2_eff[i] = ref.coord2_eff[i];
+        o.count_1[i] = ref.count_1[i];
+        o.count_2[i] = ref.count_2[i];
+        const size_t q = (size_t(m) * ndv + i) * 2;
+        o.raw[2 * i] = raw[q];
+        o.raw[2 * i + 1] = raw[q + 1];
+        o.shot[2 * i] = shot[q];
+        o.shot[2 * i + 1] = shot[q + 1];
+      }
     }
   }
 
@@ -2139,17 +2418,7 @@ int trvg_compute_bispec_in_gpp_box_batch(
       trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
                         "Batch offsets must not decrease.");
   run(ctx, params, false, [&](auto& e) {
-    for (int i = 0; i < n_mocks; ++i) {
-      // Mock i: the slice [offsets[i], offsets[i + 1]) of every column.
-      trvg_catalogue c = *particles;
-      const int64_t o = offsets[i];
-      c.n = offsets[i + 1] - o;
-      c.x = particles->x + o;
-      c.y = particles->y + o;
-      c.z = particles->z + o;
-      if (particles->w != nullptr) c.w = particles->w + o;
-      e.bispec(&c, nullptr, 1., kbinning, norm_factors[i], &outs[i], false);
-    }
+    e.bispec_batch(particles, n_mocks, offsets, kbinning, norm_factors, outs);
   });
   TRVG_API_END
 }

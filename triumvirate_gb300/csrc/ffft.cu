@@ -492,8 +492,16 @@ __device__ __forceinline__ FF inv_window(const FFBuild& b, const Geom& g,
 
 // E[c][b][a] (c in [0, Kg], (a, b) on the M grid) of G: the cube values
 // with |sx|, |sy| <= Kg, times 1 / (W V); k = 0 from `k0`.
+__device__ __forceinline__ FFC k0_value(FFC k0, const double* k0_dev) {
+  return k0_dev != nullptr
+             ? FFC{ff_from_double(k0_dev[0]), ff_from_double(k0_dev[1])}
+             : k0;
+}
+
 __global__ void ff_build_G_kernel(Geom g, FFBuild bd, const float4* cube,
-                                  int Kg, FFC k0, float4* E) {
+                                  int Kg, FFC k0h, const double* k0_dev,
+                                  float4* E) {
+  const FFC k0 = k0_value(k0h, k0_dev);
   const int64_t count = int64_t(Kg + 1) * bd.M1 * bd.M0;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
        t += int64_t(gridDim.x) * blockDim.x) {
@@ -514,8 +522,9 @@ __global__ void ff_build_G_kernel(Geom g, FFBuild bd, const float4* cube,
 // E[q][c][b][a] (c in [0, K]) of the shell fields: each mode of shell q
 // (from the table on the M half grid) times y_l0(k) / W; E is zeroed first.
 __global__ void ff_build_F_kernel(Geom g, FFBuild bd, int M2, const float4* cube,
-                                  int K, const int16_t* tab, int ell, FFC k0,
-                                  float4* E) {
+                                  int K, const int16_t* tab, int ell, FFC k0h,
+                                  const double* k0_dev, float4* E) {
+  const FFC k0 = k0_value(k0h, k0_dev);
   const int64_t plane = int64_t(K + 1) * bd.M1 * bd.M0;
   const int Mh = M2 / 2 + 1;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < plane;
@@ -842,7 +851,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
 
 void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, const float2* const iw[3],
-                       cd k0, float4* E) {
+                       cd k0, float4* E, const double* k0_dev) {
   FFBuild bd{M[0], M[1], Kg, {iw[0], iw[1], iw[2]},
              FF{float(1. / g.vol), float(1. / g.vol - double(float(1. / g.vol)))}};
   const FFC k0f{FF{float(k0.re), float(k0.re - double(float(k0.re)))},
@@ -850,14 +859,14 @@ void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
   const int64_t count = int64_t(Kg + 1) * M[1] * M[0];
   TRVG_KBEGIN(ctx, "ff_build_kernel");
   ff_build_G_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
-      g, bd, cube, Kg, k0f, E);
+      g, bd, cube, Kg, k0f, k0_dev, E);
   TRVG_LAUNCHED(ctx);
 }
 
 void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, int K, const int16_t* tab,
                        int nq, int ell, const float2* const iw[3], cd k0,
-                       float4* E) {
+                       float4* E, const double* k0_dev) {
   FFBuild bd{M[0], M[1], Kg, {iw[0], iw[1], iw[2]}, FF{0.f, 0.f}};
   const FFC k0f{FF{float(k0.re), float(k0.re - double(float(k0.re)))},
                 FF{float(k0.im), float(k0.im - double(float(k0.im)))}};
@@ -866,7 +875,7 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                             ctx.stream));
   TRVG_KBEGIN(ctx, "ff_build_kernel");
   ff_build_F_kernel<<<grid_for(plane, 256), 256, 0, ctx.stream>>>(
-      g, bd, M[2], cube, K, tab, ell, k0f, E);
+      g, bd, M[2], cube, K, tab, ell, k0f, k0_dev, E);
   TRVG_LAUNCHED(ctx);
 }
 

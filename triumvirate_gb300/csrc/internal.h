@@ -108,6 +108,9 @@ struct StatsPlan {
   std::vector<long long> nmodes;
   std::vector<double> ksum;
   std::vector<double> snsum;  // re, im per bin
+  // Device copies of nmodes (as doubles) and snsum for replayed batches.
+  const double* dev_nmodes = nullptr;
+  const double* dev_snsum = nullptr;
 };
 
 struct Context {
@@ -133,6 +136,10 @@ struct Context {
   bool sort_catalogue = true;
   // FP32-mixed: float-float transforms of the shell fields.
   bool ff_transforms = true;
+  // Batches: replay one captured mock as a CUDA graph (batch.cu).
+  bool graph_batch = true;
+  // Mocks replayed from the captured graph by the last batch call.
+  int64_t graph_replays = 0;
   // Deposits made so far (FieldSpec::mesh_gen).
   int64_t mesh_gen = 0;
   // Profiling: per-launch events of the current call, per-name totals of

@@ -29,7 +29,7 @@ struct Geom {
 
 // Particle arrays in device memory.
 struct DevCatalogue {
-  int64_t n = 0;
+  int64_t n = 0;  // particle count (the largest count in a replayed batch)
   const double* x = nullptr;
   const double* y = nullptr;
   const double* z = nullptr;
@@ -37,6 +37,16 @@ struct DevCatalogue {
   const double* lx = nullptr;
   const double* ly = nullptr;
   const double* lz = nullptr;
+  // Replayed batches: the current mock's count and first particle are read
+  // on the device (the columns then start at x + *dev_first).
+  const int64_t* dev_n = nullptr;
+  const int64_t* dev_first = nullptr;
+  __device__ __forceinline__ int64_t count() const {
+    return dev_n != nullptr ? *dev_n : n;
+  }
+  __device__ __forceinline__ int64_t first() const {
+    return dev_first != nullptr ? *dev_first : 0;
+  }
 };
 
 // Per-particle weight scale * w^power * [conj] y_lm(los).
@@ -60,6 +70,8 @@ struct FieldSpec {
   const C* im_s = nullptr;
   cd k0 = {0., 0.};
   bool k0_set = false;
+  // Replayed batches: the k = 0 mode (re, im) in device memory instead.
+  const double* k0_dev = nullptr;
   // The real FP32 mesh the spectrum came from (real fields without
   // interlacing), valid while mesh_gen equals the context's counter.
   const Real* mesh = nullptr;
@@ -208,7 +220,8 @@ void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
                           const float4* ffcube, int Kc, cd k0a, cd k0b,
                           int nbins, int max_count, const int* off,
                           const uint32_t* list, const double2* coef,
-                          double* pk);
+                          double* pk, const double* k0a_dev = nullptr,
+                          const double* k0b_dev = nullptr);
 
 template <class Real>
 void launch_twopt_stats(Context& ctx, const Geom& g, const Cube& cube,
@@ -230,7 +243,10 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
 void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
                                  const float2* fa, const float2* fb,
                                  const float* const inv_alias[3], float shot,
-                                 float2 p0, float2* out);
+                                 float2 p0, float2* out,
+                                 const double* k0a = nullptr,
+                                 const double* k0b = nullptr,
+                                 const double* shotp = nullptr);
 
 // ---- reduce.cu -----------------------------------------------------------
 template <class Real>
@@ -273,13 +289,14 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
                             int Kg, float4* T1, float4* T2, float4* cube);
 // Evaluation-grid half spectra E[c][b][a] of G (planes c <= Kg) and
 // E[q][c][b][a] of nq shell fields (planes c <= K) from the cube.
+// k0_dev (re, im in device memory), when given, replaces the host k0.
 void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, const float2* const iw[3],
-                       cd k0, float4* E);
+                       cd k0, float4* E, const double* k0_dev = nullptr);
 void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, int K, const int16_t* tab,
                        int nq, int ell, const float2* const iw[3], cd k0,
-                       float4* E);
+                       float4* E, const double* k0_dev = nullptr);
 // Real fields on the M grid of nf half spectra E with planes c <= Kcf and
 // band |sx|, |sy| <= Kf, as float-float words: field f at out + f ld (hi)
 // and out_lo + f ld, cells [a][b][z] (Y1, Y2: scratch of
@@ -297,6 +314,50 @@ void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,
                             const float* Fah, const float* Fal,
                             const float* Fbh, const float* Fbl, const int* pa,
                             const int* pb, int npairs, double* out);
+
+// ---- batch.cu ------------------------------------------------------------
+// Scalars of the current mock of a replayed batch (device memory).
+struct MockState {
+  int64_t index;      // position in the replay order
+  int64_t mock;       // mock number order[index]
+  int64_t first;      // first particle of the mock
+  int64_t count;      // particle count
+  double count_d[2];  // (count, 0): unit-weight deposit and S-bar
+  double k0_dn[2];    // k = 0 mode of delta n: deposit - count
+  double k0_nf[2];    // k = 0 mode of N: the deposit
+  double norm;        // normalisation
+};
+
+// Per-term inputs of the host's B and shot-noise combinations: pair sums
+// `comp`, statistics sums of the row / column legs (null when unused) with
+// their plans' mode counts and shot weights, and shot-noise pair sums.
+struct MockTermArgs {
+  int ndv;
+  const int* prow;
+  const int* pcol;
+  const double* nmodes;  // shell mode counts per bin
+  const double* comp;    // 2 ndv
+  double fac, coupling, vol_cell, mirror, mirror_w3j, phase_re, phase_im;
+  bool sn_const;         // ell1 = ell2 = 0: + coupling S-bar
+  const double* pk_row;
+  const double* nst_row;
+  const double* snsum_row;
+  const double* pk_col;
+  const double* nst_col;
+  const double* snsum_col;
+  const double* sij;     // 2 ndv, before the cell volume
+};
+
+// acc: 4 ndv doubles (B re, im; shot re, im), zeroed by mock_begin.
+void launch_mock_begin(Context& ctx, MockState* st, const int64_t* order,
+                       const int64_t* offsets, const double* norms,
+                       double* acc, int nacc);
+void launch_mock_k0(Context& ctx, MockState* st, const double* sums);
+void launch_mock_term(Context& ctx, const MockState* st,
+                      const MockTermArgs& a, double* acc);
+// raw, shot: [mock][ndv] complex, times the mock's norm; advances index.
+void launch_mock_store(Context& ctx, MockState* st, const double* acc,
+                       int ndv, double* raw, double* shot);
 
 // ---- adjoint.cu ----------------------------------------------------------
 // Cotangent bookkeeping of the bispectrum adjoint: the partners of bin a in

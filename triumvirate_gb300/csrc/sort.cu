@@ -27,11 +27,12 @@ __device__ __forceinline__ int cell_of(double x, int n, double ratio) {
 __global__ void tile_key_kernel(DevCatalogue cat, int n0, int n1, int n2,
                                 double r0, double r1, double r2, int t1,
                                 int t2, int* key, int* rank, int* count) {
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < cat.n;
+  const int64_t np = cat.count(), p0 = cat.first();
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < np;
        p += int64_t(gridDim.x) * blockDim.x) {
-    const int tx = cell_of(cat.x[p], n0, r0) >> kTileShift;
-    const int ty = cell_of(cat.y[p], n1, r1) >> kTileShift;
-    const int tz = cell_of(cat.z[p], n2, r2) >> kTileShift;
+    const int tx = cell_of(cat.x[p0 + p], n0, r0) >> kTileShift;
+    const int ty = cell_of(cat.y[p0 + p], n1, r1) >> kTileShift;
+    const int tz = cell_of(cat.z[p0 + p], n2, r2) >> kTileShift;
     const int k = (tx * t1 + ty) * t2 + tz;
     key[p] = k;
     rank[p] = atomicAdd(count + k, 1);
@@ -108,17 +109,19 @@ struct SortedOut {
 __global__ void scatter_kernel(DevCatalogue in, const int* key,
                                const int* rank, const int* offset,
                                SortedOut out) {
-  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < in.n;
+  const int64_t np = in.count(), p0 = in.first();
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < np;
        p += int64_t(gridDim.x) * blockDim.x) {
     const int64_t d = int64_t(offset[key[p]]) + rank[p];
-    out.x[d] = in.x[p];
-    out.y[d] = in.y[p];
-    out.z[d] = in.z[p];
-    if (out.w != nullptr) out.w[d] = in.w[p];
+    const int64_t q = p0 + p;
+    out.x[d] = in.x[q];
+    out.y[d] = in.y[q];
+    out.z[d] = in.z[q];
+    if (out.w != nullptr) out.w[d] = in.w[q];
     if (out.lx != nullptr) {
-      out.lx[d] = in.lx[p];
-      out.ly[d] = in.ly[p];
-      out.lz[d] = in.lz[p];
+      out.lx[d] = in.lx[q];
+      out.ly[d] = in.ly[q];
+      out.lz[d] = in.lz[q];
     }
   }
 }
@@ -188,6 +191,7 @@ DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
   d.lx = o.lx;
   d.ly = o.ly;
   d.lz = o.lz;
+  d.dev_n = in.dev_n;  // the sorted copy starts at its first element
   return d;
 }
 

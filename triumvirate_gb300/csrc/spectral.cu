@@ -403,11 +403,13 @@ struct CubeModes {
   const float4* cube;
   int Kc;
   cd k0a, k0b;
+  const double* k0a_dev;  // device k = 0 values of a replayed batch
+  const double* k0b_dev;
   __device__ __forceinline__ void values(const Geom&, int sx, int sy, int sz,
                                          cd& va, cd& vb) const {
     if (sx == 0 && sy == 0 && sz == 0) {
-      va = k0a;
-      vb = k0b;
+      va = k0a_dev ? cd{k0a_dev[0], k0a_dev[1]} : k0a;
+      vb = k0b_dev ? cd{k0b_dev[0], k0b_dev[1]} : k0b;
       return;
     }
     const bool neg = sz < 0;
@@ -807,7 +809,17 @@ __global__ void __launch_bounds__(256)
 twopt_field_real_f32_kernel(uint32_t nhalf, int n1, int nzh, const float2* fa,
                             const float2* fb, const float* iax,
                             const float* iay, const float* iaz, float shot,
-                            float inv_vol, float2 p0, float2* out) {
+                            float inv_vol, float2 p0, const double* k0a,
+                            const double* k0b, const double* shotp,
+                            double vol, float2* out) {
+  if (k0a != nullptr) {
+    // The k = 0 modes and S of the current mock, from device memory:
+    // (a0 conj(b0) - S) / V as for the host values.
+    const double ar = k0a[0], ai = k0a[1], br = k0b[0], bi = k0b[1];
+    shot = float(shotp[0]);
+    p0 = make_float2(float((ar * br + ai * bi - shotp[0]) / vol),
+                     float((ai * br - ar * bi - shotp[1]) / vol));
+  }
   const bool same = fa == fb;  // |f|^2: one read of the spectrum
   const uint32_t npair = nhalf / 2;
   for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < npair;
@@ -912,14 +924,16 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
 void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
                                  const float2* fa, const float2* fb,
                                  const float* const inv_alias[3], float shot,
-                                 float2 p0, float2* out) {
+                                 float2 p0, float2* out, const double* k0a,
+                                 const double* k0b, const double* shotp) {
   if (g.nhalf >= (int64_t(1) << 32))
     throw_error(TRVG_ERR_INVALID_PARAMETER, "Mesh too large.");
   TRVG_KBEGIN(ctx, "twopt_field_kernel");
   twopt_field_real_f32_kernel<<<grid_for(g.nhalf / 2, 256), 256, 0,
                                 ctx.stream>>>(
       uint32_t(g.nhalf), g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1],
-      inv_alias[2], shot, float(1. / g.vol), p0, out);
+      inv_alias[2], shot, float(1. / g.vol), p0, k0a, k0b, shotp, g.vol,
+      out);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -1001,12 +1015,14 @@ void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
                           const float4* ffcube, int Kc, cd k0a, cd k0b,
                           int nbins, int max_count, const int* off,
                           const uint32_t* list, const double2* coef,
-                          double* pk) {
+                          double* pk, const double* k0a_dev,
+                          const double* k0b_dev) {
   if (nbins <= 0 || max_count <= 0) return;
   const int bx = int(std::min<int64_t>((max_count + 1023) / 1024, 64));
   TRVG_KBEGIN(ctx, "twopt_stats_kernel");
   stats_pk_kernel<<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
-      g, cube, CubeModes{ffcube, Kc, k0a, k0b}, off, list, coef, pk);
+      g, cube, CubeModes{ffcube, Kc, k0a, k0b, k0a_dev, k0b_dev}, off, list,
+      coef, pk);
   TRVG_LAUNCHED(ctx);
 }
 
