@@ -454,7 +454,8 @@ def run_gb300(args):
         "dtype": "f32 meshes/FFTs, f64 offsets/Ylm/reductions/shot noise",
         "data": "synthetic (seeded uniform catalogue)",
         "config": {**workload(args), "parallelism": f"replicas x{world}",
-                   "evaluation_grid": list(st.get('pruned_grid', []))},
+                   "evaluation_grid": list(st.get('pruned_grid', [])),
+                   "autotuned": ctx.tuned()},
         "e2e": {"value": round(value_e2e, 6), "unit": UNIT,
                 "h2d_bytes_per_step": int(st_e2e['h2d_bytes']),
                 "d2h_bytes_per_step": int(res32['k1_bin'].size * 72)},
@@ -632,6 +633,7 @@ def run_mocks(args):
         return statistics.median(times)
 
     t = timed_batches(args.steps)
+    graph_replays = ctx.stats()['graph_replays']
 
     # Accuracy against FP64 on the first mocks, and the same workload with
     # the FP32 cuFFT transforms instead of the float-float ones.
@@ -684,7 +686,11 @@ def run_mocks(args):
                                 f"(total {ntot}), {MOCK_NGRID}^3 mesh, CIC, "
                                 "L=1000 Mpc/h, B_000 and B_202 diag, 24 lin "
                                 "bins 0.005-0.245 h/Mpc"),
-                   "batching": "one library call per multipole"},
+                   "batching": "one library call per multipole; the "
+                               "largest mock warms up, the others replay "
+                               "one captured CUDA graph",
+                   "graph_replays_per_call": graph_replays,
+                   "autotuned": ctx.tuned()},
         "kernel_ms_per_mock": per_kernel,
         "max_rel_err_vs_fp64": {"mocks": nchk, **err_ff},
         "fp32_cufft_variant": {"mocks_per_s": round(args.mocks / t_fp32fft, 2),

@@ -202,8 +202,16 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           in float-float arithmetic (default 1);
  *   "graph_batch"      0/1: FP32-mixed batches: capture one mock as a CUDA
  *                           graph and replay it for the others (default 1;
- *                           off while profiling). */
+ *                           off while profiling);
+ *   "autotune"         0/1: time candidate launch shapes (catalogue-sort
+ *                           tile side, pair-reduction bin batch) on first
+ *                           use and keep the fastest (default 1; 0 also
+ *                           forgets earlier choices). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
+/* Launch shapes the autotuner chose so far: key and value. */
+int trvg_tuned_count(const trvg_context* ctx, int* count);
+int trvg_tuned_get(const trvg_context* ctx, int index, char* key,
+                   int key_len, int64_t* value);
 /* Per-kernel device time of the last call (profiling on). */
 int trvg_kernel_time_count(const trvg_context* ctx, int* count);
 int trvg_kernel_time_get(const trvg_context* ctx, int index, char* name,

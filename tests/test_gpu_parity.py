@@ -649,6 +649,33 @@ def test_batch_graph_replay_matches_single_calls(degrees):
             assert np.max(np.abs(b[k] - s64[k])) / scale < 1e-5, (i, k)
 
 
+def test_autotuner_picks_candidates_and_keeps_results():
+    """The tuned sort tile and pair bin batch come from their candidate
+    sets and change nothing beyond FP32 deposit order."""
+    box = 1000.
+    cat = ParticleCatalogue(*_uniform(80000, box, 7).T, nz=80000 / box ** 3)
+    kw = dict(degrees=(0, 0, 0), form='diag',
+              binning=Binning('fourier', 'lin', 0.005, 0.045, 4),
+              sampling_params=_sampling('fp32mixed', 64, box=box))
+    ctx = _lib.default_context(None)
+    ctx.set_option('autotune', 0)
+    ctx.set_option('autotune', 1)
+    tuned_res = compute_bispec_in_gpp_box(cat, **kw)
+    tuned = ctx.tuned()
+    tiles = [v for k, v in tuned.items() if k.startswith('sort_tile_shift')]
+    batches = [v for k, v in tuned.items() if k.startswith('pair_bin_batch')]
+    assert tiles and set(tiles) <= {2, 3, 4}
+    assert batches and set(batches) <= {4, 8, 16}
+    ctx.set_option('autotune', 0)
+    try:
+        plain = compute_bispec_in_gpp_box(cat, **kw)
+    finally:
+        ctx.set_option('autotune', 1)
+    for k in ('bk_raw', 'bk_shot'):
+        scale = np.max(np.abs(plain[k]))
+        assert np.max(np.abs(tuned_res[k] - plain[k])) / scale < 1e-6, k
+
+
 # ---------------------------------------------------------------------------
 # Float-float shell-field transforms (FP32-mixed default)
 # ---------------------------------------------------------------------------

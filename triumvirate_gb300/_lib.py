@@ -41,7 +41,7 @@ EXPORTED = [
     "trvg_kernel_time_count", "trvg_kernel_time_get",
     "trvg_calc_grid_based_powlaw_norm_noalloc",
     "trvg_compute_bispec_in_gpp_box_batch", "trvg_bispec_gpp_adjoint",
-    "trvg_compute_3pcf_window",
+    "trvg_compute_3pcf_window", "trvg_tuned_count", "trvg_tuned_get",
 ]
 
 
@@ -207,6 +207,8 @@ def _declare(lib):
     lib.trvg_reduced_ylm.argtypes = [ip, ip, P(dp), C.c_int64, P(dp)]
     lib.trvg_context_set_stream.argtypes = [vp, vp]
     lib.trvg_set_option.argtypes = [vp, C.c_char_p, C.c_int64]
+    lib.trvg_tuned_count.argtypes = [vp, P(ip)]
+    lib.trvg_tuned_get.argtypes = [vp, ip, C.c_char_p, ip, P(C.c_int64)]
     lib.trvg_kernel_time_count.argtypes = [vp, P(ip)]
     lib.trvg_kernel_time_get.argtypes = [vp, ip, C.c_char_p, ip, P(dp),
                                          P(C.c_int64)]
@@ -271,6 +273,19 @@ class Context:
             check(lib.trvg_kernel_time_get(self._h, i, buf, 64, C.byref(ms),
                                            C.byref(cnt)))
             out[buf.value.decode()] = (ms.value, cnt.value)
+        return out
+
+    def tuned(self) -> dict:
+        """{key: value} of the launch shapes the autotuner has chosen."""
+        lib = load()
+        n = C.c_int()
+        check(lib.trvg_tuned_count(self._h, C.byref(n)))
+        out = {}
+        buf = C.create_string_buffer(128)
+        for i in range(n.value):
+            v = C.c_int64()
+            check(lib.trvg_tuned_get(self._h, i, buf, 128, C.byref(v)))
+            out[buf.value.decode()] = v.value
         return out
 
     def release_workspace(self):

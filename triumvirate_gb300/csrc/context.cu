@@ -2,6 +2,7 @@
 // the host-side maths entry points of the C ABI.
 #include <cstdarg>
 #include <cstring>
+#include <iterator>
 #include <string>
 
 #include "internal.h"
@@ -272,6 +273,9 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     ctx->impl.ff_transforms = value != 0;
   } else if (k == "graph_batch") {
     ctx->impl.graph_batch = value != 0;
+  } else if (k == "autotune") {
+    ctx->impl.autotune = value != 0;
+    if (value == 0) ctx->impl.tuned.clear();
   } else {
     trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Unknown option '%s'.",
                       key);
@@ -299,6 +303,29 @@ int trvg_kernel_time_get(const trvg_context* ctx, int index, char* name,
   std::snprintf(name, size_t(name_len), "%s", kt[index].first.c_str());
   *ms = kt[index].second.first;
   *launches = kt[index].second.second;
+  TRVG_API_END
+}
+
+int trvg_tuned_count(const trvg_context* ctx, int* count) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || count == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  *count = int(ctx->impl.tuned.size());
+  TRVG_API_END
+}
+
+int trvg_tuned_get(const trvg_context* ctx, int index, char* key,
+                   int key_len, int64_t* value) {
+  TRVG_API_BEGIN
+  if (ctx == nullptr || key == nullptr || key_len <= 0 || value == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null argument.");
+  const auto& t = ctx->impl.tuned;
+  if (index < 0 || index >= int(t.size()))
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Index out of range.");
+  auto it = t.begin();
+  std::advance(it, index);
+  std::snprintf(key, size_t(key_len), "%s", it->first.c_str());
+  *value = it->second;
   TRVG_API_END
 }
 

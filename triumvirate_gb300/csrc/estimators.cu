@@ -500,10 +500,62 @@ struct Engine {
     return sort ? spatially_sorted(d, tag) : d;
   }
 
-  // Large catalogues are reordered by mesh tile before assignment.
+  // The project's autotuner: the fastest of `candidates` for `key`, timed
+  // once per context with CUDA events on the context's stream (`run(c)`
+  // issues one candidate's work; each is run twice and the second timed),
+  // then cached.  Replays, profiling and contexts with autotuning off take
+  // the cached choice or the first candidate.
+  template <class F>
+  int tuned(const std::string& key, const vector<int>& candidates, F&& run) {
+    auto it = ctx.tuned.find(key);
+    if (it != ctx.tuned.end()) return it->second;
+    if (replay != nullptr || !ctx.autotune || ctx.profiling ||
+        candidates.size() < 2)
+      return candidates.front();
+    cudaEvent_t e0, e1;
+    TRVG_CUDA(cudaEventCreate(&e0));
+    TRVG_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int pick = candidates.front();
+    for (size_t i = 0; i < candidates.size(); ++i) {
+      run(candidates[i]);
+      TRVG_CUDA(cudaEventRecord(e0, ctx.stream));
+      run(candidates[i]);
+      TRVG_CUDA(cudaEventRecord(e1, ctx.stream));
+      TRVG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      TRVG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (i == 0 || ms < best) {
+        best = ms;
+        pick = candidates[i];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx.tuned[key] = pick;
+    ctx.log(10, "autotune %s -> %d (%.4f ms)", key.c_str(), pick,
+            double(best));
+    return pick;
+  }
+
+  // Large catalogues are reordered by mesh tile before assignment; the
+  // tile side is tuned together with a trial deposit into the mesh buffer
+  // (which the field build overwrites next), where it matters.
   DevCatalogue spatially_sorted(const DevCatalogue& d, const std::string& tag) {
     if (d.n < (int64_t(1) << 16) || !ctx.sort_catalogue) return d;
-    return sort_catalogue(ctx, g, d, tag);
+    int lg = 0;
+    while ((int64_t(1) << (lg + 1)) <= d.n) ++lg;
+    char key[96];
+    std::snprintf(key, sizeof(key), "sort_tile_shift.%dx%dx%d.order%d.n2^%d",
+                  g.n[0], g.n[1], g.n[2], p.assignment_order, lg);
+    const int shift = tuned(key, {3, 2, 4}, [&](int sh) {
+      const DevCatalogue sd = sort_catalogue(ctx, g, d, tag, sh);
+      Real* m = ctx.buf<Real>("mesh.re", g.nmesh);
+      double* sums = ctx.buf<double>("assign.sums", 4);
+      launch_assign<Real>(ctx, g, p.assignment_order, false, sd,
+                          WeightSpec(), m, nullptr, nullptr, nullptr, sums);
+    });
+    return sort_catalogue(ctx, g, d, tag, shift);
   }
 
   // Assign all parts into one (complex if `cplx`) mesh, with the shadow when
@@ -1334,9 +1386,17 @@ struct Engine {
     const int* dpa = upload("pairs.a", pa);
     const int* dpb = upload("pairs.b", pb);
     double* dout = ctx.buf<double>("pairs.out", 2 * size_t(np));
+    char key[96];
+    std::snprintf(key, sizeof(key), "pair_bin_batch.%dx%dx%d.pairs%d.%s",
+                  M[0], M[1], M[2], np, shared ? "shared" : "two");
+    const int ppb = tuned(key, {8, 4, 16}, [&](int c) {
+      zero(dout, 2 * np * sizeof(double));
+      launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb,
+                             np, dout, c);
+    });
     zero(dout, 2 * np * sizeof(double));
     launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
-                           dout);
+                           dout, ppb);
     ff_taken = true;
     dev_pairs = dout;
     if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));

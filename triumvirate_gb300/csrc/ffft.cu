@@ -794,17 +794,38 @@ int radix_mask(const FFPlan& P) {
 template <int M>
 using RadixSet = std::integral_constant<int, M>;
 
-// Calls f with the specialised radix set that holds all radices of P:
-// powers of two for the mesh passes, {3, 5} and {2, 3} for the usual
-// evaluation grids, the generic kernels otherwise.
+// Calls f with the specialised radix set that holds all radices of P, or
+// the generic kernels.  Mesh passes (forward) see power-of-two lengths and
+// 3 * 2^k; evaluation-grid passes (inverse) the 5-smooth lengths of
+// good_fft_size.
+template <int... SETS>
+struct RadixSets {};
+
+template <class F, int FIRST, int... REST>
+void dispatch_radix(int m, F&& f, RadixSets<FIRST, REST...>) {
+  if ((m & ~FIRST) == 0) f(RadixSet<FIRST>{});
+  else dispatch_radix(m, f, RadixSets<REST...>{});
+}
 template <class F>
-void with_radix_set(const FFPlan& P, F&& f) {
-  const int m = radix_mask(P);
-  if ((m & ~kRadix8) == 0) f(RadixSet<kRadix8>{});
-  else if ((m & ~(kRadix8 | kRadix4)) == 0) f(RadixSet<kRadix8 | kRadix4>{});
-  else if ((m & ~(kRadix3 | kRadix5)) == 0) f(RadixSet<kRadix3 | kRadix5>{});
-  else if ((m & ~(kRadix2 | kRadix3)) == 0) f(RadixSet<kRadix2 | kRadix3>{});
-  else f(RadixSet<kRadixAll>{});
+void dispatch_radix(int, F&& f, RadixSets<>) {
+  f(RadixSet<kRadixAll>{});
+}
+
+template <class F>
+void with_mesh_radix_set(const FFPlan& P, F&& f) {
+  dispatch_radix(radix_mask(P), f,
+                 RadixSets<kRadix8, kRadix8 | kRadix4, kRadix8 | kRadix2,
+                           kRadix8 | kRadix2 | kRadix3>{});
+}
+
+template <class F>
+void with_grid_radix_set(const FFPlan& P, F&& f) {
+  dispatch_radix(radix_mask(P), f,
+                 RadixSets<kRadix3 | kRadix5, kRadix2 | kRadix3,
+                           kRadix8 | kRadix4 | kRadix5,
+                           kRadix4 | kRadix3 | kRadix5,
+                           kRadix8 | kRadix2 | kRadix3,
+                           kRadix2 | kRadix3 | kRadix5>{});
 }
 
 }  // namespace
@@ -814,7 +835,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
   const FFPlan Pz = ff_plan(ctx, g.n[2]);
   const FFPlan Py = ff_plan(ctx, g.n[1]);
   const FFPlan Px = ff_plan(ctx, g.n[0]);
-  with_radix_set(Pz, [&](auto set) {
+  with_mesh_radix_set(Pz, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Pz);
     const int64_t npair = int64_t(g.n[0]) * g.n[1] / 2;
@@ -825,7 +846,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
         g, mesh, Pz, lb, Kg, T1);
     TRVG_LAUNCHED(ctx);
   });
-  with_radix_set(Py, [&](auto set) {
+  with_mesh_radix_set(Py, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(g.n[0]) * (Kg + 1);
@@ -836,7 +857,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
         g, T1, Py, lb, Kg, Kg, T2);
     TRVG_LAUNCHED(ctx);
   });
-  with_radix_set(Px, [&](auto set) {
+  with_mesh_radix_set(Px, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(2 * Kg + 1) * (Kg + 1);
@@ -885,7 +906,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
   const FFPlan Px = ff_plan(ctx, M[0]);
   const FFPlan Py = ff_plan(ctx, M[1]);
   const FFPlan Pz = ff_plan(ctx, M[2]);
-  with_radix_set(Px, [&](auto set) {
+  with_grid_radix_set(Px, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Px);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * (2 * Kf + 1);
@@ -896,7 +917,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
         M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1);
     TRVG_LAUNCHED(ctx);
   });
-  with_radix_set(Py, [&](auto set) {
+  with_grid_radix_set(Py, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);
     const int64_t nl = int64_t(nf) * (Kcf + 1) * M[0];
@@ -907,7 +928,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
         M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2);
     TRVG_LAUNCHED(ctx);
   });
-  with_radix_set(Pz, [&](auto set) {
+  with_grid_radix_set(Pz, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Pz);
     const int64_t np = (int64_t(nf) * M[0] * M[1] + 1) / 2;

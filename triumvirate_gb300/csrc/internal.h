@@ -138,6 +138,10 @@ struct Context {
   bool ff_transforms = true;
   // Batches: replay one captured mock as a CUDA graph (batch.cu).
   bool graph_batch = true;
+  // Autotuner: launch shapes picked by timing (tile side of the catalogue
+  // sort, bin batch of the pair reduction), cached by key.
+  bool autotune = true;
+  std::map<std::string, int> tuned;
   // Mocks replayed from the captured graph by the last batch call.
   int64_t graph_replays = 0;
   // Deposits made so far (FieldSpec::mesh_gen).

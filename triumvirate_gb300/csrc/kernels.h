@@ -123,9 +123,10 @@ void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
                         const double* dsum, double hsum);
 
 // ---- sort.cu -------------------------------------------------------------
-// Copy of `in` ordered by 8^3-cell mesh tile (device buffers named by tag).
+// Copy of `in` ordered by mesh tiles of 2^shift cells a side (device
+// buffers named by tag).
 DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
-                            const std::string& tag);
+                            const std::string& tag, int shift = 3);
 
 // ---- spectral.cu ---------------------------------------------------------
 // Mode cube: frequencies s in [-K, K] per axis, or the whole axis when
@@ -309,11 +310,13 @@ inline int64_t ff_field_stride(int64_t ncell) { return (ncell + 3) / 4 * 4; }
 // sum_x F_a F_b G of float-float fields (hi, lo words; field q of a leg at
 // q ld, ld a multiple of 4, 16-byte aligned bases) for every pair (real
 // parts at out[2 p]).
+// pairs_per_block: the bin batch of one block (4, 8 or 16; autotuned).
 void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,
                             const float* Gh, const float* Gl,
                             const float* Fah, const float* Fal,
                             const float* Fbh, const float* Fbl, const int* pa,
-                            const int* pb, int npairs, double* out);
+                            const int* pb, int npairs, double* out,
+                            int pairs_per_block = 8);
 
 // ---- batch.cu ------------------------------------------------------------
 // Scalars of the current mock of a replayed batch (device memory).

@@ -234,6 +234,7 @@ __device__ __forceinline__ void ff_quad(FF& acc, float4 ah, float4 al,
   ff_merge(acc, ff_prod3(ah.w, al.w, bh.w, bl.w, gh.w, gl.w));
 }
 
+template <int CHUNK>
 __global__ void __launch_bounds__(256)
 reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
                        const float* __restrict__ Gh,
@@ -243,18 +244,18 @@ reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
                        const float* __restrict__ Fbh,
                        const float* __restrict__ Fbl, const int* pa,
                        const int* pb, int npairs, double* out) {
-  __shared__ double red[kPairChunk * 32];
-  const int p0 = blockIdx.y * kPairChunk;
-  int64_t oa[kPairChunk], ob[kPairChunk];
-  bool ok[kPairChunk], same[kPairChunk];
+  __shared__ double red[CHUNK * 32];
+  const int p0 = blockIdx.y * CHUNK;
+  int64_t oa[CHUNK], ob[CHUNK];
+  bool ok[CHUNK], same[CHUNK];
 #pragma unroll
-  for (int q = 0; q < kPairChunk; ++q) {
+  for (int q = 0; q < CHUNK; ++q) {
     ok[q] = (p0 + q) < npairs;
     oa[q] = ok[q] ? int64_t(pa[p0 + q]) * ld : 0;
     ob[q] = ok[q] ? int64_t(pb[p0 + q]) * ld : 0;
     same[q] = Fah == Fbh && oa[q] == ob[q];
   }
-  Acc<float> acc[kPairChunk];
+  Acc<float> acc[CHUNK];
   const int64_t nquad = ncell / 4;
   auto q4 = [](const float* p, int64_t off, int64_t t) {
     return reinterpret_cast<const float4*>(p + off)[t];
@@ -263,7 +264,7 @@ reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
        t += int64_t(gridDim.x) * blockDim.x) {
     const float4 gh = q4(Gh, 0, t), gl = q4(Gl, 0, t);
 #pragma unroll
-    for (int q = 0; q < kPairChunk; ++q) {
+    for (int q = 0; q < CHUNK; ++q) {
       if (!ok[q]) continue;
       const float4 ah = q4(Fah, oa[q], t), al = q4(Fal, oa[q], t);
       if (same[q]) {
@@ -277,7 +278,7 @@ reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
   if (blockIdx.x == 0) {
     for (int64_t c = nquad * 4 + threadIdx.x; c < ncell; c += blockDim.x) {
 #pragma unroll
-      for (int q = 0; q < kPairChunk; ++q) {
+      for (int q = 0; q < CHUNK; ++q) {
         if (!ok[q]) continue;
         ff_merge(acc[q].v, ff_prod3(Fah[oa[q] + c], Fal[oa[q] + c],
                                     Fbh[ob[q] + c], Fbl[ob[q] + c], Gh[c],
@@ -285,7 +286,7 @@ reduce_pairs_ff_kernel(int64_t ncell, int64_t ld,
       }
     }
   }
-  block_add_acc<kPairChunk, float>(acc, out + 2 * p0, 2, npairs - p0, red);
+  block_add_acc<CHUNK, float>(acc, out + 2 * p0, 2, npairs - p0, red);
 }
 
 // Sum of xi * y_a * y_b per integer key s_x^2 + s_y^2 + s_z^2 (cubic cells).
@@ -667,17 +668,25 @@ void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,
                             const float* Gh, const float* Gl,
                             const float* Fah, const float* Fal,
                             const float* Fbh, const float* Fbl, const int* pa,
-                            const int* pb, int npairs, double* out) {
+                            const int* pb, int npairs, double* out,
+                            int pairs_per_block) {
   if (npairs <= 0) return;
   if (ld % 4 != 0 || ld < ncell)
     throw_error(TRVG_ERR_INVALID_PARAMETER,
                 "Field stride %lld is not a multiple of 4 cells >= %lld.",
                 (long long)ld, (long long)ncell);
-  const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
-  dim3 grid(grid_for((ncell + 3) / 4, 256, 152 * 4), chunks);
-  TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
-  reduce_pairs_ff_kernel<<<grid, 256, 0, ctx.stream>>>(
-      ncell, ld, Gh, Gl, Fah, Fal, Fbh, Fbl, pa, pb, npairs, out);
+  auto go = [&](auto kernel, int chunk) {
+    dim3 grid(grid_for((ncell + 3) / 4, 256, 152 * 4),
+              (npairs + chunk - 1) / chunk);
+    TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
+    kernel<<<grid, 256, 0, ctx.stream>>>(ncell, ld, Gh, Gl, Fah, Fal, Fbh,
+                                         Fbl, pa, pb, npairs, out);
+  };
+  switch (pairs_per_block) {
+    case 4: go(reduce_pairs_ff_kernel<4>, 4); break;
+    case 16: go(reduce_pairs_ff_kernel<16>, 16); break;
+    default: go(reduce_pairs_ff_kernel<8>, 8); break;
+  }
   TRVG_LAUNCHED(ctx);
 }
 

@@ -3,9 +3,10 @@
 // The assignment deposits every particle into order^3 mesh cells with
 // atomics.  In input order (e.g. uniformly random) consecutive particles
 // touch unrelated cache lines of a mesh far larger than L2, so most atomics
-// miss.  Sorting by 8^3-cell tile first (one counting pass, one scan, one
+// miss.  Sorting by mesh tile first (one counting pass, one scan, one
 // scatter) makes the deposits of neighbouring threads share lines, and the
-// mesh streams through L2 about once.  The order of deposits does not
+// mesh streams through L2 about once.  The tile side, 2^shift cells, is
+// picked by the autotuner (default 8).  The order of deposits does not
 // change the result beyond floating-point association.
 #include <algorithm>
 
@@ -14,8 +15,6 @@
 namespace trvg {
 
 namespace {
-
-constexpr int kTileShift = 3;  // 8 cells per tile side
 
 // Approximate cell (the tile only orders the deposits): one multiply by
 // n / L, no division.
@@ -26,13 +25,14 @@ __device__ __forceinline__ int cell_of(double x, int n, double ratio) {
 
 __global__ void tile_key_kernel(DevCatalogue cat, int n0, int n1, int n2,
                                 double r0, double r1, double r2, int t1,
-                                int t2, int* key, int* rank, int* count) {
+                                int t2, int shift, int* key, int* rank,
+                                int* count) {
   const int64_t np = cat.count(), p0 = cat.first();
   for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < np;
        p += int64_t(gridDim.x) * blockDim.x) {
-    const int tx = cell_of(cat.x[p0 + p], n0, r0) >> kTileShift;
-    const int ty = cell_of(cat.y[p0 + p], n1, r1) >> kTileShift;
-    const int tz = cell_of(cat.z[p0 + p], n2, r2) >> kTileShift;
+    const int tx = cell_of(cat.x[p0 + p], n0, r0) >> shift;
+    const int ty = cell_of(cat.y[p0 + p], n1, r1) >> shift;
+    const int tz = cell_of(cat.z[p0 + p], n2, r2) >> shift;
     const int k = (tx * t1 + ty) * t2 + tz;
     key[p] = k;
     rank[p] = atomicAdd(count + k, 1);
@@ -137,13 +137,14 @@ int grid_for(int64_t work, int block) {
 }  // namespace
 
 DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
-                            const std::string& tag) {
+                            const std::string& tag, int shift) {
   if (in.n < 2) return in;
   if (in.n > int64_t(2147483647))
     throw_error(TRVG_ERR_INVALID_DATA, "Catalogue larger than 2^31 particles.");
-  const int t0 = (g.n[0] + 7) >> kTileShift;
-  const int t1 = (g.n[1] + 7) >> kTileShift;
-  const int t2 = (g.n[2] + 7) >> kTileShift;
+  const int side = 1 << shift;
+  const int t0 = (g.n[0] + side - 1) >> shift;
+  const int t1 = (g.n[1] + side - 1) >> shift;
+  const int t2 = (g.n[2] + side - 1) >> shift;
   const int64_t ntiles = int64_t(t0) * t1 * t2;
   if (ntiles > int64_t(1) << 30) return in;
   int* key = ctx.buf<int>(tag + ".sort.key", size_t(in.n));
@@ -154,7 +155,7 @@ DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
   TRVG_KBEGIN(ctx, "tile_key_kernel");
   tile_key_kernel<<<grid_for(in.n, 256), 256, 0, ctx.stream>>>(
       in, g.n[0], g.n[1], g.n[2], g.n[0] / g.L[0], g.n[1] / g.L[1],
-      g.n[2] / g.L[2], t1, t2, key, rank, count);
+      g.n[2] / g.L[2], t1, t2, shift, key, rank, count);
   TRVG_LAUNCHED(ctx);
   const int nscan = int((ntiles + kScanTile - 1) / kScanTile);
   int* tile_sum = ctx.buf<int>(tag + ".sort.tiles", size_t(nscan));
