@@ -15,6 +15,8 @@
  *                                      (include/threept.hpp:257)
  *   trvg_compute_3pcf_window        <- trv::compute_3pcf_window
  *                                      (include/threept.hpp:310)
+ *   trvg_hankel_*                   <- trv::maths::HankelTransform
+ *                                      (include/fftlog.hpp:68-257)
  *   trvg_compute_powspec_in_gpp_box <- trv::compute_powspec_in_gpp_box
  *                                      (include/twopt.hpp:283)
  *   trvg_compute_powspec            <- trv::compute_powspec
@@ -216,6 +218,32 @@ int trvg_tuned_get(const trvg_context* ctx, int index, char* key,
 int trvg_kernel_time_count(const trvg_context* ctx, int* count);
 int trvg_kernel_time_get(const trvg_context* ctx, int index, char* name,
                          int name_len, double* ms, int64_t* launches);
+
+/* ---- FFTLog Hankel transforms (fftlog.cpp) --------------------------- */
+
+typedef struct trvg_hankel trvg_hankel;
+
+/* trv::maths::HankelTransform(mu, q) followed by
+ * initialise(sample_pts, kr_c, lowring, extrap, extrap_exp)
+ * (include/fftlog.hpp:90, 164): n log-spaced points x, pivot kr_c (adjusted
+ * by the low-ringing condition when lowring != 0), native extrapolation 0
+ * none, 1 zero, 2 constant, 3 linear, 4 log-linear to the power of 2 >=
+ * extrap_exp n. */
+int trvg_hankel_create(double mu, double q, const double* x, int n,
+                       double kr_c, int lowring, int extrap,
+                       double extrap_exp, trvg_hankel** out);
+/* Sample size, transform size, pivot, log spacing, and the n points before
+ * and after the transform (any output may be NULL). */
+int trvg_hankel_info(const trvg_hankel* h, int* n, int* n_trans,
+                     double* pivot, double* logres, double* pre_sampts,
+                     double* post_sampts);
+/* HankelTransform::biased_transform (include/fftlog.hpp:187) of `batch`
+ * rows of n complex samples at once: a and b are host arrays of
+ * 2 n batch doubles (re, im interleaved, row after row); rows are taken as
+ * real when extrapolating. */
+int trvg_hankel_transform(trvg_context* ctx, const trvg_hankel* h, int batch,
+                          const double* a, double* b);
+int trvg_hankel_destroy(trvg_hankel* h);
 
 /* Length of the data vector of a three-point measurement
  * (threept.cpp:1495-1521). */

@@ -1181,3 +1181,88 @@ def compute_los(x, y, z):
                 + np.asarray(z) ** 2)
     n = np.where(n == 0., 1., n)
     return np.stack([x / n, y / n, z / n], axis=-1)
+
+
+# ---------------------------------------------------------------------------
+# FFTLog Hankel transform (fftlog.cpp; include/fftlog.hpp:68-257)
+# ---------------------------------------------------------------------------
+
+def _lngamma(z):
+    from scipy.special import loggamma
+    return loggamma(z)
+
+
+def fftlog_lowring_pivot(mu, q, dL, kr_c=1.):
+    """``HankelTransform::calc_lowring_pivot`` (fftlog.cpp:254-295)."""
+    y = np.pi / (2. * dL)
+    if kr_c > 0.:
+        gp = _lngamma(complex((mu + 1. + q) / 2., y))
+        gm = _lngamma(complex((mu + 1. - q) / 2., y))
+        argphase = np.log(2. / kr_c) / dL + (gp.imag + gm.imag) / np.pi
+        return kr_c * np.exp(dL * (argphase - np.round(argphase)))
+    nu = complex(q, 2. * y)
+    lr = _lngamma((mu + 1. + nu) / 2.) - _lngamma((mu + 1. - nu) / 2.)
+    lnkr = np.log(2.) + lr.imag / (2. * y)
+    return np.exp(lnkr - np.floor(lnkr / dL) * dL)
+
+
+def fftlog_kernel(mu, q, N, dL, kr_c):
+    """``HankelTransform::compute_kernel_coeff`` (fftlog.cpp:297-356)."""
+    y = np.pi / (N * dL)
+    t = -2. * y * np.log(kr_c / 2.)
+    m = np.arange(N // 2 + 1)
+    if q == 0.:
+        ge = _lngamma((mu + 1.) / 2. + 1j * m * y)
+        half = np.exp(1j * (m * t + 2. * ge.imag))
+    else:
+        gp = _lngamma((mu + 1. + q) / 2. + 1j * m * y)
+        gm = _lngamma((mu + 1. - q) / 2. + 1j * m * y)
+        half = np.exp(q * np.log(2.) + gp.real - gm.real) \
+            * np.exp(1j * (m * t + gp.imag + gm.imag))
+    u = np.empty(N, dtype=complex)
+    u[:N // 2 + 1] = half
+    u[N // 2 + 1:] = np.conj(half[1:N - N // 2][::-1])
+    if N % 2 == 0:
+        u[N // 2] = u[N // 2].real
+    return u
+
+
+def _extend_native(a, n_ext, option):
+    """``extrap_pad`` / ``extrap_lin`` / ``extrap_loglin``
+    (arrayops.cpp:94-203) on a real row."""
+    left_i = np.arange(-n_ext, 0)
+    right_i = np.arange(1, n_ext + 1)
+    if option == 1:
+        lo, hi = np.zeros(n_ext), np.zeros(n_ext)
+    elif option == 2:
+        lo, hi = np.full(n_ext, a[0]), np.full(n_ext, a[-1])
+    elif option == 3:
+        lo = a[0] + left_i * (a[1] - a[0])
+        hi = a[-1] + right_i * (a[-1] - a[-2])
+    else:
+        lo = a[0] * np.exp(left_i * np.log(a[1] / a[0]))
+        hi = a[-1] * np.exp(right_i * np.log(a[-1] / a[-2]))
+    return np.concatenate([lo, a, hi])
+
+
+def hankel_transform(mu, q, x, a, kr_c=1., lowring=True, extrap=0,
+                     extrap_exp=2.):
+    """``HankelTransform::initialise`` + ``biased_transform``
+    (fftlog.cpp:108-252, 358-478): post-transform points and samples."""
+    x = np.asarray(x, dtype=float)
+    N = len(x)
+    dL = np.log(x[-1] / x[0]) / (N - 1)
+    if extrap:
+        Nt = int(2 ** np.ceil(np.log2(extrap_exp * N)))
+        n_ext = (Nt - N) // 2
+    else:
+        Nt, n_ext = N, 0
+    piv = fftlog_lowring_pivot(mu, q, dL, kr_c) if lowring else kr_c
+    u = fftlog_kernel(mu, q, Nt, dL, piv)
+    post = piv * np.exp(-dL) / x[::-1]
+    if extrap:
+        pre = _extend_native(np.real(np.asarray(a)), n_ext, extrap)
+    else:
+        pre = np.asarray(a, dtype=complex)
+    b = np.fft.fft(np.fft.fft(pre) * u / Nt)
+    return post, b[n_ext:n_ext + N]

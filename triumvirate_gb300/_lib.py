@@ -42,6 +42,8 @@ EXPORTED = [
     "trvg_calc_grid_based_powlaw_norm_noalloc",
     "trvg_compute_bispec_in_gpp_box_batch", "trvg_bispec_gpp_adjoint",
     "trvg_compute_3pcf_window", "trvg_tuned_count", "trvg_tuned_get",
+    "trvg_hankel_create", "trvg_hankel_info", "trvg_hankel_transform",
+    "trvg_hankel_destroy",
 ]
 
 
@@ -207,6 +209,12 @@ def _declare(lib):
     lib.trvg_reduced_ylm.argtypes = [ip, ip, P(dp), C.c_int64, P(dp)]
     lib.trvg_context_set_stream.argtypes = [vp, vp]
     lib.trvg_set_option.argtypes = [vp, C.c_char_p, C.c_int64]
+    lib.trvg_hankel_create.argtypes = [dp, dp, P(dp), ip, dp, ip, ip, dp,
+                                       P(vp)]
+    lib.trvg_hankel_info.argtypes = [vp, P(ip), P(ip), P(dp), P(dp), P(dp),
+                                     P(dp)]
+    lib.trvg_hankel_transform.argtypes = [vp, vp, ip, P(dp), P(dp)]
+    lib.trvg_hankel_destroy.argtypes = [vp]
     lib.trvg_tuned_count.argtypes = [vp, P(ip)]
     lib.trvg_tuned_get.argtypes = [vp, ip, C.c_char_p, ip, P(C.c_int64)]
     lib.trvg_kernel_time_count.argtypes = [vp, P(ip)]

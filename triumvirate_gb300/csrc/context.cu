@@ -87,6 +87,27 @@ cufftHandle Context::plan(int type, const int n[3], int batch) {
   return h;
 }
 
+cufftHandle Context::plan1d(int type, int n, int batch) {
+  PlanKey key{type, {n, -1, -1}, batch};
+  auto it = plans.find(key);
+  if (it != plans.end()) return it->second;
+  cufftHandle h;
+  TRVG_CUFFT(cufftCreate(&h));
+  TRVG_CUFFT(cufftSetStream(h, stream));
+  long long nn[1] = {n};
+  size_t work = 0;
+  cufftResult r = cufftMakePlanMany64(h, 1, nn, nullptr, 1, n, nullptr, 1, n,
+                                      cufftType(type), batch, &work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    throw_error(r == CUFFT_ALLOC_FAILED ? TRVG_ERR_ALLOC : TRVG_ERR_CUFFT,
+                "cuFFT 1-d plan (type %d, length %d, batch %d) failed: %d",
+                type, n, batch, int(r));
+  }
+  plans[key] = h;
+  return h;
+}
+
 namespace {
 cudaEvent_t next_event(Context& c) {
   if (c.events_used == c.event_pool.size()) {

@@ -176,6 +176,8 @@ struct Context {
     return static_cast<T*>(buffer(name, count * sizeof(T)));
   }
   cufftHandle plan(int type, const int n[3], int batch);
+  // Batched 1-D plan of length n (cached with the 3-D ones).
+  cufftHandle plan1d(int type, int n, int batch);
   void release();
   void log(int level, const char* fmt, ...) const;
 };
