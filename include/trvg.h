@@ -17,6 +17,12 @@
  *                                      (include/threept.hpp:310)
  *   trvg_hankel_*                   <- trv::maths::HankelTransform
  *                                      (include/fftlog.hpp:68-257)
+ *   trvg_dcat_*                     <- trv::ParticleCatalogue loading and
+ *                                      preparation (particles.cpp:94-510,
+ *                                      570-888) and the Python
+ *                                      ParticleCatalogue's centre / pad /
+ *                                      periodise / compute_los
+ *                                      (catalogue.py:437-676)
  *   trvg_compute_powspec_in_gpp_box <- trv::compute_powspec_in_gpp_box
  *                                      (include/twopt.hpp:283)
  *   trvg_compute_powspec            <- trv::compute_powspec
@@ -244,6 +250,90 @@ int trvg_hankel_info(const trvg_hankel* h, int* n, int* n_trans,
 int trvg_hankel_transform(trvg_context* ctx, const trvg_hankel* h, int batch,
                           const double* a, double* b);
 int trvg_hankel_destroy(trvg_hankel* h);
+
+/* ---- Device-resident particle catalogues (particles.cpp) ------------- */
+
+/* A catalogue whose columns x, y, z, nz, ws, wc and w = ws wc (and, once
+ * computed, the lines of sight) live in device memory of the context's
+ * GPU.  trvg_dcat_view hands it to every estimator as a TRVG_MEM_DEVICE
+ * trvg_catalogue without a copy. */
+typedef struct trvg_dcat trvg_dcat;
+
+/* ParticleCatalogue::load_catalogue_file (particles.cpp:94-510) for text
+ * files: `path` may join sub-files with "::"; `columns` names the file's
+ * columns, comma-separated, from x, y, z, nz, ws, wc (others are skipped);
+ * lines that are empty or start with '#' are skipped.  Absent columns take
+ * nz = ntotal / volume (0 if volume <= 0) and ws = wc = 1.  HDF5 paths
+ * (.h5, .hdf5) give TRVG_ERR_INVALID_DATA, as a build without HDF5 does.
+ * Parsing runs on all host threads; the columns are copied to the device
+ * once. */
+int trvg_dcat_read_text(trvg_context* ctx, const char* path,
+                        const char* columns, double volume, trvg_dcat** out);
+/* A catalogue from n host particles; nz, ws, wc may be NULL (0, 1, 1). */
+int trvg_dcat_from_host(trvg_context* ctx, int64_t n, const double* x,
+                        const double* y, const double* z, const double* nz,
+                        const double* ws, const double* wc, trvg_dcat** out);
+/* One catalogue holding `count` catalogues back to back (device-to-device
+ * copies; lines of sight kept when every part has them), e.g. the
+ * particles of a batch of mocks. */
+int trvg_dcat_concat(trvg_context* ctx, const trvg_dcat* const* cats,
+                     int count, trvg_dcat** out);
+/* Size, weight totals (calc_total_weights, particles.cpp:570-602) and
+ * coordinate extents (calc_pos_extents, particles.cpp:604-656); any output
+ * may be NULL.  The totals come from a fixed-order device reduction. */
+int trvg_dcat_info(trvg_context* ctx, const trvg_dcat* c, int64_t* n,
+                   double* wtotal, double* wstotal, double* pos_min,
+                   double* pos_max);
+/* x -= dpos[0], y -= dpos[1], z -= dpos[2]
+ * (offset_coords, particles.cpp:658-676). */
+int trvg_dcat_offset(trvg_context* ctx, trvg_dcat* c, const double* dpos);
+/* centre_in_box (particles.cpp:701-778; catalogue.py:490-545): the
+ * mid-point of ref's extents (c's if ref is NULL) moves to boxsize / 2 and
+ * both catalogues move by the same offset. */
+int trvg_dcat_centre(trvg_context* ctx, trvg_dcat* c, trvg_dcat* ref,
+                     const double* boxsize);
+/* pad_in_box / pad_grids (particles.cpp:780-888): the minimum of ref's
+ * extents (c's if ref is NULL) moves to boxsize_pad * boxsize, or to
+ * ngrid_pad * boxsize / ngrid evaluated left to right as pad_grids does;
+ * give exactly one of boxsize_pad and ngrid_pad (three values each). */
+int trvg_dcat_pad(trvg_context* ctx, trvg_dcat* c, trvg_dcat* ref,
+                  const double* boxsize, const double* boxsize_pad,
+                  const double* ngrid, const double* ngrid_pad);
+/* offset_coords_for_periodicity (particles.cpp:678-699): coordinates
+ * x >= L become fmod(x, L) and x < 0 become fmod(x, L) + L. */
+int trvg_dcat_wrap_box(trvg_context* ctx, trvg_dcat* c,
+                       const double* boxsize);
+/* ParticleCatalogue.periodise (catalogue.py:648-676): each coordinate
+ * becomes (x + L/2 - (max + min)/2) mod L with the remainder taking the
+ * sign of L, bit for bit as numpy computes it. */
+int trvg_dcat_periodise(trvg_context* ctx, trvg_dcat* c,
+                        const double* boxsize);
+/* ParticleCatalogue.compute_los (catalogue.py:437-458): unit end-point
+ * lines of sight x / |x| (1 where |x| = 0), kept on the device and
+ * included in trvg_dcat_view. */
+int trvg_dcat_compute_los(trvg_context* ctx, trvg_dcat* c);
+/* Set 'nz', 'ws' or 'wc' to a constant (w follows); compute_mean_density
+ * (catalogue.py:460-488) is nz = ntotal / volume. */
+int trvg_dcat_set_column(trvg_context* ctx, trvg_dcat* c, const char* column,
+                         double value);
+/* Replace column x, y, z, nz, ws, wc, los_x, los_y or los_z with n host
+ * doubles (w follows ws and wc). */
+int trvg_dcat_upload(trvg_context* ctx, trvg_dcat* c, const char* column,
+                     const double* values);
+/* sum ws nz^(order-1) wc^order over the particles, the denominator of the
+ * particle normalisation (order 2: twopt.cpp:56-99; order 3:
+ * threept.cpp:96-136), and the number of particles with nz != 0; either
+ * output may be NULL. */
+int trvg_dcat_norm_sum(trvg_context* ctx, const trvg_dcat* c, int order,
+                       double* sum, int64_t* nonzero_nz);
+/* A TRVG_MEM_DEVICE trvg_catalogue over c's columns (valid until c is
+ * destroyed or its lines of sight are first computed). */
+int trvg_dcat_view(const trvg_dcat* c, trvg_catalogue* out);
+/* Copy column x, y, z, nz, ws, wc, w, los_x, los_y or los_z to n host
+ * doubles. */
+int trvg_dcat_download(trvg_context* ctx, const trvg_dcat* c,
+                       const char* column, double* out);
+int trvg_dcat_destroy(trvg_dcat* c);
 
 /* Length of the data vector of a three-point measurement
  * (threept.cpp:1495-1521). */

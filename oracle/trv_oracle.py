@@ -1183,6 +1183,84 @@ def compute_los(x, y, z):
     return np.stack([x / n, y / n, z / n], axis=-1)
 
 
+def pad(x, y, z, boxsize, ngrid=None, boxsize_pad=None, ngrid_pad=None,
+        ref=None):
+    """``ParticleCatalogue.pad`` (catalogue.py:547-646): the reference
+    catalogue's minimum moves to boxsize_pad * boxsize, or to
+    ngrid_pad * (boxsize / ngrid)."""
+    ref = (x, y, z) if ref is None else ref
+    origin = np.array([np.min(r) for r in ref])
+    if boxsize_pad is not None:
+        origin -= np.multiply(boxsize_pad, boxsize)
+    if ngrid_pad is not None:
+        origin -= np.multiply(ngrid_pad, np.divide(boxsize, ngrid))
+    return [np.asarray(c, dtype=np.float64) - o
+            for c, o in zip((x, y, z), origin)], origin
+
+
+def pad_cpp(x, y, z, boxsize, ngrid=None, boxsize_pad=None, ngrid_pad=None,
+            ref=None):
+    """``ParticleCatalogue::pad_in_box`` / ``pad_grids``
+    (particles.cpp:780-888): the same shift with pad_grids' association
+    ngrid_pad * boxsize / ngrid, evaluated left to right."""
+    ref = (x, y, z) if ref is None else ref
+    origin = []
+    for a in range(3):
+        o = float(np.min(ref[a]))
+        if boxsize_pad is not None:
+            o = o - boxsize_pad[a] * boxsize[a]
+        if ngrid_pad is not None:
+            o = o - ngrid_pad[a] * boxsize[a] / float(ngrid[a])
+        origin.append(o)
+    return [np.asarray(c, dtype=np.float64) - o
+            for c, o in zip((x, y, z), origin)], origin
+
+
+def offset_coords_for_periodicity(x, y, z, boxsize):
+    """``ParticleCatalogue::offset_coords_for_periodicity``
+    (particles.cpp:678-699): x >= L -> fmod(x, L); x < 0 ->
+    fmod(x, L) + L."""
+    out = []
+    for c, L in zip((x, y, z), boxsize):
+        c = np.asarray(c, dtype=np.float64)
+        r = c.copy()
+        hi, lo = c >= L, c < 0.
+        r[hi] = np.fmod(c[hi], L)
+        r[lo] = np.fmod(c[lo], L) + L
+        out.append(r)
+    return out
+
+
+def load_catalogue_text(paths, columns, volume=0.):
+    """``ParticleCatalogue::load_catalogue_file`` for text files
+    (particles.cpp:94-510), one Python float per entry: `paths` joined by
+    "::", lines that are empty or start with '#' skipped, field f taken
+    from the first column named f; absent nz = ntotal / volume (0 if
+    volume <= 0), absent ws = wc = 1, w = ws wc."""
+    names = columns.split(',')
+    fields = ['x', 'y', 'z', 'nz', 'ws', 'wc']
+    index = {f: (names.index(f) if f in names else -1) for f in fields}
+    rows = []
+    for path in [p for p in paths.split('::') if p]:
+        with open(path) as fin:
+            for line in fin:
+                line = line.rstrip('\n')
+                if not line.strip() or line.startswith('#'):
+                    continue
+                rows.append([float(v) for v in line.split()])
+    n = len(rows)
+    nz_default = n / volume if volume > 0. else 0.
+    out = {}
+    for f in fields:
+        if index[f] >= 0:
+            out[f] = np.array([r[index[f]] for r in rows], dtype=np.float64)
+        else:
+            v = nz_default if f == 'nz' else 1.
+            out[f] = np.full(n, v)
+    out['w'] = out['ws'] * out['wc']
+    return out
+
+
 # ---------------------------------------------------------------------------
 # FFTLog Hankel transform (fftlog.cpp; include/fftlog.hpp:68-257)
 # ---------------------------------------------------------------------------

@@ -68,6 +68,28 @@ class HostCatalogue:
         self.c = c
 
 
+def catalogue_arg(cat, los=None, with_los=False):
+    """The ``trvg_catalogue`` (attribute ``c``) of a ParticleCatalogue
+    (host columns) or a DeviceCatalogue (device columns, no copy), with
+    lines of sight when `with_los` (`los`, else computed)."""
+    if hasattr(cat, '_view'):
+        return cat._view(los, with_los)
+    x, y, z, w = cat._columns()
+    if with_los and los is None:
+        los = cat.compute_los()
+    return HostCatalogue(x, y, z, w, np.asarray(los) if with_los else None)
+
+
+def context_for(device, *catalogues):
+    """The context of `device`; by default that of the first device
+    catalogue among `catalogues`, else the process-wide default."""
+    if device is None:
+        for c in catalogues:
+            if hasattr(c, '_ctx'):
+                return c._ctx
+    return _lib.default_context(device)
+
+
 def device_catalogue(n, x_ptr, y_ptr, z_ptr, w_ptr=None, los_ptrs=None):
     """``trvg_catalogue`` over device pointers (e.g. torch ``data_ptr()``)."""
     c = _lib.Catalogue()

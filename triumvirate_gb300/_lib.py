@@ -44,6 +44,12 @@ EXPORTED = [
     "trvg_compute_3pcf_window", "trvg_tuned_count", "trvg_tuned_get",
     "trvg_hankel_create", "trvg_hankel_info", "trvg_hankel_transform",
     "trvg_hankel_destroy",
+    "trvg_dcat_read_text", "trvg_dcat_from_host", "trvg_dcat_info",
+    "trvg_dcat_offset", "trvg_dcat_centre", "trvg_dcat_pad",
+    "trvg_dcat_wrap_box", "trvg_dcat_periodise", "trvg_dcat_compute_los",
+    "trvg_dcat_set_column", "trvg_dcat_upload", "trvg_dcat_norm_sum",
+    "trvg_dcat_view", "trvg_dcat_download", "trvg_dcat_destroy",
+    "trvg_dcat_concat",
 ]
 
 
@@ -220,6 +226,24 @@ def _declare(lib):
     lib.trvg_kernel_time_count.argtypes = [vp, P(ip)]
     lib.trvg_kernel_time_get.argtypes = [vp, ip, C.c_char_p, ip, P(dp),
                                          P(C.c_int64)]
+    i64, cp = C.c_int64, C.c_char_p
+    lib.trvg_dcat_read_text.argtypes = [vp, cp, cp, dp, P(vp)]
+    lib.trvg_dcat_from_host.argtypes = [vp, i64] + [P(dp)] * 6 + [P(vp)]
+    lib.trvg_dcat_info.argtypes = [vp, vp, P(i64), P(dp), P(dp), P(dp),
+                                   P(dp)]
+    lib.trvg_dcat_offset.argtypes = [vp, vp, P(dp)]
+    lib.trvg_dcat_centre.argtypes = [vp, vp, vp, P(dp)]
+    lib.trvg_dcat_pad.argtypes = [vp, vp, vp, P(dp), P(dp), P(dp), P(dp)]
+    lib.trvg_dcat_wrap_box.argtypes = [vp, vp, P(dp)]
+    lib.trvg_dcat_periodise.argtypes = [vp, vp, P(dp)]
+    lib.trvg_dcat_compute_los.argtypes = [vp, vp]
+    lib.trvg_dcat_set_column.argtypes = [vp, vp, cp, dp]
+    lib.trvg_dcat_upload.argtypes = [vp, vp, cp, P(dp)]
+    lib.trvg_dcat_norm_sum.argtypes = [vp, vp, ip, P(dp), P(i64)]
+    lib.trvg_dcat_view.argtypes = [vp, P(Catalogue)]
+    lib.trvg_dcat_download.argtypes = [vp, vp, cp, P(dp)]
+    lib.trvg_dcat_destroy.argtypes = [vp]
+    lib.trvg_dcat_concat.argtypes = [vp, P(vp), ip, P(vp)]
 
 
 def check(status: int):

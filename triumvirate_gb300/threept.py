@@ -8,6 +8,7 @@ import warnings
 import numpy as np
 
 from . import _engine, _lib, io
+from .catalogue import DeviceCatalogue
 from .dataobjs import Binning
 from .parameters import (ParameterSet, _as_dict,
                          _modify_measurement_parameters,
@@ -67,13 +68,23 @@ def _boxsize(paramset):
     return [float(paramset['boxsize'][ax]) for ax in ['x', 'y', 'z']]
 
 
-def _norm_particle(nz, ws, wc, alpha, order, strict=True):
+def _has_nz(catalogue):
+    """Whether any particle has a nonzero 'nz' (summed on the device for a
+    DeviceCatalogue)."""
+    if hasattr(catalogue, '_has_nz'):
+        return catalogue._has_nz()
+    return bool(np.asarray(catalogue['nz']).any())
+
+
+def _norm_particle(catalogue, alpha, order, strict=True):
     """1 / (alpha sum ws nz^(order-1) wc^order) (threept.cpp:96-136,
     twopt.cpp:56-99)."""
-    if order == 3:
-        norm = float(np.sum(ws * nz ** 2 * wc ** 3))
+    if hasattr(catalogue, '_norm_sum'):
+        norm = catalogue._norm_sum(order)
     else:
-        norm = float(np.sum(ws * nz * wc ** 2))
+        nz, ws, wc = (np.asarray(catalogue[k]) for k in ('nz', 'ws', 'wc'))
+        norm = float(np.sum(ws * nz ** 2 * wc ** 3) if order == 3
+                     else np.sum(ws * nz * wc ** 2))
     if norm == 0.:
         if not strict:
             return float('inf')
@@ -89,24 +100,24 @@ def _norm_mesh(ctx, params_c, cat_c, alpha, order):
         / alpha ** order
 
 
-def _norm_factor(paramset, ctx, params_c, cat_c, nz, ws, wc, alpha, order):
+def _norm_factor(paramset, ctx, params_c, cat_c, catalogue, alpha, order):
     """Particle / mesh normalisation of the chosen convention."""
     conv = paramset['norm_convention']
     if conv == 'none':
         return 1.
     if conv == 'particle':
-        return _norm_particle(nz, ws, wc, alpha, order)
+        return _norm_particle(catalogue, alpha, order)
     if conv == 'mesh':
         return _norm_mesh(ctx, params_c, cat_c, alpha, order)
     raise ValueError(f"Unsupported normalisation convention: {conv}.")
 
 
-def _save(results, paramset, save, ctx, params_c, cat_c, nz, ws, wc, alpha,
+def _save(results, paramset, save, ctx, params_c, cat_c, catalogue, alpha,
           order, catalogue_data, catalogue_rand=None):
     """Write the measurements with the library's header: catalogue
     attributes, sampling parameters and every normalisation alternative
     (threept.py:707-735, twopt.py:633-663)."""
-    part = _norm_particle(nz, ws, wc, alpha, order, strict=False)
+    part = _norm_particle(catalogue, alpha, order, strict=False)
     mesh = _norm_mesh(ctx, params_c, cat_c, alpha, order)
     header = "\n".join([
         catalogue_data.write_attrs_as_header(catalogue_ref=catalogue_rand),
@@ -135,23 +146,21 @@ def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
         _set_ngrid_from_cutoff(pd)
         paramset['ngrid'] = pd['ngrid']
     catalogue_data.periodise(_boxsize(paramset))
-    if not catalogue_data['nz'].any():
+    if not _has_nz(catalogue_data):
         catalogue_data.compute_mean_density(boxsize=_boxsize(paramset))
 
-    ctx = _lib.default_context(device)
+    ctx = _engine.context_for(device, catalogue_data)
     params_c = _engine.make_params(paramset, '3pt')
-    x, y, z, w = catalogue_data._columns()
-    cat = _engine.HostCatalogue(x, y, z, w)
-    norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data['nz'],
-                        catalogue_data['ws'], catalogue_data['wc'], 1., 3)
+    cat = _engine.catalogue_arg(catalogue_data)
+    norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data, 1.,
+                        3)
     fn = ('trvg_compute_bispec_in_gpp_box' if kind == 'bispec'
           else 'trvg_compute_3pcf_in_gpp_box')
     results = _engine.call_threept(
         fn, ctx, params_c, cat.c, binning, norm, kind,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
     if save:
-        _save(results, paramset, save, ctx, params_c, cat.c,
-              catalogue_data['nz'], catalogue_data['ws'], catalogue_data['wc'],
+        _save(results, paramset, save, ctx, params_c, cat.c, catalogue_data,
               1., 3, catalogue_data)
     return results
 
@@ -174,8 +183,6 @@ def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
         los_data = catalogue_data.compute_los()
     if los_rand is None:
         los_rand = catalogue_rand.compute_los()
-    los_data = np.ascontiguousarray(los_data)
-    los_rand = np.ascontiguousarray(los_rand)
     if None in paramset['boxsize'].values():
         paramset['boxsize'] = {
             ax: (catalogue_rand.bounds[ax][1] - catalogue_rand.bounds[ax][0])
@@ -194,23 +201,20 @@ def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
                   'ngrid_pad': paramset['padfactor']}
         catalogue_data.pad(_boxsize(paramset), catalogue_ref=catalogue_rand,
                            **kw)
-    ctx = _lib.default_context(device)
+    ctx = _engine.context_for(device, catalogue_data, catalogue_rand)
     params_c = _engine.make_params(paramset, '3pt')
     alpha = catalogue_data.wstotal / catalogue_rand.wstotal
-    xd, yd, zd, wd = catalogue_data._columns()
-    xr, yr, zr, wr = catalogue_rand._columns()
-    dcat = _engine.HostCatalogue(xd, yd, zd, wd, los_data)
-    rcat = _engine.HostCatalogue(xr, yr, zr, wr, los_rand)
-    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
-                        catalogue_rand['ws'], catalogue_rand['wc'], alpha, 3)
+    dcat = _engine.catalogue_arg(catalogue_data, los_data, with_los=True)
+    rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
+    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand,
+                        alpha, 3)
     fn = 'trvg_compute_bispec' if kind == 'bispec' else 'trvg_compute_3pcf'
     results = _engine.call_threept(
         fn, ctx, params_c, dcat.c, binning, norm, kind, rand_c=rcat.c,
         alpha=alpha, shape=paramset['shape'],
         idx_bin=paramset.get('idx_bin') or 0)
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c,
-              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
               alpha, 3, catalogue_data, catalogue_rand)
     return results
 
@@ -261,21 +265,18 @@ def compute_3pcf_window(catalogue_rand, los_rand=None, degrees=None,
         binning = Binning.from_parameter_set(paramset)
     if los_rand is None:
         los_rand = catalogue_rand.compute_los()
-    los_rand = np.ascontiguousarray(los_rand)
     catalogue_rand.centre(_boxsize(paramset))
     catalogue_rand.periodise(_boxsize(paramset))
-    ctx = _lib.default_context(device)
+    ctx = _engine.context_for(device, catalogue_rand)
     params_c = _engine.make_params(paramset, '3pt')
-    xr, yr, zr, wr = catalogue_rand._columns()
-    rcat = _engine.HostCatalogue(xr, yr, zr, wr, los_rand)
-    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
-                        catalogue_rand['ws'], catalogue_rand['wc'], 1., 3)
+    rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
+    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand, 1.,
+                        3)
     results = _engine.call_3pcf_window(
         ctx, params_c, rcat.c, binning, norm, 1., wide_angle,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c,
-              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
               1., 3, catalogue_rand)
     return results
 
@@ -314,23 +315,27 @@ def compute_bispec_in_gpp_box_batch(catalogues, degrees=None, binning=None,
         pd = _as_dict(paramset)
         _set_ngrid_from_cutoff(pd)
         paramset['ngrid'] = pd['ngrid']
-    cols, norms, offsets = [[], [], [], []], [], [0]
-    ctx = _lib.default_context(device)
+    norms, offsets = [], [0]
+    ctx = _engine.context_for(device, *catalogues)
     params_c = _engine.make_params(paramset, '3pt')
     for cat in catalogues:
         cat.periodise(_boxsize(paramset))
-        if not cat['nz'].any():
+        if not _has_nz(cat):
             cat.compute_mean_density(boxsize=_boxsize(paramset))
-        for c, a in zip(cols, cat._columns()):
-            c.append(a)
         offsets.append(offsets[-1] + cat.ntotal)
         if paramset['norm_convention'] == 'mesh':
-            hc = _engine.HostCatalogue(*cat._columns())
-            norms.append(_norm_mesh(ctx, params_c, hc.c, 1., 3))
+            norms.append(_norm_mesh(ctx, params_c,
+                                    _engine.catalogue_arg(cat).c, 1., 3))
         else:
-            norms.append(_norm_factor(paramset, ctx, params_c, None,
-                                      cat['nz'], cat['ws'], cat['wc'], 1., 3))
-    allc = _engine.HostCatalogue(*(np.concatenate(c) for c in cols))
+            norms.append(_norm_factor(paramset, ctx, params_c, None, cat, 1.,
+                                      3))
+    if any(isinstance(c, DeviceCatalogue) for c in catalogues):
+        allc = _engine.catalogue_arg(DeviceCatalogue.concatenate(
+            catalogues, device=ctx.device))
+    else:
+        cols = [np.concatenate(c) for c in
+                zip(*(cat._columns() for cat in catalogues))]
+        allc = _engine.HostCatalogue(*cols)
     return _engine.call_bispec_batch(
         ctx, params_c, allc.c, offsets, binning, norms,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)

@@ -3,12 +3,11 @@ compute_powspec / compute_powspec_in_gpp_box, twopt.py:668-1280), computed
 on the GPU through ``libtrvg.so``."""
 from __future__ import annotations
 
-import numpy as np
-
-from . import _engine, _lib
+from . import _engine
 from .dataobjs import Binning
 from .parameters import _as_dict, _set_ngrid_from_cutoff
-from .threept import _amalgamate_parameters, _boxsize, _norm_factor, _save
+from .threept import (_amalgamate_parameters, _boxsize, _has_nz,
+                      _norm_factor, _save)
 
 
 def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
@@ -32,19 +31,17 @@ def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
         _set_ngrid_from_cutoff(pd)
         paramset['ngrid'] = pd['ngrid']
     catalogue_data.periodise(_boxsize(paramset))
-    if not catalogue_data['nz'].any():
+    if not _has_nz(catalogue_data):
         catalogue_data.compute_mean_density(boxsize=_boxsize(paramset))
-    ctx = _lib.default_context(device)
+    ctx = _engine.context_for(device, catalogue_data)
     params_c = _engine.make_params(paramset, '2pt')
-    x, y, z, w = catalogue_data._columns()
-    cat = _engine.HostCatalogue(x, y, z, w)
-    norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data['nz'],
-                        catalogue_data['ws'], catalogue_data['wc'], 1., 2)
+    cat = _engine.catalogue_arg(catalogue_data)
+    norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data, 1.,
+                        2)
     results = _engine.call_powspec('trvg_compute_powspec_in_gpp_box', ctx,
                                    params_c, cat.c, binning, norm)
     if save:
-        _save(results, paramset, save, ctx, params_c, cat.c,
-              catalogue_data['nz'], catalogue_data['ws'], catalogue_data['wc'],
+        _save(results, paramset, save, ctx, params_c, cat.c, catalogue_data,
               1., 2, catalogue_data)
     return results
 
@@ -84,20 +81,17 @@ def compute_powspec(catalogue_data, catalogue_rand, los_data=None,
                   'ngrid_pad': paramset['padfactor']}
         catalogue_data.pad(_boxsize(paramset), catalogue_ref=catalogue_rand,
                            **kw)
-    ctx = _lib.default_context(device)
+    ctx = _engine.context_for(device, catalogue_data, catalogue_rand)
     params_c = _engine.make_params(paramset, '2pt')
     alpha = catalogue_data.wstotal / catalogue_rand.wstotal
-    xd, yd, zd, wd = catalogue_data._columns()
-    xr, yr, zr, wr = catalogue_rand._columns()
-    dcat = _engine.HostCatalogue(xd, yd, zd, wd, np.asarray(los_data))
-    rcat = _engine.HostCatalogue(xr, yr, zr, wr, np.asarray(los_rand))
-    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand['nz'],
-                        catalogue_rand['ws'], catalogue_rand['wc'], alpha, 2)
+    dcat = _engine.catalogue_arg(catalogue_data, los_data, with_los=True)
+    rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
+    norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand,
+                        alpha, 2)
     results = _engine.call_powspec('trvg_compute_powspec', ctx, params_c,
                                    dcat.c, binning, norm, rand_c=rcat.c,
                                    alpha=alpha)
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c,
-              catalogue_rand['nz'], catalogue_rand['ws'], catalogue_rand['wc'],
+        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
               alpha, 2, catalogue_data, catalogue_rand)
     return results
