@@ -14,8 +14,8 @@
 #include <algorithm>
 #include <charconv>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
-#include <fstream>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -290,73 +290,131 @@ std::vector<std::string> split_paths(const std::string& s) {
   return out;
 }
 
+// Whole file in one read.
+std::string slurp(const std::string& path) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (f == nullptr)
+    throw_error(TRVG_ERR_INVALID_DATA, "Failed to open file: %s",
+                path.c_str());
+  std::string text;
+  char chunk[1 << 16];
+  if (std::fseek(f, 0, SEEK_END) == 0) {
+    const long size = std::ftell(f);
+    if (size > 0) text.reserve(size_t(size) + 1);
+    std::fseek(f, 0, SEEK_SET);
+  }
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0)
+    text.append(chunk, got);
+  std::fclose(f);
+  return text;
+}
+
+inline bool is_blank(char c) {
+  return c == ' ' || c == '\t' || c == '\v' || c == '\f' || c == '\r';
+}
+
+// Calls row(begin, end) for every line of text[lo, hi) that is neither
+// empty nor a comment ('#' first); lines start in [lo, hi).
+template <typename F>
+void for_rows(const std::string& text, size_t lo, size_t hi, F&& row) {
+  const char* base = text.data();
+  size_t pos = lo;
+  while (pos < hi) {
+    const void* nl = std::memchr(base + pos, '\n', text.size() - pos);
+    const size_t end = nl ? size_t(static_cast<const char*>(nl) - base)
+                          : text.size();
+    size_t stop = end;
+    if (stop > pos && base[stop - 1] == '\r') --stop;
+    if (stop > pos && base[pos] != '#') row(base + pos, base + stop);
+    pos = end + 1;
+  }
+}
+
 // Rows of whitespace-separated text files (particles.cpp:383-497): lines
 // that are empty or start with '#' are skipped, and field k takes row
-// entry index_of[k] (-1: absent).  Lines are parsed by all host threads
-// with std::from_chars, which rounds correctly as stream extraction does.
+// entry index_of[k] (-1: absent).  Each file is split into one chunk per
+// host thread at line boundaries; a counting pass and a prefix sum give
+// every chunk its first row, and a second pass parses the chunk into the
+// columns with std::from_chars, which rounds correctly as stream
+// extraction does.
 void parse_text(const std::vector<std::string>& paths, const int index_of[6],
                 std::vector<std::vector<double>>& cols) {
-  std::string text;
-  std::vector<std::pair<size_t, size_t>> lines;
-  for (const std::string& path : paths) {
-    std::ifstream fin(path, std::ios::binary);
-    if (!fin)
-      throw_error(TRVG_ERR_INVALID_DATA, "Failed to open file: %s",
-                  path.c_str());
-    std::stringstream ss;
-    ss << fin.rdbuf();
-    const size_t base = text.size();
-    text += ss.str();
-    text += '\n';
-    size_t pos = base;
-    while (pos < text.size()) {
-      size_t end = text.find('\n', pos);
-      if (end == std::string::npos) end = text.size();
-      size_t stop = end;
-      if (stop > pos && text[stop - 1] == '\r') --stop;
-      if (stop > pos && text[pos] != '#') lines.push_back({pos, stop});
-      pos = end + 1;
-    }
-  }
   int need = 0;
   for (int k = 0; k < 6; ++k) need = std::max(need, index_of[k] + 1);
-  const int64_t n = int64_t(lines.size());
+  const int nthr = int(std::max(1u, std::min(32u,
+                                             std::thread::hardware_concurrency())));
+  std::vector<std::string> texts;
+  std::vector<std::vector<size_t>> bounds;
+  std::vector<std::vector<int64_t>> first;
+  int64_t n = 0;
+  for (const std::string& path : paths) {
+    texts.push_back(slurp(path));
+    const std::string& text = texts.back();
+    std::vector<size_t> b(nthr + 1, text.size());
+    b[0] = 0;
+    for (int t = 1; t < nthr; ++t) {
+      size_t p = text.size() * size_t(t) / size_t(nthr);
+      const void* nl = p < text.size()
+                           ? std::memchr(text.data() + p, '\n', text.size() - p)
+                           : nullptr;
+      b[t] = nl ? size_t(static_cast<const char*>(nl) - text.data()) + 1
+                : text.size();
+      b[t] = std::max(b[t], b[t - 1]);
+    }
+    std::vector<int64_t> count(nthr, 0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; ++t)
+      pool.emplace_back([&, t] {
+        for_rows(text, b[t], b[t + 1],
+                 [&](const char*, const char*) { ++count[t]; });
+      });
+    for (auto& th : pool) th.join();
+    std::vector<int64_t> f(nthr + 1, n);
+    for (int t = 0; t < nthr; ++t) f[t + 1] = f[t] + count[t];
+    n = f[nthr];
+    bounds.push_back(std::move(b));
+    first.push_back(std::move(f));
+  }
   for (int k = 0; k < 6; ++k)
     if (index_of[k] >= 0) cols[k].assign(size_t(n), 0.);
-  const int nthr = int(std::max(1u, std::min(16u,
-                                             std::thread::hardware_concurrency())));
   std::vector<int64_t> bad(nthr, -1);
-  auto work = [&](int t) {
-    const int64_t lo = n * t / nthr, hi = n * (t + 1) / nthr;
-    std::vector<double> row;
-    for (int64_t i = lo; i < hi; ++i) {
-      const char* p = text.data() + lines[i].first;
-      const char* e = text.data() + lines[i].second;
-      row.clear();
-      while (p < e && int(row.size()) < need) {
-        while (p < e && (*p == ' ' || *p == '\t' || *p == '\v' || *p == '\f'))
-          ++p;
-        if (p >= e) break;
-        double v = 0.;
-        const char* q = (*p == '+') ? p + 1 : p;
-        const auto r = std::from_chars(q, e, v);
-        if (r.ec != std::errc() && r.ec != std::errc::result_out_of_range)
-          break;
-        row.push_back(v);
-        p = r.ptr;
-      }
-      if (int(row.size()) < need) {
-        bad[t] = i;
-        return;
-      }
-      for (int k = 0; k < 6; ++k)
-        if (index_of[k] >= 0) cols[k][i] = row[index_of[k]];
-    }
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nthr; ++t) pool.emplace_back(work, t);
-  work(0);
-  for (auto& th : pool) th.join();
+  for (size_t fi = 0; fi < texts.size(); ++fi) {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; ++t)
+      pool.emplace_back([&, t, fi] {
+        int64_t i = first[fi][t];
+        double row[6];
+        for_rows(texts[fi], bounds[fi][t], bounds[fi][t + 1],
+                 [&](const char* p, const char* e) {
+                   int got = 0;
+                   double v = 0.;
+                   while (p < e && got < need) {
+                     while (p < e && is_blank(*p)) ++p;
+                     if (p >= e) break;
+                     const char* q = (*p == '+') ? p + 1 : p;
+                     const auto r = std::from_chars(q, e, v);
+                     if (r.ec != std::errc() &&
+                         r.ec != std::errc::result_out_of_range)
+                       break;
+                     for (int k = 0; k < 6; ++k)
+                       if (index_of[k] == got) row[k] = v;
+                     ++got;
+                     p = r.ptr;
+                   }
+                   if (got < need) {
+                     if (bad[t] < 0) bad[t] = i;
+                   } else {
+                     for (int k = 0; k < 6; ++k)
+                       if (index_of[k] >= 0) cols[k][size_t(i)] = row[k];
+                   }
+                   ++i;
+                 });
+      });
+    for (auto& th : pool) th.join();
+    texts[fi].clear();
+    texts[fi].shrink_to_fit();
+  }
   for (int t = 0; t < nthr; ++t)
     if (bad[t] >= 0)
       throw_error(TRVG_ERR_INVALID_DATA,
