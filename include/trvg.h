@@ -214,7 +214,11 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *   "autotune"         0/1: time candidate launch shapes (catalogue-sort
  *                           tile side, pair-reduction bin batch) on first
  *                           use and keep the fastest (default 1; 0 also
- *                           forgets earlier choices). */
+ *                           forgets earlier choices);
+ *   "assign_path"      FP32 real meshes of sorted catalogues: 0 the
+ *                           autotuner's choice (default), 1 the
+ *                           shared-memory tiled deposit (32^3 tiles),
+ *                           2 per-particle global atomics (finer tiles). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
 /* Launch shapes the autotuner chose so far: key and value. */
 int trvg_tuned_count(const trvg_context* ctx, int* count);

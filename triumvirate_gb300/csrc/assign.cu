@@ -404,6 +404,220 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
   }
 }
 
+// ---- Tiled FP32 deposit ------------------------------------------------------
+//
+// For a catalogue sorted by 32^3-cell mesh tiles, one block owns one tile at
+// a time and deposits the tile's particles into a shared-memory window of
+// the tile plus the cells its stencils reach (one below, two above per
+// axis: (32 + 3)^3 floats), with shared-memory atomics.  The window then
+// goes to the mesh once: cells that no other tile's particles reach (tile
+// offsets 2 .. extent - 2 on every axis) are stored, the others take one
+// global atomic per nonzero cell.  Particles off the fast FP32 stencil
+// (near a tie, or outside the box) are appended to a list with
+// warp-aggregated atomics and deposited exactly by assign_deferred_kernel.
+
+constexpr int kTileShift = 5;
+constexpr int kTile = 1 << kTileShift;
+constexpr int kHaloLo = 1, kHaloHi = 2;
+constexpr int kWin = kTile + kHaloLo + kHaloHi;  // x and y extent
+// z: the window starts 4 cells below the tile so that its rows are
+// 16-byte aligned in the mesh (float4 flush); 40 = 4 + 32 + 2, rounded up.
+constexpr int kZLo = 4;
+constexpr int kWinZ = 40;
+constexpr int kGroupsZ = kWinZ / 4;
+constexpr int kWinCells = kWin * kWin * kWinZ;
+constexpr int kTiledBlock = 1024;
+
+struct TiledArgs {
+  AssignArgs a;
+  int tiles[3];
+  int* deferred;   // particle positions (from the first) taking the exact path
+  int* ndeferred;
+  const double* fill_dsum;  // the mesh holds the fill value (first deposit)
+  double fill_hsum;
+  bool store_exclusive;
+};
+
+// Window coordinate of cell `c` for a tile starting at `lo` (periodic):
+// `below` cells of the window lie under the tile, `extent` in all.
+template <int below, int extent>
+__device__ __forceinline__ int win_coord(int c, int lo, int n) {
+  int l = c - lo + below;
+  if (l < 0) l += n;
+  else if (l >= extent) l -= n;
+  return l;
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(kTiledBlock, 1)
+assign_tiled_kernel(TiledArgs t, float* mesh, double* sums) {
+  extern __shared__ __align__(16) float win[];
+  const AssignArgs& a = t.a;
+  const int ntiles = t.tiles[0] * t.tiles[1] * t.tiles[2];
+  const int64_t np = a.cat.count(), p0 = a.cat.first();
+  const bool uniform = a.cat.w == nullptr;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  float fill = 0.f;
+  if (t.store_exclusive)
+    fill = float(-((t.fill_dsum != nullptr) ? *t.fill_dsum : t.fill_hsum) /
+                 double(a.nmesh));
+  long long nland = 0;
+  double acc = 0.;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int b = a.cat.tile_start[tile];
+    const int e = (tile + 1 < ntiles) ? a.cat.tile_start[tile + 1] : int(np);
+    if (b >= e) continue;
+    const int tz = tile % t.tiles[2];
+    const int ty = (tile / t.tiles[2]) % t.tiles[1];
+    const int tx = tile / (t.tiles[2] * t.tiles[1]);
+    const int lo[3] = {tx << kTileShift, ty << kTileShift, tz << kTileShift};
+    int ext[3], wn[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      ext[i] = min(kTile, a.n[i] - lo[i]);
+      wn[i] = ext[i] + kHaloLo + kHaloHi;
+    }
+    for (int i = threadIdx.x; i < kWinCells / 4; i += blockDim.x)
+      reinterpret_cast<float4*>(win)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = (kWinCells / 4) * 4 + threadIdx.x; i < kWinCells;
+         i += blockDim.x)
+      win[i] = 0.f;
+    __syncthreads();
+    for (int base = b; base < e; base += blockDim.x) {
+      const int q = base + threadIdx.x;
+      const bool valid = q < e;
+      bool fast = false;
+      StencilF<ORDER> sx, sy, sz;
+      float wgt = 0.f;
+      if (valid) {
+        const int64_t p = p0 + q;
+        double w = (a.cat.w != nullptr) ? a.cat.w[p] : 1.0;
+        double wp = w;
+        for (int i = 1; i < a.ws.power; ++i) wp *= w;
+        const double wd = a.ws.scale * wp;
+        wgt = float(wd);
+        fast = axis_stencil_f<ORDER>(a.cat.x[p], a.n[0], a.ratio[0], sx,
+                                     nullptr) &&
+               axis_stencil_f<ORDER>(a.cat.y[p], a.n[1], a.ratio[1], sy,
+                                     nullptr) &&
+               axis_stencil_f<ORDER>(a.cat.z[p], a.n[2], a.ratio[2], sz,
+                                     nullptr);
+        if (fast) {
+          if (uniform) ++nland;
+          else acc += wd;
+        }
+      }
+      // Warp-aggregated append of the particles that take the exact path.
+      const unsigned slow = __ballot_sync(0xffffffffu, valid && !fast);
+      if (slow != 0u) {
+        const int leader = __ffs(slow) - 1;
+        int at = 0;
+        if (lane == leader) at = atomicAdd(t.ndeferred, __popc(slow));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (valid && !fast)
+          t.deferred[at + __popc(slow & ((1u << lane) - 1u))] = q;
+      }
+      if (!fast) continue;
+      int lx[ORDER], ly[ORDER], lz[ORDER];
+#pragma unroll
+      for (int k = 0; k < ORDER; ++k) {
+        lx[k] = win_coord<kHaloLo, kWin>(sx.idx[k], lo[0], a.n[0]);
+        ly[k] = win_coord<kHaloLo, kWin>(sy.idx[k], lo[1], a.n[1]);
+        lz[k] = win_coord<kZLo, kWinZ>(sz.idx[k], lo[2], a.n[2]);
+      }
+#pragma unroll
+      for (int i = 0; i < ORDER; ++i) {
+        const float wi = sx.win[i] * wgt;
+#pragma unroll
+        for (int j = 0; j < ORDER; ++j) {
+          const float wij = wi * sy.win[j];
+          float* row = win + (lx[i] * kWin + ly[j]) * kWinZ;
+#pragma unroll
+          for (int k = 0; k < ORDER; ++k) atomicAdd(row + lz[k], wij * sz.win[k]);
+        }
+      }
+    }
+    __syncthreads();
+    // Flush in float4 groups along z: groups whose four cells only this
+    // tile reaches are stored over the fill value, the other nonzero
+    // groups take one vector atomic.
+    const int rows = wn[0] * wn[1];
+    const int zlo = lo[2] - kZLo;
+    for (int i = threadIdx.x; i < rows * kGroupsZ; i += blockDim.x) {
+      const int r = i / kGroupsZ, q = i - r * kGroupsZ;
+      const int wx = r / wn[1], wy = r - wx * wn[1];
+      const float4 v =
+          reinterpret_cast<const float4*>(win + (wx * kWin + wy) * kWinZ)[q];
+      if (v.x == 0.f && v.y == 0.f && v.z == 0.f && v.w == 0.f) continue;
+      int gx = lo[0] - kHaloLo + wx, gy = lo[1] - kHaloLo + wy;
+      gx += (gx < 0) ? a.n[0] : ((gx >= a.n[0]) ? -a.n[0] : 0);
+      gy += (gy < 0) ? a.n[1] : ((gy >= a.n[1]) ? -a.n[1] : 0);
+      int gz = zlo + 4 * q;
+      gz += (gz < 0) ? a.n[2] : ((gz >= a.n[2]) ? -a.n[2] : 0);
+      float4* g = reinterpret_cast<float4*>(
+          mesh + (int64_t(gx) * a.n[1] + gy) * a.n[2] + gz);
+      // Tile offsets of the group's cells: 4q - kZLo .. 4q - kZLo + 3.
+      const int c0 = 4 * q - kZLo;
+      const bool excl = t.store_exclusive && wx >= kHaloLo + 2 &&
+                        wx < kHaloLo + ext[0] - 1 && wy >= kHaloLo + 2 &&
+                        wy < kHaloLo + ext[1] - 1 && c0 >= 2 &&
+                        c0 + 3 < ext[2] - 1;
+      if (excl)
+        *g = make_float4(fill + v.x, fill + v.y, fill + v.z, fill + v.w);
+      else
+        atomicAdd(g, v);
+    }
+    __syncthreads();
+  }
+  // Landed weight of the fast-path particles (the k = 0 mode).
+  __shared__ long long cnt[kTiledBlock / 32];
+  __shared__ double red[kTiledBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    nland += __shfl_down_sync(0xffffffffu, nland, o);
+    acc += __shfl_down_sync(0xffffffffu, acc, o);
+  }
+  if (lane == 0) {
+    cnt[wid] = nland;
+    red[wid] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long c = 0;
+    double s = 0.;
+    for (int q = 0; q < nwarps; ++q) {
+      c += cnt[q];
+      s += red[q];
+    }
+    const double land = uniform ? double(c) * a.ws.scale : s;
+    if (land != 0.) atomicAdd(sums, land);
+  }
+}
+
+// The particles the tiled deposit left to the exact FP64 stencil.
+template <int ORDER>
+__global__ void __launch_bounds__(256)
+assign_deferred_kernel(AssignArgs a, const int* deferred,
+                       const int* ndeferred, float* mesh, double* sums) {
+  const int nd = *ndeferred;
+  const int64_t p0 = a.cat.first();
+  double acc = 0.;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd;
+       i += gridDim.x * blockDim.x) {
+    const int64_t p = p0 + deferred[i];
+    const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
+    double w = (a.cat.w != nullptr) ? a.cat.w[p] : 1.0;
+    double wp = w;
+    for (int k = 1; k < a.ws.power; ++k) wp *= w;
+    cd landed[2] = {{0., 0.}, {0., 0.}};
+    exact_particle<ORDER, float>(a, pos, cd{a.ws.scale * wp, 0.}, mesh,
+                                 nullptr, nullptr, nullptr, landed);
+    acc += landed[0].re;
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0 && acc != 0.) atomicAdd(sums, acc);
+}
+
 template <class Real>
 __global__ void sum_pow_kernel(const Real* mesh, int64_t n, int order,
                                double* out) {
@@ -489,11 +703,45 @@ int grid_for(int64_t work, int block) {
 
 }  // namespace
 
+// Tiled deposit of a real FP32 mesh without interlacing, for a catalogue
+// sorted by 32^3 tiles on a mesh of at least 64 cells per axis (the window
+// of one tile then never wraps onto itself).
+template <int ORDER>
+void launch_tiled(Context& ctx, const AssignArgs& a, float* mesh,
+                  double* sums, const MeshFill* fill) {
+  TiledArgs t;
+  t.a = a;
+  for (int i = 0; i < 3; ++i) t.tiles[i] = (a.n[i] + kTile - 1) >> kTileShift;
+  t.deferred = ctx.buf<int>("assign.deferred", size_t(a.cat.n));
+  t.ndeferred = ctx.buf<int>("assign.ndeferred", 1);
+  t.fill_dsum = fill ? fill->dsum : nullptr;
+  t.fill_hsum = fill ? fill->hsum : 0.;
+  t.store_exclusive = fill != nullptr;
+  TRVG_CUDA(cudaMemsetAsync(t.ndeferred, 0, sizeof(int), ctx.stream));
+  const size_t smem = size_t(kWinCells) * sizeof(float);
+  static bool configured[64] = {};
+  if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+    TRVG_CUDA(cudaFuncSetAttribute(assign_tiled_kernel<ORDER>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(smem)));
+    if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+  }
+  const int ntiles = t.tiles[0] * t.tiles[1] * t.tiles[2];
+  TRVG_KBEGIN(ctx, "assign_tiled_kernel");
+  assign_tiled_kernel<ORDER><<<std::min(ntiles, 152), kTiledBlock, smem,
+                               ctx.stream>>>(t, mesh, sums);
+  TRVG_LAUNCHED(ctx);
+  TRVG_KBEGIN(ctx, "assign_deferred_kernel");
+  assign_deferred_kernel<ORDER><<<152, 256, 0, ctx.stream>>>(
+      a, t.deferred, t.ndeferred, mesh, sums);
+  TRVG_LAUNCHED(ctx);
+}
+
 template <class Real>
 void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                    const DevCatalogue& cat, const WeightSpec& ws,
                    Real* mesh_re, Real* mesh_im, Real* shadow_re,
-                   Real* shadow_im, double* sums) {
+                   Real* shadow_im, double* sums, const MeshFill* fill) {
   if (cat.n == 0) return;
   AssignArgs a;
   for (int i = 0; i < 3; ++i) {
@@ -511,6 +759,23 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
   };
   a.vec4 = g.n[2] % 4 == 0 && aligned16(mesh_re) && aligned16(mesh_im) &&
            aligned16(sre) && aligned16(sim);
+  if constexpr (sizeof(Real) == 4) {
+    const bool tiled = cat.tile_start != nullptr &&
+                       cat.tile_shift == kTileShift && !interlace &&
+                       mesh_im == nullptr && !ws.use_ylm && a.vec4 &&
+                       g.n[0] >= 64 &&
+                       g.n[1] >= 64 && g.n[2] >= 64 &&
+                       cat.n <= int64_t(2147483647);
+    if (tiled) {
+      switch (order) {
+        case 1: return launch_tiled<1>(ctx, a, mesh_re, sums, fill);
+        case 2: return launch_tiled<2>(ctx, a, mesh_re, sums, fill);
+        case 3: return launch_tiled<3>(ctx, a, mesh_re, sums, fill);
+        case 4: return launch_tiled<4>(ctx, a, mesh_re, sums, fill);
+        default: break;
+      }
+    }
+  }
   const int block = 256;
   // Several particles per thread: the per-block k = 0 sums are amortised.
   const int grid = std::min(grid_for(cat.n, block), 152 * 8);
@@ -579,7 +844,7 @@ void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
 #define TRVG_INST(R)                                                        \
   template void launch_assign<R>(Context&, const Geom&, int, bool,          \
                                  const DevCatalogue&, const WeightSpec&, R*, \
-                                 R*, R*, R*, double*);                      \
+                                 R*, R*, R*, double*, const MeshFill*);     \
   template void launch_mesh_sum_pow<R>(Context&, const R*, int64_t, int,    \
                                        double*);                            \
   template void launch_mesh_to_double<R>(Context&, const R*, int64_t,       \

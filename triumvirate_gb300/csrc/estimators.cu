@@ -548,7 +548,13 @@ struct Engine {
     char key[96];
     std::snprintf(key, sizeof(key), "sort_tile_shift.%dx%dx%d.order%d.n2^%d",
                   g.n[0], g.n[1], g.n[2], p.assignment_order, lg);
-    const int shift = tuned(key, {3, 2, 4}, [&](int sh) {
+    // 5: 32^3 tiles, which FP32 real meshes deposit through shared memory.
+    if (ctx.assign_path == 1) return sort_catalogue(ctx, g, d, tag, 5);
+    const vector<int> cands = ctx.assign_path == 2 ? vector<int>{3, 2, 4}
+                                                   : vector<int>{5, 3, 2, 4};
+    std::snprintf(key + std::strlen(key), sizeof(key) - std::strlen(key),
+                  ".path%d", ctx.assign_path);
+    const int shift = tuned(key, cands, [&](int sh) {
       const DevCatalogue sd = sort_catalogue(ctx, g, d, tag, sh);
       Real* m = ctx.buf<Real>("mesh.re", g.nmesh);
       double* sums = ctx.buf<double>("assign.sums", 4);
@@ -593,9 +599,11 @@ struct Engine {
     if (sim) launch_fill_offset<Real>(ctx, sim, g.nmesh, wsum_im, 0.);
     double* sums = ctx.buf<double>("assign.sums", 4);
     zero(sums, 4 * sizeof(double));
-    for (const Part& part : parts)
-      launch_assign<Real>(ctx, g, p.assignment_order, interlace, part.cat,
-                          part.ws, mre, mim, sre, sim, sums);
+    const MeshFill fill{wsum, hsum};
+    for (size_t i = 0; i < parts.size(); ++i)
+      launch_assign<Real>(ctx, g, p.assignment_order, interlace, parts[i].cat,
+                          parts[i].ws, mre, mim, sre, sim, sums,
+                          i == 0 ? &fill : nullptr);
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
     auto r2c = [&](Real* m, const char* suffix) -> const C* {
       C* o = ctx.buf<C>(name + suffix, size_t(g.nhalf));

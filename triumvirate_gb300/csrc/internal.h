@@ -142,6 +142,9 @@ struct Context {
   // sort, bin batch of the pair reduction), cached by key.
   bool autotune = true;
   std::map<std::string, int> tuned;
+  // Deposit of sorted catalogues: 0 tuned, 1 tiled (shared memory),
+  // 2 global atomics.
+  int assign_path = 0;
   // Mocks replayed from the captured graph by the last batch call.
   int64_t graph_replays = 0;
   // Deposits made so far (FieldSpec::mesh_gen).

@@ -41,12 +41,26 @@ struct DevCatalogue {
   // on the device (the columns then start at x + *dev_first).
   const int64_t* dev_n = nullptr;
   const int64_t* dev_first = nullptr;
+  // Set by sort_catalogue: particles of mesh tile k (cubes of 2^tile_shift
+  // cells, x-major) are [tile_start[k], tile_start[k + 1]), the last tile
+  // ending at count().
+  const int* tile_start = nullptr;
+  int tile_shift = 0;
   __device__ __forceinline__ int64_t count() const {
     return dev_n != nullptr ? *dev_n : n;
   }
   __device__ __forceinline__ int64_t first() const {
     return dev_first != nullptr ? *dev_first : 0;
   }
+};
+
+// The value every cell of a mesh holds before its first deposit
+// (fill_offset_kernel: -sum / ncells, sum read from dsum when given).  With
+// it the tiled assignment stores the cells that only its own tile reaches
+// instead of adding to them.
+struct MeshFill {
+  const double* dsum = nullptr;
+  double hsum = 0.;
 };
 
 // Per-particle weight scale * w^power * [conj] y_lm(los).
@@ -108,7 +122,8 @@ template <class Real>
 void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                    const DevCatalogue& cat, const WeightSpec& ws,
                    Real* mesh_re, Real* mesh_im, Real* shadow_re,
-                   Real* shadow_im, double* sums /* [4]: re, im, s_re, s_im */);
+                   Real* shadow_im, double* sums /* [4]: re, im, s_re, s_im */,
+                   const MeshFill* fill = nullptr);
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
                        const WeightSpec& ws, double* out /* [2] */);
 template <class Real>

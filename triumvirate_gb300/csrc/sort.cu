@@ -193,6 +193,8 @@ DevCatalogue sort_catalogue(Context& ctx, const Geom& g, const DevCatalogue& in,
   d.ly = o.ly;
   d.lz = o.lz;
   d.dev_n = in.dev_n;  // the sorted copy starts at its first element
+  d.tile_start = count;
+  d.tile_shift = shift;
   return d;
 }
 
