@@ -215,6 +215,9 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           tile side, pair-reduction bin batch) on first
  *                           use and keep the fastest (default 1; 0 also
  *                           forgets earlier choices);
+ *   "fused_ylm"        0/1: FP32 meshes: build the Y_lm-weighted fields of
+ *                           every order of a survey estimate in one fused
+ *                           pass per catalogue (default 1);
  *   "assign_path"      FP32 real meshes of sorted catalogues: 0 the
  *                           autotuner's choice (default), 1 the
  *                           shared-memory tiled deposit (32^3 tiles),

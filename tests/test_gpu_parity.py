@@ -792,3 +792,55 @@ def test_tiled_assignment_in_estimators(assignment, rand_catalogue_array):
         for k in ('bk_raw', 'bk_shot'):
             scale = np.max(np.abs(a[k]))
             assert np.max(np.abs(t[k] - a[k])) / scale < 1e-6, (fn, k)
+
+
+# ---------------------------------------------------------------------------
+# Y_lm-weighted fields of every order in one fused pass
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("degrees, assignment", [((2, 0, 2), 'tsc'),
+                                                 ((2, 2, 4), 'pcs'),
+                                                 ((1, 1, 0), 'cic')])
+def test_fused_ylm_fields_match_one_by_one(degrees, assignment,
+                                           rand_catalogue_array):
+    """Survey bispectrum, 3PCF and 3PCF window with every Y_lm-weighted
+    field built by one weight-sum and one deposit pass per catalogue (FP32
+    meshes) against the fields built one order at a time.  B_224 has nine
+    orders M (27 targets, two fused passes)."""
+    rng = np.random.default_rng(31)
+    d = rng.uniform(-500., 500., size=(5000, 3))
+    r = rand_catalogue_array
+    ctx = _lib.default_context(None)
+    samp = _sampling('fp32mixed', 32, assignment=assignment)
+    kb = Binning('fourier', 'lin', 0.01, 0.1, 3)
+    rb = Binning('config', 'lin', 60., 160., 3)
+
+    def cats():
+        return (ParticleCatalogue(*d.T, nz=3e-9),
+                ParticleCatalogue(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3]))
+
+    def run(fused):
+        ctx.set_option('fused_ylm', fused)
+        try:
+            dc, rc = cats()
+            b = compute_bispec(dc, rc, degrees=degrees, binning=kb,
+                               form='full', sampling_params=samp)
+            dc, rc = cats()
+            z = compute_3pcf(dc, rc, degrees=degrees, binning=rb,
+                             form='diag', sampling_params=samp)
+            _, rc = cats()
+            w = compute_3pcf_window(rc, degrees=degrees, binning=rb,
+                                    form='diag', sampling_params=samp)
+        finally:
+            ctx.set_option('fused_ylm', 1)
+        return b, z, w
+    fb, fz, fw = run(1)
+    sb, sz, sw = run(0)
+    # FP32 atomics deposit in a different order on every run; a wrong order
+    # M, power or conjugation would differ at O(1).
+    for a, b, keys in [(fb, sb, ('bk_raw', 'bk_shot')),
+                       (fz, sz, ('zeta_raw', 'zeta_shot')),
+                       (fw, sw, ('zeta_raw', 'zeta_shot'))]:
+        for k in keys:
+            scale = np.max(np.abs(b[k]))
+            assert np.max(np.abs(a[k] - b[k])) <= 1e-5 * scale, k

@@ -492,10 +492,13 @@ assign_tiled_kernel(TiledArgs t, float* mesh, double* sums) {
       float wgt = 0.f;
       if (valid) {
         const int64_t p = p0 + q;
-        double w = (a.cat.w != nullptr) ? a.cat.w[p] : 1.0;
-        double wp = w;
-        for (int i = 1; i < a.ws.power; ++i) wp *= w;
-        const double wd = a.ws.scale * wp;
+        double wd = a.ws.scale;
+        if (!uniform) {
+          const double w = a.cat.w[p];
+          double wp = w;
+          for (int i = 1; i < a.ws.power; ++i) wp *= w;
+          wd *= wp;
+        }
         wgt = float(wd);
         fast = axis_stencil_f<ORDER>(a.cat.x[p], a.n[0], a.ratio[0], sx,
                                      nullptr) &&
@@ -616,6 +619,119 @@ assign_deferred_kernel(AssignArgs a, const int* deferred,
   }
   acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0 && acc != 0.) atomicAdd(sums, acc);
+}
+
+// ---- Y_lm-weighted fields of every order in one pass -----------------------
+//
+// Per particle: the weight powers, the reduced harmonics of every order
+// (FP64 Legendre recurrences, reduced_ylm_all) and the FP32 stencil are
+// formed once; each target then deposits its complex weight.
+
+__device__ __forceinline__ cd target_weight(const YlmTarget& t,
+                                            const double* wpow,
+                                            const cd* ypos, int ell) {
+  const cd y = (ell == 0) ? cd{1., 0.} : ylm_of(ypos, t.m);
+  const cd v = t.conj ? conjg(y) : y;
+  if (ell == 0) return cd{t.scale * wpow[t.power], 0.};
+  return (t.scale * wpow[t.power]) * v;
+}
+
+__device__ __forceinline__ void particle_terms(const DevCatalogue& cat,
+                                               int64_t p, int ell,
+                                               double* wpow, cd* ypos) {
+  const double w = (cat.w != nullptr) ? cat.w[p] : 1.0;
+  wpow[0] = 1.;
+  wpow[1] = w;
+  wpow[2] = w * w;
+  wpow[3] = wpow[2] * w;
+  if (ell > 0) reduced_ylm_all(ell, cat.lx[p], cat.ly[p], cat.lz[p], ypos);
+}
+
+__global__ void __launch_bounds__(256)
+ylm_weight_sums_kernel(DevCatalogue cat, YlmTargets ts, double* out) {
+  cd acc[kMaxYlmTargets];
+#pragma unroll
+  for (int t = 0; t < kMaxYlmTargets; ++t) acc[t] = cd{0., 0.};
+  const int64_t np = cat.count(), p0 = cat.first();
+  for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
+    double wpow[4];
+    cd ypos[kMaxYlmDegree + 1];
+    particle_terms(cat, p, ts.ell, wpow, ypos);
+#pragma unroll
+    for (int t = 0; t < kMaxYlmTargets; ++t) {
+      if (t >= ts.count) break;
+      // scale applied after the sum, as in weight_sum_kernel
+      YlmTarget u = ts.t[t];
+      u.scale = 1.;
+      acc[t] = acc[t] + target_weight(u, wpow, ypos, ts.ell);
+    }
+  }
+  __shared__ double red[2][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int t = 0; t < ts.count; ++t) {
+    const double v0 = warp_sum(acc[t].re), v1 = warp_sum(acc[t].im);
+    if (lane == 0) {
+      red[0][wid] = v0;
+      red[1][wid] = v1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      double s = 0.;
+      for (int q = 0; q < int(blockDim.x >> 5); ++q) s += red[threadIdx.x][q];
+      atomicAdd(out + 2 * t + threadIdx.x, ts.t[t].scale * s);
+    }
+    __syncthreads();
+  }
+}
+
+template <int ORDER, bool SH>
+__global__ void __launch_bounds__(256)
+assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
+  const int64_t np = a.cat.count(), p0 = a.cat.first();
+  for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
+    double wpow[4];
+    cd ypos[kMaxYlmDegree + 1];
+    particle_terms(a.cat, p, ts.ell, wpow, ypos);
+    const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
+    StencilF<ORDER> sx, sy, sz, hx, hy, hz;
+    const bool fast =
+        axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                              SH ? &hx : nullptr) &&
+        axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                              SH ? &hy : nullptr) &&
+        axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                              SH ? &hz : nullptr);
+    for (int t = 0; t < ts.count; ++t) {
+      const YlmTarget& u = ts.t[t];
+      if (u.re == nullptr) continue;
+      const cd wgt = target_weight(u, wpow, ypos, ts.ell);
+      if (fast) {
+        deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), u.re);
+        if (u.im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), u.im);
+        if constexpr (SH) {
+          deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), u.sre);
+          if (u.sim != nullptr)
+            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), u.sim);
+        }
+      } else {
+        // The target's sums hold the full weight: add what did not land.
+        cd landed[2] = {{0., 0.}, {0., 0.}};
+        exact_particle<ORDER, float>(a, pos, wgt, u.re, u.im,
+                                     SH ? u.sre : nullptr,
+                                     SH ? u.sim : nullptr, landed);
+        const cd d0 = landed[0] - wgt;
+        if (d0.re != 0.) atomicAdd(u.sums + 0, d0.re);
+        if (d0.im != 0.) atomicAdd(u.sums + 1, d0.im);
+        if constexpr (SH) {
+          const cd d1 = landed[1] - wgt;
+          if (d1.re != 0.) atomicAdd(u.sums + 2, d1.re);
+          if (d1.im != 0.) atomicAdd(u.sums + 3, d1.im);
+        }
+      }
+    }
+  }
 }
 
 template <class Real>
@@ -830,6 +946,53 @@ void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
   fill_offset_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(
       mesh, n, dsum, hsum);
   TRVG_LAUNCHED(ctx);
+}
+
+void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
+                            const YlmTargets& ts, double* out) {
+  if (cat.n == 0 || ts.count == 0) return;
+  if (ts.count > kMaxYlmTargets || ts.ell > kMaxYlmDegree || ts.ell < 0)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Too many Y_lm targets.");
+  TRVG_KBEGIN(ctx, "weight_sum_kernel");
+  ylm_weight_sums_kernel<<<grid_for(cat.n, 256), 256, 0, ctx.stream>>>(
+      cat, ts, out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
+                       const DevCatalogue& cat, const YlmTargets& ts) {
+  if (cat.n == 0 || ts.count == 0) return;
+  if (ts.count > kMaxYlmTargets || ts.ell > kMaxYlmDegree || ts.ell < 0)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Too many Y_lm targets.");
+  AssignArgs a;
+  for (int i = 0; i < 3; ++i) {
+    a.n[i] = g.n[i];
+    a.L[i] = g.L[i];
+    a.ratio[i] = double(g.n[i]) / g.L[i];
+  }
+  a.nmesh = g.nmesh;
+  a.cat = cat;
+  a.ws = WeightSpec();
+  a.vec4 = g.n[2] % 4 == 0;
+  for (int t = 0; t < ts.count; ++t)
+    for (const float* q : {ts.t[t].re, ts.t[t].im, ts.t[t].sre, ts.t[t].sim})
+      if (q != nullptr && reinterpret_cast<uintptr_t>(q) % 16 != 0)
+        a.vec4 = false;
+  const int grid = std::min(grid_for(cat.n, 256), 152 * 8);
+  auto go = [&](auto kernel) {
+    TRVG_KBEGIN(ctx, "assign_kernel");
+    kernel<<<grid, 256, 0, ctx.stream>>>(a, ts);
+    TRVG_LAUNCHED(ctx);
+  };
+  switch (order) {
+    case 1: interlace ? go(assign_ylm_kernel<1, true>) : go(assign_ylm_kernel<1, false>); break;
+    case 2: interlace ? go(assign_ylm_kernel<2, true>) : go(assign_ylm_kernel<2, false>); break;
+    case 3: interlace ? go(assign_ylm_kernel<3, true>) : go(assign_ylm_kernel<3, false>); break;
+    case 4: interlace ? go(assign_ylm_kernel<4, true>) : go(assign_ylm_kernel<4, false>); break;
+    default:
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Unsupported mesh assignment order: %d.", order);
+  }
 }
 
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,

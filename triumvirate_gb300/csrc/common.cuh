@@ -141,6 +141,44 @@ TRVG_HD cd reduced_ylm(int ell, int m, double x, double y, double z) {
   return sqrt(4.0 * kPi / (2.0 * ell + 1.0)) * ylm;
 }
 
+// y_lm for m = 0..ell at once (y[m]); the distance, the polar cosine and
+// the powers of exp(i phi) are formed once, each m then takes the same
+// operations as reduced_ylm, so every value has the same bits.  Negative
+// orders follow exactly as y_l,-m = (-1)^m conj(y_lm) (ylm_of).
+TRVG_HD void reduced_ylm_all(int ell, double x, double y, double z, cd* out) {
+  if (ell == 0) {
+    out[0] = cmk(1.0, 0.0);
+    return;
+  }
+  const double eps = 1.e-9;
+  const double r = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+  if (fabs(r) < eps) {
+    for (int m = 0; m <= ell; ++m) out[m] = cmk(0.0, 0.0);
+    return;
+  }
+  const double mu = z / r;
+  const double rxy = dsqrt(dadd(dmul(x, x), dmul(y, y)));
+  double c = 1.0, s = 0.0;
+  if (fabs(rxy) >= eps) {
+    c = x / rxy;
+    s = y / rxy;
+  }
+  const double norm = sqrt(4.0 * kPi / (2.0 * ell + 1.0));
+  cd e = cmk(1.0, 0.0);
+  for (int m = 0; m <= ell; ++m) {
+    if (m > 0) e = e * cmk(c, s);
+    const double p = sph_plm(ell, m, mu);
+    out[m] = norm * conjg(p * e);
+  }
+}
+
+// y_lm of any order from the non-negative orders of reduced_ylm_all.
+TRVG_HD cd ylm_of(const cd* ypos, int m) {
+  if (m >= 0) return ypos[m];
+  const cd v = conjg(ypos[-m]);
+  return (m & 1) ? -1.0 * v : v;
+}
+
 // ---------------------------------------------------------------------------
 // Spherical Bessel functions (maths.cpp:309-375).
 // ---------------------------------------------------------------------------

@@ -631,6 +631,153 @@ struct Engine {
     return f;
   }
 
+  // Y_lm-weighted fields of degree `ell` for several orders, weight powers
+  // and conjugations, each the data (scale_d) and randoms (scale_r) parts
+  // (compute_ylm_wgtd_field / compute_ylm_wgtd_quad_field,
+  // field.cpp:1246-1500).  FP32 meshes are built by one weight-sum pass and
+  // one fused deposit pass per catalogue for every target (the harmonics of
+  // a particle are evaluated once); other precisions, or the option
+  // fused_ylm off, build them one by one.  A target without a name only
+  // sums its weights (sums[0..1]).
+  struct YlmField {
+    std::string name;  // empty: weight sum only
+    int m = 0;
+    int power = 1;
+    bool conj = false;
+    double scale_d = 1., scale_r = 0.;
+    bool cplx = false;
+  };
+
+  vector<Field> make_ylm_fields(int ell, const DevCatalogue* dd,
+                                const DevCatalogue* dr,
+                                const vector<YlmField>& ts) {
+    auto ws_of = [&](const YlmField& t, double scale) {
+      WeightSpec w;
+      w.scale = scale;
+      w.power = t.power;
+      w.use_ylm = !(ell == 0 && t.m == 0);
+      w.ell = ell;
+      w.m = t.m;
+      w.conj_ylm = t.conj;
+      return w;
+    };
+    vector<Field> out(ts.size());
+    const bool fused = sizeof(Real) == 4 && ctx.fused_ylm &&
+                       replay == nullptr && ell <= kMaxYlmDegree;
+    if (fused && ts.size() > size_t(kMaxYlmTargets)) {
+      for (size_t i0 = 0; i0 < ts.size(); i0 += kMaxYlmTargets) {
+        const size_t i1 = std::min(ts.size(), i0 + kMaxYlmTargets);
+        const vector<Field> part = make_ylm_fields(
+            ell, dd, dr, vector<YlmField>(ts.begin() + i0, ts.begin() + i1));
+        std::copy(part.begin(), part.end(), out.begin() + i0);
+      }
+      return out;
+    }
+    if (!fused) {
+      for (size_t i = 0; i < ts.size(); ++i) {
+        const YlmField& t = ts[i];
+        if (t.name.empty()) {
+          cplx s(0., 0.);
+          if (dd) s += weight_sum(*dd, ws_of(t, t.scale_d));
+          if (dr) s += weight_sum(*dr, ws_of(t, t.scale_r));
+          out[i].sums[0] = s.real();
+          out[i].sums[1] = s.imag();
+          continue;
+        }
+        vector<Part> parts;
+        if (dd) parts.push_back({*dd, ws_of(t, t.scale_d)});
+        if (dr) parts.push_back({*dr, ws_of(t, t.scale_r)});
+        out[i] = make_field(t.name, parts, t.cplx);
+      }
+      return out;
+    }
+    const int nt = int(ts.size());
+    YlmTargets tg;
+    tg.ell = ell;
+    tg.count = nt;
+    double* wsum = ctx.buf<double>("ylm.wsum", 2 * nt);
+    double* sums = ctx.buf<double>("ylm.sums", 4 * nt);
+    zero(wsum, 2 * nt * sizeof(double));
+    for (int i = 0; i < nt; ++i) {
+      YlmTarget& u = tg.t[i];
+      u.m = ts[i].m;
+      u.power = ts[i].power;
+      u.conj = ts[i].conj;
+      u.sums = sums + 4 * i;
+      if (ts[i].name.empty()) continue;
+      const std::string& nm = ts[i].name;
+      u.re = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.re", g.nmesh));
+      if (ts[i].cplx)
+        u.im = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.im", g.nmesh));
+      if (interlace) {
+        u.sre =
+            reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.sre", g.nmesh));
+        if (ts[i].cplx)
+          u.sim = reinterpret_cast<float*>(
+              ctx.buf<Real>(nm + ".mesh.sim", g.nmesh));
+      }
+    }
+    auto with_scales = [&](bool data) {
+      YlmTargets v = tg;
+      for (int i = 0; i < nt; ++i)
+        v.t[i].scale = data ? ts[i].scale_d : ts[i].scale_r;
+      return v;
+    };
+    if (dd) launch_ylm_weight_sums(ctx, *dd, with_scales(true), wsum);
+    if (dr) launch_ylm_weight_sums(ctx, *dr, with_scales(false), wsum);
+    // Each mesh starts at minus the mean of its deposit (make_field); the
+    // landed sums start at the full weight sums.
+    for (int i = 0; i < nt; ++i) {
+      const YlmTarget& u = tg.t[i];
+      TRVG_CUDA(cudaMemcpyAsync(sums + 4 * i, wsum + 2 * i, 2 * sizeof(double),
+                                cudaMemcpyDeviceToDevice, ctx.stream));
+      TRVG_CUDA(cudaMemcpyAsync(sums + 4 * i + 2, wsum + 2 * i,
+                                2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                ctx.stream));
+      if (u.re == nullptr) continue;
+      launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.re), g.nmesh,
+                               wsum + 2 * i, 0.);
+      if (u.im)
+        launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.im), g.nmesh,
+                                 wsum + 2 * i + 1, 0.);
+      if (u.sre)
+        launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.sre), g.nmesh,
+                                 wsum + 2 * i, 0.);
+      if (u.sim)
+        launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.sim), g.nmesh,
+                                 wsum + 2 * i + 1, 0.);
+    }
+    if (dd)
+      launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dd,
+                        with_scales(true));
+    if (dr)
+      launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dr,
+                        with_scales(false));
+    cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
+    auto r2c = [&](const float* m, const std::string& nm) -> const C* {
+      C* o = ctx.buf<C>(nm, size_t(g.nhalf));
+      ctx.kbegin("cufft.r2c.mesh");
+      FFT<Real>::r2c(h, reinterpret_cast<Real*>(const_cast<float*>(m)), o);
+      ctx.kend();
+      ctx.fft_launches++;
+      return o;
+    };
+    for (int i = 0; i < nt; ++i) {
+      const YlmTarget& u = tg.t[i];
+      if (u.re == nullptr) continue;
+      const std::string& nm = ts[i].name;
+      out[i].spec.re = r2c(u.re, nm + ".re");
+      if (u.im) out[i].spec.im = r2c(u.im, nm + ".im");
+      if (u.sre) out[i].spec.re_s = r2c(u.sre, nm + ".sre");
+      if (u.sim) out[i].spec.im_s = r2c(u.sim, nm + ".sim");
+      ++ctx.mesh_gen;
+    }
+    const vector<double> hs = download(sums, 4 * nt);
+    for (int i = 0; i < nt; ++i)
+      for (int k = 0; k < 4; ++k) out[i].sums[k] = hs[4 * i + k];
+    return out;
+  }
+
   // Field spectrum with its exact k = 0 mode: (main sum + shift) combined
   // with the shadow sum when interlacing.
   FieldSpec<Real> k0_view(const Field& f, double shift) const {
@@ -1649,6 +1796,30 @@ struct Engine {
     if (!survey) xi = twopt_xi(dn, nf, cplx(double(dd.n), 0.));
     vector<double> no_radii;
 
+    // Survey: delta n_LM, N_LM and S-bar_LM of every order M of the terms
+    // (threept.cpp:1640-1680), built together.
+    std::map<int, FieldSpec<Real>> dn_of, N_of;
+    std::map<int, cplx> sbar_of;
+    if (survey) {
+      vector<int> Ms;
+      for (const Term& t : terms)
+        if (std::find(Ms.begin(), Ms.end(), t.M) == Ms.end())
+          Ms.push_back(t.M);
+      vector<YlmField> ts;
+      for (int M : Ms) {
+        const std::string sfx = "." + std::to_string(M);
+        ts.push_back({"dnLM" + sfx, M, 1, false, 1., -alpha, M != 0});
+        ts.push_back({"NLM" + sfx, M, 2, true, 1., alpha * alpha, M != 0});
+        ts.push_back({"", M, 3, false, 1., alpha * alpha * alpha, false});
+      }
+      const vector<Field> fs = make_ylm_fields(p.ELL, &dd, &dr, ts);
+      for (size_t j = 0; j < Ms.size(); ++j) {
+        dn_of[Ms[j]] = k0_view(fs[3 * j], 0.);
+        N_of[Ms[j]] = k0_view(fs[3 * j + 1], 0.);
+        sbar_of[Ms[j]] = cplx(fs[3 * j + 2].sums[0], fs[3 * j + 2].sums[1]);
+      }
+    }
+
     for (const Term& t : terms) {
       const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
       const double mirror = zero_t ? 0. : ((p.ELL & 1) ? -1. : 1.);
@@ -1656,21 +1827,9 @@ struct Engine {
       FieldSpec<Real> dnLM = dn, NLM;
       cplx Sbar;
       if (survey) {
-        const bool cplxM = (t.M != 0);
-        Field fdn = make_field("dnLM",
-                               {{dd, ylm_ws(1., 1, p.ELL, t.M, false)},
-                                {dr, ylm_ws(-alpha, 1, p.ELL, t.M, false)}},
-                               cplxM);
-        dnLM = k0_view(fdn, 0.);
-        Field fN = make_field(
-            "NLM",
-            {{dd, ylm_ws(1., 2, p.ELL, t.M, true)},
-             {dr, ylm_ws(alpha * alpha, 2, p.ELL, t.M, true)}},
-            cplxM);
-        NLM = k0_view(fN, 0.);
-        Sbar = weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false)) +
-               alpha * alpha * alpha *
-                   weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
+        dnLM = dn_of[t.M];
+        NLM = N_of[t.M];
+        Sbar = sbar_of[t.M];
       } else {
         NLM = nf;
         Sbar = cplx(double(dd.n), 0.);
@@ -2207,6 +2366,29 @@ struct Engine {
     Xi xi;
     if (!survey) xi = twopt_xi(dn, nf, cplx(double(dd.n), 0.));
 
+    // Survey: delta n_LM and S-bar_LM (threept.cpp:156-236; the randoms
+    // alone for the window) of every order M of the terms, built together.
+    std::map<int, FieldSpec<Real>> dn_of;
+    std::map<int, cplx> sbar_of;
+    if (survey) {
+      vector<int> Ms;
+      for (const Term& t : terms)
+        if (std::find(Ms.begin(), Ms.end(), t.M) == Ms.end())
+          Ms.push_back(t.M);
+      vector<YlmField> ts;
+      for (int M : Ms) {
+        ts.push_back({"dnLM." + std::to_string(M), M, 1, false, 1.,
+                      window ? alpha : -alpha, M != 0});
+        ts.push_back({"", M, 3, false, 1., alpha * alpha * alpha, false});
+      }
+      const vector<Field> fs =
+          make_ylm_fields(p.ELL, window ? nullptr : &dd, &dr, ts);
+      for (size_t j = 0; j < Ms.size(); ++j) {
+        dn_of[Ms[j]] = k0_view(fs[2 * j], 0.);
+        sbar_of[Ms[j]] = cplx(fs[2 * j + 1].sums[0], fs[2 * j + 1].sums[1]);
+      }
+    }
+
     bool first = true;
     for (const Term& t : terms) {
       const bool zero_t = (t.m1 == 0 && t.m2 == 0 && t.M == 0);
@@ -2214,16 +2396,8 @@ struct Engine {
       const double mirror_w3j = zero_t ? 0. : 1.;
       FieldSpec<Real> dnLM = dn;
       if (survey) {
-        const bool cplxM = (t.M != 0);
-        Field fdn = make_field(
-            "dnLM", parts(window ? alpha : -alpha, 1, p.ELL, t.M, false),
-            cplxM);
-        dnLM = k0_view(fdn, 0.);
-        // S-bar_LM (threept.cpp:156-236; randoms alone for the window).
-        cplx Sbar = alpha * alpha * alpha *
-                    weight_sum(dr, ylm_ws(1., 3, p.ELL, t.M, false));
-        if (!window) Sbar += weight_sum(dd, ylm_ws(1., 3, p.ELL, t.M, false));
-        xi = twopt_xi(dnLM, nf, Sbar);
+        dnLM = dn_of[t.M];
+        xi = twopt_xi(dnLM, nf, sbar_of[t.M]);
       }
 
       // Shot noise (field.cpp:3090-3196; threept.cpp:2307-2345).

@@ -54,6 +54,33 @@ struct DevCatalogue {
   }
 };
 
+// Several Y_lm-weighted fields of one degree built in one pass over a
+// catalogue (compute_ylm_wgtd_field / compute_ylm_wgtd_quad_field,
+// field.cpp:1246-1500, for every order
+// at once): target t deposits scale_t * w^power_t * [conj] y_l,m_t(los)
+// into its own meshes (re; im for complex fields; shadows when
+// interlacing).  A target without meshes only sums the weights.
+constexpr int kMaxYlmTargets = 16;
+constexpr int kMaxYlmDegree = 8;
+
+struct YlmTarget {
+  int m = 0;
+  int power = 1;
+  bool conj = false;
+  double scale = 1.;
+  float* re = nullptr;
+  float* im = nullptr;
+  float* sre = nullptr;
+  float* sim = nullptr;
+  double* sums = nullptr;  // [4]: landed weight (re, im, shadow re, im)
+};
+
+struct YlmTargets {
+  int ell = 0;
+  int count = 0;
+  YlmTarget t[kMaxYlmTargets];
+};
+
 // The value every cell of a mesh holds before its first deposit
 // (fill_offset_kernel: -sum / ncells, sum read from dsum when given).  With
 // it the tiled assignment stores the cells that only its own tile reaches
@@ -124,6 +151,16 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                    Real* mesh_re, Real* mesh_im, Real* shadow_re,
                    Real* shadow_im, double* sums /* [4]: re, im, s_re, s_im */,
                    const MeshFill* fill = nullptr);
+// sum_p scale_t * w^power_t * [conj] y_lm_t for every target, added to
+// out[2 t], out[2 t + 1].
+void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
+                            const YlmTargets& ts, double* out);
+// Deposit of every target's weights into its meshes (FP32), the stencil
+// of each particle formed once; targets' sums must hold their weight sums
+// (launch_ylm_weight_sums): particles off the fast stencil add the
+// difference between their landed and their full weight.
+void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
+                       const DevCatalogue& cat, const YlmTargets& ts);
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
                        const WeightSpec& ws, double* out /* [2] */);
 template <class Real>
