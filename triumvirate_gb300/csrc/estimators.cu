@@ -1805,18 +1805,24 @@ struct Engine {
       for (const Term& t : terms)
         if (std::find(Ms.begin(), Ms.end(), t.M) == Ms.end())
           Ms.push_back(t.M);
+      // L = M = 0: delta n_00 and N_00 are the fields built above.
+      const bool reuse = p.ELL == 0;
       vector<YlmField> ts;
       for (int M : Ms) {
         const std::string sfx = "." + std::to_string(M);
-        ts.push_back({"dnLM" + sfx, M, 1, false, 1., -alpha, M != 0});
-        ts.push_back({"NLM" + sfx, M, 2, true, 1., alpha * alpha, M != 0});
+        if (!reuse) {
+          ts.push_back({"dnLM" + sfx, M, 1, false, 1., -alpha, M != 0});
+          ts.push_back({"NLM" + sfx, M, 2, true, 1., alpha * alpha, M != 0});
+        }
         ts.push_back({"", M, 3, false, 1., alpha * alpha * alpha, false});
       }
       const vector<Field> fs = make_ylm_fields(p.ELL, &dd, &dr, ts);
+      const size_t per = reuse ? 1 : 3;
       for (size_t j = 0; j < Ms.size(); ++j) {
-        dn_of[Ms[j]] = k0_view(fs[3 * j], 0.);
-        N_of[Ms[j]] = k0_view(fs[3 * j + 1], 0.);
-        sbar_of[Ms[j]] = cplx(fs[3 * j + 2].sums[0], fs[3 * j + 2].sums[1]);
+        dn_of[Ms[j]] = reuse ? dn : k0_view(fs[per * j], 0.);
+        N_of[Ms[j]] = reuse ? nf : k0_view(fs[per * j + 1], 0.);
+        const Field& sb = fs[per * j + per - 1];
+        sbar_of[Ms[j]] = cplx(sb.sums[0], sb.sums[1]);
       }
     }
 
@@ -2375,17 +2381,22 @@ struct Engine {
       for (const Term& t : terms)
         if (std::find(Ms.begin(), Ms.end(), t.M) == Ms.end())
           Ms.push_back(t.M);
+      // L = M = 0: delta n_00 is the field built above.
+      const bool reuse = p.ELL == 0;
       vector<YlmField> ts;
       for (int M : Ms) {
-        ts.push_back({"dnLM." + std::to_string(M), M, 1, false, 1.,
-                      window ? alpha : -alpha, M != 0});
+        if (!reuse)
+          ts.push_back({"dnLM." + std::to_string(M), M, 1, false, 1.,
+                        window ? alpha : -alpha, M != 0});
         ts.push_back({"", M, 3, false, 1., alpha * alpha * alpha, false});
       }
       const vector<Field> fs =
           make_ylm_fields(p.ELL, window ? nullptr : &dd, &dr, ts);
+      const size_t per = reuse ? 1 : 2;
       for (size_t j = 0; j < Ms.size(); ++j) {
-        dn_of[Ms[j]] = k0_view(fs[2 * j], 0.);
-        sbar_of[Ms[j]] = cplx(fs[2 * j + 1].sums[0], fs[2 * j + 1].sums[1]);
+        dn_of[Ms[j]] = reuse ? dn : k0_view(fs[per * j], 0.);
+        const Field& sb = fs[per * j + per - 1];
+        sbar_of[Ms[j]] = cplx(sb.sums[0], sb.sums[1]);
       }
     }
 
