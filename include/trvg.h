@@ -215,6 +215,11 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           tile side, pair-reduction bin batch) on first
  *                           use and keep the fastest (default 1; 0 also
  *                           forgets earlier choices);
+ *   "xi_octant"        0/1: FP32 periodic-box bispectra with m = 0 legs of
+ *                           even total degree: keep the shot-noise field
+ *                           averaged over sign flips on one octant (three
+ *                           DCT-I passes) instead of the full mesh
+ *                           (default 1);
  *   "fused_ylm"        0/1: FP32 meshes: build the Y_lm-weighted fields of
  *                           every order of a survey estimate in one fused
  *                           pass per catalogue (default 1);

@@ -297,6 +297,8 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
   } else if (k == "autotune") {
     ctx->impl.autotune = value != 0;
     if (value == 0) ctx->impl.tuned.clear();
+  } else if (k == "xi_octant") {
+    ctx->impl.xi_octant = value != 0;
   } else if (k == "fused_ylm") {
     ctx->impl.fused_ylm = value != 0;
   } else if (k == "assign_path") {

@@ -1064,7 +1064,71 @@ struct Engine {
     const void* re = nullptr;
     const void* im = nullptr;
     bool dbl = false;
+    // Flip-averaged FP32 field on the octant (twopt_xi_octant) instead.
+    const float2* oct = nullptr;
   };
+
+  // Whether the shot-noise field may be kept on one octant: FP32 real
+  // fields without interlacing, even mesh numbers, cubic cells, and legs
+  // whose weights y_la0 y_lb0 are even under every sign flip.
+  bool xi_octant_ok(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                    cplx shot, const vector<Term>& terms) const {
+    if (sizeof(Real) != 4 || ctx.shotnoise_fp64 || !ctx.xi_octant ||
+        interlace || shot.imag() != 0.)
+      return false;
+    if (fa.im || fb.im || fa.im_s || fb.im_s || fa.re_s || fb.re_s ||
+        !fa.k0_set || !fb.k0_set)
+      return false;
+    for (int a = 0; a < 3; ++a)
+      if (g.n[a] % 2 != 0 || g.dr[a] != g.dr[0]) return false;
+    if ((p.ell1 + p.ell2) % 2 != 0) return false;
+    for (const Term& t : terms)
+      if (t.m1 != 0 || t.m2 != 0) return false;
+    return true;
+  }
+
+  // Flip-averaged shot-noise field on the octant 0 <= a, b, c <= n/2:
+  // three DCT-I passes of n/2 + 1 points, each a batched real FFT of length
+  // n of the lines' even extensions, with tiled transposes between them.
+  Xi twopt_xi_octant(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                     cplx shot) {
+    const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
+    const int64_t l1 = int64_t(hx + 1) * (hy + 1);
+    const int64_t l2 = int64_t(hx + 1) * (hz + 1);
+    const int64_t l3 = int64_t(hz + 1) * (hy + 1);
+    const size_t next = size_t(std::max({l1 * g.n[2], l2 * g.n[1],
+                                         l3 * g.n[0]}));
+    const size_t nout = size_t(std::max({l1 * (hz + 1), l2 * (hy + 1),
+                                         l3 * (hx + 1)}));
+    float* ext = ctx.buf<float>("xio.ext", next);
+    float2* out = ctx.buf<float2>("xio.out", nout);
+    const cplx a0(fa.k0.re, fa.k0.im), b0(fb.k0.re, fb.k0.im);
+    const cplx p0 = (a0 * std::conj(b0) - shot) / g.vol;
+    launch_xi_octant_spectrum(
+        ctx, g, reinterpret_cast<const float2*>(fa.re),
+        reinterpret_cast<const float2*>(fb.re), inv_alias_f,
+        float(shot.real()), make_float2(float(p0.real()), float(p0.imag())),
+        fa.k0_dev, fb.k0_dev, replay ? replay->state->count_d : nullptr, ext);
+    auto pass = [&](int n, int64_t lines) {
+      cufftHandle h = ctx.plan1d(CUFFT_R2C, n, int(lines));
+      ctx.kbegin("cufft.r2c.xi_octant");
+      TRVG_CUFFT(cufftExecR2C(h, ext, reinterpret_cast<cufftComplex*>(out)));
+      ctx.kend();
+      ctx.fft_launches++;
+    };
+    pass(g.n[2], l1);  // z: lines (p, q) -> (p, q, c)
+    launch_octant_transpose(ctx, out, int64_t(hy + 1) * (hz + 1), hz + 1, ext,
+                            int64_t(hz + 1) * g.n[1], g.n[1], hx + 1, hy + 1,
+                            hz + 1, g.n[1]);
+    pass(g.n[1], l2);  // y: lines (p, c) -> (p, c, b)
+    launch_octant_transpose(ctx, out, hy + 1, int64_t(hz + 1) * (hy + 1), ext,
+                            int64_t(hy + 1) * g.n[0], g.n[0], hz + 1, hx + 1,
+                            hy + 1, g.n[0]);
+    pass(g.n[0], l3);  // x: lines (c, b) -> (c, b, a)
+    Xi xi;
+    xi.oct = out;
+    return xi;
+  }
 
   template <class XR>
   Xi twopt_xi_t(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
@@ -1167,7 +1231,18 @@ struct Engine {
     double* out = ctx.buf<double>("sn.out", 2 * size_t(np));
     zero(out, 2 * np * sizeof(double));
     const bool cubic = g.dr[0] == g.dr[1] && g.dr[1] == g.dr[2];
-    if (cubic) {
+    if (xi.oct != nullptr) {
+      if (ma != 0 || mb != 0 || (la + lb) % 2 != 0)
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Octant shot-noise field for m = 0, even degrees only.");
+      int64_t nkeys = 1;
+      for (int a = 0; a < 3; ++a) nkeys += int64_t(g.n[a] / 2) * (g.n[a] / 2);
+      double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
+      zero(hist, 2 * nkeys * sizeof(double));
+      launch_octant_hist(ctx, g, xi.oct, la, lb, hist);
+      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
+                              true, out);
+    } else if (cubic) {
       int64_t nkeys = 1;
       for (int a = 0; a < 3; ++a) {
         const int64_t smx = g.n[a] - g.n[a] / 2;
@@ -1793,7 +1868,11 @@ struct Engine {
     vector<cplx> bk(ndv, 0.), sn(ndv, 0.);
 
     Xi xi;
-    if (!survey) xi = twopt_xi(dn, nf, cplx(double(dd.n), 0.));
+    if (!survey) {
+      const cplx shot(double(dd.n), 0.);
+      xi = xi_octant_ok(dn, nf, shot, terms) ? twopt_xi_octant(dn, nf, shot)
+                                             : twopt_xi(dn, nf, shot);
+    }
     vector<double> no_radii;
 
     // Survey: delta n_LM, N_LM and S-bar_LM of every order M of the terms

@@ -142,6 +142,8 @@ struct Context {
   // sort, bin batch of the pair reduction), cached by key.
   bool autotune = true;
   std::map<std::string, int> tuned;
+  // Shot-noise field of m = 0, even-degree legs on one octant (FP32).
+  bool xi_octant = true;
   // Y_lm-weighted fields of every order in one fused pass (FP32 meshes).
   bool fused_ylm = true;
   // Deposit of sorted catalogues: 0 tuned, 1 tiled (shared memory),

@@ -144,6 +144,22 @@ struct BinsDev {
   const int* smax = nullptr;   // one past the last
 };
 
+// ---- shot-noise field on one octant (spectral.cu, reduce.cu) --------------
+// Flip-averaged FP32 spectrum of a real two-point field as the even
+// extensions of its z lines ((n_x/2 + 1)(n_y/2 + 1) lines of n_z floats).
+void launch_xi_octant_spectrum(Context& ctx, const Geom& g, const float2* fa,
+                               const float2* fb, const float* const inv_alias[3],
+                               float shot, float2 p0, const double* k0a,
+                               const double* k0b, const double* shotp,
+                               float* ext);
+// dst[s dS + k dK + r] = dst[s dS + k dK + len - r] = src[s sS + r sR + k].x.
+void launch_octant_transpose(Context& ctx, const float2* src, int64_t sS,
+                             int64_t sR, float* dst, int64_t dS, int64_t dK,
+                             int nslab, int nrow, int ncol, int len);
+// Radial sums of the octant xi (weights y_l0 y_l'0 for degrees > 0).
+void launch_octant_hist(Context& ctx, const Geom& g, const float2* xo,
+                        int ell_a, int ell_b, double* hist);
+
 // ---- assign.cu -----------------------------------------------------------
 template <class Real>
 void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,

@@ -317,6 +317,34 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
   }
 }
 
+// The same sums from the flip-averaged xi on the octant (even mesh numbers,
+// cubic cells): cell (a, b, c) stands for its 1, 2, 4 or 8 mirror cells
+// (one per coordinate not 0 or n/2), xo[(c (hy + 1) + b) (hx + 1) + a].x.
+// KIND as for orbit_rows_kernel (0 or 1).
+template <int KIND>
+__global__ void __launch_bounds__(256)
+octant_hist_kernel(Geom g, const float2* xo, int ell_a, int ell_b,
+                   double* hist) {
+  const int hx = g.n[0] / 2, hy = g.n[1] / 2;
+  const int c = blockIdx.y, b = blockIdx.x;
+  const int64_t row = (int64_t(c) * (hy + 1) + b) * (hx + 1);
+  const int wbc = ((b == 0 || b == hy) ? 1 : 2) *
+                  ((c == 0 || c == g.n[2] / 2) ? 1 : 2);
+  const int64_t key_bc = int64_t(b) * b + int64_t(c) * c;
+  for (int a = threadIdx.x; a <= hx; a += blockDim.x) {
+    const int w = wbc * ((a == 0 || a == hx) ? 1 : 2);
+    double v = double(w) * double(xo[row + a].x);
+    if constexpr (KIND == 1) {
+      const double rx = dmul(double(a), g.dr[0]);
+      const double ry = dmul(double(b), g.dr[1]);
+      const double rz = dmul(double(c), g.dr[2]);
+      v *= (reduced_ylm(ell_a, 0, rx, ry, rz) *
+            reduced_ylm(ell_b, 0, rx, ry, rz)).re;
+    }
+    atomicAdd(hist + 2 * (key_bc + int64_t(a) * a), v);
+  }
+}
+
 // The same sums for even mesh numbers, with one atomic per orbit row
 // instead of one per cell.  The cells (+-s_x, +-s_y, +-s_z) -- and, when
 // n_x = n_y, their x <-> y swaps -- share the key a^2 + b^2 + c^2 with
@@ -720,6 +748,20 @@ void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,
   TRVG_KBEGIN(ctx, "radial_hist_kernel");
   radial_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
       g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, hist);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_octant_hist(Context& ctx, const Geom& g, const float2* xo,
+                        int ell_a, int ell_b, double* hist) {
+  dim3 grid(g.n[1] / 2 + 1, g.n[2] / 2 + 1);
+  const int threads = std::min(256, ((g.n[0] / 2 + 1 + 31) / 32) * 32);
+  TRVG_KBEGIN(ctx, "orbit_rows_kernel");
+  if (ell_a == 0 && ell_b == 0)
+    octant_hist_kernel<0><<<grid, threads, 0, ctx.stream>>>(g, xo, ell_a,
+                                                            ell_b, hist);
+  else
+    octant_hist_kernel<1><<<grid, threads, 0, ctx.stream>>>(g, xo, ell_a,
+                                                            ell_b, hist);
   TRVG_LAUNCHED(ctx);
 }
 

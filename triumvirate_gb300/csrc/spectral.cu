@@ -841,6 +841,92 @@ twopt_field_real_f32_kernel(uint32_t nhalf, int n1, int nzh, const float2* fa,
   }
 }
 
+// ---- Shot-noise field on one octant -----------------------------------------
+//
+// For weights symmetric under every sign flip of r (m = 0 legs of even
+// total degree) the shot-noise sums need only xi averaged over the flips,
+//   xi_s(a, b, c) = sum_k P(k) cos(k_x a dr) cos(k_y b dr) cos(k_z c dr),
+// on 0 <= a, b, c <= n/2: the sum over the half-mesh octant of the flip-
+// averaged spectrum with weights 1 (index 0 or n/2) or 2, i.e. three
+// DCT-I passes of length n/2 + 1.  Each pass is a real FFT of length n of
+// the even extension e[j] = e[n - j] of a line (the real parts of its
+// first n/2 + 1 outputs).
+
+// P averaged over (+-k_x, +-k_y), k_z >= 0 (its real part: the imaginary
+// parts cancel in xi_s), written as the even extensions of the z lines:
+// ext[(p (hy + 1) + q) n_z + j], j and n_z - j both holding k_z index r.
+__global__ void __launch_bounds__(256)
+xi_octant_spectrum_kernel(int n0, int n1, int nzh, const float2* fa,
+                          const float2* fb, const float* iax,
+                          const float* iay, const float* iaz, float shot,
+                          float inv_vol, float2 p0, const double* k0a,
+                          const double* k0b, const double* shotp, double vol,
+                          float* ext) {
+  if (k0a != nullptr) {
+    const double ar = k0a[0], ai = k0a[1], br = k0b[0], bi = k0b[1];
+    shot = float(shotp[0]);
+    p0 = make_float2(float((ar * br + ai * bi - shotp[0]) / vol),
+                     float((ai * br - ar * bi - shotp[1]) / vol));
+  }
+  const int hx = n0 / 2, hy = n1 / 2, hz = nzh - 1, nz = 2 * hz;
+  const int64_t total = int64_t(hx + 1) * (hy + 1) * (hz + 1);
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int r = int(t % (hz + 1));
+    const int64_t pq = t / (hz + 1);
+    const int q = int(pq % (hy + 1)), pp = int(pq / (hy + 1));
+    const int is[2] = {pp, (n0 - pp) % n0};
+    const int js[2] = {q, (n1 - q) % n1};
+    float acc = 0.f;
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int64_t idx = (int64_t(is[u]) * n1 + js[v]) * nzh + r;
+        float2 o;
+        if (idx == 0) {
+          o = p0;
+        } else {
+          const float2 a = fa[idx], b = fb[idx];
+          const float inv = iax[is[u]] * iay[js[v]] * iaz[r];
+          o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
+        }
+        acc += o.x;
+      }
+    const float v = 0.25f * acc;
+    float* line = ext + pq * nz;
+    line[r] = v;
+    if (r != 0 && r != hz) line[nz - r] = v;
+  }
+}
+
+// Real parts of R2C outputs, transposed into the even extensions of the
+// next axis: for slab s, src row r and column k,
+//   dst[s dS + k dK + r] = dst[s dS + k dK + (len - r)] = src[s sS + r sR + k].x
+// (rows r = 0 .. len/2, columns k = 0 .. ncol - 1), through 32 x 32 tiles.
+__global__ void __launch_bounds__(256)
+octant_transpose_kernel(const float2* src, int64_t sS, int64_t sR, float* dst,
+                        int64_t dS, int64_t dK, int nrow, int ncol, int len) {
+  __shared__ float tile[32][33];
+  const int s = blockIdx.z;
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows a pass
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, k = k0 + tx;
+    if (r < nrow && k < ncol) tile[i][tx] = src[s * sS + r * sR + k].x;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int k = k0 + i, r = r0 + tx;
+    if (r < nrow && k < ncol) {
+      float* line = dst + s * dS + k * dK;
+      const float v = tile[tx][i];
+      line[r] = v;
+      if (r != 0 && r != len / 2) line[len - r] = v;
+    }
+  }
+}
+
 }  // namespace
 
 void launch_count_modes(Context& ctx, const Geom& g, const Cube& cube,
@@ -934,6 +1020,30 @@ void launch_twopt_field_real_f32(Context& ctx, const Geom& g,
       uint32_t(g.nhalf), g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1],
       inv_alias[2], shot, float(1. / g.vol), p0, k0a, k0b, shotp, g.vol,
       out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_xi_octant_spectrum(Context& ctx, const Geom& g, const float2* fa,
+                               const float2* fb, const float* const inv_alias[3],
+                               float shot, float2 p0, const double* k0a,
+                               const double* k0b, const double* shotp,
+                               float* ext) {
+  const int64_t total =
+      int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) * (g.n[2] / 2 + 1);
+  TRVG_KBEGIN(ctx, "xi_octant_kernel");
+  xi_octant_spectrum_kernel<<<grid_for(total, 256), 256, 0, ctx.stream>>>(
+      g.n[0], g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1], inv_alias[2],
+      shot, float(1. / g.vol), p0, k0a, k0b, shotp, g.vol, ext);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_octant_transpose(Context& ctx, const float2* src, int64_t sS,
+                             int64_t sR, float* dst, int64_t dS, int64_t dK,
+                             int nslab, int nrow, int ncol, int len) {
+  dim3 grid((ncol + 31) / 32, (nrow + 31) / 32, nslab);
+  TRVG_KBEGIN(ctx, "xi_octant_kernel");
+  octant_transpose_kernel<<<grid, 256, 0, ctx.stream>>>(src, sS, sR, dst, dS,
+                                                        dK, nrow, ncol, len);
   TRVG_LAUNCHED(ctx);
 }
 
