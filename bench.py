@@ -61,6 +61,9 @@ def parse_args():
                     help="'mocks': the batched lognormal-mock workload "
                          "(its own JSON line)")
     ap.add_argument('--mocks', type=int, default=256)
+    ap.add_argument('--assign-path', type=int, default=0, choices=[0, 1, 2],
+                    help='deposit of sorted catalogues: 0 autotuned, '
+                         '1 shared-memory tiled, 2 per-particle atomics')
     return ap.parse_args()
 
 
@@ -281,6 +284,7 @@ def run_gb300(args):
     norm = 1. / (n * nbar ** 2)        # threept.cpp:96-136, alpha = 1
 
     ctx = _lib.Context(local)
+    ctx.set_option('assign_path', args.assign_path)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
 

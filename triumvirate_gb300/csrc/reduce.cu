@@ -321,6 +321,20 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
 // cubic cells): cell (a, b, c) stands for its 1, 2, 4 or 8 mirror cells
 // (one per coordinate not 0 or n/2), xo[(c (hy + 1) + b) (hx + 1) + a].x.
 // KIND as for orbit_rows_kernel (0 or 1).
+// f * 2^e2 as a double, formed from the bits of f with integer operations
+// (exact; GB300 runs float-to-double conversions on its FP64 pipe).  Zero,
+// subnormal and non-finite f take the conversion.
+__device__ __forceinline__ double f2d_pow2(float f, int e2) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return double(f) * double(1 << e2);
+  const unsigned long long bits =
+      (static_cast<unsigned long long>(u >> 31) << 63) |
+      (static_cast<unsigned long long>(ex + 896u + unsigned(e2)) << 52) |
+      (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(256)
 octant_hist_kernel(Geom g, const float2* xo, int ell_a, int ell_b,
@@ -328,12 +342,13 @@ octant_hist_kernel(Geom g, const float2* xo, int ell_a, int ell_b,
   const int hx = g.n[0] / 2, hy = g.n[1] / 2;
   const int c = blockIdx.y, b = blockIdx.x;
   const int64_t row = (int64_t(c) * (hy + 1) + b) * (hx + 1);
-  const int wbc = ((b == 0 || b == hy) ? 1 : 2) *
-                  ((c == 0 || c == g.n[2] / 2) ? 1 : 2);
+  // Mirror cells per coordinate: 1 at 0 and n/2, else 2 (as a power of 2).
+  const int ebc = ((b == 0 || b == hy) ? 0 : 1) +
+                  ((c == 0 || c == g.n[2] / 2) ? 0 : 1);
   const int64_t key_bc = int64_t(b) * b + int64_t(c) * c;
   for (int a = threadIdx.x; a <= hx; a += blockDim.x) {
-    const int w = wbc * ((a == 0 || a == hx) ? 1 : 2);
-    double v = double(w) * double(xo[row + a].x);
+    const int e = ebc + ((a == 0 || a == hx) ? 0 : 1);
+    double v = f2d_pow2(xo[row + a].x, e);
     if constexpr (KIND == 1) {
       const double rx = dmul(double(a), g.dr[0]);
       const double ry = dmul(double(b), g.dr[1]);

@@ -877,22 +877,31 @@ xi_octant_spectrum_kernel(int n0, int n1, int nzh, const float2* fa,
     const int q = int(pq % (hy + 1)), pp = int(pq / (hy + 1));
     const int is[2] = {pp, (n0 - pp) % n0};
     const int js[2] = {q, (n1 - q) % n1};
+    // The four images' loads first (one field when both legs share it).
+    float2 av[4], bv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      av[u] = fa[(int64_t(is[u >> 1]) * n1 + js[u & 1]) * nzh + r];
+    if (fa != fb) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        bv[u] = fb[(int64_t(is[u >> 1]) * n1 + js[u & 1]) * nzh + r];
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) bv[u] = av[u];
+    }
     float acc = 0.f;
 #pragma unroll
-    for (int u = 0; u < 2; ++u)
-#pragma unroll
-      for (int v = 0; v < 2; ++v) {
-        const int64_t idx = (int64_t(is[u]) * n1 + js[v]) * nzh + r;
-        float2 o;
-        if (idx == 0) {
-          o = p0;
-        } else {
-          const float2 a = fa[idx], b = fb[idx];
-          const float inv = iax[is[u]] * iay[js[v]] * iaz[r];
-          o.x = ((a.x * b.x + a.y * b.y) * inv - shot) * inv_vol;
-        }
-        acc += o.x;
+    for (int u = 0; u < 4; ++u) {
+      const int i = is[u >> 1], j = js[u & 1];
+      if (i == 0 && j == 0 && r == 0) {
+        acc += p0.x;
+      } else {
+        const float inv = iax[i] * iay[j] * iaz[r];
+        acc += ((av[u].x * bv[u].x + av[u].y * bv[u].y) * inv - shot) *
+               inv_vol;
       }
+    }
     const float v = 0.25f * acc;
     float* line = ext + pq * nz;
     line[r] = v;
