@@ -324,10 +324,14 @@ radial_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
 // f * 2^e2 as a double, formed from the bits of f with integer operations
 // (exact; GB300 runs float-to-double conversions on its FP64 pipe).  Zero,
 // subnormal and non-finite f take the conversion.
+__device__ __noinline__ double f2d_pow2_slow(float f, int e2) {
+  return double(f) * double(1 << e2);
+}
+
 __device__ __forceinline__ double f2d_pow2(float f, int e2) {
   const unsigned u = __float_as_uint(f);
   const unsigned ex = (u >> 23) & 0xffu;
-  if (ex == 0u || ex == 0xffu) return double(f) * double(1 << e2);
+  if (ex == 0u || ex == 0xffu) return f2d_pow2_slow(f, e2);
   const unsigned long long bits =
       (static_cast<unsigned long long>(u >> 31) << 63) |
       (static_cast<unsigned long long>(ex + 896u + unsigned(e2)) << 52) |
