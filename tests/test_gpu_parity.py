@@ -786,12 +786,15 @@ def test_tiled_assignment_in_estimators(assignment, rand_catalogue_array):
         return compute_bispec(
             ParticleCatalogue(*(d - box / 2).T, nz=3e-9),
             ParticleCatalogue(*rr.T, nz=3e-9), **kw)
+    # FP32 atomics deposit in a different order in the two paths (the
+    # survey field nearly cancels data against randoms): 1e-5 of the
+    # largest entry, the FP32-mixed contract.
     for fn in (gpp, lpp):
         t = _with_assign_path(ctx, 1, fn)
         a = _with_assign_path(ctx, 2, fn)
         for k in ('bk_raw', 'bk_shot'):
             scale = np.max(np.abs(a[k]))
-            assert np.max(np.abs(t[k] - a[k])) / scale < 1e-6, (fn, k)
+            assert np.max(np.abs(t[k] - a[k])) / scale < 1e-5, (fn, k)
 
 
 # ---------------------------------------------------------------------------

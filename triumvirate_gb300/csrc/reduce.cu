@@ -339,6 +339,19 @@ __device__ __forceinline__ double f2d_pow2(float f, int e2) {
   return __longlong_as_double(static_cast<long long>(bits));
 }
 
+// Legendre polynomial P_l(mu) by the three-term recurrence, in FP32:
+// y_l0 of a unit vector with z component mu (reduced_ylm).
+__device__ __forceinline__ float legendre_f(int ell, float mu) {
+  if (ell == 0) return 1.f;
+  float pm = 1.f, p = mu;
+  for (int n = 1; n < ell; ++n) {
+    const float pn = (float(2 * n + 1) * mu * p - float(n) * pm) / float(n + 1);
+    pm = p;
+    p = pn;
+  }
+  return p;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(256)
 octant_hist_kernel(Geom g, const float2* xo, int ell_a, int ell_b,
@@ -352,15 +365,19 @@ octant_hist_kernel(Geom g, const float2* xo, int ell_a, int ell_b,
   const int64_t key_bc = int64_t(b) * b + int64_t(c) * c;
   for (int a = threadIdx.x; a <= hx; a += blockDim.x) {
     const int e = ebc + ((a == 0 || a == hx) ? 0 : 1);
-    double v = f2d_pow2(xo[row + a].x, e);
+    const int64_t key = key_bc + int64_t(a) * a;
+    float x = xo[row + a].x;
     if constexpr (KIND == 1) {
-      const double rx = dmul(double(a), g.dr[0]);
-      const double ry = dmul(double(b), g.dr[1]);
-      const double rz = dmul(double(c), g.dr[2]);
-      v *= (reduced_ylm(ell_a, 0, rx, ry, rz) *
-            reduced_ylm(ell_b, 0, rx, ry, rz)).re;
+      // y_la0 y_lb0 at mu = c / |(a, b, c)| (cubic cells; 0 at r = 0);
+      // a^2 + b^2 + c^2 < 2^24 is exact in FP32.
+      float f = 0.f;
+      if (key != 0) {
+        const float mu = sqrtf(float(int64_t(c) * c) / float(key));
+        f = legendre_f(ell_a, mu) * legendre_f(ell_b, mu);
+      }
+      x *= f;
     }
-    atomicAdd(hist + 2 * (key_bc + int64_t(a) * a), v);
+    atomicAdd(hist + 2 * key, f2d_pow2(x, e));
   }
 }
 
