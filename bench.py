@@ -57,9 +57,10 @@ def parse_args():
     ap.add_argument('--variants', action='store_true',
                     help='also time the FP32-mixed precision options')
     ap.add_argument('--workload', default='metric',
-                    choices=['metric', 'mocks'],
-                    help="'mocks': the batched lognormal-mock workload "
-                         "(its own JSON line)")
+                    choices=['metric', 'mocks', 'survey'],
+                    help="'mocks': the batched lognormal-mock workload; "
+                         "'survey': survey bispectra from device "
+                         "catalogues (each its own JSON line)")
     ap.add_argument('--mocks', type=int, default=256)
     ap.add_argument('--assign-path', type=int, default=0, choices=[0, 1, 2],
                     help='deposit of sorted catalogues: 0 autotuned, '
@@ -703,12 +704,110 @@ def run_mocks(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Survey bispectra: data and randoms with lines of sight (local
+# plane-parallel estimator), catalogues held on the device.
+# ---------------------------------------------------------------------------
+
+def survey_catalogue(n, seed, ndata=1_000_000):
+    """Observer at the origin, directions uniform on the z > 0 hemisphere,
+    radii ~ N(1500, 300) Mpc/h (r > 0), nz(r) = N_data N(r; 1500, 300) /
+    (2 pi r^2), FKP w_c = 1 / (1 + nz 1e4), w_s = 1."""
+    rng = np.random.default_rng(seed)
+    u = rng.normal(size=(n, 3))
+    u[:, 2] = np.abs(u[:, 2])
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    r = rng.normal(1500., 300., n)
+    while (r <= 0.).any():
+        bad = r <= 0.
+        r[bad] = rng.normal(1500., 300., int(bad.sum()))
+    pdf = np.exp(-0.5 * ((r - 1500.) / 300.) ** 2) / (300. * np.sqrt(2 * np.pi))
+    nz = ndata * pdf / (2 * np.pi * r ** 2)
+    pos = u * r[:, None]
+    return pos, nz, 1. / (1. + nz * 1e4)
+
+
+def run_survey(args):
+    """Config: survey bispectra from 1e6 data and 5e6 random particles
+    (seeds 1, 2), 256^3 mesh, PCS, box = random extents, 20 lin bins
+    0.005-0.205 h/Mpc; B_000 full (triu, 210 pairs) and B_202 full (400
+    pairs), FP32-mixed, with the Y_lm-weighted fields of all orders built in
+    one fused pass and, for comparison, one order at a time."""
+    from triumvirate_gb300 import _lib
+    from triumvirate_gb300.catalogue import DeviceCatalogue
+    from triumvirate_gb300.dataobjs import Binning
+    from triumvirate_gb300.threept import compute_bispec
+    pd, nzd, wcd = survey_catalogue(1_000_000, 1)
+    pr, nzr, wcr = survey_catalogue(5_000_000, 2)
+    ctx = _lib.default_context(0)
+    binning = Binning('fourier', 'lin', 0.005, 0.205, 20)
+    samp = {'ngrid': [256] * 3, 'assignment': 'pcs', 'interlace': False,
+            'precision': 'fp32mixed'}
+
+    def cats():
+        return (DeviceCatalogue(*pd.T, nz=nzd, wc=wcd),
+                DeviceCatalogue(*pr.T, nz=nzr, wc=wcr))
+
+    def estimate(degrees, form):
+        dc, rc = cats()
+        ctx.set_option('profiling', 0)
+        t0 = time.perf_counter()
+        compute_bispec(dc, rc, degrees=degrees, binning=binning, form=form,
+                       sampling_params=samp)
+        return time.perf_counter() - t0
+
+    def kernel_ms(degrees, form):
+        dc, rc = cats()
+        ctx.set_option('profiling', 1)
+        compute_bispec(dc, rc, degrees=degrees, binning=binning, form=form,
+                       sampling_params=samp)
+        kt = ctx.kernel_times()
+        ctx.set_option('profiling', 0)
+        return kt
+
+    res = {}
+    for name, degrees, form in [('B000', (0, 0, 0), 'full'),
+                                ('B202', (2, 0, 2), 'full')]:
+        for fused in (1, 0):
+            ctx.set_option('fused_ylm', fused)
+            for _ in range(max(1, args.warmup)):
+                estimate(degrees, form)
+            t = statistics.median(estimate(degrees, form)
+                                  for _ in range(max(1, args.steps)))
+            kt = kernel_ms(degrees, form)
+            top = sorted(kt.items(), key=lambda kv: -kv[1][0])[:8]
+            res[f"{name}.{'fused' if fused else 'per_order'}"] = {
+                "s_per_estimate": round(t, 4),
+                "kernel_ms": round(sum(v[0] for v in kt.values()), 2),
+                "top_kernels_ms": {k: round(v[0], 3) for k, v in top}}
+        ctx.set_option('fused_ylm', 1)
+    line = {
+        "metric": "survey bispectrum s/estimate (1e6 data + 5e6 randoms, "
+                  "256^3, PCS, B_202 full, 400 pairs)",
+        "value": res["B202.fused"]["s_per_estimate"], "unit": "s/estimate",
+        "higher_is_better": False, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 meshes/FFTs, f64 offsets/Ylm/reductions",
+        "data": "synthetic (seeded hemisphere survey, FKP weights)",
+        "config": {"workload": "survey B_000 full (triu) and B_202 full, "
+                               "1e6 data + 5e6 randoms, 256^3, PCS, 20 lin "
+                               "bins 0.005-0.205 h/Mpc, device catalogues",
+                   "timing": "wall time per estimate (device-resident "
+                             "catalogues, centring and lines of sight "
+                             "on the device)"},
+        "estimates": res,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == 'reference':
         run_reference(args)
     elif args.workload == 'mocks':
         run_mocks(args)
+    elif args.workload == 'survey':
+        run_survey(args)
     else:
         run_gb300(args)
 

@@ -1261,16 +1261,23 @@ struct Engine {
       launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
                               !xi.dbl, out);
     } else {
+      // Cells of unequal sides: keyed by (|s_x|, |s_y|, |s_z|), which fixes
+      // |r|, with the radius of each key in a table.
+      const int64_t nkeys = int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) *
+                            (g.n[2] / 2 + 1);
+      double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
+      double* rkey = ctx.buf<double>("sn.rkey", size_t(nkeys));
+      zero(hist, 2 * nkeys * sizeof(double));
       if (xi.dbl)
-        launch_pair_bessel_direct<double>(
+        launch_octant_cell_hist<double>(
             ctx, g, static_cast<const double*>(xi.re),
-            static_cast<const double*>(xi.im), la, ma, lb, mb, sja, sjb, dka,
-            dkb, np, out);
+            static_cast<const double*>(xi.im), la, ma, lb, mb, hist, rkey);
       else
-        launch_pair_bessel_direct<float>(
+        launch_octant_cell_hist<float>(
             ctx, g, static_cast<const float*>(xi.re),
-            static_cast<const float*>(xi.im), la, ma, lb, mb, sja, sjb, dka,
-            dkb, np, out);
+            static_cast<const float*>(xi.im), la, ma, lb, mb, hist, rkey);
+      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
+                              !xi.dbl, out, rkey);
     }
     dev_sij = out;
     if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));

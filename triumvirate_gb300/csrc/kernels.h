@@ -472,14 +472,15 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* hist, const SplineTable& sja,
                              const SplineTable& sjb, const double* ka,
                              const double* kb, int npairs, bool ff,
-                             double* out);
-
+                             double* out,
+                             const double* rkey = nullptr);
+// Sums of xi y_a y_b over cells of any shape, keyed by (|s_x|, |s_y|,
+// |s_z|) on (n/2 + 1)^3 keys, with each key's radius in rkey.
 template <class Real>
-void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,
-                               const Real* xi_im, int ell_a, int m_a,
-                               int ell_b, int m_b, const SplineTable& sja,
-                               const SplineTable& sjb, const double* ka,
-                               const double* kb, int npairs, double* out);
+void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
+                             const Real* xi_im, int ell_a, int m_a, int ell_b,
+                             int m_b, double* hist, double* rkey);
+
 
 template <class Real>
 void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,

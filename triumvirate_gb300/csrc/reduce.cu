@@ -9,7 +9,9 @@
 //    (field.cpp:3349-3396).  With cubic cells r depends on x only through
 //    the integer key s_x^2 + s_y^2 + s_z^2, so xi * y_a * y_b is first
 //    summed per key and the Bessel weights are applied per key and pair.
-//  * pair_bessel_direct: the same sum evaluated cell by cell (any cells).
+//  * octant_cell_hist: the same sums for cells of unequal sides, keyed by
+//    (|s_x|, |s_y|, |s_z|), which fixes |r|; pair_bessel_sums then reads
+//    each key's radius from a table.
 //  * shotnoise_3pcf_bins: r-binned sums of the 3PCF shot noise
 //    (field.cpp:3090-3196) with exact per-cell separations.
 #include <algorithm>
@@ -494,9 +496,9 @@ constexpr int kKeyPairChunk = 8;
 // One thread per key: r = dr sqrt(key) once, then the Bessel weights of a
 // chunk of pairs (one spline evaluation when both legs coincide).
 __global__ void __launch_bounds__(256)
-pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* hist,
-                        PairBesselArgs a, int npairs, bool same_leg,
-                        double* out) {
+pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* rkey,
+                        const double* hist, PairBesselArgs a, int npairs,
+                        bool same_leg, double* out) {
   __shared__ double red[2 * kKeyPairChunk * 32];
   const int p0 = blockIdx.y * kKeyPairChunk;
   double ka[kKeyPairChunk], kb[kKeyPairChunk];
@@ -513,7 +515,7 @@ pair_bessel_sums_kernel(int64_t nkeys, double dr, const double* hist,
        key < nkeys; key += int64_t(gridDim.x) * blockDim.x) {
     const double hr = hist[2 * key], hi = hist[2 * key + 1];
     if (hr == 0. && hi == 0.) continue;
-    const double r = dr * sqrt(double(key));
+    const double r = rkey != nullptr ? rkey[key] : dr * sqrt(double(key));
 #pragma unroll
     for (int q = 0; q < kKeyPairChunk; ++q) {
       const double ja = spline_eval(a.ja, ka[q] * r);
@@ -562,9 +564,9 @@ __device__ __forceinline__ FF spline_eval_ff(const SplineTable& t, FF x) {
 // float-float, Bessel weights from spline_eval_ff, products and sums in
 // float-float; FP64 only per key (the histogram words) and at the end.
 __global__ void __launch_bounds__(256)
-pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* hist,
-                           PairBesselArgs a, int npairs, bool same_leg,
-                           double* out) {
+pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* rkey,
+                           const double* hist, PairBesselArgs a, int npairs,
+                           bool same_leg, double* out) {
   __shared__ double red[2 * kKeyPairChunk * 32];
   const int p0 = blockIdx.y * kKeyPairChunk;
   FF ka[kKeyPairChunk], kb[kKeyPairChunk];
@@ -585,13 +587,18 @@ pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* hist,
     const double2 h = reinterpret_cast<const double2*>(hist)[key];
     if (h.x == 0. && h.y == 0.) continue;
     const FF hr = ff_from_double(h.x), hi = ff_from_double(h.y);
-    // sqrt(key) in float-float (key < 2^24 is exact in FP32).
-    const float kf = float(key);
-    const float sh = __fsqrt_rn(kf);
-    const float sl = sh > 0.f
-                         ? __fdiv_rn(__fmaf_rn(-sh, sh, kf), __fmul_rn(2.f, sh))
-                         : 0.f;
-    const FF r = ffmul(drf, FF{sh, sl});
+    FF r;
+    if (rkey != nullptr) {
+      r = ff_from_double(rkey[key]);
+    } else {
+      // sqrt(key) in float-float (key < 2^24 is exact in FP32).
+      const float kf = float(key);
+      const float sh = __fsqrt_rn(kf);
+      const float sl =
+          sh > 0.f ? __fdiv_rn(__fmaf_rn(-sh, sh, kf), __fmul_rn(2.f, sh))
+                   : 0.f;
+      r = ffmul(drf, FF{sh, sl});
+    }
 #pragma unroll
     for (int q = 0; q < kKeyPairChunk; ++q) {
       const FF ja = spline_eval_ff(a.ja, ffmul(ka[q], r));
@@ -607,40 +614,49 @@ pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* hist,
   block_add<2 * kKeyPairChunk>(v, out + 2 * p0, red, 2 * (npairs - p0));
 }
 
-constexpr int kBesselChunk = 4;
-
+// Cells of any shape grouped by (|s_x|, |s_y|, |s_z|), which fixes |r|:
+// hist[key] += xi y_a y_b, key = (|s_x| D_y + |s_y|) D_z + |s_z| with
+// D = n/2 + 1 per axis, and rkey[key] = |r| (the sign of s does not change
+// a product s dr, so every cell of a key has this radius).
 template <class Real>
 __global__ void __launch_bounds__(256)
-pair_bessel_direct_kernel(Geom g, const Real* xi_re, const Real* xi_im,
-                          int ell_a, int m_a, int ell_b, int m_b,
-                          PairBesselArgs a, int npairs, double* out) {
-  __shared__ double red[2 * kBesselChunk * 32];
-  const int p0 = blockIdx.y * kBesselChunk;
-  double acc[2 * kBesselChunk];
-#pragma unroll
-  for (int q = 0; q < 2 * kBesselChunk; ++q) acc[q] = 0.;
+octant_cell_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im,
+                        int ell_a, int m_a, int ell_b, int m_b,
+                        double* hist) {
+  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+  const int dy = g.n[1] / 2 + 1, dz = g.n[2] / 2 + 1;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
     const int k = int(t % g.n[2]);
     const int j = int((t / g.n[2]) % g.n[1]);
     const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
-    const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
-    const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
-    const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
-    const double r = vec3_mag(rx, ry, rz);
+    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
+              sz = shift_index(k, g.n[2]);
+    const int64_t key = (int64_t(abs(sx)) * dy + abs(sy)) * dz + abs(sz);
     cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
-    v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
-             reduced_ylm(ell_b, m_b, rx, ry, rz));
-#pragma unroll
-    for (int q = 0; q < kBesselChunk; ++q) {
-      if (p0 + q >= npairs) continue;
-      const double w = spline_eval(a.ja, a.ka[p0 + q] * r) *
-                       spline_eval(a.jb, a.kb[p0 + q] * r);
-      acc[2 * q] += w * v.re;
-      acc[2 * q + 1] += w * v.im;
+    if (!trivial) {
+      const double rx = dmul(double(sx), g.dr[0]);
+      const double ry = dmul(double(sy), g.dr[1]);
+      const double rz = dmul(double(sz), g.dr[2]);
+      v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
+               reduced_ylm(ell_b, m_b, rx, ry, rz));
     }
+    atomicAdd(hist + 2 * key, v.re);
+    if (v.im != 0.) atomicAdd(hist + 2 * key + 1, v.im);
   }
-  block_add<2 * kBesselChunk>(acc, out + 2 * p0, red, 2 * (npairs - p0));
+}
+
+__global__ void octant_radius_kernel(Geom g, double* rkey) {
+  const int dx = g.n[0] / 2 + 1, dy = g.n[1] / 2 + 1, dz = g.n[2] / 2 + 1;
+  const int64_t nk = int64_t(dx) * dy * dz;
+  for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       key < nk; key += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(key % dz);
+    const int b = int((key / dz) % dy);
+    const int a = int(key / (int64_t(dz) * dy));
+    rkey[key] = vec3_mag(dmul(double(a), g.dr[0]), dmul(double(b), g.dr[1]),
+                         dmul(double(c), g.dr[2]));
+  }
 }
 
 template <class Real>
@@ -805,7 +821,7 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* hist, const SplineTable& sja,
                              const SplineTable& sjb, const double* ka,
                              const double* kb, int npairs, bool ff,
-                             double* out) {
+                             double* out, const double* rkey) {
   if (npairs <= 0) return;
   PairBesselArgs a{sja, sjb, ka, kb};
   const bool same_leg = sja.ell == sjb.ell;
@@ -814,26 +830,26 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
   TRVG_KBEGIN(ctx, "pair_bessel_sums_kernel");
   if (ff && sja.q != nullptr && sjb.q != nullptr)
     pair_bessel_sums_ff_kernel<<<grid, 256, 0, ctx.stream>>>(
-        nkeys, g.dr[0], hist, a, npairs, same_leg, out);
+        nkeys, g.dr[0], rkey, hist, a, npairs, same_leg, out);
   else
     pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(
-        nkeys, g.dr[0], hist, a, npairs, same_leg, out);
+        nkeys, g.dr[0], rkey, hist, a, npairs, same_leg, out);
   TRVG_LAUNCHED(ctx);
 }
 
 template <class Real>
-void launch_pair_bessel_direct(Context& ctx, const Geom& g, const Real* xi_re,
-                               const Real* xi_im, int ell_a, int m_a,
-                               int ell_b, int m_b, const SplineTable& sja,
-                               const SplineTable& sjb, const double* ka,
-                               const double* kb, int npairs, double* out) {
-  if (npairs <= 0) return;
-  PairBesselArgs a{sja, sjb, ka, kb};
-  dim3 grid(grid_for(g.nmesh, 256, 152 * 4),
-            (npairs + kBesselChunk - 1) / kBesselChunk);
-  TRVG_KBEGIN(ctx, "pair_bessel_direct_kernel");
-  pair_bessel_direct_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
-      g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, a, npairs, out);
+void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
+                             const Real* xi_im, int ell_a, int m_a, int ell_b,
+                             int m_b, double* hist, double* rkey) {
+  const int64_t nk = int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) *
+                     (g.n[2] / 2 + 1);
+  TRVG_KBEGIN(ctx, "orbit_rows_kernel");
+  octant_cell_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0,
+                                  ctx.stream>>>(g, xi_re, xi_im, ell_a, m_a,
+                                                ell_b, m_b, hist);
+  TRVG_LAUNCHED(ctx);
+  TRVG_KBEGIN(ctx, "orbit_rows_kernel");
+  octant_radius_kernel<<<grid_for(nk, 256), 256, 0, ctx.stream>>>(g, rkey);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -862,10 +878,9 @@ void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
                                             const int*, int, double*);        \
   template void launch_radial_hist<R>(Context&, const Geom&, const R*,        \
                                       const R*, int, int, int, int, double*); \
-  template void launch_pair_bessel_direct<R>(                                 \
-      Context&, const Geom&, const R*, const R*, int, int, int, int,          \
-      const SplineTable&, const SplineTable&, const double*, const double*,   \
-      int, double*);                                                          \
+  template void launch_octant_cell_hist<R>(Context&, const Geom&, const R*,   \
+                                           const R*, int, int, int, int,      \
+                                           double*, double*);                 \
   template void launch_shotnoise_3pcf_bins<R>(                                \
       Context&, const Geom&, const R*, const R*, int, int, int, int,          \
       const BinsDev&, long long*, double*, double*);
