@@ -747,10 +747,12 @@ struct Engine {
         launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.sim), g.nmesh,
                                  wsum + 2 * i + 1, 0.);
     }
-    if (dd)
+    bool any_mesh = false;
+    for (int i = 0; i < nt; ++i) any_mesh = any_mesh || tg.t[i].re != nullptr;
+    if (dd && any_mesh)
       launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dd,
                         with_scales(true));
-    if (dr)
+    if (dr && any_mesh)
       launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dr,
                         with_scales(false));
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
