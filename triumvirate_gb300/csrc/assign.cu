@@ -638,13 +638,15 @@ __device__ __forceinline__ cd target_weight(const YlmTarget& t,
 
 __device__ __forceinline__ void particle_terms(const DevCatalogue& cat,
                                                int64_t p, int ell,
+                                               const double* cnorm,
                                                double* wpow, cd* ypos) {
   const double w = (cat.w != nullptr) ? cat.w[p] : 1.0;
   wpow[0] = 1.;
   wpow[1] = w;
   wpow[2] = w * w;
   wpow[3] = wpow[2] * w;
-  if (ell > 0) reduced_ylm_all(ell, cat.lx[p], cat.ly[p], cat.lz[p], ypos);
+  if (ell > 0)
+    reduced_ylm_all(ell, cnorm, cat.lx[p], cat.ly[p], cat.lz[p], ypos);
 }
 
 __global__ void __launch_bounds__(256)
@@ -657,7 +659,7 @@ ylm_weight_sums_kernel(DevCatalogue cat, YlmTargets ts, double* out) {
        p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
     double wpow[4];
     cd ypos[kMaxYlmDegree + 1];
-    particle_terms(cat, p, ts.ell, wpow, ypos);
+    particle_terms(cat, p, ts.ell, ts.cnorm, wpow, ypos);
 #pragma unroll
     for (int t = 0; t < kMaxYlmTargets; ++t) {
       if (t >= ts.count) break;
@@ -693,7 +695,7 @@ assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
        p < p0 + np; p += int64_t(gridDim.x) * blockDim.x) {
     double wpow[4];
     cd ypos[kMaxYlmDegree + 1];
-    particle_terms(a.cat, p, ts.ell, wpow, ypos);
+    particle_terms(a.cat, p, ts.ell, ts.cnorm, wpow, ypos);
     const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
     StencilF<ORDER> sx, sy, sz, hx, hy, hz;
     const bool fast =
@@ -953,9 +955,11 @@ void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
   if (cat.n == 0 || ts.count == 0) return;
   if (ts.count > kMaxYlmTargets || ts.ell > kMaxYlmDegree || ts.ell < 0)
     throw_error(TRVG_ERR_INVALID_PARAMETER, "Too many Y_lm targets.");
+  YlmTargets tn = ts;
+  ylm_all_norms(tn.ell, tn.cnorm);
   TRVG_KBEGIN(ctx, "weight_sum_kernel");
   ylm_weight_sums_kernel<<<grid_for(cat.n, 256), 256, 0, ctx.stream>>>(
-      cat, ts, out);
+      cat, tn, out);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -978,10 +982,12 @@ void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
     for (const float* q : {ts.t[t].re, ts.t[t].im, ts.t[t].sre, ts.t[t].sim})
       if (q != nullptr && reinterpret_cast<uintptr_t>(q) % 16 != 0)
         a.vec4 = false;
+  YlmTargets tn = ts;
+  ylm_all_norms(tn.ell, tn.cnorm);
   const int grid = std::min(grid_for(cat.n, 256), 152 * 8);
   auto go = [&](auto kernel) {
     TRVG_KBEGIN(ctx, "assign_kernel");
-    kernel<<<grid, 256, 0, ctx.stream>>>(a, ts);
+    kernel<<<grid, 256, 0, ctx.stream>>>(a, tn);
     TRVG_LAUNCHED(ctx);
   };
   switch (order) {

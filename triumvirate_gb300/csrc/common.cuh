@@ -141,34 +141,57 @@ TRVG_HD cd reduced_ylm(int ell, int m, double x, double y, double z) {
   return sqrt(4.0 * kPi / (2.0 * ell + 1.0)) * ylm;
 }
 
-// y_lm for m = 0..ell at once (y[m]); the distance, the polar cosine and
-// the powers of exp(i phi) are formed once, each m then takes the same
-// operations as reduced_ylm, so every value has the same bits.  Negative
-// orders follow exactly as y_l,-m = (-1)^m conj(y_lm) (ylm_of).
-TRVG_HD void reduced_ylm_all(int ell, double x, double y, double z, cd* out) {
+// y_lm for m = 0..ell at once (y[m]), for the fused field passes: with
+// mu = z / r and Q_l^m(mu) = P_l^m(mu) / sin^m(theta) (Condon-Shortley
+// phase included), a polynomial,
+//   y_lm = sqrt((l-m)! / (l+m)!) Q_l^m(mu) ((x - i y) / r)^m,
+// since sin^m(theta) exp(-i m phi) = ((x - i y) / r)^m: one square root
+// and one division per vector.  Q_m^m = (-1)^m (2m-1)!!,
+// Q_{m+1}^m = (2m+1) mu Q_m^m and
+// Q_l^m = ((2l-1) mu Q_{l-1}^m - (l+m-1) Q_{l-2}^m) / (l-m).
+// cnorm[m] = (-1)^m (2m-1)!! sqrt((l-m)! / (l+m)!) (ylm_all_norms).  The
+// values agree with reduced_ylm to FP64 rounding; y_lm = 0 at |v| < 1e-9.
+TRVG_HD void reduced_ylm_all(int ell, const double* cnorm, double x, double y,
+                             double z, cd* out) {
   if (ell == 0) {
     out[0] = cmk(1.0, 0.0);
     return;
   }
-  const double eps = 1.e-9;
   const double r = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
-  if (fabs(r) < eps) {
+  if (fabs(r) < 1.e-9) {
     for (int m = 0; m <= ell; ++m) out[m] = cmk(0.0, 0.0);
     return;
   }
-  const double mu = z / r;
-  const double rxy = dsqrt(dadd(dmul(x, x), dmul(y, y)));
-  double c = 1.0, s = 0.0;
-  if (fabs(rxy) >= eps) {
-    c = x / rxy;
-    s = y / rxy;
-  }
-  const double norm = sqrt(4.0 * kPi / (2.0 * ell + 1.0));
-  cd e = cmk(1.0, 0.0);
+  const double inv = 1.0 / r;
+  const double mu = z * inv;
+  const cd u = cmk(x * inv, -y * inv);
+  cd e = cmk(1.0, 0.0);  // ((x - i y) / r)^m
   for (int m = 0; m <= ell; ++m) {
-    if (m > 0) e = e * cmk(c, s);
-    const double p = sph_plm(ell, m, mu);
-    out[m] = norm * conjg(p * e);
+    if (m > 0) e = e * u;
+    double q2 = 1.0, q1 = 0.0, q = 1.0;  // Q_m^m / ((-1)^m (2m-1)!!)
+    if (ell > m) {
+      q1 = q2;
+      q = double(2 * m + 1) * mu * q1;  // Q_{m+1}^m
+      for (int l = m + 2; l <= ell; ++l) {
+        const double qn =
+            (double(2 * l - 1) * mu * q - double(l + m - 1) * q1) /
+            double(l - m);
+        q1 = q;
+        q = qn;
+      }
+    }
+    out[m] = (cnorm[m] * q) * e;
+  }
+}
+
+// cnorm[m] of reduced_ylm_all for degree ell (host or device).
+TRVG_HD void ylm_all_norms(int ell, double* cnorm) {
+  for (int m = 0; m <= ell; ++m) {
+    double ratio = 1.0;  // (l-m)! / (l+m)!
+    for (int k = ell - m + 1; k <= ell + m; ++k) ratio /= double(k);
+    double df = 1.0;  // (2m-1)!!
+    for (int k = 2 * m - 1; k > 1; k -= 2) df *= double(k);
+    cnorm[m] = ((m & 1) ? -df : df) * sqrt(ratio);
   }
 }
 

@@ -78,6 +78,7 @@ struct YlmTarget {
 struct YlmTargets {
   int ell = 0;
   int count = 0;
+  double cnorm[kMaxYlmDegree + 1] = {};  // ylm_all_norms(ell), by the launchers
   YlmTarget t[kMaxYlmTargets];
 };
 
