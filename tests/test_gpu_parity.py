@@ -31,7 +31,8 @@ PRECISIONS = ['fp64', 'fp32mixed']
 
 def _sampling(precision, ngrid=NMESH, assignment='tsc', interlace=False,
               box=BOX):
-    return {'boxsize': [box] * 3, 'ngrid': [ngrid] * 3,
+    return {'boxsize': [box] * 3 if np.isscalar(box) else list(box),
+            'ngrid': [ngrid] * 3 if np.isscalar(ngrid) else list(ngrid),
             'assignment': assignment, 'interlace': interlace,
             'precision': precision}
 
@@ -248,8 +249,9 @@ def _oracle_survey(kind, d, r, wd, wr, box, ngrid, assignment, degrees,
                    form, idx_bin, bins, interlace=False):
     los_d = O.compute_los(*d.T)
     los_r = O.compute_los(*r.T)
-    (dx, dy, dz), _ = O.centre(*d.T, [box] * 3, ref=tuple(r.T))
-    (rx, ry, rz), _ = O.centre(*r.T, [box] * 3)
+    box3 = [box] * 3 if np.isscalar(box) else list(box)
+    (dx, dy, dz), _ = O.centre(*d.T, box3, ref=tuple(r.T))
+    (rx, ry, rz), _ = O.centre(*r.T, box3)
     data = dict(pos=np.stack([dx, dy, dz], -1), los=los_d, w=wd,
                 ws=np.ones_like(wd))
     rand = dict(pos=np.stack([rx, ry, rz], -1), los=los_r, w=wr,
@@ -882,3 +884,23 @@ def test_octant_shot_noise_matches_full_mesh(degrees, box, ngrid):
     for k in ('bk_raw', 'bk_shot'):
         scale = np.max(np.abs(f[k]))
         assert np.max(np.abs(o[k] - f[k])) <= 1e-5 * scale, k
+
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_oracle_lpp_unequal_cells(precision):
+    """Survey bispectrum on cells of unequal sides (the shot-noise sums keyed
+    by (|s_x|, |s_y|, |s_z|) with a radius table, y_a y_b of nonzero
+    orders M) against the oracle."""
+    box, ngrid = [900., 1000., 800.], [32, 36, 28]
+    d, r, wd, wr = _survey_inputs(1500, 6000, seed=91)
+    bins = (0.01, 0.1, 3)
+    ref = _oracle_survey('bispec', d, r, wd, wr, box, ngrid, 'tsc',
+                         (2, 0, 2), 'full', None, bins)
+    res = compute_bispec(ParticleCatalogue(*d.T, nz=1e-4, wc=wd),
+                         ParticleCatalogue(*r.T, nz=1e-4, wc=wr),
+                         degrees=(2, 0, 2),
+                         binning=Binning('fourier', 'lin', *bins), form='full',
+                         sampling_params=_sampling(precision, ngrid, 'tsc',
+                                                   box=box))
+    assert_close_threept(res, ref, 'bispec', precision)

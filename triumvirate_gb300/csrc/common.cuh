@@ -184,6 +184,34 @@ TRVG_HD void reduced_ylm_all(int ell, const double* cnorm, double x, double y,
   }
 }
 
+// One order of the same form: y_lm with cnorm_am = cnorm[|m|] of
+// ylm_all_norms(ell), mu = z / r and u = (x - i y) / r of a vector with
+// |r| >= 1e-9 (y_l,-m = (-1)^m conj(y_lm)).
+TRVG_HD cd ylm_lean(int ell, int m, double cnorm_am, double mu, cd u) {
+  if (ell == 0) return cmk(1.0, 0.0);
+  const int am = m < 0 ? -m : m;
+  cd e = cmk(1.0, 0.0);
+  for (int i = 0; i < am; ++i) e = e * u;
+  double q1 = 0.0, q = 1.0;
+  if (ell > am) {
+    q1 = 1.0;
+    q = double(2 * am + 1) * mu;
+    for (int l = am + 2; l <= ell; ++l) {
+      const double qn =
+          (double(2 * l - 1) * mu * q - double(l + am - 1) * q1) /
+          double(l - am);
+      q1 = q;
+      q = qn;
+    }
+  }
+  cd v = (cnorm_am * q) * e;
+  if (m < 0) {
+    v = conjg(v);
+    if (am & 1) v = -1.0 * v;
+  }
+  return v;
+}
+
 // cnorm[m] of reduced_ylm_all for degree ell (host or device).
 TRVG_HD void ylm_all_norms(int ell, double* cnorm) {
   for (int m = 0; m <= ell; ++m) {

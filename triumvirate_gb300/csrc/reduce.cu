@@ -621,8 +621,8 @@ pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* rkey,
 template <class Real>
 __global__ void __launch_bounds__(256)
 octant_cell_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im,
-                        int ell_a, int m_a, int ell_b, int m_b,
-                        double* hist) {
+                        int ell_a, int m_a, int ell_b, int m_b, double cna,
+                        double cnb, double* hist) {
   const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
   const int dy = g.n[1] / 2 + 1, dz = g.n[2] / 2 + 1;
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -635,13 +635,23 @@ octant_cell_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im,
     const int64_t key = (int64_t(abs(sx)) * dy + abs(sy)) * dz + abs(sz);
     cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
     if (!trivial) {
+      // y_a y_b from the form of reduced_ylm_all (cna, cnb: the norms of
+      // |m_a|, |m_b|); zero at r = 0 unless a degree is 0.
       const double rx = dmul(double(sx), g.dr[0]);
       const double ry = dmul(double(sy), g.dr[1]);
       const double rz = dmul(double(sz), g.dr[2]);
-      v = v * (reduced_ylm(ell_a, m_a, rx, ry, rz) *
-               reduced_ylm(ell_b, m_b, rx, ry, rz));
+      const double r = dsqrt(dadd(dadd(dmul(rx, rx), dmul(ry, ry)),
+                                  dmul(rz, rz)));
+      if (fabs(r) < 1.e-9) {
+        v = cd{0., 0.};
+      } else {
+        const double inv = 1.0 / r;
+        const cd u = cmk(rx * inv, -ry * inv);
+        v = v * (ylm_lean(ell_a, m_a, cna, rz * inv, u) *
+                 ylm_lean(ell_b, m_b, cnb, rz * inv, u));
+      }
     }
-    atomicAdd(hist + 2 * key, v.re);
+    if (v.re != 0.) atomicAdd(hist + 2 * key, v.re);
     if (v.im != 0.) atomicAdd(hist + 2 * key + 1, v.im);
   }
 }
@@ -843,10 +853,17 @@ void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
                              int m_b, double* hist, double* rkey) {
   const int64_t nk = int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) *
                      (g.n[2] / 2 + 1);
+  double na[kMaxYlmDegree + 1], nb[kMaxYlmDegree + 1];
+  if (ell_a > kMaxYlmDegree || ell_b > kMaxYlmDegree)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Degree above %d.",
+                kMaxYlmDegree);
+  ylm_all_norms(ell_a, na);
+  ylm_all_norms(ell_b, nb);
   TRVG_KBEGIN(ctx, "orbit_rows_kernel");
   octant_cell_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0,
-                                  ctx.stream>>>(g, xi_re, xi_im, ell_a, m_a,
-                                                ell_b, m_b, hist);
+                                  ctx.stream>>>(
+      g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, na[std::abs(m_a)],
+      nb[std::abs(m_b)], hist);
   TRVG_LAUNCHED(ctx);
   TRVG_KBEGIN(ctx, "orbit_rows_kernel");
   octant_radius_kernel<<<grid_for(nk, 256), 256, 0, ctx.stream>>>(g, rkey);
