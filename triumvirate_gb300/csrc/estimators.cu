@@ -1232,6 +1232,36 @@ struct Engine {
     const double* dkb = upload("sn.kb", kb);
     double* out = ctx.buf<double>("sn.out", 2 * size_t(np));
     zero(out, 2 * np * sizeof(double));
+    // Float-float Bessel sums as a Gram product over the distinct bins of
+    // each leg (one list when both legs have one degree).
+    auto bessel_sums = [&](int64_t nkeys, const double* hist, bool ff,
+                           const double* rkey) {
+      if (ff) {
+        const bool same = sja.ell == sjb.ell;
+        vector<double> da, db;
+        vector<int> pa(np), pb(np);
+        auto index_of = [](vector<double>& v, double k) {
+          for (size_t i = 0; i < v.size(); ++i)
+            if (v[i] == k) return int(i);
+          v.push_back(k);
+          return int(v.size() - 1);
+        };
+        for (int i = 0; i < np; ++i) {
+          pa[i] = index_of(da, ka[i]);
+          pb[i] = index_of(same ? da : db, kb[i]);
+        }
+        const double* dda = upload("sn.kda", da);
+        const double* ddb = same ? dda : upload("sn.kdb", db);
+        const int* dpa = upload("sn.pa", pa);
+        const int* dpb = upload("sn.pb", pb);
+        if (launch_pair_bessel_gram(ctx, g, nkeys, hist, sja, sjb, dda,
+                                    int(da.size()), ddb, int(db.size()), same,
+                                    dpa, dpb, np, out, rkey))
+          return;
+      }
+      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np, ff,
+                              out, rkey);
+    };
     const bool cubic = g.dr[0] == g.dr[1] && g.dr[1] == g.dr[2];
     if (xi.oct != nullptr) {
       if (ma != 0 || mb != 0 || (la + lb) % 2 != 0)
@@ -1242,8 +1272,7 @@ struct Engine {
       double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
       zero(hist, 2 * nkeys * sizeof(double));
       launch_octant_hist(ctx, g, xi.oct, la, lb, hist);
-      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
-                              true, out);
+      bessel_sums(nkeys, hist, true, nullptr);
     } else if (cubic) {
       int64_t nkeys = 1;
       for (int a = 0; a < 3; ++a) {
@@ -1260,8 +1289,7 @@ struct Engine {
         launch_radial_hist<float>(ctx, g, static_cast<const float*>(xi.re),
                                   static_cast<const float*>(xi.im), la, ma, lb,
                                   mb, hist);
-      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
-                              !xi.dbl, out);
+      bessel_sums(nkeys, hist, !xi.dbl, nullptr);
     } else {
       // Cells of unequal sides: keyed by (|s_x|, |s_y|, |s_z|), which fixes
       // |r|, with the radius of each key in a table.
@@ -1278,8 +1306,7 @@ struct Engine {
         launch_octant_cell_hist<float>(
             ctx, g, static_cast<const float*>(xi.re),
             static_cast<const float*>(xi.im), la, ma, lb, mb, hist, rkey);
-      launch_pair_bessel_sums(ctx, g, nkeys, hist, sja, sjb, dka, dkb, np,
-                              !xi.dbl, out, rkey);
+      bessel_sums(nkeys, hist, !xi.dbl, rkey);
     }
     dev_sij = out;
     if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));

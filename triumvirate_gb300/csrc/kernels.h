@@ -475,6 +475,16 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
                              const double* kb, int npairs, bool ff,
                              double* out,
                              const double* rkey = nullptr);
+// launch_pair_bessel_sums (float-float) as a Gram product over the
+// distinct bins of each leg (ka_d[nka], kb_d[nkb]; pair p uses ka_d[pa[p]],
+// kb_d[pb[p]]; same: one leg).  Returns false, launching nothing, when its
+// tables do not fit in shared memory.
+bool launch_pair_bessel_gram(Context& ctx, const Geom& g, int64_t nkeys,
+                             const double* hist, const SplineTable& sja,
+                             const SplineTable& sjb, const double* ka_d,
+                             int nka, const double* kb_d, int nkb, bool same,
+                             const int* pa, const int* pb, int npairs,
+                             double* out, const double* rkey = nullptr);
 // Sums of xi y_a y_b over cells of any shape, keyed by (|s_x|, |s_y|,
 // |s_z|) on (n/2 + 1)^3 keys, with each key's radius in rkey.
 template <class Real>

@@ -614,6 +614,114 @@ pair_bessel_sums_ff_kernel(int64_t nkeys, double dr, const double* rkey,
   block_add<2 * kKeyPairChunk>(v, out + 2 * p0, red, 2 * (npairs - p0));
 }
 
+// pair_bessel_sums_ff_kernel as a Gram product: the weight of pair p at a
+// key is J_a(key) J_b(key) with J_a = j_la(k_a r) of bin a, so a block
+// evaluates J for every distinct bin over a chunk of keys into shared
+// memory (per key 2 x bins spline evaluations instead of 2 x pairs) and
+// accumulates sum_key H J_a J_b for its pairs from there, in float-float.
+// ka_d[nka], kb_d[nkb]: the distinct k of the two legs; pa, pb: each pair's
+// indices into them.
+constexpr int kGramKeys = 128;
+// J rows one element longer than a chunk: lanes reading different rows at
+// one key fall in different banks.
+constexpr int kGramRow = kGramKeys + 1;
+constexpr int kGramPairsPerThread = 2;
+
+struct GramArgs {
+  SplineTable ja, jb;
+  const double* ka_d;
+  const double* kb_d;
+  int nka, nkb;
+  bool same;  // one leg: J_b = J_a
+  const int* pa;
+  const int* pb;
+};
+
+__global__ void __launch_bounds__(256)
+pair_bessel_gram_ff_kernel(int64_t nkeys, double dr, const double* rkey,
+                           const double* hist, GramArgs g, int npairs,
+                           double* out) {
+  // Shared memory: the histogram words of the chunk, then the J rows of
+  // leg a and of leg b (absent when one leg), kGramRow apart.
+  extern __shared__ float4 gsm[];
+  const int nrows = g.nka + (g.same ? 0 : g.nkb);
+  float4* H = gsm;
+  float2* J = reinterpret_cast<float2*>(gsm + kGramKeys);
+  const int boff = g.same ? 0 : g.nka;
+  const int pbase = blockIdx.y * blockDim.x * kGramPairsPerThread;
+  int ia[kGramPairsPerThread], ib[kGramPairsPerThread];
+  bool on[kGramPairsPerThread];
+  FF acc[2 * kGramPairsPerThread];
+#pragma unroll
+  for (int u = 0; u < kGramPairsPerThread; ++u) {
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    on[u] = pp < npairs;
+    ia[u] = on[u] ? g.pa[pp] : 0;
+    ib[u] = on[u] ? boff + g.pb[pp] : 0;
+    acc[2 * u] = acc[2 * u + 1] = FF{0.f, 0.f};
+  }
+  const FF drf = ff_from_double(dr);
+  for (int64_t k0 = int64_t(blockIdx.x) * kGramKeys; k0 < nkeys;
+       k0 += int64_t(gridDim.x) * kGramKeys) {
+    __syncthreads();  // the previous chunk is consumed
+    for (int k = threadIdx.x; k < kGramKeys; k += blockDim.x) {
+      const int64_t key = k0 + k;
+      double2 h = make_double2(0., 0.);
+      if (key < nkeys) h = reinterpret_cast<const double2*>(hist)[key];
+      const FF hr = ff_from_double(h.x), hi = ff_from_double(h.y);
+      H[k] = make_float4(hr.hi, hr.lo, hi.hi, hi.lo);
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < nrows * kGramKeys; w += blockDim.x) {
+      const int row = w / kGramKeys, k = w - row * kGramKeys;
+      const float4 h = H[k];
+      FF v{0.f, 0.f};
+      if (h.x != 0.f || h.z != 0.f) {
+        const int64_t key = k0 + k;
+        FF r;
+        if (rkey != nullptr) {
+          r = ff_from_double(rkey[key]);
+        } else {
+          // sqrt(key) in float-float (key < 2^24 is exact in FP32).
+          const float kf = float(key);
+          const float sh = __fsqrt_rn(kf);
+          const float sl =
+              sh > 0.f ? __fdiv_rn(__fmaf_rn(-sh, sh, kf), __fmul_rn(2.f, sh))
+                       : 0.f;
+          r = ffmul(drf, FF{sh, sl});
+        }
+        const bool leg_a = row < g.nka;
+        const FF kk =
+            ff_from_double(leg_a ? g.ka_d[row] : g.kb_d[row - g.nka]);
+        v = spline_eval_ff(leg_a ? g.ja : g.jb, ffmul(kk, r));
+      }
+      J[row * kGramRow + k] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kGramPairsPerThread; ++u) {
+      if (!on[u]) continue;
+      const float2* ja = J + ia[u] * kGramRow;
+      const float2* jb = J + ib[u] * kGramRow;
+      for (int k = 0; k < kGramKeys; ++k) {
+        const float4 h = H[k];
+        if (h.x == 0.f && h.z == 0.f) continue;
+        const float2 a = ja[k], b = jb[k];
+        const FF w = ffmul(FF{a.x, a.y}, FF{b.x, b.y});
+        ff_merge(acc[2 * u], ffnorm(ffmul(w, FF{h.x, h.y})));
+        ff_merge(acc[2 * u + 1], ffnorm(ffmul(w, FF{h.z, h.w})));
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kGramPairsPerThread; ++u) {
+    if (!on[u]) continue;
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    atomicAdd(out + 2 * pp, ff_value(acc[2 * u]));
+    atomicAdd(out + 2 * pp + 1, ff_value(acc[2 * u + 1]));
+  }
+}
+
 // Cells of any shape grouped by (|s_x|, |s_y|, |s_z|), which fixes |r|:
 // hist[key] += xi y_a y_b, key = (|s_x| D_y + |s_y|) D_z + |s_z| with
 // D = n/2 + 1 per axis, and rkey[key] = |r| (the sign of s does not change
@@ -845,6 +953,39 @@ void launch_pair_bessel_sums(Context& ctx, const Geom& g, int64_t nkeys,
     pair_bessel_sums_kernel<<<grid, 256, 0, ctx.stream>>>(
         nkeys, g.dr[0], rkey, hist, a, npairs, same_leg, out);
   TRVG_LAUNCHED(ctx);
+}
+
+// The Gram form of pair_bessel_sums_ff_kernel; false when its shared
+// memory would not fit (the caller then uses launch_pair_bessel_sums).
+bool launch_pair_bessel_gram(Context& ctx, const Geom& g, int64_t nkeys,
+                             const double* hist, const SplineTable& sja,
+                             const SplineTable& sjb, const double* ka_d,
+                             int nka, const double* kb_d, int nkb, bool same,
+                             const int* pa, const int* pb, int npairs,
+                             double* out, const double* rkey) {
+  if (npairs <= 0) return true;
+  if (sja.q == nullptr || sjb.q == nullptr) return false;
+  const int nrows = nka + (same ? 0 : nkb);
+  const size_t smem = size_t(nrows) * kGramRow * sizeof(float2) +
+                      kGramKeys * sizeof(float4);
+  if (smem > 200 * 1024) return false;
+  static bool configured[64] = {};
+  if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+    TRVG_CUDA(cudaFuncSetAttribute(pair_bessel_gram_ff_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   200 * 1024));
+    if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+  }
+  GramArgs a{sja, sjb, ka_d, kb_d, nka, nkb, same, pa, pb};
+  const int per_block = 256 * kGramPairsPerThread;
+  const int64_t chunks = (nkeys + kGramKeys - 1) / kGramKeys;
+  dim3 grid(unsigned(std::min<int64_t>(chunks, 152 * 4)),
+            unsigned((npairs + per_block - 1) / per_block));
+  TRVG_KBEGIN(ctx, "pair_bessel_sums_kernel");
+  pair_bessel_gram_ff_kernel<<<grid, 256, smem, ctx.stream>>>(
+      nkeys, g.dr[0], rkey, hist, a, npairs, out);
+  TRVG_LAUNCHED(ctx);
+  return true;
 }
 
 template <class Real>
