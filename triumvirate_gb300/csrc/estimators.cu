@@ -1807,10 +1807,12 @@ struct Engine {
         zero(dout, 2 * idx.size() * sizeof(double));
         if (real)
           launch_reduce_pairs_real<FR>(ctx, Mc, Gr, FAr, FBr, dpa, dpb,
-                                       int(idx.size()), dout);
+                                       int(idx.size()), dout, int(bA.size()),
+                                       int(bB.size()));
         else
           launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb,
-                                  int(idx.size()), dout);
+                                  int(idx.size()), dout, int(bA.size()),
+                                  int(bB.size()));
         vector<double> h = download(dout, 2 * idx.size());
         for (size_t q = 0; q < idx.size(); ++q)
           res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);

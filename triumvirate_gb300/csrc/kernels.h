@@ -325,13 +325,15 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
                          const typename CplxOf<Real>::type* Fa,
                          const typename CplxOf<Real>::type* Fb,
                          const int* pa, const int* pb, int npairs,
-                         double* out /* 2 * npairs */);
+                         double* out /* 2 * npairs */, int na = 0,
+                         int nb = 0 /* fields per leg: FP32 tiled form */);
 
 template <class Real>
 void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
                               const Real* Fa, const Real* Fb, const int* pa,
                               const int* pb, int npairs,
-                              double* out /* 2 * npairs, imaginary 0 */);
+                              double* out /* 2 * npairs, imaginary 0 */, int na = 0,
+                              int nb = 0);
 
 // ---- ffft.cu -------------------------------------------------------------
 // Float-float transforms of the shell fields: a plan is the radix list of

@@ -150,6 +150,124 @@ reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
                                       red);
 }
 
+// FP32 complex fields as a Gram product: a block loads a tile of cells of
+// every leg-a field and of every leg-b field times G into shared memory
+// (each field is read once per launch instead of once per pair) and
+// accumulates sum_x F_a (F_b G) for its pairs from there in float-float.
+constexpr int kRedTile = 64;
+constexpr int kRedRow = kRedTile + 1;  // padded: rows fall in other banks
+constexpr int kRedPairsPerThread = 2;
+
+__global__ void __launch_bounds__(256)
+reduce_pairs_gram_kernel(int64_t ncell, const float2* G, const float2* Fa,
+                         int na, const float2* Fb, int nb, const int* pa,
+                         const int* pb, int npairs, double* out) {
+  extern __shared__ float2 rsm[];
+  float2* A = rsm;                  // [na][kRedRow]: F_a
+  float2* B = rsm + na * kRedRow;   // [nb][kRedRow]: F_b G
+  const int pbase = blockIdx.y * blockDim.x * kRedPairsPerThread;
+  int ia[kRedPairsPerThread], ib[kRedPairsPerThread];
+  bool on[kRedPairsPerThread];
+  FF acc[2 * kRedPairsPerThread];
+#pragma unroll
+  for (int u = 0; u < kRedPairsPerThread; ++u) {
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    on[u] = pp < npairs;
+    ia[u] = on[u] ? pa[pp] : 0;
+    ib[u] = on[u] ? pb[pp] : 0;
+    acc[2 * u] = acc[2 * u + 1] = FF{0.f, 0.f};
+  }
+  const int nrows = na + nb;
+  for (int64_t c0 = int64_t(blockIdx.x) * kRedTile; c0 < ncell;
+       c0 += int64_t(gridDim.x) * kRedTile) {
+    __syncthreads();  // the previous tile is consumed
+    for (int w = threadIdx.x; w < nrows * kRedTile; w += blockDim.x) {
+      const int row = w / kRedTile, c = w - row * kRedTile;
+      const int64_t cell = c0 + c;
+      float2 v = make_float2(0.f, 0.f);
+      if (cell < ncell) {
+        if (row < na) {
+          v = Fa[int64_t(row) * ncell + cell];
+        } else {
+          v = cmulc(Fb[int64_t(row - na) * ncell + cell], G[cell]);
+        }
+      }
+      if (row < na) A[row * kRedRow + c] = v;
+      else B[(row - na) * kRedRow + c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kRedPairsPerThread; ++u) {
+      if (!on[u]) continue;
+      const float2* ra = A + ia[u] * kRedRow;
+      const float2* rb = B + ib[u] * kRedRow;
+      for (int c = 0; c < kRedTile; ++c) {
+        const float2 q = cmulc(ra[c], rb[c]);
+        ff_add(acc[2 * u], q.x);
+        ff_add(acc[2 * u + 1], q.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kRedPairsPerThread; ++u) {
+    if (!on[u]) continue;
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    atomicAdd(out + 2 * pp, ff_value(acc[2 * u]));
+    atomicAdd(out + 2 * pp + 1, ff_value(acc[2 * u + 1]));
+  }
+}
+
+// The same tiled Gram form for FP32 real fields (imaginary output zero).
+__global__ void __launch_bounds__(256)
+reduce_pairs_gram_real_kernel(int64_t ncell, const float* G, const float* Fa,
+                              int na, const float* Fb, int nb, const int* pa,
+                              const int* pb, int npairs, double* out) {
+  extern __shared__ float rsr[];
+  float* A = rsr;                  // [na][kRedRow]: F_a
+  float* B = rsr + na * kRedRow;   // [nb][kRedRow]: F_b G
+  const int pbase = blockIdx.y * blockDim.x * kRedPairsPerThread;
+  int ia[kRedPairsPerThread], ib[kRedPairsPerThread];
+  bool on[kRedPairsPerThread];
+  FF acc[kRedPairsPerThread];
+#pragma unroll
+  for (int u = 0; u < kRedPairsPerThread; ++u) {
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    on[u] = pp < npairs;
+    ia[u] = on[u] ? pa[pp] : 0;
+    ib[u] = on[u] ? pb[pp] : 0;
+    acc[u] = FF{0.f, 0.f};
+  }
+  const int nrows = na + nb;
+  for (int64_t c0 = int64_t(blockIdx.x) * kRedTile; c0 < ncell;
+       c0 += int64_t(gridDim.x) * kRedTile) {
+    __syncthreads();
+    for (int w = threadIdx.x; w < nrows * kRedTile; w += blockDim.x) {
+      const int row = w / kRedTile, c = w - row * kRedTile;
+      const int64_t cell = c0 + c;
+      float v = 0.f;
+      if (cell < ncell)
+        v = (row < na) ? Fa[int64_t(row) * ncell + cell]
+                       : Fb[int64_t(row - na) * ncell + cell] * G[cell];
+      if (row < na) A[row * kRedRow + c] = v;
+      else B[(row - na) * kRedRow + c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kRedPairsPerThread; ++u) {
+      if (!on[u]) continue;
+      const float* ra = A + ia[u] * kRedRow;
+      const float* rb = B + ib[u] * kRedRow;
+      for (int c = 0; c < kRedTile; ++c) ff_add(acc[u], ra[c] * rb[c]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kRedPairsPerThread; ++u) {
+    if (!on[u]) continue;
+    const int pp = pbase + u * blockDim.x + threadIdx.x;
+    atomicAdd(out + 2 * pp, ff_value(acc[u]));
+  }
+}
+
 // Real fields: sum_x F_a F_b G; the imaginary part of the output is left
 // at zero.
 template <class Real>
@@ -839,8 +957,29 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
                          const typename CplxOf<Real>::type* Fa,
                          const typename CplxOf<Real>::type* Fb,
                          const int* pa, const int* pb, int npairs,
-                         double* out) {
+                         double* out, int na, int nb) {
   if (npairs <= 0) return;
+  if constexpr (sizeof(Real) == 4) {
+    const size_t smem = size_t(na + nb) * kRedRow * sizeof(float2);
+    if (na > 0 && nb > 0 && smem <= 200 * 1024) {
+      static bool configured[64] = {};
+      if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+        TRVG_CUDA(cudaFuncSetAttribute(
+            reduce_pairs_gram_kernel,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+      }
+      const int per_block = 256 * kRedPairsPerThread;
+      const int64_t tiles = (ncell + kRedTile - 1) / kRedTile;
+      dim3 grid(unsigned(std::min<int64_t>(tiles, 152 * 8)),
+                unsigned((npairs + per_block - 1) / per_block));
+      TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
+      reduce_pairs_gram_kernel<<<grid, 256, smem, ctx.stream>>>(
+          ncell, G, Fa, na, Fb, nb, pa, pb, npairs, out);
+      TRVG_LAUNCHED(ctx);
+      return;
+    }
+  }
   const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
   dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
   TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
@@ -852,8 +991,30 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
 template <class Real>
 void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
                               const Real* Fa, const Real* Fb, const int* pa,
-                              const int* pb, int npairs, double* out) {
+                              const int* pb, int npairs, double* out, int na,
+                              int nb) {
   if (npairs <= 0) return;
+  if constexpr (sizeof(Real) == 4) {
+    const size_t smem = size_t(na + nb) * kRedRow * sizeof(float);
+    if (na > 0 && nb > 0 && smem <= 200 * 1024) {
+      static bool configured[64] = {};
+      if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+        TRVG_CUDA(cudaFuncSetAttribute(
+            reduce_pairs_gram_real_kernel,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+      }
+      const int per_block = 256 * kRedPairsPerThread;
+      const int64_t tiles = (ncell + kRedTile - 1) / kRedTile;
+      dim3 grid(unsigned(std::min<int64_t>(tiles, 152 * 8)),
+                unsigned((npairs + per_block - 1) / per_block));
+      TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
+      reduce_pairs_gram_real_kernel<<<grid, 256, smem, ctx.stream>>>(
+          ncell, G, Fa, na, Fb, nb, pa, pb, npairs, out);
+      TRVG_LAUNCHED(ctx);
+      return;
+    }
+  }
   const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
   dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
   TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
@@ -1030,10 +1191,11 @@ void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
                                        const CplxOf<R>::type*,                \
                                        const CplxOf<R>::type*,                \
                                        const CplxOf<R>::type*, const int*,    \
-                                       const int*, int, double*);             \
+                                       const int*, int, double*, int, int);   \
   template void launch_reduce_pairs_real<R>(Context&, int64_t, const R*,     \
                                             const R*, const R*, const int*,   \
-                                            const int*, int, double*);        \
+                                            const int*, int, double*, int,    \
+                                            int);                             \
   template void launch_radial_hist<R>(Context&, const Geom&, const R*,        \
                                       const R*, int, int, int, int, double*); \
   template void launch_octant_cell_hist<R>(Context&, const Geom&, const R*,   \
