@@ -78,69 +78,6 @@ TRVG_HD double vec3_mag(double x, double y, double z) {
 // FFT-ordered index -> signed frequency / offset (field.cpp:538-542).
 TRVG_HD int shift_index(int i, int n) { return (i < n / 2) ? i : i - n; }
 
-// ---------------------------------------------------------------------------
-// Reduced spherical harmonics (maths.cpp:171-220).
-//
-// y_lm(v) = (-1)^m [m < 0] * conj(Y_l^m(v)) * sqrt(4 pi / (2l + 1)), with
-// y_00 = 1 and y_lm = 0 for |v| < 1e-9.  Y_l^m uses the normalised
-// associated Legendre function with the Condon-Shortley phase; the azimuthal
-// factor exp(i m phi) is formed from (x + i y) / r_xy, which equals the
-// reference's phi = arccos(x / r_xy) (reflected for y < 0) without the
-// inverse cosine.
-// ---------------------------------------------------------------------------
-
-// Normalised associated Legendre function
-//   sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) P_l^m(x),  0 <= m <= l,
-// from the standard stable recurrence in l at fixed m (start from P_m^m,
-// step with the normalised three-term relation).
-TRVG_HD double sph_plm(int l, int m, double x) {
-  double pmm = 1.0;
-  const double omx2 = (1.0 - x) * (1.0 + x);
-  double fact = 1.0;
-  for (int i = 1; i <= m; ++i) {
-    pmm *= omx2 * fact / (fact + 1.0);
-    fact += 2.0;
-  }
-  pmm = sqrt((2 * m + 1) * pmm / (4.0 * kPi));
-  if (m & 1) pmm = -pmm;
-  if (l == m) return pmm;
-  double pmmp1 = x * sqrt(2.0 * m + 3.0) * pmm;
-  if (l == m + 1) return pmmp1;
-  double oldfact = sqrt(2.0 * m + 3.0);
-  double pll = 0.0;
-  for (int ll = m + 2; ll <= l; ++ll) {
-    const double f = sqrt((4.0 * ll * ll - 1.0) / double(ll * ll - m * m));
-    pll = (x * pmmp1 - pmm / oldfact) * f;
-    oldfact = f;
-    pmm = pmmp1;
-    pmmp1 = pll;
-  }
-  return pll;
-}
-
-TRVG_HD cd reduced_ylm(int ell, int m, double x, double y, double z) {
-  if (ell == 0 && m == 0) return cmk(1.0, 0.0);
-  const double eps = 1.e-9;
-  const double r = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
-  if (fabs(r) < eps) return cmk(0.0, 0.0);
-  const double mu = z / r;
-  const double rxy = dsqrt(dadd(dmul(x, x), dmul(y, y)));
-  double c = 1.0, s = 0.0;  // cos(phi), sin(phi)
-  if (fabs(rxy) >= eps) {
-    c = x / rxy;
-    s = y / rxy;
-  }
-  const int am = m < 0 ? -m : m;
-  // exp(i |m| phi) by repeated multiplication.
-  cd e = cmk(1.0, 0.0);
-  for (int i = 0; i < am; ++i) e = e * cmk(c, s);
-  if (m < 0) e = conjg(e);
-  const double p = sph_plm(ell, am, mu);
-  cd ylm = conjg(p * e);
-  if (m < 0 && (am & 1)) ylm = -1.0 * ylm;
-  return sqrt(4.0 * kPi / (2.0 * ell + 1.0)) * ylm;
-}
-
 // y_lm for m = 0..ell at once (y[m]), for the fused field passes: with
 // mu = z / r and Q_l^m(mu) = P_l^m(mu) / sin^m(theta) (Condon-Shortley
 // phase included), a polynomial,
@@ -221,6 +158,31 @@ TRVG_HD void ylm_all_norms(int ell, double* cnorm) {
     for (int k = 2 * m - 1; k > 1; k -= 2) df *= double(k);
     cnorm[m] = ((m & 1) ? -df : df) * sqrt(ratio);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Reduced spherical harmonics (maths.cpp:171-220):
+//   y_lm(v) = (-1)^m [m < 0] conj(Y_l^m(v)) sqrt(4 pi / (2l + 1)),
+// Y_l^m with the normalised associated Legendre function and the
+// Condon-Shortley phase; y_00 = 1 and y_lm = 0 for |v| < 1e-9.  Formed as
+// sqrt((l-|m|)! / (l+|m|)!) Q_l^|m|(mu) ((x - i y) / r)^|m| (conjugated,
+// with (-1)^m, for m < 0), where Q_l^m = P_l^m / sin^m(theta) comes from the
+// rational three-term recurrence: one square root and one division for the
+// vector, one for the norm, instead of the reference's arccos and the
+// square roots of the normalised recurrence.
+// ---------------------------------------------------------------------------
+TRVG_HD cd reduced_ylm(int ell, int m, double x, double y, double z) {
+  if (ell == 0 && m == 0) return cmk(1.0, 0.0);
+  const double r = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+  if (fabs(r) < 1.e-9) return cmk(0.0, 0.0);
+  const int am = m < 0 ? -m : m;
+  double ratio = 1.0;  // (l-m)! / (l+m)!
+  for (int k = ell - am + 1; k <= ell + am; ++k) ratio /= double(k);
+  double df = 1.0;  // (2m-1)!!
+  for (int k = 2 * am - 1; k > 1; k -= 2) df *= double(k);
+  const double cn = ((am & 1) ? -df : df) * sqrt(ratio);
+  const double inv = 1.0 / r;
+  return ylm_lean(ell, m, cn, z * inv, cmk(x * inv, -y * inv));
 }
 
 // y_lm of any order from the non-negative orders of reduced_ylm_all.
