@@ -215,6 +215,10 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           tile side, pair-reduction bin batch) on first
  *                           use and keep the fastest (default 1; 0 also
  *                           forgets earlier choices);
+ *   "overlap"          0/1: run the shot-noise field of an FP32
+ *                           periodic-box bispectrum on a second stream next
+ *                           to the float-float shell fields (default 1; off
+ *                           while profiling and in batch replays);
  *   "xi_octant"        0/1: FP32 periodic-box bispectra with m = 0 legs of
  *                           even total degree: keep the shot-noise field
  *                           averaged over sign flips on one octant (three

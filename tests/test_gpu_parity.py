@@ -904,3 +904,28 @@ def test_oracle_lpp_unequal_cells(precision):
                          sampling_params=_sampling(precision, ngrid, 'tsc',
                                                    box=box))
     assert_close_threept(res, ref, 'bispec', precision)
+
+
+def test_side_stream_shot_noise_matches_one_stream():
+    """The periodic-box bispectrum with its shot-noise field on the second
+    stream (next to the float-float shell fields) equals the one-stream
+    estimate and the FP64 one within the FP32-mixed tolerance."""
+    box = 1000.
+    pos = _uniform(200000, box, 61)
+    kw = dict(degrees=(0, 0, 0), form='diag',
+              binning=Binning('fourier', 'lin', 0.005, 0.105, 8))
+    ctx = _lib.default_context(None)
+
+    def run(overlap, precision='fp32mixed'):
+        ctx.set_option('overlap', overlap)
+        try:
+            return compute_bispec_in_gpp_box(
+                ParticleCatalogue(*pos.T, nz=len(pos) / box ** 3),
+                sampling_params=_sampling(precision, 128, box=box), **kw)
+        finally:
+            ctx.set_option('overlap', 1)
+    two, one, ref = run(1), run(0), run(1, 'fp64')
+    for k in ('bk_raw', 'bk_shot'):
+        scale = np.max(np.abs(ref[k]))
+        assert np.max(np.abs(two[k] - one[k])) <= 1e-5 * scale, k
+        assert np.max(np.abs(two[k] - ref[k])) <= 1e-5 * scale, k

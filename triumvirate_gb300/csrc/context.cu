@@ -119,6 +119,15 @@ cudaEvent_t next_event(Context& c) {
 }
 }  // namespace
 
+cudaStream_t Context::side_stream() {
+  if (side == nullptr) {
+    TRVG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    TRVG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    TRVG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  }
+  return side;
+}
+
 void Context::kbegin(const char* name) {
   if (!profiling) return;
   pending = name;
@@ -235,6 +244,9 @@ int trvg_context_destroy(trvg_context* ctx) {
   if (ctx->impl.ev_start) cudaEventDestroy(ctx->impl.ev_start);
   if (ctx->impl.ev_h2d) cudaEventDestroy(ctx->impl.ev_h2d);
   if (ctx->impl.ev_stop) cudaEventDestroy(ctx->impl.ev_stop);
+  if (ctx->impl.ev_fork) cudaEventDestroy(ctx->impl.ev_fork);
+  if (ctx->impl.ev_join) cudaEventDestroy(ctx->impl.ev_join);
+  if (ctx->impl.side) cudaStreamDestroy(ctx->impl.side);
   trvg::destroy_events(ctx->impl);
   if (ctx->impl.own_stream) cudaStreamDestroy(ctx->impl.own_stream);
   delete ctx;
@@ -297,6 +309,8 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
   } else if (k == "autotune") {
     ctx->impl.autotune = value != 0;
     if (value == 0) ctx->impl.tuned.clear();
+  } else if (k == "overlap") {
+    ctx->impl.overlap = value != 0;
   } else if (k == "xi_octant") {
     ctx->impl.xi_octant = value != 0;
   } else if (k == "fused_ylm") {

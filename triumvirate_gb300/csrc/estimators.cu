@@ -566,8 +566,10 @@ struct Engine {
 
   // Assign all parts into one (complex if `cplx`) mesh, with the shadow when
   // interlacing, and transform each component mesh once (R2C).
+  // defer_r2c: a real field without interlacing whose R2C the caller issues
+  // later (run_pending_r2c); its spectrum buffer is assigned already.
   Field make_field(const std::string& name, const vector<Part>& parts,
-                   bool cplx) {
+                   bool cplx, bool defer_r2c = false) {
     Field f;
     Real* mre = ctx.buf<Real>("mesh.re", g.nmesh);
     Real* mim = cplx ? ctx.buf<Real>("mesh.im", g.nmesh) : nullptr;
@@ -607,13 +609,20 @@ struct Engine {
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
     auto r2c = [&](Real* m, const char* suffix) -> const C* {
       C* o = ctx.buf<C>(name + suffix, size_t(g.nhalf));
+      TRVG_CUFFT(cufftSetStream(h, ctx.stream));
       ctx.kbegin("cufft.r2c.mesh");
       FFT<Real>::r2c(h, m, o);
       ctx.kend();
       ctx.fft_launches++;
       return o;
     };
-    f.spec.re = r2c(mre, ".re");
+    if (defer_r2c && mim == nullptr && sre == nullptr) {
+      C* o = ctx.buf<C>(name + ".re", size_t(g.nhalf));
+      pending_r2c = {mre, o};
+      f.spec.re = o;
+    } else {
+      f.spec.re = r2c(mre, ".re");
+    }
     ++ctx.mesh_gen;
     if (mim == nullptr && sre == nullptr) {
       f.spec.mesh = mre;
@@ -778,6 +787,24 @@ struct Engine {
     for (int i = 0; i < nt; ++i)
       for (int k = 0; k < 4; ++k) out[i].sums[k] = hs[4 * i + k];
     return out;
+  }
+
+  // A mesh R2C deferred by make_field (defer_r2c): issued on the current
+  // stream.
+  struct PendingR2C {
+    Real* mesh = nullptr;
+    C* out = nullptr;
+  } pending_r2c;
+
+  void run_pending_r2c() {
+    if (pending_r2c.mesh == nullptr) return;
+    cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
+    TRVG_CUFFT(cufftSetStream(h, ctx.stream));
+    ctx.kbegin("cufft.r2c.mesh");
+    FFT<Real>::r2c(h, pending_r2c.mesh, pending_r2c.out);
+    ctx.kend();
+    ctx.fft_launches++;
+    pending_r2c = PendingR2C{};
   }
 
   // Field spectrum with its exact k = 0 mode: (main sum + shift) combined
@@ -1113,6 +1140,7 @@ struct Engine {
         fa.k0_dev, fb.k0_dev, replay ? replay->state->count_d : nullptr, ext);
     auto pass = [&](int n, int64_t lines) {
       cufftHandle h = ctx.plan1d(CUFFT_R2C, n, int(lines));
+      TRVG_CUFFT(cufftSetStream(h, ctx.stream));
       ctx.kbegin("cufft.r2c.xi_octant");
       TRVG_CUFFT(cufftExecR2C(h, ext, reinterpret_cast<cufftComplex*>(out)));
       ctx.kend();
@@ -1165,6 +1193,7 @@ struct Engine {
                                    him);
     }
     cufftHandle h = ctx.plan(FFT<XR>::kC2R, g.n, 1);
+    TRVG_CUFFT(cufftSetStream(h, ctx.stream));
     Xi xi;
     xi.dbl = sizeof(XR) == 8;
     XR* re = ctx.buf<XR>("xi.re", size_t(g.nmesh));
@@ -1868,7 +1897,10 @@ struct Engine {
       dn.k0_dev = replay->state->k0_dn;
       nf.k0_dev = replay->state->k0_nf;
     } else if (!survey) {
-      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      // The R2C of the mesh feeds only the shot-noise side of the estimate
+      // here; it is issued below, on the second stream when that applies.
+      Field base = make_field("N", {{dd, WeightSpec()}}, false,
+                              sizeof(Real) == 4);
       const double nbar = double(dd.n) / g.vol;
       dn = k0_view(base, -nbar * g.vol);
       nf = k0_view(base, 0.);
@@ -1906,11 +1938,39 @@ struct Engine {
     vector<cplx> bk(ndv, 0.), sn(ndv, 0.);
 
     Xi xi;
+    bool forked = false;
     if (!survey) {
       const cplx shot(double(dd.n), 0.);
-      xi = xi_octant_ok(dn, nf, shot, terms) ? twopt_xi_octant(dn, nf, shot)
-                                             : twopt_xi(dn, nf, shot);
+      const bool octant = xi_octant_ok(dn, nf, shot, terms);
+      // The float-float shell fields read the mesh, not its spectrum, so
+      // the R2C and the octant shot-noise field (memory-bound) can run on
+      // the second stream next to them (FP32-issue-bound) until the first
+      // reader of the spectrum or of xi (joined after the pair sums).
+      const Leg la0{p.ell1, 0}, lb0{p.ell2, 0};
+      if (pending_r2c.mesh != nullptr && octant && ctx.overlap &&
+          !ctx.profiling && replay == nullptr &&
+          real_fields(dn, dn, la0, lb0, M) &&
+          ff_applicable(dn, dn, la0, lb0, pairs, hb, M, K)) {
+        const cudaStream_t main = ctx.stream, side = ctx.side_stream();
+        TRVG_CUDA(cudaEventRecord(ctx.ev_fork, main));
+        TRVG_CUDA(cudaStreamWaitEvent(side, ctx.ev_fork, 0));
+        ctx.stream = side;
+        try {
+          run_pending_r2c();
+          xi = twopt_xi_octant(dn, nf, shot);
+        } catch (...) {
+          ctx.stream = main;
+          throw;
+        }
+        ctx.stream = main;
+        TRVG_CUDA(cudaEventRecord(ctx.ev_join, side));
+        forked = true;
+      } else {
+        run_pending_r2c();
+        xi = octant ? twopt_xi_octant(dn, nf, shot) : twopt_xi(dn, nf, shot);
+      }
     }
+    run_pending_r2c();
     vector<double> no_radii;
 
     // Survey: delta n_LM, N_LM and S-bar_LM of every order M of the terms
@@ -1962,6 +2022,10 @@ struct Engine {
       Leg la{p.ell1, t.m1}, lb{p.ell2, t.m2};
       const vector<cplx> comp =
           pair_sums(dn, dnLM, la, lb, pairs, hb, no_radii, M, K, Kg);
+      if (forked) {  // the spectrum and xi are read from here on
+        TRVG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.ev_join, 0));
+        forked = false;
+      }
       if (replay != nullptr) {
         // The same combinations on the device (batch.cu).
         MockTermArgs a{};
@@ -2035,6 +2099,7 @@ struct Engine {
       }
     }
 
+    if (forked) TRVG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.ev_join, 0));
     if (replay != nullptr) {
       launch_mock_store(ctx, replay->state, replay->acc, ndv, replay->raw,
                         replay->shot);

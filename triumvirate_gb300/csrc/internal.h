@@ -120,6 +120,12 @@ struct Context {
   std::map<std::string, DeviceBuffer> buffers;
   std::map<PlanKey, cufftHandle> plans;
   cudaEvent_t ev_start = nullptr, ev_h2d = nullptr, ev_stop = nullptr;
+  // Second stream for memory-bound work next to FP32-issue-bound work of
+  // the same estimate (created on first use), with its fork / join events.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool overlap = true;
+  cudaStream_t side_stream();
   int verbose = 0;
   // Counters of the current / last call.
   int64_t kernel_launches = 0;
