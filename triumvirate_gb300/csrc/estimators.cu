@@ -1406,7 +1406,7 @@ struct Engine {
       const double* dlo = upload(tag + ".lo", lo);
       const double* dhi = upload(tag + ".hi", hi);
       launch_build_F<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo,
-                               dhi, nb, hmax, out);
+                               dhi, nb, hmax, out, disjoint(lo, hi));
     }
     cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, nb);
     ctx.kbegin("cufft.c2c.F");

@@ -224,7 +224,8 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const int K[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
-                    double hi_max, typename CplxOf<FR>::type* out);
+                    double hi_max, typename CplxOf<FR>::type* out,
+                    bool disjoint_bins = false);
 
 template <class Real, class FR>
 void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,

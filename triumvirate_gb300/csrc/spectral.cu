@@ -67,6 +67,55 @@ __device__ __forceinline__ cd field_value(const FieldSpec<Real>& f,
   return v;
 }
 
+// field_value for FP32 spectra without interlacing, in FP32.
+template <class Real>
+__device__ __forceinline__ float2 field_value_f(const FieldSpec<Real>& f,
+                                               const Geom& g, int i, int j,
+                                               int k) {
+  if (f.k0_set && i == 0 && j == 0 && k == 0)
+    return make_float2(float(f.k0.re), float(f.k0.im));
+  auto half = [&](const float2* h) {
+    if (k < g.nzh) return h[(int64_t(i) * g.n[1] + j) * g.nzh + k];
+    const int ii = (i == 0) ? 0 : g.n[0] - i;
+    const int jj = (j == 0) ? 0 : g.n[1] - j;
+    const float2 v = h[(int64_t(ii) * g.n[1] + jj) * g.nzh + (g.n[2] - k)];
+    return make_float2(v.x, -v.y);
+  };
+  float2 v = half(reinterpret_cast<const float2*>(f.re));
+  if (f.im != nullptr) {
+    const float2 b = half(reinterpret_cast<const float2*>(f.im));
+    v = make_float2(v.x - b.y, v.y + b.x);  // v + i b
+  }
+  return v;
+}
+
+// ylm_lean in FP32 (cnm = cnorm[|m|] of ylm_all_norms).
+__device__ __forceinline__ float2 ylm_lean_f(int ell, int m, float cnm,
+                                             float mu, float2 u) {
+  const int am = m < 0 ? -m : m;
+  float2 e = make_float2(1.f, 0.f);
+  for (int i = 0; i < am; ++i)
+    e = make_float2(e.x * u.x - e.y * u.y, e.x * u.y + e.y * u.x);
+  float q1 = 0.f, q = 1.f;
+  if (ell > am) {
+    q1 = 1.f;
+    q = float(2 * am + 1) * mu;
+    for (int l = am + 2; l <= ell; ++l) {
+      const float qn =
+          (float(2 * l - 1) * mu * q - float(l + am - 1) * q1) / float(l - am);
+      q1 = q;
+      q = qn;
+    }
+  }
+  const float c = cnm * q;
+  float2 v = make_float2(c * e.x, c * e.y);
+  if (m < 0) {
+    v.y = -v.y;
+    if (am & 1) v = make_float2(-v.x, -v.y);
+  }
+  return v;
+}
+
 // Shot-noise aliasing C_1(k) (field.cpp:3463-3509).
 __device__ __forceinline__ double alias_sn(const AxisTablesDev& ax, int i,
                                            int j, int k) {
@@ -181,10 +230,13 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
 template <class Real, class FR>
 __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
                                int K2, FieldSpec<Real> f, AxisTablesDev ax,
-                               int ell, int m, const double* lo,
+                               int ell, int m, float cnm, const double* lo,
                                const double* hi, int nb, double hi_max,
-                               typename CplxOf<FR>::type* out) {
+                               bool sparse, typename CplxOf<FR>::type* out) {
   using C = typename CplxOf<FR>::type;
+  // FP32 fields without interlacing: only |k| (shell membership) in FP64.
+  constexpr bool f32 = sizeof(FR) == 4 && sizeof(Real) == 4;
+  const bool fast = f32 && f.re_s == nullptr && ell <= kMaxYlmDegree;
   const uint32_t count = uint32_t(M0) * M1 * M2;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
        t += gridDim.x * blockDim.x) {
@@ -199,6 +251,7 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
                     (M2 == g.n[2] || abs(sz) <= K2);
     double k = -1.;
     cd val = {0., 0.};
+    float2 valf = make_float2(0.f, 0.f);
     if (in) {
       const double kx = dmul(double(sx), g.dk[0]);
       const double ky = dmul(double(sy), g.dk[1]);
@@ -207,17 +260,43 @@ __global__ void build_F_kernel(Geom g, int M0, int M1, int M2, int K0, int K1,
       if (k < hi_max) {
         const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
                   kk = wrap(sz, g.n[2]);
-        const cd v = field_value(f, g, i, j, kk);
-        const double w = window_pow(ax, i, j, kk);
-        const cd y = reduced_ylm(ell, m, kx, ky, kz);
-        val = y * cdivr(v, w);
+        if (fast) {
+          const float2 v = field_value_f(f, g, i, j, kk);
+          const float iw = 1.f / float(window_pow(ax, i, j, kk));
+          float2 y = make_float2(ell == 0 ? 1.f : 0.f, 0.f);
+          if (ell > 0 && k >= 1.e-9) {
+            const float ik = 1.f / float(k);
+            y = ylm_lean_f(ell, m, cnm, float(kz) * ik,
+                           make_float2(float(kx) * ik, -float(ky) * ik));
+          }
+          const float2 vw = make_float2(v.x * iw, v.y * iw);
+          valf = make_float2(y.x * vw.x - y.y * vw.y, y.x * vw.y + y.y * vw.x);
+        } else {
+          const cd v = field_value(f, g, i, j, kk);
+          const double w = window_pow(ax, i, j, kk);
+          const cd y = reduced_ylm(ell, m, kx, ky, kz);
+          val = y * cdivr(v, w);
+        }
       }
+    }
+    if (sparse) {
+      // Disjoint bins, output zeroed: only the bin holding k is written.
+      if (in && k < hi_max)
+        for (int q = 0; q < nb; ++q)
+          if (lo[q] <= k && k < hi[q]) {
+            C o;
+            o.x = fast ? FR(valf.x) : FR(val.re);
+            o.y = fast ? FR(valf.y) : FR(val.im);
+            out[int64_t(q) * count + t] = o;
+            break;
+          }
+      continue;
     }
     for (int q = 0; q < nb; ++q) {
       C o;
       const bool sel = in && (lo[q] <= k) && (k < hi[q]);
-      o.x = sel ? FR(val.re) : FR(0);
-      o.y = sel ? FR(val.im) : FR(0);
+      o.x = sel ? (fast ? FR(valf.x) : FR(val.re)) : FR(0);
+      o.y = sel ? (fast ? FR(valf.y) : FR(val.im)) : FR(0);
       out[int64_t(q) * count + t] = o;
     }
   }
@@ -967,14 +1046,25 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     const int K[3], const FieldSpec<Real>& f,
                     const AxisTablesDev& ax, int ell, int m,
                     const double* lo, const double* hi, int nb,
-                    double hi_max, typename CplxOf<FR>::type* out) {
+                    double hi_max, typename CplxOf<FR>::type* out,
+                    bool disjoint_bins) {
   const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  if (disjoint_bins)
+    TRVG_CUDA(cudaMemsetAsync(
+        out, 0, size_t(nb) * size_t(count) * sizeof(typename CplxOf<FR>::type),
+        ctx.stream));
   if (count >= (int64_t(1) << 32))
     throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  double cn[kMaxYlmDegree + 1] = {};
+  float cnm = 0.f;
+  if (ell <= kMaxYlmDegree) {
+    ylm_all_norms(ell, cn);
+    cnm = float(cn[std::abs(m)]);
+  }
   TRVG_KBEGIN(ctx, "build_F_kernel");
   build_F_kernel<Real, FR><<<grid_for(count, 256), 256, 0, ctx.stream>>>(
-      g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, lo, hi, nb,
-      hi_max, out);
+      g, M[0], M[1], M[2], K[0], K[1], K[2], f, ax, ell, m, cnm, lo, hi, nb,
+      hi_max, disjoint_bins, out);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -1240,7 +1330,7 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
   template void launch_build_F<R, F>(                                        \
       Context&, const Geom&, const int*, const int*, const FieldSpec<R>&,    \
       const AxisTablesDev&, int, int, const double*, const double*, int,     \
-      double, CplxOf<F>::type*);                                             \
+      double, CplxOf<F>::type*, bool);                                       \
   template void launch_build_F_sjl<R, F>(                                    \
       Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
       int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
