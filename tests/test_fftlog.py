@@ -94,3 +94,36 @@ def test_resampling(sampts, size, func, ndim):
             rs, rv = fn(sampts, samples, size=size)
             assert np.allclose(rv, func(*np.meshgrid(rs[0], rs[-1],
                                                      indexing='ij')))
+
+
+def test_extrap_loglin_oscil_matches_reference_goldens():
+    """Extrapolation option 5 against the reference's own outputs on its
+    branches: oscillating and monotonic tails, tails growing outwards
+    (constant padding with a DivergenceWarning), sign changes and zeros
+    (tests/golden/make_extrap_fixtures.py)."""
+    import warnings
+    from pathlib import Path
+
+    from triumvirate_gb300._arrayops import (DivergenceWarning,
+                                             extrap2d_loglin_oscil,
+                                             extrap_loglin_oscil)
+    d = np.load(Path(__file__).resolve().parent / "golden" /
+                "extrap_loglin_oscil.npz")
+    names = sorted({k.split("__")[0] for k in d.files})
+    assert len(names) == 8
+    for name in names:
+        with warnings.catch_warnings(record=True) as caught:
+            warnings.simplefilter("always")
+            got = extrap_loglin_oscil(d[name + "__in"], 16)
+        assert np.array_equal(got, d[name + "__out"]), name
+        if name == "growing_tails":
+            assert any(issubclass(w.category, DivergenceWarning)
+                       for w in caught)
+    # 2-d: rows, then columns.
+    a = np.outer(d["damped_oscillation__in"][:12], d["power_law__in"][:10])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        out = extrap2d_loglin_oscil(a, (3, 4))
+        rows = np.array([extrap_loglin_oscil(r, 4) for r in a])
+        ref = np.array([extrap_loglin_oscil(c, 3) for c in rows.T]).T
+    assert out.shape == (18, 18) and np.array_equal(out, ref)

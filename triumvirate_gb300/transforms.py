@@ -10,17 +10,18 @@ with the factors r^{3/2} before and (2 pi / k)^{3/2} after (so that
 Bessel transform, and (2 pi)^-3 i^l times it backwards).
 ``DoubleSphericalBesselTransform`` applies one along each axis of a 2-d
 array; every row (then every column) goes to the GPU in one batched call.
-Extrapolation options 1-4 are supported ('outer' layer: the samples are
-extended before the pre-factors, 'native': inside the FFTLog plan).
+Extrapolation options 1-5 are supported ('outer' layer: the samples are
+extended before the pre-factors, 'native': inside the FFTLog plan, options
+1-4).
 """
 from collections.abc import Sequence
 
 import numpy as np
 from scipy.interpolate import InterpolatedUnivariateSpline, RectBivariateSpline
 
-from ._arrayops import (extrap2d_lin, extrap2d_loglin, extrap2d_pad,
-                        extrap_lin, extrap_loglin, extrap_loglin_oscil,
-                        extrap_pad)
+from ._arrayops import (extrap2d_lin, extrap2d_loglin, extrap2d_loglin_oscil,
+                        extrap2d_pad, extrap_lin, extrap_loglin,
+                        extrap_loglin_oscil, extrap_pad)
 from ._fftlog import HankelTransform
 
 
@@ -183,7 +184,7 @@ class DoubleSphericalBesselTransform:
         if self._extrap == 4:
             return extrap2d_loglin(arr, self._n_ext)
         if self._extrap == 5:
-            return extrap_loglin_oscil(arr, self._n_ext)
+            return extrap2d_loglin_oscil(arr, self._n_ext)
         return np.asarray(arr)
 
     def _axis(self, t, rows):
