@@ -271,3 +271,38 @@ def test_batch_of_device_catalogues_matches_host_batch():
         assert np.array_equal(a['nmodes_1'], b['nmodes_1'])
         for k in ('bk_raw', 'bk_shot'):
             assert rel_err(a[k], b[k]) < 1e-10, k
+
+
+def test_device_catalogues_in_3pcf_window_and_powspec(rand_catalogue_array):
+    """The 3PCF window (randoms alone), the periodic-box power spectrum and
+    the survey 3PCF from device catalogues equal those from host ones."""
+    from triumvirate_gb300.threept import compute_3pcf, compute_3pcf_window
+    from triumvirate_gb300.twopt import compute_powspec_in_gpp_box
+    r = rand_catalogue_array
+    rng = np.random.default_rng(5)
+    d = rng.uniform(-500., 500., size=(3000, 3))
+    rb = Binning('config', 'lin', 50., 150., 4)
+    kb = Binning('fourier', 'lin', *KBINS)
+    samp = _sampling('fp64')
+
+    def rc(device):
+        cls = DeviceCatalogue if device else ParticleCatalogue
+        return cls(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3])
+
+    def dc(device):
+        cls = DeviceCatalogue if device else ParticleCatalogue
+        return cls(*d.T, nz=3e-9)
+    for device in (False, True):
+        w = compute_3pcf_window(rc(device), degrees=(2, 0, 2), binning=rb,
+                                form='diag', sampling_params=samp)
+        p = compute_powspec_in_gpp_box(dc(device), degree=2, binning=kb,
+                                       sampling_params=samp)
+        z = compute_3pcf(dc(device), rc(device), degrees=(0, 0, 0),
+                         binning=rb, form='diag', sampling_params=samp)
+        if not device:
+            ref = (w, p, z)
+    for got, want, keys in [(w, ref[0], ('zeta_raw', 'zeta_shot')),
+                            (p, ref[1], ('pk_raw', 'pk_shot')),
+                            (z, ref[2], ('zeta_raw', 'zeta_shot'))]:
+        for k in keys:
+            assert rel_err(got[k], want[k]) < 1e-12, k
