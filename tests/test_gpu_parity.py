@@ -727,12 +727,15 @@ def _with_assign_path(ctx, path, fn):
 
 @pytest.mark.parametrize("assignment", ['ngp', 'cic', 'tsc', 'pcs'])
 @pytest.mark.parametrize("box, ngrid", [(500., [64, 64, 64]),
+                                        ([450., 600., 520.], [70, 96, 68]),
                                         ([450., 600., 520.], [70, 96, 65])])
 def test_tiled_assignment_matches_oracle(assignment, box, ngrid):
     """Sorted catalogues (>= 65536 particles) of an FP32 mesh deposit tile
     by tile through shared memory; particles on cell edges, half cells and
-    the box edge take the deferred exact path.  Partial tiles (70, 96, 65
-    cells) and every stencil order are covered."""
+    the box edge take the deferred exact path.  Partial tiles in x and z
+    (70, 96, 68 cells) and every stencil order are covered; with 65 cells
+    along z the rows are not 16-byte aligned and the atomic deposit is
+    used instead."""
     boxv = np.array([box] * 3 if np.isscalar(box) else box, dtype=float)
     n = 70000
     rng = np.random.default_rng(17)
