@@ -12,8 +12,13 @@ Lines printed by rank 0 (one JSON object):
   e2e    -- the same through the C ABI with pinned host particle arrays,
             host->device copies inside the timed region;
   fp64   -- the FP64 path on the same inputs, its time and the FP32-mixed
-            error against it;
+            per-bin error against it;
+  b202_diag -- B_202 diag on the same catalogue (FP32-mixed and FP64);
+  oracle_check -- the FP32-mixed and FP64 estimates against the CPU
+            oracle's own values of two bins at the full workload size;
+  cold_first_call_s -- the first estimate of a fresh context;
   roofline, cpu_baseline, clocks, gpu_launches.
+Step times are the median of the timed steps.
 ``--impl reference`` times the CPU oracle (a numpy restatement of the
 reference algorithm) on the host cores instead.
 """
@@ -52,6 +57,8 @@ def parse_args():
     ap.add_argument('--nbins', type=int, default=20)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--no-b202', action='store_true',
+                    help='skip the B_202 diag timing and error')
     ap.add_argument('--profile-only', action='store_true',
                     help='run two estimates (for an ncu launch list)')
     ap.add_argument('--variants', action='store_true',
@@ -289,11 +296,11 @@ def run_gb300(args):
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
 
-    def params(precision):
+    def params(precision, degrees=(0, 0, 0)):
         pd = {'boxsize': {'x': box, 'y': box, 'z': box},
               'ngrid': {'x': N, 'y': N, 'z': N}, 'assignment_order': 3,
               'interlace': False,
-              'degrees': {'ell1': 0, 'ell2': 0, 'ELL': 0},
+              'degrees': dict(zip(('ell1', 'ell2', 'ELL'), degrees)),
               'form': 'diag', 'shape': 'diag', 'precision': precision,
               'verbose': 0}
         return _engine.make_params(pd, '3pt')
@@ -362,29 +369,45 @@ def run_gb300(args):
     nprof = 2
     _, _, ktimes, _, _ = timed(p32, dcat, nprof, profile=True)
 
-    # Max over ranks of the summed device time.
+    # Median step time per rank, then the maximum over ranks; the ranks
+    # run their estimates side by side, so the job finishes `world`
+    # estimates per such step.
+    med_s = statistics.median(ms) / 1e3
+    med_e2e = statistics.median(ms_e2e) / 1e3
     total_s = sum(ms) / 1e3
-    total_e2e = sum(ms_e2e) / 1e3
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([total_s, total_e2e], device=dev, dtype=torch.float64)
+        t = torch.tensor([med_s, med_e2e, total_s], device=dev,
+                         dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s, total_e2e = float(t[0]), float(t[1])
-    value = total_s / (args.steps * world)
-    value_e2e = total_e2e / (args.steps * world)
+        med_s, med_e2e, total_s = float(t[0]), float(t[1]), float(t[2])
+    value = med_s / world
+    value_e2e = med_e2e / world
+
+    # First estimate of a fresh context: FFT plans, autotuning trials,
+    # spline / shell / statistics tables and workspace (the process has
+    # already initialised CUDA and loaded the library).
+    cold = _lib.Context(local)
+    cold.set_option('assign_path', args.assign_path)
+    cold.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    _engine.call_threept('trvg_compute_bispec_in_gpp_box', cold, p32, dcat,
+                         binning, norm, 'bispec', shape='diag')
+    torch.cuda.synchronize(dev)
+    cold_first_call_s = time.perf_counter() - t0
+    del cold
 
     fp64 = None
+    res64 = None
     if not args.no_fp64:
         estimate(p64, dcat)
         n64 = max(1, min(args.steps, 3))
         ms64, _, _, res64, _ = timed(p64, dcat, n64)
-        err = {}
-        for key in ('bk_raw', 'bk_shot'):
-            a, b = res32[key], res64[key]
-            err[key] = float(np.max(np.abs(a - b) / np.abs(b)))
-        fp64 = {"s_per_estimate": sum(ms64) / 1e3 / n64,
-                "fp32mixed_speedup": (sum(ms64) / n64) / (sum(ms) / len(ms)),
-                "max_rel_err_fp32mixed": err,
+        fp64 = {"s_per_estimate": statistics.median(ms64) / 1e3,
+                "fp32mixed_speedup": statistics.median(ms64) /
+                statistics.median(ms),
+                "max_rel_err_fp32mixed": per_bin_err(res32, res64),
                 "nmodes_equal": bool(np.array_equal(res32['nmodes_1'],
                                                     res64['nmodes_1']))}
         ctx.set_option('full_mesh_shells', 1)
@@ -392,7 +415,8 @@ def run_gb300(args):
             estimate(p64, dcat)
             msd, _, _, resd, _ = timed(p64, dcat, 1)
             fp64["plain_full_mesh_s_per_estimate"] = sum(msd) / 1e3
-            fp64["fp32mixed_speedup_vs_plain"] = sum(msd) / (sum(ms) / len(ms))
+            fp64["fp32mixed_speedup_vs_plain"] = sum(msd) / \
+                statistics.median(ms)
             fp64["plain_vs_pruned_max_rel"] = float(max(
                 np.max(np.abs(resd[k] - res64[k]) / np.abs(res64[k]))
                 for k in ('bk_raw', 'bk_shot')))
@@ -401,6 +425,24 @@ def run_gb300(args):
             fp64["plain_error"] = str(e)[:200]
         finally:
             ctx.set_option('full_mesh_shells', 0)
+
+    # B_202 diag on the same catalogue: FP32-mixed and FP64 (pruned).
+    b202 = None
+    if not args.no_b202:
+        q32, q64 = params('fp32mixed', (2, 0, 2)), params('fp64', (2, 0, 2))
+        estimate(q32, dcat)
+        ms2, _, _, r2_32, _ = timed(q32, dcat, max(1, min(args.steps, 5)))
+        b202 = {"s_per_estimate": round(statistics.median(ms2) / 1e3, 6)}
+        if not args.no_fp64:
+            estimate(q64, dcat)
+            ms2d, _, _, r2_64, _ = timed(q64, dcat, 1)
+            b202.update({
+                "fp64_s_per_estimate": round(sum(ms2d) / 1e3, 6),
+                "fp32mixed_speedup": round(sum(ms2d) /
+                                           statistics.median(ms2), 2),
+                "max_rel_err_fp32mixed": per_bin_err(r2_32, r2_64),
+                "nmodes_equal": bool(np.array_equal(r2_32['nmodes_1'],
+                                                    r2_64['nmodes_1']))})
 
     variants = None
     if args.variants and fp64 is not None:
@@ -454,7 +496,10 @@ def run_gb300(args):
     line = {
         "metric": METRIC, "value": round(value, 6), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * total_s / args.steps, 3),
+        "ms_per_step": round(1e3 * med_s, 3),
+        "step_statistic": "median of the timed steps, max over ranks",
+        "mean_ms_per_step": round(1e3 * total_s / args.steps, 3),
+        "cold_first_call_s": round(cold_first_call_s, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 meshes/FFTs, f64 offsets/Ylm/reductions/shot noise",
         "data": "synthetic (seeded uniform catalogue)",
@@ -471,11 +516,13 @@ def run_gb300(args):
         # of ms_per_step is host work between launches.
         "kernel_ms_per_estimate": round(kernel_ms, 3),
         "fp64": fp64,
+        "b202_diag": b202,
         "precision_variants": variants,
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args)
+        line["cpu_baseline"], line["oracle_check"] = cpu_baseline(
+            args, norm, res32, res64)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -483,25 +530,52 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(args, pair_steps=1):
+def per_bin_err(a, b):
+    """Largest per-bin relative error |a - b| / |b| (complex modulus) of
+    bk_raw and bk_shot."""
+    return {k: float(np.max(np.abs(a[k] - b[k]) / np.abs(b[k])))
+            for k in ('bk_raw', 'bk_shot')}
+
+
+def cpu_baseline(args, norm, res32, res64=None):
     """The CPU oracle on a bounded sample of the workload: the mesh set-up
-    once plus `pair_steps` bin pairs, extrapolated to the whole estimate."""
+    once plus two bin pairs (the lowest bin and the middle one), the
+    median pair time extrapolated to the whole estimate.  The two pairs'
+    normalised values are the oracle's own at the full workload size, so
+    the GPU estimates are checked against them per bin."""
     from oracle.sample import GppBispecSample
     s = GppBispecSample(args.npart, args.boxsize, args.ngrid, args.nbins)
     t0 = time.perf_counter()
     s.setup()
     t_setup = time.perf_counter() - t0
-    tp = []
-    for i in range(pair_steps):
+    bins = [0, args.nbins // 2]
+    tp, check = [], {"bins": bins, "nmodes_equal": True,
+                     "rel_err_fp32mixed": {"bk_raw": [], "bk_shot": []},
+                     "rel_err_fp64": {"bk_raw": [], "bk_shot": []}}
+    for b in bins:
         t0 = time.perf_counter()
-        s.pair(args.nbins // 2 + i)
+        s.pair(b)
         tp.append(time.perf_counter() - t0)
+        raw, shot, nm = s.entry(b, norm)
+        check["nmodes_equal"] &= bool(nm == res32['nmodes_1'][b])
+        for name, res in (("rel_err_fp32mixed", res32), ("rel_err_fp64",
+                                                         res64)):
+            if res is None:
+                continue
+            for k, ref in (('bk_raw', raw), ('bk_shot', shot)):
+                check[name][k].append(float(abs(res[k][b] - ref) / abs(ref)))
+    if res64 is None:
+        del check["rel_err_fp64"]
+    check["max_rel_err_fp32mixed"] = max(
+        max(v) for v in check["rel_err_fp32mixed"].values())
     t_pair = statistics.median(tp)
-    return {"value": round(t_setup + args.nbins * t_pair, 3), "unit": UNIT,
+    base = {"value": round(t_setup + args.nbins * t_pair, 3), "unit": UNIT,
             "cores": s.threads, "kind": "port",
             "sample": (f"oracle set-up ({t_setup:.1f} s: assignment, "
-                       f"forward FFTs, G) + {pair_steps} of {args.nbins} bin "
-                       f"pairs ({t_pair:.1f} s each), extrapolated")}
+                       f"forward FFTs, G, two-point statistics) + "
+                       f"{len(bins)} of {args.nbins} bin pairs "
+                       f"({t_pair:.1f} s median), extrapolated")}
+    return base, check
 
 
 def run_reference(args):
@@ -520,14 +594,14 @@ def run_reference(args):
         t0 = time.perf_counter()
         s.pair((args.warmup + i) % args.nbins)
         tp.append(time.perf_counter() - t0)
-    value = t_setup + args.nbins * statistics.mean(tp)
+    value = t_setup + args.nbins * statistics.median(tp)
     sample = (f"oracle (numpy restatement of threept.cpp:1473-2188) set-up "
-              f"{t_setup:.1f} s once + mean of {args.steps} bin pairs "
-              f"({statistics.mean(tp):.1f} s) x {args.nbins}")
+              f"{t_setup:.1f} s once + median of {args.steps} bin pairs "
+              f"({statistics.median(tp):.1f} s) x {args.nbins}")
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * statistics.mean(tp), 1),
+        "ms_per_step": round(1e3 * statistics.median(tp), 1),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded uniform catalogue)",
         "config": {**workload(args), "parallelism": "cpu"},

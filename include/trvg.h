@@ -455,8 +455,11 @@ int trvg_calc_grid_based_powlaw_norm(
  *    entry;
  *  - the scratch is one per device: overlapping calls on one device race
  *    and must be serialised by the caller;
- *  - the first call on a device looks up the scratch address on that
- *    device; make it before any stream capture. */
+ *  - the call synchronises `stream` to read its result back, so it must
+ *    not be made while `stream` (or, in global capture mode, any stream)
+ *    is being captured;
+ *  - the first call on a device also looks up the scratch address on
+ *    that device (a one-off host-side step). */
 int trvg_calc_grid_based_powlaw_norm_noalloc(
   const trvg_params* params, const trvg_catalogue* particles, int order,
   void* stream, double* norm_factor);

@@ -11,6 +11,11 @@ repeats for every pair:
 * pair: two band-limited inverse FFTs, the triple-product reduction, the
   shot-noise inverse FFT and its spline-weighted reduction
   (threept.cpp:1675-1723, 2126-2140).
+
+The set-up also forms the fine-binned two-point statistics of the
+single-leg shot-noise terms (threept.cpp:1974-2060), so that ``entry``
+returns the oracle's normalised bk_raw, bk_shot and mode count of one
+diagonal bin: the check of the GPU estimate at the full workload size.
 """
 from __future__ import annotations
 
@@ -46,6 +51,13 @@ class GppBispecSample:
         self.rmag = O.vec3_mag(*O.grid_positions(p))
         self.ones = np.ones(self.kmag.shape, dtype=np.complex128)
         self.sj = O.SphericalBessel(0)
+        # Single-leg shot-noise terms S_i_jk = S_ik_j (ell1 = ell2 = 0).
+        win_pk = self.alias
+        st = O.twopt_stats_in_fourier(
+            self.dn_k, self.N_k, complex(float(self.npart)), 0, 0,
+            self.edges, self.centres, p, O.grid_wavevectors(p), self.kmag,
+            win_pk, self.alias)
+        self.S_leg = st['pk'] - st['sn']
 
     def pair(self, b):
         p = self.p
@@ -60,4 +72,16 @@ class GppBispecSample:
                            self.alias, self.alias)
         s = O.shotnoise_bispec_per_bin(xi, 1., 1., self.sj, self.sj,
                                        self.rmag, keff, keff, p)
+        self.last = (b, comp, s, nm)
         return comp, s
+
+    def entry(self, b, norm):
+        """bk_raw, bk_shot and nmodes of diagonal entry (b, b) of B_000
+        (coupling 1, no mirror term; threept.cpp:1703-1723, 1974-2140),
+        from the last ``pair(b)``."""
+        if getattr(self, 'last', (None,))[0] != b:
+            self.pair(b)
+        _, comp, s, nm = self.last
+        raw = norm * self.p.vol_cell * comp
+        shot = norm * (complex(float(self.npart)) + 2. * self.S_leg[b] + s)
+        return raw, shot, nm

@@ -10,6 +10,7 @@ Usage::
 
     python tests/golden/make_extrap_fixtures.py [REFERENCE_ROOT]
 """
+import os
 import importlib.util
 import sys
 import warnings
@@ -36,7 +37,12 @@ def inputs():
     return cases
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("TRIUMVIRATE_REFERENCE")
+    if not ref_root:
+        sys.exit("usage: python %s REFERENCE_ROOT "
+                 "(or set TRIUMVIRATE_REFERENCE to the reference checkout)"
+                 % Path(__file__).name)
     path = Path(ref_root) / "src" / "triumvirate" / "_arrayops.py"
     spec = importlib.util.spec_from_file_location("ref_arrayops", path)
     ref = importlib.util.module_from_spec(spec)

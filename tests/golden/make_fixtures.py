@@ -18,6 +18,7 @@ Usage::
 
     python tests/golden/make_fixtures.py [REFERENCE_ROOT]
 """
+import os
 import shutil
 import sys
 from pathlib import Path
@@ -40,7 +41,12 @@ FILES = [
 ]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("TRIUMVIRATE_REFERENCE")
+    if not ref_root:
+        sys.exit("usage: python %s REFERENCE_ROOT "
+                 "(or set TRIUMVIRATE_REFERENCE to the reference checkout)"
+                 % Path(__file__).name)
     src = Path(ref_root) / "tests" / "test_input"
     dst = Path(__file__).resolve().parent
     for rel in FILES:

@@ -162,3 +162,22 @@ def test_oracle_wide_angle_kernel():
     far = r > 0
     assert np.allclose(out[far], g[far] / r[far] ** 2)
     assert np.array_equal(O.wide_angle_pow_law(g, r, 0, 0), g)
+
+
+def test_bench_sample_entries_match_oracle_estimate():
+    """The bench's bounded oracle sample (set-up + one bin pair) gives the
+    same normalised diagonal entries as the oracle's whole B_000 estimate;
+    it is the oracle check of the GPU estimate at the full workload size."""
+    from oracle.sample import GppBispecSample
+    npart, box, ngrid, nbins = 3000, 1000., 64, 20
+    s = GppBispecSample(npart, box, ngrid, nbins, seed=5)
+    s.setup()
+    norm = O.bispec_norm_from_particles(np.full(npart, npart / box ** 3),
+                                        1., 1.)
+    p = O.Params(box, ngrid, 'tsc', False, 0, 0, 0, form='diag')
+    ref = O.compute_bispec_in_gpp_box(s.pos, p, s.edges, s.centres, norm)
+    for b in (0, nbins // 2):
+        raw, shot, nm = s.entry(b, norm)
+        assert nm == ref['nmodes_1'][b]
+        assert abs(raw - ref['bk_raw'][b]) <= 1e-12 * abs(ref['bk_raw'][b])
+        assert abs(shot - ref['bk_shot'][b]) <= 1e-12 * abs(ref['bk_shot'][b])

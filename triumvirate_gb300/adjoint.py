@@ -129,6 +129,7 @@ def bispec_gpp(positions, weights, cfg):
             pos, wts = ctx.saved_tensors
             g = bispec_gpp_adjoint(pos, wts, grad_out.detach().cpu().numpy(),
                                    cfg)
-            return g['grad_pos'], g['grad_w']
+            # No gradient flows to an absent weight column.
+            return g['grad_pos'], (g['grad_w'] if wts is not None else None)
 
     return _Bispec.apply(positions, weights)

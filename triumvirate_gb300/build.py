@@ -4,6 +4,11 @@ Each ``csrc/*.cu`` file is compiled by nvcc in parallel and linked into
 ``triumvirate_gb300/libtrvg.so`` in the source tree.  Host code is compiled
 with ``-ffp-contract=off`` so that wavevector magnitudes and bin edges round
 exactly as in the reference on every host architecture.
+
+Then the C++ drop-in layer (``csrc/dropin/trv_dropin.cpp``, the reference's
+``trv::`` estimator interface over the C ABI) is compiled by the host C++
+compiler into ``triumvirate_gb300/libtrv_dropin.so``, and the C++ test
+program ``tests/cpp/dropin_bispec_gpp.cpp`` into ``_build/``.
 """
 from __future__ import annotations
 
@@ -20,6 +25,10 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libtrvg.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+DROPIN_SRC = CSRC / "dropin" / "trv_dropin.cpp"
+DROPIN_LIB = PKG / "libtrv_dropin.so"
+DROPIN_TEST_SRC = ROOT / "tests" / "cpp" / "dropin_bispec_gpp.cpp"
+DROPIN_TEST = BUILD / "dropin_bispec_gpp"
 
 
 def _nvcc():
@@ -88,7 +97,44 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_dropin(force=force)
     return LIB
+
+
+def _cxx():
+    return os.environ.get("CXX") or shutil.which("g++") or "c++"
+
+
+def _run(cmd, what):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{what} failed:\n{r.stderr}")
+
+
+def build_dropin(force: bool = False) -> Path:
+    """The C++ drop-in library and its test program (host C++ only)."""
+    cxx = _cxx()
+    inc = [f"-I{ROOT / 'include'}"]
+    newest = max(LIB.stat().st_mtime, DROPIN_SRC.stat().st_mtime,
+                 (ROOT / "include" / "trv_dropin.hpp").stat().st_mtime,
+                 (ROOT / "include" / "trvg.h").stat().st_mtime)
+    if force or not DROPIN_LIB.exists() or \
+            DROPIN_LIB.stat().st_mtime < newest:
+        tmp = DROPIN_LIB.with_suffix(".so.tmp")
+        _run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared",
+              "-ffp-contract=off", *inc, str(DROPIN_SRC), "-o", str(tmp),
+              f"-L{PKG}", "-ltrvg", "-Wl,-rpath,$ORIGIN"],
+             "drop-in library build")
+        os.replace(tmp, DROPIN_LIB)
+    BUILD.mkdir(exist_ok=True)
+    if force or not DROPIN_TEST.exists() or \
+            DROPIN_TEST.stat().st_mtime < max(
+                DROPIN_LIB.stat().st_mtime,
+                DROPIN_TEST_SRC.stat().st_mtime):
+        _run([cxx, "-std=c++17", "-O2", *inc, str(DROPIN_TEST_SRC), "-o",
+              str(DROPIN_TEST), f"-L{PKG}", "-ltrv_dropin", "-ltrvg",
+              f"-Wl,-rpath,{PKG}"], "drop-in test program build")
+    return DROPIN_LIB
 
 
 if __name__ == "__main__":

@@ -19,9 +19,12 @@
 //  - one scratch array per device: calls that overlap on one device (from
 //    different host threads, or on different streams before the previous
 //    call returned) race on it and must be serialised by the caller;
+//  - the call reads its result back and synchronises `stream`, so it must
+//    not be made while `stream` (or, in global capture mode, any stream)
+//    is being captured;
 //  - the first call on a device looks up the scratch address on that
-//    device (the one current on the calling thread), so it should be made
-//    before any stream capture.
+//    device (the one current on the calling thread) with
+//    cudaGetSymbolAddress, a one-off host-side step.
 #include <cmath>
 #include <mutex>
 
@@ -150,6 +153,12 @@ int trvg_calc_grid_based_powlaw_norm_noalloc(const trvg_params* params,
   launch_assign<double>(ctx, g, params->assignment_order, false, cat,
                         WeightSpec(), mesh, nullptr, nullptr, nullptr, sums);
   launch_mesh_sum_pow<double>(ctx, mesh, g.nmesh, order, acc);
+  // The launch helpers take their scratch from a context's workspace when
+  // a path needs one; none may have been drawn here.
+  if (!ctx.buffers.empty())
+    throw_error(TRVG_ERR_ALLOC,
+                "The allocation-free normalisation drew %zu workspace "
+                "buffers.", ctx.buffers.size());
   double s = 0.;
   TRVG_CUDA(cudaMemcpyAsync(&s, acc, sizeof(double), cudaMemcpyDeviceToHost,
                             ctx.stream));

@@ -68,6 +68,25 @@ def _boxsize(paramset):
     return [float(paramset['boxsize'][ax]) for ax in ['x', 'y', 'z']]
 
 
+def _log(logger, msg, *args):
+    """Progress message at the reference's 'stat' level where the logger
+    has one (the library's own logger, logger.py), else at INFO
+    (threept.py:490-738 log the same stages)."""
+    if logger is None:
+        return
+    fn = getattr(logger, 'stat', None) or logger.info
+    fn(msg, *args)
+
+
+_STAT_NAMES = {'bispec': 'bispectrum', '3pcf': 'three-point correlation '
+               'function', 'powspec': 'power spectrum'}
+
+
+def _log_norm(logger, paramset, norm):
+    _log(logger, "Normalisation factor: %.6e (%s; used).", norm,
+         paramset['norm_convention'])
+
+
 def _has_nz(catalogue):
     """Whether any particle has a nonzero 'nz' (summed on the device for a
     DeviceCatalogue)."""
@@ -135,17 +154,22 @@ def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
         paramset=paramset, params_sampling=params_sampling, degrees=degrees,
         binning=binning, form=form, idx_bin=idx_bin,
         catalogue_type='sim', statistic_type=stat)
+    _log(logger, "Parameter set have been initialised.")
     if binning is None:
         binning = Binning.from_parameter_set(paramset)
+    _log(logger, "Binning has been initialised.")
     if None in paramset['boxsize'].values():
         paramset['boxsize'] = {
             ax: (catalogue_data.bounds[ax][1] - catalogue_data.bounds[ax][0])
             * paramset['expand'] for ax in ['x', 'y', 'z']}
+        _log(logger, "Box size is set to [%.3f, %.3f, %.3f].",
+             *_boxsize(paramset))
     if None in paramset['ngrid'].values():
         pd = _as_dict(paramset)
         _set_ngrid_from_cutoff(pd)
         paramset['ngrid'] = pd['ngrid']
     catalogue_data.periodise(_boxsize(paramset))
+    _log(logger, "Catalogue box has been periodised.")
     if not _has_nz(catalogue_data):
         catalogue_data.compute_mean_density(boxsize=_boxsize(paramset))
 
@@ -154,14 +178,20 @@ def _compute_3pt_stats_sim_like(kind, catalogue_data, paramset=None,
     cat = _engine.catalogue_arg(catalogue_data)
     norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data, 1.,
                         3)
+    _log_norm(logger, paramset, norm)
     fn = ('trvg_compute_bispec_in_gpp_box' if kind == 'bispec'
           else 'trvg_compute_3pcf_in_gpp_box')
+    _log(logger, "Measuring %s from a catalogue in a periodic box in the "
+         "global plane-parallel approximation...", _STAT_NAMES[stat])
     results = _engine.call_threept(
         fn, ctx, params_c, cat.c, binning, norm, kind,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
+    _log(logger, "... measured %s from a catalogue in a periodic box in "
+         "the global plane-parallel approximation.", _STAT_NAMES[stat])
     if save:
-        _save(results, paramset, save, ctx, params_c, cat.c, catalogue_data,
-              1., 3, catalogue_data)
+        path = _save(results, paramset, save, ctx, params_c, cat.c,
+                     catalogue_data, 1., 3, catalogue_data)
+        _log(logger, "Measurements saved to %s.", path)
     return results
 
 
@@ -177,12 +207,15 @@ def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
         paramset=paramset, params_sampling=params_sampling, degrees=degrees,
         binning=binning, form=form, idx_bin=idx_bin,
         catalogue_type='survey', statistic_type=stat)
+    _log(logger, "Parameter set have been initialised.")
     if binning is None:
         binning = Binning.from_parameter_set(paramset)
+    _log(logger, "Binning has been initialised.")
     if los_data is None:
         los_data = catalogue_data.compute_los()
     if los_rand is None:
         los_rand = catalogue_rand.compute_los()
+    _log(logger, "Lines of sight have been initialised.")
     if None in paramset['boxsize'].values():
         paramset['boxsize'] = {
             ax: (catalogue_rand.bounds[ax][1] - catalogue_rand.bounds[ax][0])
@@ -201,21 +234,29 @@ def _compute_3pt_stats_survey_like(kind, catalogue_data, catalogue_rand,
                   'ngrid_pad': paramset['padfactor']}
         catalogue_data.pad(_boxsize(paramset), catalogue_ref=catalogue_rand,
                            **kw)
+    _log(logger, "Catalogues have been aligned.")
     ctx = _engine.context_for(device, catalogue_data, catalogue_rand)
     params_c = _engine.make_params(paramset, '3pt')
     alpha = catalogue_data.wstotal / catalogue_rand.wstotal
+    _log(logger, "Alpha contrast: %.6e.", alpha)
     dcat = _engine.catalogue_arg(catalogue_data, los_data, with_los=True)
     rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
     norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand,
                         alpha, 3)
+    _log_norm(logger, paramset, norm)
     fn = 'trvg_compute_bispec' if kind == 'bispec' else 'trvg_compute_3pcf'
+    _log(logger, "Measuring %s from paired survey-type catalogues in the "
+         "local plane-parallel approximation...", _STAT_NAMES[stat])
     results = _engine.call_threept(
         fn, ctx, params_c, dcat.c, binning, norm, kind, rand_c=rcat.c,
         alpha=alpha, shape=paramset['shape'],
         idx_bin=paramset.get('idx_bin') or 0)
+    _log(logger, "... measured %s from paired survey-type catalogues in "
+         "the local plane-parallel approximation.", _STAT_NAMES[stat])
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
-              alpha, 3, catalogue_data, catalogue_rand)
+        path = _save(results, paramset, save, ctx, params_c, rcat.c,
+                     catalogue_rand, alpha, 3, catalogue_data, catalogue_rand)
+        _log(logger, "Measurements saved to %s.", path)
     return results
 
 
@@ -261,23 +302,33 @@ def compute_3pcf_window(catalogue_rand, los_rand=None, degrees=None,
         paramset=paramset, params_sampling=sampling_params, degrees=degrees,
         wa_orders=wa_orders, binning=binning, form=form, idx_bin=idx_bin,
         catalogue_type='random', statistic_type='3pcf-win')
+    _log(logger, "Parameter set have been initialised.")
     if binning is None:
         binning = Binning.from_parameter_set(paramset)
+    _log(logger, "Binning has been initialised.")
     if los_rand is None:
         los_rand = catalogue_rand.compute_los()
+    _log(logger, "Lines of sight have been initialised.")
     catalogue_rand.centre(_boxsize(paramset))
     catalogue_rand.periodise(_boxsize(paramset))
+    _log(logger, "Catalogue box has been periodised.")
     ctx = _engine.context_for(device, catalogue_rand)
     params_c = _engine.make_params(paramset, '3pt')
     rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
     norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand, 1.,
                         3)
+    _log_norm(logger, paramset, norm)
+    _log(logger, "Measuring three-point correlation function window from "
+         "a random catalogue...")
     results = _engine.call_3pcf_window(
         ctx, params_c, rcat.c, binning, norm, 1., wide_angle,
         shape=paramset['shape'], idx_bin=paramset.get('idx_bin') or 0)
+    _log(logger, "... measured three-point correlation function window "
+         "from a random catalogue.")
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
-              1., 3, catalogue_rand)
+        path = _save(results, paramset, save, ctx, params_c, rcat.c,
+                     catalogue_rand, 1., 3, catalogue_rand)
+        _log(logger, "Measurements saved to %s.", path)
     return results
 
 

@@ -6,8 +6,8 @@ from __future__ import annotations
 from . import _engine
 from .dataobjs import Binning
 from .parameters import _as_dict, _set_ngrid_from_cutoff
-from .threept import (_amalgamate_parameters, _boxsize, _has_nz,
-                      _norm_factor, _save)
+from .threept import (_amalgamate_parameters, _boxsize, _has_nz, _log,
+                      _log_norm, _norm_factor, _save)
 
 
 def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
@@ -31,6 +31,7 @@ def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
         _set_ngrid_from_cutoff(pd)
         paramset['ngrid'] = pd['ngrid']
     catalogue_data.periodise(_boxsize(paramset))
+    _log(logger, "Catalogue box has been periodised.")
     if not _has_nz(catalogue_data):
         catalogue_data.compute_mean_density(boxsize=_boxsize(paramset))
     ctx = _engine.context_for(device, catalogue_data)
@@ -38,11 +39,17 @@ def compute_powspec_in_gpp_box(catalogue_data, degree=None, binning=None,
     cat = _engine.catalogue_arg(catalogue_data)
     norm = _norm_factor(paramset, ctx, params_c, cat.c, catalogue_data, 1.,
                         2)
+    _log_norm(logger, paramset, norm)
+    _log(logger, "Measuring power spectrum from a catalogue in a periodic "
+         "box in the global plane-parallel approximation...")
     results = _engine.call_powspec('trvg_compute_powspec_in_gpp_box', ctx,
                                    params_c, cat.c, binning, norm)
+    _log(logger, "... measured power spectrum from a catalogue in a "
+         "periodic box in the global plane-parallel approximation.")
     if save:
-        _save(results, paramset, save, ctx, params_c, cat.c, catalogue_data,
-              1., 2, catalogue_data)
+        path = _save(results, paramset, save, ctx, params_c, cat.c,
+                     catalogue_data, 1., 2, catalogue_data)
+        _log(logger, "Measurements saved to %s.", path)
     return results
 
 
@@ -81,17 +88,25 @@ def compute_powspec(catalogue_data, catalogue_rand, los_data=None,
                   'ngrid_pad': paramset['padfactor']}
         catalogue_data.pad(_boxsize(paramset), catalogue_ref=catalogue_rand,
                            **kw)
+    _log(logger, "Catalogues have been aligned.")
     ctx = _engine.context_for(device, catalogue_data, catalogue_rand)
     params_c = _engine.make_params(paramset, '2pt')
     alpha = catalogue_data.wstotal / catalogue_rand.wstotal
+    _log(logger, "Alpha contrast: %.6e.", alpha)
     dcat = _engine.catalogue_arg(catalogue_data, los_data, with_los=True)
     rcat = _engine.catalogue_arg(catalogue_rand, los_rand, with_los=True)
     norm = _norm_factor(paramset, ctx, params_c, rcat.c, catalogue_rand,
                         alpha, 2)
+    _log_norm(logger, paramset, norm)
+    _log(logger, "Measuring power spectrum from paired survey-type "
+         "catalogues in the local plane-parallel approximation...")
     results = _engine.call_powspec('trvg_compute_powspec', ctx, params_c,
                                    dcat.c, binning, norm, rand_c=rcat.c,
                                    alpha=alpha)
+    _log(logger, "... measured power spectrum from paired survey-type "
+         "catalogues in the local plane-parallel approximation.")
     if save:
-        _save(results, paramset, save, ctx, params_c, rcat.c, catalogue_rand,
-              alpha, 2, catalogue_data, catalogue_rand)
+        path = _save(results, paramset, save, ctx, params_c, rcat.c,
+                     catalogue_rand, alpha, 2, catalogue_data, catalogue_rand)
+        _log(logger, "Measurements saved to %s.", path)
     return results
