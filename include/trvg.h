@@ -230,7 +230,18 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *   "assign_path"      FP32 real meshes of sorted catalogues: 0 the
  *                           autotuner's choice (default), 1 the
  *                           shared-memory tiled deposit (32^3 tiles),
- *                           2 per-particle global atomics (finer tiles). */
+ *                           2 per-particle global atomics (finer tiles);
+ *                           the tiled deposit serves uncompensated meshes;
+ *   "mesh_comp"        FP32-mixed: deposit with float-float windows and
+ *                           compensated atomics, each FP32 mesh keeping
+ *                           its rounding errors in a second FP32 mesh:
+ *                           0 never, 1 always, 2 (default) for fields of
+ *                           several catalogues (data minus alpha randoms,
+ *                           whose sum cancels);
+ *   "mesh_renorm"      0/1: FP32-mixed: round every compensated mesh to
+ *                           its correctly rounded FP32 sum before the FP32
+ *                           transforms (default 0: only fields of several
+ *                           catalogues are). */
 int trvg_set_option(trvg_context* ctx, const char* key, int64_t value);
 /* Launch shapes the autotuner chose so far: key and value. */
 int trvg_tuned_count(const trvg_context* ctx, int* count);

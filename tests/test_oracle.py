@@ -33,16 +33,17 @@ def _survey(d, r):
     return data, rand, nd / nr
 
 
-def check_threept(res, ext, kind):
+def check_threept(res, ext, kind, rtol=1e-5):
     keys = (['k1_bin', 'k1_eff', 'nmodes_1', 'k2_bin', 'k2_eff', 'nmodes_2',
              'bk_raw', 'bk_shot'] if kind == 'bispec' else
             ['r1_bin', 'r1_eff', 'npairs_1', 'r2_bin', 'r2_eff', 'npairs_2',
              'zeta_raw', 'zeta_shot'])
     for i, k in enumerate(keys[:6]):
         assert np.allclose(res[k], ext[i]), k
-    assert np.allclose(res[keys[6]], ext[-4] + 1j * ext[-3]), keys[6]
-    assert np.allclose(res[keys[7]], ext[-2] + 1j * ext[-1], atol=1e-6), \
-        keys[7]
+    assert np.allclose(res[keys[6]], ext[-4] + 1j * ext[-3], rtol=rtol), \
+        keys[6]
+    assert np.allclose(res[keys[7]], ext[-2] + 1j * ext[-1], rtol=rtol,
+                       atol=1e-6), keys[7]
 
 
 def check_powspec(res, ext):

@@ -8,6 +8,9 @@
 // accumulated with atomics.  The mesh stores the deposited weight per cell
 // (the reference's n(x) * dV), which is what its forward FFT consumes after
 // the vol_cell scaling (field.cpp:1503-1510).
+#include <type_traits>
+
+#include "ff.cuh"
 #include "kernels.h"
 #include "stencil.cuh"
 
@@ -35,7 +38,29 @@ struct AssignArgs {
   DevCatalogue cat;
   WeightSpec ws;
   bool vec4;        // z rows 16-byte aligned in every target mesh
+  // Compensated FP32 deposit: each target mesh has a second FP32 mesh
+  // lo_off elements after it that collects the rounding errors of the
+  // products and of the atomic sums (0: none).
+  int64_t lo_off;
 };
+
+// Rounding error of s = fl(a + b): a + b = s + err exactly (Knuth's
+// TwoSum; the _rn intrinsics keep the compiler from contracting it).
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  const float bb = __fsub_rn(s, a);
+  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Compensated atomic add of the float-float value (vh, vl) to cell p: the
+// add to p returns the cell's previous value, from which the exact
+// rounding error of the add follows (a float atomic add rounds to
+// nearest); the error and vl go to the compensation cell.
+__device__ __forceinline__ void atomic_add_comp(float* p, int64_t lo_off,
+                                                float vh, float vl) {
+  const float old = atomicAdd(p, vh);
+  const float e = __fadd_rn(two_sum_err(old, vh, __fadd_rn(old, vh)), vl);
+  if (e != 0.f) atomicAdd(p + lo_off, e);
+}
 
 // ---- FP32-mesh fast stencil ------------------------------------------------
 //
@@ -107,6 +132,74 @@ __device__ __forceinline__ void fill_stencil_f(int idx, float s, int n,
   }
 }
 
+// The same stencil with float-float windows (about 2^-44 relative), for
+// the compensated deposit: the offset s = s.hi + s.lo carries the 48
+// leading fraction bits of loc, and every window is formed from it with
+// error-free float operations (1 - s, 1/2 +- s and 3/2 - s are exact in
+// s.hi because s.hi holds 24 fraction bits).
+template <int ORDER>
+struct StencilFF {
+  int idx[ORDER];
+  FF win[ORDER];
+};
+
+__device__ __forceinline__ FF ff_const(float v) { return FF{v, 0.f}; }
+
+template <int ORDER>
+__device__ __forceinline__ void fill_stencil_ff(int idx, FF s, int n,
+                                                bool shadow,
+                                                StencilFF<ORDER>& st) {
+  if (ORDER == 1) {
+    int i0 = idx;
+    if (s.hi >= 0.5f) i0 = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[0] = i0;
+    st.win[0] = ff_const(1.f);
+  } else if (ORDER == 2) {
+    st.idx[0] = idx;
+    st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+    st.win[0] = FF{1.f - s.hi, -s.lo};
+    st.win[1] = s;
+  } else if (ORDER == 3) {
+    if (s.hi < 0.5f) {
+      st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+      st.idx[1] = idx;
+      st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+      const FF u = FF{0.5f - s.hi, -s.lo}, v = FF{0.5f + s.hi, s.lo};
+      st.win[0] = ffscale2(ffmul(u, u), 0.5f);
+      st.win[1] = ffsub(ff_const(0.75f), ffmul(s, s));
+      st.win[2] = ffscale2(ffmul(v, v), 0.5f);
+    } else {
+      st.idx[0] = idx;
+      st.idx[1] = (idx == n - 1) ? 0 : idx + 1;
+      if (shadow) {
+        st.idx[2] = (idx == n - 1) ? 0 : st.idx[1] + 1;
+      } else {
+        st.idx[2] = (st.idx[1] == n - 1) ? 0 : st.idx[1] + 1;
+      }
+      const FF t = FF{1.f - s.hi, -s.lo};
+      const FF u = FF{1.5f - s.hi, -s.lo}, v = FF{s.hi - 0.5f, s.lo};
+      st.win[0] = ffscale2(ffmul(u, u), 0.5f);
+      st.win[1] = ffsub(ff_const(0.75f), ffmul(t, t));
+      st.win[2] = ffscale2(ffmul(v, v), 0.5f);
+    }
+  } else {
+    st.idx[0] = (idx == 0) ? n - 1 : idx - 1;
+    st.idx[1] = idx;
+    st.idx[2] = (idx == n - 1) ? 0 : idx + 1;
+    st.idx[3] = (st.idx[2] == n - 1) ? 0 : st.idx[2] + 1;
+    const FF t = FF{1.f - s.hi, -s.lo};
+    const FF c = FF{0x1.555556p-3f, -0x1.555556p-28f};  // 1/6
+    const FF s2 = ffmul(s, s), s3 = ffmul(s2, s);
+    const FF t2 = ffmul(t, t), t3 = ffmul(t2, t);
+    st.win[0] = ffmul(c, t3);
+    st.win[1] = ffmul(c, ffadd(ffadd(ff_const(4.f), ffmul(ff_const(-6.f), s2)),
+                               ffmul(ff_const(3.f), s3)));
+    st.win[2] = ffmul(c, ffadd(ffadd(ff_const(4.f), ffmul(ff_const(-6.f), t2)),
+                               ffmul(ff_const(3.f), t3)));
+    st.win[3] = ffmul(c, s3);
+  }
+}
+
 // Main (and, if `shadow` is given, shadow) stencil of one axis; false when
 // the particle must take the exact path.  The shadow cell follows from the
 // main one: loc + 1/2 stays in cell idx when s < 1/2 and moves to the next
@@ -140,6 +233,38 @@ __device__ __forceinline__ void split_offset(double loc, int& idx, float& s) {
   }
 }
 
+// split_offset with the fraction as float-float: s.hi the leading 24 bits
+// (as split_offset gives them), s.lo the next ones.
+__device__ __forceinline__ void split_offset_ff(double loc, int& idx, FF& s) {
+  const long long bits = __double_as_longlong(loc);
+  const int e = int((bits >> 52) & 0x7ff) - 1023;
+  if (bits < 0) {
+    idx = -1;
+    s = FF{0.f, 0.f};
+  } else if (e < 0) {  // 0 <= loc < 1: the rare cell 0 takes FP64 once
+    idx = 0;
+    const float h = float(loc);
+    s = FF{h, float(loc - double(h))};
+  } else if (e >= 30) {
+    idx = 0x7fffffff;
+    s = FF{0.f, 0.f};
+  } else {
+    const unsigned long long m =
+        (static_cast<unsigned long long>(bits) & ((1ull << 52) - 1)) |
+        (1ull << 52);
+    const int sh = 52 - e;  // fraction bits, 23..52
+    idx = int(m >> sh);
+    const unsigned long long f = m & ((1ull << sh) - 1);
+    if (sh > 24) {
+      s.hi = float(unsigned(f >> (sh - 24))) * 0x1p-24f;
+      const unsigned long long r = f & ((1ull << (sh - 24)) - 1);
+      s.lo = ldexpf(float(r), -sh);
+    } else {
+      s = FF{ldexpf(float(unsigned(f)), -sh), 0.f};
+    }
+  }
+}
+
 template <int ORDER>
 __device__ __forceinline__ bool axis_stencil_f(double pos, int n, double ratio,
                                                StencilF<ORDER>& main,
@@ -158,6 +283,30 @@ __device__ __forceinline__ bool axis_stencil_f(double pos, int n, double ratio,
     else
       fill_stencil_f<ORDER>((idx == n - 1) ? 0 : idx + 1, s - 0.5f, n, true,
                             *shadow);
+  }
+  return true;
+}
+
+// axis_stencil_f with float-float windows (same cells and tie test).
+template <int ORDER>
+__device__ __forceinline__ bool axis_stencil_ff(double pos, int n,
+                                                double ratio,
+                                                StencilFF<ORDER>& main,
+                                                StencilFF<ORDER>* shadow) {
+  const double loc = pos * ratio;
+  int idx;
+  FF s;
+  split_offset_ff(loc, idx, s);
+  if (idx < 0 || idx >= n || !(s.hi >= kTieMargin) ||
+      s.hi > 1.f - kTieMargin || fabsf(s.hi - 0.5f) < kTieMargin)
+    return false;
+  fill_stencil_ff<ORDER>(idx, s, n, false, main);
+  if (shadow != nullptr) {
+    if (s.hi < 0.5f)
+      fill_stencil_ff<ORDER>(idx, FF{s.hi + 0.5f, s.lo}, n, true, *shadow);
+    else
+      fill_stencil_ff<ORDER>((idx == n - 1) ? 0 : idx + 1,
+                             FF{s.hi - 0.5f, s.lo}, n, true, *shadow);
   }
   return true;
 }
@@ -211,6 +360,94 @@ __device__ __forceinline__ void deposit_f(const AssignArgs& a,
   }
 }
 
+// deposit_f with float-float windows and products, deposited with
+// compensated atomics.
+template <int ORDER>
+__device__ __forceinline__ void deposit_ff(const AssignArgs& a,
+                                           const StencilFF<ORDER>& sx,
+                                           const StencilFF<ORDER>& sy,
+                                           const StencilFF<ORDER>& sz, FF wgt,
+                                           bool unit, float* mesh) {
+  bool run = a.vec4;
+#pragma unroll
+  for (int k = 1; k < ORDER; ++k) run = run && (sz.idx[k] == sz.idx[0] + k);
+  if (!run) {
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i) {
+      const FF wi = unit ? sx.win[i] : ffmul(sx.win[i], wgt);
+#pragma unroll
+      for (int j = 0; j < ORDER; ++j) {
+        float* row =
+            mesh + (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
+        const FF wij = ffmul(wi, sy.win[j]);
+#pragma unroll
+        for (int k = 0; k < ORDER; ++k) {
+          const FF v = ffmul(wij, sz.win[k]);
+          atomic_add_comp(row + sz.idx[k], a.lo_off, v.hi, v.lo);
+        }
+      }
+    }
+    return;
+  }
+  // Float4 runs along z.  Per x cell, the value atomics of all its y rows
+  // are issued first and their returned values awaited together, so that
+  // several round trips to L2 overlap; the compensation atomics follow.
+  const int z0 = sz.idx[0], off = z0 & 3;
+  const bool two = off + ORDER > 4;
+  auto lanes = [&](const FF* v, float* q, float* ql) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      float x = 0.f, y = 0.f;
+#pragma unroll
+      for (int k = 0; k < ORDER; ++k) {
+        x = (l == off + k) ? v[k].hi : x;
+        y = (l == off + k) ? v[k].lo : y;
+      }
+      q[l] = x;
+      ql[l] = y;
+    }
+  };
+  auto err = [](float o, float h, float l) {
+    return __fadd_rn(two_sum_err(o, h, __fadd_rn(o, h)), l);
+  };
+#pragma unroll
+  for (int i = 0; i < ORDER; ++i) {
+    const FF wi = unit ? sx.win[i] : ffmul(sx.win[i], wgt);
+    float4 o1[ORDER], o2[ORDER];
+    FF v[ORDER][ORDER];
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) {
+      float4* p = reinterpret_cast<float4*>(
+          mesh + (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2] +
+          (z0 - off));
+      const FF wij = ffmul(wi, sy.win[j]);
+#pragma unroll
+      for (int k = 0; k < ORDER; ++k) v[j][k] = ffmul(wij, sz.win[k]);
+      float q[8], ql[8];
+      lanes(v[j], q, ql);
+      o1[j] = atomicAdd(p, make_float4(q[0], q[1], q[2], q[3]));
+      if (two) o2[j] = atomicAdd(p + 1, make_float4(q[4], q[5], q[6], q[7]));
+    }
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) {
+      float4* pl = reinterpret_cast<float4*>(
+          mesh + a.lo_off +
+          (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2] + (z0 - off));
+      float q[8], ql[8];
+      lanes(v[j], q, ql);
+      atomicAdd(pl, make_float4(err(o1[j].x, q[0], ql[0]),
+                                err(o1[j].y, q[1], ql[1]),
+                                err(o1[j].z, q[2], ql[2]),
+                                err(o1[j].w, q[3], ql[3])));
+      if (two)
+        atomicAdd(pl + 1, make_float4(err(o2[j].x, q[4], ql[4]),
+                                      err(o2[j].y, q[5], ql[5]),
+                                      err(o2[j].z, q[6], ql[6]),
+                                      err(o2[j].w, q[7], ql[7])));
+    }
+  }
+}
+
 // Deposit one stencil; returns the weight that landed inside the mesh.
 // Stencil indices and window values are FP64 (they decide the cells); the
 // products deposited into an FP32 mesh are formed in FP32.  The landed
@@ -253,6 +490,14 @@ __device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
           all_in = false;
           continue;
         }
+        if constexpr (sizeof(Real) == 4) {
+          if (a.lo_off != 0) {
+            const double v = sx.win[i] * wgt.re * sy.win[j] * sz.win[k];
+            const float vh = float(v);
+            atomic_add_comp(re + gid, a.lo_off, vh, float(v - double(vh)));
+            continue;
+          }
+        }
         atomic_add_real(re + gid, wij * wz[k]);
       }
     }
@@ -269,6 +514,14 @@ __device__ __forceinline__ cd deposit(const AssignArgs& a, const double pos[3],
         for (int k = 0; k < ORDER; ++k) {
           const int64_t gid = row + sz.idx[k];
           if (gid < 0 || gid >= a.nmesh) continue;
+          if constexpr (sizeof(Real) == 4) {
+            if (a.lo_off != 0) {
+              const double v = sx.win[i] * wgt.im * sy.win[j] * sz.win[k];
+              const float vh = float(v);
+              atomic_add_comp(im + gid, a.lo_off, vh, float(v - double(vh)));
+              continue;
+            }
+          }
           atomic_add_real(im + gid, wij * wz[k]);
         }
       }
@@ -307,8 +560,54 @@ __device__ __noinline__ void exact_particle(const AssignArgs& a,
     landed[1] = deposit<ORDER, Real>(a, pos, true, wgt, sre, sim);
 }
 
-// SH: the interlacing shadow is deposited too (sre != nullptr).
-template <int ORDER, class Real, bool SH>
+// Fast-path deposit of one particle (main and shadow) into FP32 meshes,
+// plain or compensated (COMP, float-float windows); false if the particle
+// must take the exact path.
+template <int ORDER, bool SH, bool COMP>
+__device__ __forceinline__ bool fast_particle(const AssignArgs& a,
+                                              const double* pos, cd wgt,
+                                              float* re, float* im,
+                                              float* sre, float* sim) {
+  if constexpr (COMP) {
+    StencilFF<ORDER> sx, sy, sz, hx, hy, hz;
+    if (!(axis_stencil_ff<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                                 SH ? &hx : nullptr) &&
+          axis_stencil_ff<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                                 SH ? &hy : nullptr) &&
+          axis_stencil_ff<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                                 SH ? &hz : nullptr)))
+      return false;
+    const bool unit_re = wgt.re == 1.;
+    const FF wr = ff_from_double(wgt.re), wi = ff_from_double(wgt.im);
+    deposit_ff<ORDER>(a, sx, sy, sz, wr, unit_re, re);
+    if (im != nullptr) deposit_ff<ORDER>(a, sx, sy, sz, wi, false, im);
+    if constexpr (SH) {
+      deposit_ff<ORDER>(a, hx, hy, hz, wr, unit_re, sre);
+      if (sim != nullptr) deposit_ff<ORDER>(a, hx, hy, hz, wi, false, sim);
+    }
+  } else {
+    StencilF<ORDER> sx, sy, sz, hx, hy, hz;
+    if (!(axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                                SH ? &hx : nullptr) &&
+          axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                                SH ? &hy : nullptr) &&
+          axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                                SH ? &hz : nullptr)))
+      return false;
+    deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), re);
+    if (im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), im);
+    if constexpr (SH) {
+      deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), sre);
+      if (sim != nullptr)
+        deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), sim);
+    }
+  }
+  return true;
+}
+
+// SH: the interlacing shadow is deposited too (sre != nullptr).  COMP: FP32
+// meshes with compensation meshes (a.lo_off).
+template <int ORDER, class Real, bool SH, bool COMP>
 __global__ void __launch_bounds__(256)
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
@@ -331,22 +630,9 @@ assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
       wgt = (a.ws.scale * wp) * y;
     }
     if constexpr (sizeof(Real) == 4) {
-      StencilF<ORDER> sx, sy, sz, hx, hy, hz;
-      if (axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
-                                SH ? &hx : nullptr) &&
-          axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
-                                SH ? &hy : nullptr) &&
-          axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
-                                SH ? &hz : nullptr)) {
+      if (fast_particle<ORDER, SH, COMP>(a, pos, wgt, re, im, sre, sim)) {
         // Every cell is inside the mesh and the windows sum to one: the
         // landed weight is the weight itself.
-        deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), re);
-        if (im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), im);
-        if constexpr (SH) {
-          deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), sre);
-          if (sim != nullptr)
-            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), sim);
-        }
         if (uniform) {
           ++nland;
         } else {
@@ -687,7 +973,7 @@ ylm_weight_sums_kernel(DevCatalogue cat, YlmTargets ts, double* out) {
   }
 }
 
-template <int ORDER, bool SH>
+template <int ORDER, bool SH, bool COMP>
 __global__ void __launch_bounds__(256)
 assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
   const int64_t np = a.cat.count(), p0 = a.cat.first();
@@ -697,25 +983,48 @@ assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
     cd ypos[kMaxYlmDegree + 1];
     particle_terms(a.cat, p, ts.ell, ts.cnorm, wpow, ypos);
     const double pos[3] = {a.cat.x[p], a.cat.y[p], a.cat.z[p]};
-    StencilF<ORDER> sx, sy, sz, hx, hy, hz;
-    const bool fast =
-        axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
-                              SH ? &hx : nullptr) &&
-        axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
-                              SH ? &hy : nullptr) &&
-        axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
-                              SH ? &hz : nullptr);
+    using St = typename std::conditional<COMP, StencilFF<ORDER>,
+                                         StencilF<ORDER>>::type;
+    St sx, sy, sz, hx, hy, hz;
+    bool fast;
+    if constexpr (COMP)
+      fast = axis_stencil_ff<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                                    SH ? &hx : nullptr) &&
+             axis_stencil_ff<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                                    SH ? &hy : nullptr) &&
+             axis_stencil_ff<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                                    SH ? &hz : nullptr);
+    else
+      fast = axis_stencil_f<ORDER>(pos[0], a.n[0], a.ratio[0], sx,
+                                   SH ? &hx : nullptr) &&
+             axis_stencil_f<ORDER>(pos[1], a.n[1], a.ratio[1], sy,
+                                   SH ? &hy : nullptr) &&
+             axis_stencil_f<ORDER>(pos[2], a.n[2], a.ratio[2], sz,
+                                   SH ? &hz : nullptr);
     for (int t = 0; t < ts.count; ++t) {
       const YlmTarget& u = ts.t[t];
       if (u.re == nullptr) continue;
       const cd wgt = target_weight(u, wpow, ypos, ts.ell);
       if (fast) {
-        deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), u.re);
-        if (u.im != nullptr) deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), u.im);
-        if constexpr (SH) {
-          deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), u.sre);
-          if (u.sim != nullptr)
-            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), u.sim);
+        if constexpr (COMP) {
+          const FF wr = ff_from_double(wgt.re), wi = ff_from_double(wgt.im);
+          deposit_ff<ORDER>(a, sx, sy, sz, wr, false, u.re);
+          if (u.im != nullptr)
+            deposit_ff<ORDER>(a, sx, sy, sz, wi, false, u.im);
+          if constexpr (SH) {
+            deposit_ff<ORDER>(a, hx, hy, hz, wr, false, u.sre);
+            if (u.sim != nullptr)
+              deposit_ff<ORDER>(a, hx, hy, hz, wi, false, u.sim);
+          }
+        } else {
+          deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), u.re);
+          if (u.im != nullptr)
+            deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), u.im);
+          if constexpr (SH) {
+            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), u.sre);
+            if (u.sim != nullptr)
+              deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), u.sim);
+          }
         }
       } else {
         // The target's sums hold the full weight: add what did not land.
@@ -770,11 +1079,35 @@ __global__ void to_double_kernel(const Real* mesh, int64_t n, double scale,
 // deposit to come.  `sum` is read from device memory when `dsum` is given.
 template <class Real>
 __global__ void fill_offset_kernel(Real* mesh, int64_t n, const double* dsum,
-                                   double hsum) {
-  const Real v = Real(-((dsum != nullptr) ? *dsum : hsum) / double(n));
+                                   double hsum, int64_t lo_off) {
+  const double f = -((dsum != nullptr) ? *dsum : hsum) / double(n);
+  const Real v = Real(f);
+  // A compensation mesh starts at the rounding error of the fill value.
+  const Real vl = Real(f - double(v));
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    mesh[i] = v;
+    if (lo_off != 0) mesh[i + lo_off] = vl;
+  }
+}
+
+template <class Real>
+__global__ void mesh_copy_kernel(const float* src, int64_t n, Real* dst) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
-    mesh[i] = v;
+    dst[i] = Real(src[i]);
+}
+
+// hi + lo -> (fl(hi + lo), exact remainder): the FP32 mesh becomes the
+// correctly rounded value of the compensated sum.
+__global__ void mesh_renorm_kernel(float* mesh, int64_t n, int64_t lo_off) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const float h = mesh[i], l = mesh[i + lo_off];
+    const float s = __fadd_rn(h, l);
+    mesh[i] = s;
+    mesh[i + lo_off] = two_sum_err(h, l, s);
+  }
 }
 
 // sum_p scale * w_p^power * [conj] y_lm(los_p) in FP64
@@ -859,9 +1192,12 @@ template <class Real>
 void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                    const DevCatalogue& cat, const WeightSpec& ws,
                    Real* mesh_re, Real* mesh_im, Real* shadow_re,
-                   Real* shadow_im, double* sums, const MeshFill* fill) {
+                   Real* shadow_im, double* sums, const MeshFill* fill,
+                   int64_t lo_off) {
   if (cat.n == 0) return;
+  if (sizeof(Real) != 4) lo_off = 0;
   AssignArgs a;
+  a.lo_off = lo_off;
   for (int i = 0; i < 3; ++i) {
     a.n[i] = g.n[i];
     a.L[i] = g.L[i];
@@ -878,7 +1214,7 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
   a.vec4 = g.n[2] % 4 == 0 && aligned16(mesh_re) && aligned16(mesh_im) &&
            aligned16(sre) && aligned16(sim);
   if constexpr (sizeof(Real) == 4) {
-    const bool tiled = cat.tile_start != nullptr &&
+    const bool tiled = lo_off == 0 && cat.tile_start != nullptr &&
                        cat.tile_shift == kTileShift && !interlace &&
                        mesh_im == nullptr && !ws.use_ylm && a.vec4 &&
                        g.n[0] >= 64 &&
@@ -903,22 +1239,24 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                                            sums);
   };
   const bool sh = sre != nullptr;
-  switch (order) {
-    case 1:
-      sh ? go(assign_kernel<1, Real, true>) : go(assign_kernel<1, Real, false>);
-      break;
-    case 2:
-      sh ? go(assign_kernel<2, Real, true>) : go(assign_kernel<2, Real, false>);
-      break;
-    case 3:
-      sh ? go(assign_kernel<3, Real, true>) : go(assign_kernel<3, Real, false>);
-      break;
-    case 4:
-      sh ? go(assign_kernel<4, Real, true>) : go(assign_kernel<4, Real, false>);
-      break;
-    default:
-      throw_error(TRVG_ERR_INVALID_PARAMETER,
-                  "Unsupported mesh assignment order: %d.", order);
+  auto by_order = [&](auto sh_c, auto comp_c) {
+    constexpr bool S = decltype(sh_c)::value, P = decltype(comp_c)::value;
+    switch (order) {
+      case 1: go(assign_kernel<1, Real, S, P>); break;
+      case 2: go(assign_kernel<2, Real, S, P>); break;
+      case 3: go(assign_kernel<3, Real, S, P>); break;
+      case 4: go(assign_kernel<4, Real, S, P>); break;
+      default:
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Unsupported mesh assignment order: %d.", order);
+    }
+  };
+  using T = std::true_type;
+  using F = std::false_type;
+  if (sizeof(Real) == 4 && lo_off != 0) {
+    sh ? by_order(T(), T()) : by_order(F(), T());
+  } else {
+    sh ? by_order(T(), F()) : by_order(F(), F());
   }
   TRVG_LAUNCHED(ctx);
 }
@@ -943,10 +1281,27 @@ void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
 
 template <class Real>
 void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
-                        const double* dsum, double hsum) {
+                        const double* dsum, double hsum, int64_t lo_off) {
   TRVG_KBEGIN(ctx, "fill_offset_kernel");
   fill_offset_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(
-      mesh, n, dsum, hsum);
+      mesh, n, dsum, hsum, lo_off);
+  TRVG_LAUNCHED(ctx);
+}
+
+template <class Real>
+void launch_mesh_copy(Context& ctx, const float* src, int64_t n, Real* dst) {
+  TRVG_KBEGIN(ctx, "mesh_copy_kernel");
+  mesh_copy_kernel<Real><<<grid_for(n, 256), 256, 0, ctx.stream>>>(src, n,
+                                                                   dst);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_mesh_renorm(Context& ctx, float* mesh, int64_t n,
+                        int64_t lo_off) {
+  if (mesh == nullptr || lo_off == 0) return;
+  TRVG_KBEGIN(ctx, "mesh_renorm_kernel");
+  mesh_renorm_kernel<<<grid_for(n, 256), 256, 0, ctx.stream>>>(mesh, n,
+                                                               lo_off);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -964,7 +1319,8 @@ void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
 }
 
 void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
-                       const DevCatalogue& cat, const YlmTargets& ts) {
+                       const DevCatalogue& cat, const YlmTargets& ts,
+                       int64_t lo_off) {
   if (cat.n == 0 || ts.count == 0) return;
   if (ts.count > kMaxYlmTargets || ts.ell > kMaxYlmDegree || ts.ell < 0)
     throw_error(TRVG_ERR_INVALID_PARAMETER, "Too many Y_lm targets.");
@@ -977,6 +1333,7 @@ void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
   a.nmesh = g.nmesh;
   a.cat = cat;
   a.ws = WeightSpec();
+  a.lo_off = lo_off;
   a.vec4 = g.n[2] % 4 == 0;
   for (int t = 0; t < ts.count; ++t)
     for (const float* q : {ts.t[t].re, ts.t[t].im, ts.t[t].sre, ts.t[t].sim})
@@ -990,14 +1347,24 @@ void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
     kernel<<<grid, 256, 0, ctx.stream>>>(a, tn);
     TRVG_LAUNCHED(ctx);
   };
-  switch (order) {
-    case 1: interlace ? go(assign_ylm_kernel<1, true>) : go(assign_ylm_kernel<1, false>); break;
-    case 2: interlace ? go(assign_ylm_kernel<2, true>) : go(assign_ylm_kernel<2, false>); break;
-    case 3: interlace ? go(assign_ylm_kernel<3, true>) : go(assign_ylm_kernel<3, false>); break;
-    case 4: interlace ? go(assign_ylm_kernel<4, true>) : go(assign_ylm_kernel<4, false>); break;
-    default:
-      throw_error(TRVG_ERR_INVALID_PARAMETER,
-                  "Unsupported mesh assignment order: %d.", order);
+  auto by_order = [&](auto sh_c, auto comp_c) {
+    constexpr bool S = decltype(sh_c)::value, P = decltype(comp_c)::value;
+    switch (order) {
+      case 1: go(assign_ylm_kernel<1, S, P>); break;
+      case 2: go(assign_ylm_kernel<2, S, P>); break;
+      case 3: go(assign_ylm_kernel<3, S, P>); break;
+      case 4: go(assign_ylm_kernel<4, S, P>); break;
+      default:
+        throw_error(TRVG_ERR_INVALID_PARAMETER,
+                    "Unsupported mesh assignment order: %d.", order);
+    }
+  };
+  using T = std::true_type;
+  using F = std::false_type;
+  if (lo_off != 0) {
+    interlace ? by_order(T(), T()) : by_order(F(), T());
+  } else {
+    interlace ? by_order(T(), F()) : by_order(F(), F());
   }
 }
 
@@ -1013,13 +1380,15 @@ void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
 #define TRVG_INST(R)                                                        \
   template void launch_assign<R>(Context&, const Geom&, int, bool,          \
                                  const DevCatalogue&, const WeightSpec&, R*, \
-                                 R*, R*, R*, double*, const MeshFill*);     \
+                                 R*, R*, R*, double*, const MeshFill*,      \
+                                 int64_t);                                  \
   template void launch_mesh_sum_pow<R>(Context&, const R*, int64_t, int,    \
                                        double*);                            \
   template void launch_mesh_to_double<R>(Context&, const R*, int64_t,       \
                                          double, double*);                  \
   template void launch_fill_offset<R>(Context&, R*, int64_t, const double*, \
-                                      double);
+                                      double, int64_t);                     \
+  template void launch_mesh_copy<R>(Context&, const float*, int64_t, R*);
 TRVG_INST(float)
 TRVG_INST(double)
 #undef TRVG_INST

@@ -315,6 +315,13 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     ctx->impl.xi_octant = value != 0;
   } else if (k == "fused_ylm") {
     ctx->impl.fused_ylm = value != 0;
+  } else if (k == "mesh_comp") {
+    if (value < 0 || value > 2)
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "mesh_comp must be 0, 1 or 2.");
+    ctx->impl.mesh_comp = int(value);
+  } else if (k == "mesh_renorm") {
+    ctx->impl.mesh_renorm = value != 0;
   } else if (k == "assign_path") {
     if (value < 0 || value > 2)
       trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,

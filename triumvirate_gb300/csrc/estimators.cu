@@ -550,18 +550,33 @@ struct Engine {
                   g.n[0], g.n[1], g.n[2], p.assignment_order, lg);
     // 5: 32^3 tiles, which FP32 real meshes deposit through shared memory.
     if (ctx.assign_path == 1) return sort_catalogue(ctx, g, d, tag, 5);
-    const vector<int> cands = ctx.assign_path == 2 ? vector<int>{3, 2, 4}
-                                                   : vector<int>{5, 3, 2, 4};
+    // The compensated deposit has no tiled form: 32^3 tiles only pay off
+    // for the shared-memory deposit of uncompensated FP32 meshes.
+    const int64_t lo = mesh_lo_off(false);
+    const vector<int> cands = (ctx.assign_path == 2 || lo != 0)
+                                  ? vector<int>{3, 2, 4}
+                                  : vector<int>{5, 3, 2, 4};
     std::snprintf(key + std::strlen(key), sizeof(key) - std::strlen(key),
-                  ".path%d", ctx.assign_path);
+                  ".path%d%s", ctx.assign_path, lo != 0 ? ".comp" : "");
     const int shift = tuned(key, cands, [&](int sh) {
       const DevCatalogue sd = sort_catalogue(ctx, g, d, tag, sh);
-      Real* m = ctx.buf<Real>("mesh.re", g.nmesh);
+      Real* m = ctx.buf<Real>("mesh.re", size_t(g.nmesh + lo));
       double* sums = ctx.buf<double>("assign.sums", 4);
       launch_assign<Real>(ctx, g, p.assignment_order, false, sd,
-                          WeightSpec(), m, nullptr, nullptr, nullptr, sums);
+                          WeightSpec(), m, nullptr, nullptr, nullptr, sums,
+                          nullptr, lo);
     });
     return sort_catalogue(ctx, g, d, tag, shift);
+  }
+
+  // Offset of the compensation mesh after each FP32 mesh (0: none) for a
+  // field of one catalogue or of several (option "mesh_comp": 1 always,
+  // 2 for several, whose weights cancel in the sum).
+  int64_t mesh_lo_off(bool several) const {
+    if (sizeof(Real) != 4) return 0;
+    if (ctx.mesh_comp == 1 || (ctx.mesh_comp == 2 && several))
+      return (g.nmesh + 3) / 4 * 4;  // float4-aligned rows stay aligned
+    return 0;
   }
 
   // Assign all parts into one (complex if `cplx`) mesh, with the shadow when
@@ -571,10 +586,12 @@ struct Engine {
   Field make_field(const std::string& name, const vector<Part>& parts,
                    bool cplx, bool defer_r2c = false) {
     Field f;
-    Real* mre = ctx.buf<Real>("mesh.re", g.nmesh);
-    Real* mim = cplx ? ctx.buf<Real>("mesh.im", g.nmesh) : nullptr;
-    Real* sre = interlace ? ctx.buf<Real>("mesh.sre", g.nmesh) : nullptr;
-    Real* sim = (interlace && cplx) ? ctx.buf<Real>("mesh.sim", g.nmesh)
+    const int64_t lo = mesh_lo_off(parts.size() > 1);
+    const size_t cells = size_t(g.nmesh + lo);
+    Real* mre = ctx.buf<Real>("mesh.re", cells);
+    Real* mim = cplx ? ctx.buf<Real>("mesh.im", cells) : nullptr;
+    Real* sre = interlace ? ctx.buf<Real>("mesh.sre", cells) : nullptr;
+    Real* sim = (interlace && cplx) ? ctx.buf<Real>("mesh.sim", cells)
                                     : nullptr;
     // Each mesh starts at minus the mean of its deposit instead of zero.
     // Only the k = 0 mode changes, and every reader replaces that mode by
@@ -595,17 +612,23 @@ struct Engine {
         launch_weight_sum(ctx, part.cat, part.ws, wsum);
     }
     const double* wsum_im = (wsum != nullptr) ? wsum + 1 : nullptr;
-    launch_fill_offset<Real>(ctx, mre, g.nmesh, wsum, hsum);
-    if (mim) launch_fill_offset<Real>(ctx, mim, g.nmesh, wsum_im, 0.);
-    if (sre) launch_fill_offset<Real>(ctx, sre, g.nmesh, wsum, hsum);
-    if (sim) launch_fill_offset<Real>(ctx, sim, g.nmesh, wsum_im, 0.);
+    launch_fill_offset<Real>(ctx, mre, g.nmesh, wsum, hsum, lo);
+    if (mim) launch_fill_offset<Real>(ctx, mim, g.nmesh, wsum_im, 0., lo);
+    if (sre) launch_fill_offset<Real>(ctx, sre, g.nmesh, wsum, hsum, lo);
+    if (sim) launch_fill_offset<Real>(ctx, sim, g.nmesh, wsum_im, 0., lo);
     double* sums = ctx.buf<double>("assign.sums", 4);
     zero(sums, 4 * sizeof(double));
     const MeshFill fill{wsum, hsum};
     for (size_t i = 0; i < parts.size(); ++i)
       launch_assign<Real>(ctx, g, p.assignment_order, interlace, parts[i].cat,
                           parts[i].ws, mre, mim, sre, sim, sums,
-                          i == 0 ? &fill : nullptr);
+                          i == 0 ? &fill : nullptr, lo);
+    // Several parts (data minus alpha randoms) cancel in the sum: the FP32
+    // meshes the FFTs read become the correctly rounded compensated sums.
+    if (lo != 0 && (parts.size() > 1 || ctx.mesh_renorm))
+      for (Real* m : {mre, mim, sre, sim})
+        if (m != nullptr)
+          launch_mesh_renorm(ctx, reinterpret_cast<float*>(m), g.nmesh, lo);
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
     auto r2c = [&](Real* m, const char* suffix) -> const C* {
       C* o = ctx.buf<C>(name + suffix, size_t(g.nhalf));
@@ -626,6 +649,7 @@ struct Engine {
     ++ctx.mesh_gen;
     if (mim == nullptr && sre == nullptr) {
       f.spec.mesh = mre;
+      f.spec.mesh_lo = lo != 0 ? mre + lo : nullptr;
       f.spec.mesh_gen = ctx.mesh_gen;
     }
     if (mim) f.spec.im = r2c(mim, ".im");
@@ -715,17 +739,19 @@ struct Engine {
       u.sums = sums + 4 * i;
       if (ts[i].name.empty()) continue;
       const std::string& nm = ts[i].name;
-      u.re = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.re", g.nmesh));
+      const size_t cells = size_t(g.nmesh + mesh_lo_off(dd && dr));
+      u.re = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.re", cells));
       if (ts[i].cplx)
-        u.im = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.im", g.nmesh));
+        u.im = reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.im", cells));
       if (interlace) {
         u.sre =
-            reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.sre", g.nmesh));
+            reinterpret_cast<float*>(ctx.buf<Real>(nm + ".mesh.sre", cells));
         if (ts[i].cplx)
           u.sim = reinterpret_cast<float*>(
-              ctx.buf<Real>(nm + ".mesh.sim", g.nmesh));
+              ctx.buf<Real>(nm + ".mesh.sim", cells));
       }
     }
+    const int64_t lo = mesh_lo_off(dd && dr);
     auto with_scales = [&](bool data) {
       YlmTargets v = tg;
       for (int i = 0; i < nt; ++i)
@@ -745,25 +771,31 @@ struct Engine {
                                 ctx.stream));
       if (u.re == nullptr) continue;
       launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.re), g.nmesh,
-                               wsum + 2 * i, 0.);
+                               wsum + 2 * i, 0., lo);
       if (u.im)
         launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.im), g.nmesh,
-                                 wsum + 2 * i + 1, 0.);
+                                 wsum + 2 * i + 1, 0., lo);
       if (u.sre)
         launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.sre), g.nmesh,
-                                 wsum + 2 * i, 0.);
+                                 wsum + 2 * i, 0., lo);
       if (u.sim)
         launch_fill_offset<Real>(ctx, reinterpret_cast<Real*>(u.sim), g.nmesh,
-                                 wsum + 2 * i + 1, 0.);
+                                 wsum + 2 * i + 1, 0., lo);
     }
     bool any_mesh = false;
     for (int i = 0; i < nt; ++i) any_mesh = any_mesh || tg.t[i].re != nullptr;
     if (dd && any_mesh)
       launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dd,
-                        with_scales(true));
+                        with_scales(true), lo);
     if (dr && any_mesh)
       launch_assign_ylm(ctx, g, p.assignment_order, interlace, *dr,
-                        with_scales(false));
+                        with_scales(false), lo);
+    // Data minus alpha randoms: FP32 meshes become the correctly rounded
+    // compensated sums before their transforms.
+    if (lo != 0 && ((dd && dr) || ctx.mesh_renorm))
+      for (int i = 0; i < nt; ++i)
+        for (float* m : {tg.t[i].re, tg.t[i].im, tg.t[i].sre, tg.t[i].sim})
+          if (m != nullptr) launch_mesh_renorm(ctx, m, g.nmesh, lo);
     cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
     auto r2c = [&](const float* m, const std::string& nm) -> const C* {
       C* o = ctx.buf<C>(nm, size_t(g.nhalf));
@@ -1613,7 +1645,8 @@ struct Engine {
     float4* cube = ctx.buf<float4>(
         "ff.cube", size_t(2 * kg + 1) * (2 * kg + 1) * (kg + 1));
     launch_ff_forward_cube(ctx, g, reinterpret_cast<const float*>(src.mesh),
-                           kg, T1, T2, cube);
+                           reinterpret_cast<const float*>(src.mesh_lo), kg,
+                           T1, T2, cube);
     ff_cube = {cube, kg, src.re, src.mesh_gen};
 
     const bool shared = la.ell == lb.ell && la.m == lb.m;

@@ -167,7 +167,7 @@ __device__ __forceinline__ void ff_stage_body(float4* A, int nl, int ln,
                                       const FFPlan& P, int s,
                                       const float4* tw) {
   constexpr int IMAX = StageItems<R>::value;
-  const int nb = P.nb[s], Ns = P.ns[s], tstep = P.tstep[s];
+  const int nb = P.nb[s], Ns = P.ns[s];
   const unsigned mnb = P.mnb[s], mns = P.mns[s];
   const int items = nl * nb;
   FFC v[IMAX][R];
@@ -178,12 +178,12 @@ __device__ __forceinline__ void ff_stage_body(float4* A, int nl, int ln,
     const int l = fdiv(w, nb, mnb), j = w - l * nb;
     const int q = fdiv(j, Ns, mns), k = j - q * Ns;
     const float4* in = A + l * ln;
-    const int step = tstep * k;  // r * step < n
+    const int tb = P.twoff[s] - Ns + k;  // + r Ns: entry (r - 1) Ns + k
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       v[it][r] = ffc_load(in + pidx(j + r * nb));
       if (r > 0 && k > 0) {
-        const float4 t = tw[r * step];
+        const float4 t = tw[tb + r * Ns];
         FFC wv{FF{t.x, t.y}, FF{t.z, t.w}};
         if (D < 0) wv.im = ffneg(wv.im);
         v[it][r] = ffc_mul(v[it][r], wv);
@@ -218,7 +218,7 @@ template <int R, int D>
 __device__ __forceinline__ void ff_stage_warp_body(float4* L, const FFPlan& P,
                                                    int s, const float4* tw) {
   constexpr int IMAX = WarpItems<R>::value;
-  const int nb = P.nb[s], Ns = P.ns[s], tstep = P.tstep[s];
+  const int nb = P.nb[s], Ns = P.ns[s];
   const unsigned mns = P.mns[s];
   const int lane = threadIdx.x & 31;
   FFC v[IMAX][R];
@@ -227,12 +227,12 @@ __device__ __forceinline__ void ff_stage_warp_body(float4* L, const FFPlan& P,
     const int j = lane + 32 * it;
     if (j >= nb) break;
     const int k = j - fdiv(j, Ns, mns) * Ns;
-    const int step = tstep * k;
+    const int tb = P.twoff[s] - Ns + k;  // + r Ns: entry (r - 1) Ns + k
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       v[it][r] = ffc_load(L + pidx(j + r * nb));
       if (r > 0 && k > 0) {
-        const float4 t = tw[r * step];
+        const float4 t = tw[tb + r * Ns];
         FFC wv{FF{t.x, t.y}, FF{t.z, t.w}};
         if (D < 0) wv.im = ffneg(wv.im);
         v[it][r] = ffc_mul(v[it][r], wv);
@@ -363,8 +363,9 @@ __device__ __forceinline__ int lines_shift(int nl) {
 // into T1[x][kz][y].
 template <int MASK>
 __global__ void __launch_bounds__(256, 2)
-ff_fwd_z_kernel(Geom g, const float* mesh, __grid_constant__ const FFPlan P,
-                int LB, int Kz, float4* T1) {
+ff_fwd_z_kernel(Geom g, const float* mesh, const float* mesh_lo,
+                __grid_constant__ const FFPlan P, int LB, int Kz,
+                float4* T1) {
   extern __shared__ float4 smem[];
   __shared__ int64_t obase[2 * kMaxLines];
   const int n2 = g.n[2], ls = line_stride(n2);
@@ -382,8 +383,16 @@ ff_fwd_z_kernel(Geom g, const float* mesh, __grid_constant__ const FFPlan P,
   }
   for (int l = warp; l < nl; l += nw) {
     const float* row = mesh + 2 * (p0 + l) * n2;
-    for (int i = lane; i < n2; i += 32)
-      A[l * ls + pidx(i)] = make_float4(row[i], 0.f, row[n2 + i], 0.f);
+    if (mesh_lo != nullptr) {
+      // Compensated mesh: each cell is the float-float value hi + lo.
+      const float* rlo = mesh_lo + 2 * (p0 + l) * n2;
+      for (int i = lane; i < n2; i += 32)
+        A[l * ls + pidx(i)] =
+            make_float4(row[i], rlo[i], row[n2 + i], rlo[n2 + i]);
+    } else {
+      for (int i = lane; i < n2; i += 32)
+        A[l * ls + pidx(i)] = make_float4(row[i], 0.f, row[n2 + i], 0.f);
+    }
   }
   ff_fft_lines<-1, MASK>(A, nl, ls, P, tw);
   const int sh = lines_shift(2 * nl);
@@ -755,19 +764,32 @@ FFPlan ff_plan(Context& ctx, int n) {
     const int items = (R == 8 || R == 5) ? 1 : (R == 2 ? 3 : 2);  // WarpItems
     if (P.nb[s] > 32 * items) P.warp_lines = false;
   }
-  const std::string name = "fftw." + std::to_string(n);
+  // Stage-major twiddle table: sum over stages of (radix - 1) ns = n - 1
+  // entries.
+  int off = 0;
+  for (int s = 0; s < P.nstage; ++s) {
+    P.twoff[s] = off;
+    off += (P.radix[s] - 1) * P.ns[s];
+  }
+  const std::string name = "fftw.staged." + std::to_string(n);
   auto it = ctx.buffers.find(name);
   if (it != ctx.buffers.end() && it->second.bytes >= size_t(n) * sizeof(float4)) {
     P.tw = static_cast<const float4*>(it->second.ptr);
     return P;
   }
-  std::vector<float4> h(n);
-  for (int k = 0; k < n; ++k) {
-    const double a = 2. * M_PI * double(k) / double(n);
-    const double c = std::cos(a), s = std::sin(a);
-    const float ch = float(c), sh = float(s);
-    h[k] = make_float4(ch, float(c - double(ch)), sh, float(s - double(sh)));
-  }
+  std::vector<float4> h(n, make_float4(1.f, 0.f, 0.f, 0.f));
+  for (int s = 0; s < P.nstage; ++s)
+    for (int r = 1; r < P.radix[s]; ++r)
+      for (int k = 0; k < P.ns[s]; ++k) {
+        // exp(2 pi i e / n) with e = r k tstep < n; direction D < 0 takes
+        // the conjugate in the stage bodies.
+        const int64_t e = int64_t(r) * k * P.tstep[s];
+        const double a = 2. * M_PI * double(e) / double(n);
+        const double c = std::cos(a), sn = std::sin(a);
+        const float ch = float(c), sh = float(sn);
+        h[P.twoff[s] + (r - 1) * P.ns[s] + k] =
+            make_float4(ch, float(c - double(ch)), sh, float(sn - double(sh)));
+      }
   float4* d = ctx.buf<float4>(name, n);
   TRVG_CUDA(cudaMemcpyAsync(d, h.data(), n * sizeof(float4),
                             cudaMemcpyHostToDevice, ctx.stream));
@@ -831,7 +853,8 @@ void with_grid_radix_set(const FFPlan& P, F&& f) {
 }  // namespace
 
 void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
-                            int Kg, float4* T1, float4* T2, float4* cube) {
+                            const float* mesh_lo, int Kg, float4* T1,
+                            float4* T2, float4* cube) {
   const FFPlan Pz = ff_plan(ctx, g.n[2]);
   const FFPlan Py = ff_plan(ctx, g.n[1]);
   const FFPlan Px = ff_plan(ctx, g.n[0]);
@@ -843,7 +866,7 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
     TRVG_KBEGIN(ctx, "ff_fwd_z_kernel");
     ff_fwd_z_kernel<MASK><<<int((npair + lb - 1) / lb), 256,
                             smem_bytes(g.n[2], lb), ctx.stream>>>(
-        g, mesh, Pz, lb, Kg, T1);
+        g, mesh, mesh_lo, Pz, lb, Kg, T1);
     TRVG_LAUNCHED(ctx);
   });
   with_mesh_radix_set(Py, [&](auto set) {

@@ -155,6 +155,14 @@ struct Context {
   // Deposit of sorted catalogues: 0 tuned, 1 tiled (shared memory),
   // 2 global atomics.
   int assign_path = 0;
+  // FP32-mixed meshes deposited with float-float windows and compensated
+  // atomics into a second FP32 mesh: 0 never, 1 always, 2 fields built
+  // from several catalogues (data minus randoms, which cancel).  The tiled
+  // deposit serves uncompensated meshes only.
+  int mesh_comp = 2;
+  // Round every compensated mesh to its correctly rounded FP32 sum before
+  // the FP32 transforms (always done for fields of several catalogues).
+  bool mesh_renorm = false;
   // Mocks replayed from the captured graph by the last batch call.
   int64_t graph_replays = 0;
   // Deposits made so far (FieldSpec::mesh_gen).

@@ -117,6 +117,8 @@ struct FieldSpec {
   // The real FP32 mesh the spectrum came from (real fields without
   // interlacing), valid while mesh_gen equals the context's counter.
   const Real* mesh = nullptr;
+  // Its compensation mesh (compensated FP32 deposit), or nullptr.
+  const Real* mesh_lo = nullptr;
   int64_t mesh_gen = -1;
 };
 
@@ -167,7 +169,10 @@ void launch_assign(Context& ctx, const Geom& g, int order, bool interlace,
                    const DevCatalogue& cat, const WeightSpec& ws,
                    Real* mesh_re, Real* mesh_im, Real* shadow_re,
                    Real* shadow_im, double* sums /* [4]: re, im, s_re, s_im */,
-                   const MeshFill* fill = nullptr);
+                   const MeshFill* fill = nullptr, int64_t lo_off = 0);
+// lo_off != 0 (FP32 meshes): every target mesh m has a compensation mesh
+// at m + lo_off; windows and products are float-float and the atomic sums
+// compensated, so that m + (m + lo_off) holds the deposit to about 2^-44.
 // sum_p scale_t * w^power_t * [conj] y_lm_t for every target, added to
 // out[2 t], out[2 t + 1].
 void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
@@ -177,7 +182,8 @@ void launch_ylm_weight_sums(Context& ctx, const DevCatalogue& cat,
 // (launch_ylm_weight_sums): particles off the fast stencil add the
 // difference between their landed and their full weight.
 void launch_assign_ylm(Context& ctx, const Geom& g, int order, bool interlace,
-                       const DevCatalogue& cat, const YlmTargets& ts);
+                       const DevCatalogue& cat, const YlmTargets& ts,
+                       int64_t lo_off = 0);
 void launch_weight_sum(Context& ctx, const DevCatalogue& cat,
                        const WeightSpec& ws, double* out /* [2] */);
 template <class Real>
@@ -186,10 +192,16 @@ void launch_mesh_sum_pow(Context& ctx, const Real* mesh, int64_t n, int order,
 template <class Real>
 void launch_mesh_to_double(Context& ctx, const Real* mesh, int64_t n,
                            double scale, double* out);
-// Fill a mesh with -(sum / n), sum from device memory (`dsum`) or `hsum`.
+// Fill a mesh with -(sum / n), sum from device memory (`dsum`) or `hsum`
+// (and its compensation mesh, lo_off != 0, with the fill's rounding error).
 template <class Real>
 void launch_fill_offset(Context& ctx, Real* mesh, int64_t n,
-                        const double* dsum, double hsum);
+                        const double* dsum, double hsum, int64_t lo_off = 0);
+// dst = src (an FP32 mesh of the caller) in precision Real.
+template <class Real>
+void launch_mesh_copy(Context& ctx, const float* src, int64_t n, Real* dst);
+// Compensated FP32 mesh -> (correctly rounded sum, remainder).
+void launch_mesh_renorm(Context& ctx, float* mesh, int64_t n, int64_t lo_off);
 
 // ---- sort.cu -------------------------------------------------------------
 // Copy of `in` ordered by mesh tiles of 2^shift cells a side (device
@@ -351,6 +363,11 @@ struct FFPlan {
   unsigned mnb[16], mns[16];
   // Every stage fits one warp per line (WarpItems butterflies per lane).
   bool warp_lines;
+  // Twiddles stage by stage: stage s holds exp(2 pi i r k tstep / n) (the
+  // forward direction takes the conjugate) at twoff[s] + (r - 1) ns + k for
+  // 1 <= r < radix, 0 <= k < ns, so that the butterflies of a warp
+  // (consecutive k) read consecutive entries.
+  int twoff[16];
   const float4* tw;
 };
 bool ff_length_ok(int n);
@@ -359,7 +376,8 @@ FFPlan ff_plan(Context& ctx, int n);
 // cube[sx + Kg][sy + Kg][sz] (T1, T2: scratch of n0 (Kg+1) n1 and
 // (2Kg+1)(Kg+1) n0 float4).
 void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
-                            int Kg, float4* T1, float4* T2, float4* cube);
+                            const float* mesh_lo, int Kg, float4* T1,
+                            float4* T2, float4* cube);
 // Evaluation-grid half spectra E[c][b][a] of G (planes c <= Kg) and
 // E[q][c][b][a] of nq shell fields (planes c <= K) from the cube.
 // k0_dev (re, im in device memory), when given, replaces the host k0.
