@@ -64,11 +64,16 @@ def parse_args():
     ap.add_argument('--variants', action='store_true',
                     help='also time the FP32-mixed precision options')
     ap.add_argument('--workload', default='metric',
-                    choices=['metric', 'mocks', 'survey'],
+                    choices=['metric', 'mocks', 'survey', 'large'],
                     help="'mocks': the batched lognormal-mock workload; "
                          "'survey': survey bispectra from device "
-                         "catalogues (each its own JSON line)")
+                         "catalogues; 'large': the 1024^3 lognormal box "
+                         "(bispectra full 40x40, 3PCF on 30 bins); each "
+                         "prints its own JSON line")
     ap.add_argument('--mocks', type=int, default=256)
+    ap.add_argument('--mesh-comp', type=int, default=2, choices=[0, 1, 2],
+                    help='compensated FP32 mesh deposit (library option '
+                         '"mesh_comp")')
     ap.add_argument('--assign-path', type=int, default=0, choices=[0, 1, 2],
                     help='deposit of sorted catalogues: 0 autotuned, '
                          '1 shared-memory tiled, 2 per-particle atomics')
@@ -205,12 +210,13 @@ def good_fft_size(n):
 
 
 def band_half_width(args):
-    """Largest |s| of a shell mode of the workload (k < 0.205)."""
-    return int(np.floor(0.205 / (2 * np.pi / args.boxsize))) + 1
+    """Largest |s| of a shell mode of the workload (k < kmax)."""
+    kmax = getattr(args, 'kmax', 0.205)
+    return int(np.floor(kmax / (2 * np.pi / args.boxsize))) + 1
 
 
 def eval_grid(args):
-    """Evaluation-grid size M of the workload's shells (k < 0.205)."""
+    """Evaluation-grid size M of the workload's shells (k < kmax)."""
     return min(args.ngrid, good_fft_size(4 * band_half_width(args) + 1))
 
 
@@ -293,6 +299,7 @@ def run_gb300(args):
 
     ctx = _lib.Context(local)
     ctx.set_option('assign_path', args.assign_path)
+    ctx.set_option('mesh_comp', args.mesh_comp)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
 
@@ -389,6 +396,7 @@ def run_gb300(args):
     # already initialised CUDA and loaded the library).
     cold = _lib.Context(local)
     cold.set_option('assign_path', args.assign_path)
+    cold.set_option('mesh_comp', args.mesh_comp)
     cold.set_stream(stream.cuda_stream)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -441,6 +449,8 @@ def run_gb300(args):
                 "fp32mixed_speedup": round(sum(ms2d) /
                                            statistics.median(ms2), 2),
                 "max_rel_err_fp32mixed": per_bin_err(r2_32, r2_64),
+                "per_bin_detail": per_bin_err_keys(r2_32, r2_64,
+                                                   ('bk_raw', 'bk_shot')),
                 "nmodes_equal": bool(np.array_equal(r2_32['nmodes_1'],
                                                     r2_64['nmodes_1']))})
 
@@ -673,6 +683,7 @@ def run_mocks(args):
     norms = 1. / (counts * nbar ** 2)
     binning = Binning('fourier', 'lin', 0.005, 0.245, 24)
     ctx = _lib.Context(0)
+    ctx.set_option('mesh_comp', args.mesh_comp)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     cat = _engine.device_catalogue(ntot, x.data_ptr(), y.data_ptr(),
@@ -732,6 +743,11 @@ def run_mocks(args):
             e[name] = {k: float(max(np.max(np.abs(a[k] - b[k]) / np.abs(b[k]))
                                     for a, b in zip(r32, r64)))
                        for k in ('bk_raw', 'bk_shot')}
+            # The worst entry of each mock, with its modulus relative to
+            # the mock's largest entry.
+            e[name]['per_mock'] = [per_bin_err_keys(a, b, ('bk_raw',
+                                                            'bk_shot'))
+                                   for a, b in zip(r32, r64)]
             # Normwise: max |error| over max |B| of the mock.
             e[name]['normwise'] = {
                 k: float(max(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k]))
@@ -803,10 +819,12 @@ def survey_catalogue(n, seed, ndata=1_000_000):
 
 def run_survey(args):
     """Config: survey bispectra from 1e6 data and 5e6 random particles
-    (seeds 1, 2), 256^3 mesh, PCS, box = random extents, 20 lin bins
-    0.005-0.205 h/Mpc; B_000 full (triu, 210 pairs) and B_202 full (400
-    pairs), FP32-mixed, with the Y_lm-weighted fields of all orders built in
-    one fused pass and, for comparison, one order at a time."""
+    (seeds 1, 2), 256^3 mesh, PCS (interlacing requested; three-point
+    statistics turn it off), box = random extents, 20 lin bins 0.01-0.2
+    h/Mpc; B_000 full (triu, 210 pairs) and B_202 full (400 pairs),
+    FP32-mixed, with the Y_lm-weighted fields of all orders built in one
+    fused pass and, for comparison, one order at a time; per-bin error of
+    the FP32-mixed estimates against the FP64 path."""
     from triumvirate_gb300 import _lib
     from triumvirate_gb300.catalogue import DeviceCatalogue
     from triumvirate_gb300.dataobjs import Binning
@@ -814,8 +832,9 @@ def run_survey(args):
     pd, nzd, wcd = survey_catalogue(1_000_000, 1)
     pr, nzr, wcr = survey_catalogue(5_000_000, 2)
     ctx = _lib.default_context(0)
-    binning = Binning('fourier', 'lin', 0.005, 0.205, 20)
-    samp = {'ngrid': [256] * 3, 'assignment': 'pcs', 'interlace': False,
+    ctx.set_option('mesh_comp', args.mesh_comp)
+    binning = Binning('fourier', 'lin', 0.01, 0.2, 20)
+    samp = {'ngrid': [256] * 3, 'assignment': 'pcs', 'interlace': True,
             'precision': 'fp32mixed'}
 
     def cats():
@@ -855,6 +874,16 @@ def run_survey(args):
                 "kernel_ms": round(sum(v[0] for v in kt.values()), 2),
                 "top_kernels_ms": {k: round(v[0], 3) for k, v in top}}
         ctx.set_option('fused_ylm', 1)
+        if not args.no_fp64:
+            dc, rc = cats()
+            r32 = compute_bispec(dc, rc, degrees=degrees, binning=binning,
+                                 form=form, sampling_params=samp)
+            dc, rc = cats()
+            r64 = compute_bispec(dc, rc, degrees=degrees, binning=binning,
+                                 form=form,
+                                 sampling_params={**samp, 'precision': 'fp64'})
+            res[f"{name}.max_rel_err_fp32mixed_vs_fp64"] = per_bin_err_keys(
+                r32, r64, ('bk_raw', 'bk_shot'))
     line = {
         "metric": "survey bispectrum s/estimate (1e6 data + 5e6 randoms, "
                   "256^3, PCS, B_202 full, 400 pairs)",
@@ -865,11 +894,148 @@ def run_survey(args):
         "data": "synthetic (seeded hemisphere survey, FKP weights)",
         "config": {"workload": "survey B_000 full (triu) and B_202 full, "
                                "1e6 data + 5e6 randoms, 256^3, PCS, 20 lin "
-                               "bins 0.005-0.205 h/Mpc, device catalogues",
+                               "bins 0.01-0.2 h/Mpc, device catalogues",
                    "timing": "wall time per estimate (device-resident "
                              "catalogues, centring and lines of sight "
                              "on the device)"},
         "estimates": res,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Large mesh: a 1024^3 lognormal-Poisson box.
+# ---------------------------------------------------------------------------
+
+def per_bin_err_keys(a, b, keys):
+    """Largest per-bin relative error (complex modulus) of each key, with
+    the entry and its modulus relative to the largest entry."""
+    out = {}
+    for k in keys:
+        x, y = np.asarray(a[k]), np.asarray(b[k])
+        mod = np.abs(y)
+        rel = np.abs(x - y) / mod
+        i = int(np.argmax(rel))
+        out[k] = {"max": float(rel[i]), "entry": i,
+                  "modulus_over_max": float(mod[i] / mod.max()),
+                  "normwise": float(np.max(np.abs(x - y)) / mod.max())}
+    return out
+
+
+def run_large(args):
+    """Config: 2e7 lognormal-Poisson particles (the mocks' P(k)) in a
+    2000 Mpc/h box, 1024^3 mesh, PCS (interlacing is off for three-point
+    statistics); B_000 and B_202 full form on 40 linear bins 0.005-0.3
+    h/Mpc, zeta_000 and zeta_110 (diag) on 30 linear bins 10-150 Mpc/h.
+    FP32-mixed timed (median of the steps), FP64 per-bin errors, per-kernel
+    times and the HBM roofline of each estimate's dominant kernel."""
+    import torch
+
+    from triumvirate_gb300 import _engine, _lib
+    from triumvirate_gb300.dataobjs import Binning
+    dev = torch.device('cuda', 0)
+    torch.cuda.set_device(dev)
+    box, ngrid, npart = 2000., 1024, 20_000_000
+    x, y, z = lognormal_mock(torch, dev, 2025, npart, box=box, n=ngrid)
+    torch.cuda.synchronize(dev)
+    n = x.numel()
+    cat = _engine.device_catalogue(n, x.data_ptr(), y.data_ptr(),
+                                   z.data_ptr())
+    norm = 1. / (n * (n / box ** 3) ** 2)
+    ctx = _lib.Context(0)
+    ctx.set_option('mesh_comp', args.mesh_comp)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    kb = Binning('fourier', 'lin', 0.005, 0.3, 40)
+    rb = Binning('config', 'lin', 10., 150., 30)
+    peak, peak_kind = hbm_peak()
+
+    def params(degrees, form, precision):
+        return _engine.make_params(
+            {'boxsize': {a: box for a in 'xyz'},
+             'ngrid': {a: ngrid for a in 'xyz'}, 'assignment_order': 4,
+             'interlace': False,
+             'degrees': dict(zip(['ell1', 'ell2', 'ELL'], degrees)),
+             'form': form, 'shape': form, 'precision': precision,
+             'verbose': 0}, '3pt')
+
+    jobs = [('B000', 'bispec', (0, 0, 0), 'full', kb),
+            ('B202', 'bispec', (2, 0, 2), 'full', kb),
+            ('zeta000', '3pcf', (0, 0, 0), 'diag', rb),
+            ('zeta110', '3pcf', (1, 1, 0), 'diag', rb)]
+    fa = argparse.Namespace(ngrid=ngrid, npart=n, boxsize=box, nbins=40,
+                            kmax=0.3)
+    out = {}
+    for name, kind, deg, form, binning in jobs:
+        shape = 'triu' if (form == 'full' and deg[0] == deg[1]) else form
+        fn = ('trvg_compute_bispec_in_gpp_box' if kind == 'bispec'
+              else 'trvg_compute_3pcf_in_gpp_box')
+
+        def est(precision):
+            pp = params(deg, shape, precision)
+            return _engine.call_threept(fn, ctx, pp, cat, binning, norm,
+                                        kind, shape=shape)
+        est('fp32mixed')
+        times = []
+        for _ in range(max(1, min(args.steps, 3))):
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r32 = est('fp32mixed')
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1) / 1e3)
+        ctx.set_option('profiling', 1)
+        est('fp32mixed')
+        kt = ctx.kernel_times()
+        ctx.set_option('profiling', 0)
+        mine = {k: v for k, v in kt.items() if not k.startswith('cufft')}
+        dom = max(mine, key=lambda k: mine[k][0])
+        dom_ms = mine[dom][0] / mine[dom][1]
+        alg = algorithmic_bytes(dom, fa, 4) if kind == 'bispec' else None
+        roof = {"kernel": dom, "ms_per_launch": round(dom_ms, 4)}
+        if alg is not None:
+            ach = alg / (dom_ms * 1e-3) / 1e9
+            roof.update({"bound": "hbm", "achieved": round(ach, 1),
+                         "peak": peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                         "unit": "GB/s", "frac": round(ach / peak, 4),
+                         "algorithmic_bytes": alg})
+        entry = {"s_per_estimate": round(statistics.median(times), 4),
+                 "entries": int(np.asarray(r32['k1_bin' if kind == 'bispec'
+                                               else 'r1_bin']).size),
+                 "kernel_ms": round(sum(v[0] for v in kt.values()), 2),
+                 "top_kernels_ms": {k: round(v[0], 3) for k, v in sorted(
+                     kt.items(), key=lambda kv: -kv[1][0])[:6]},
+                 "roofline_dominant": roof,
+                 "evaluation_grid": list(ctx.stats()['pruned_grid'])}
+        if not args.no_fp64:
+            t0 = time.perf_counter()
+            r64 = est('fp64')
+            torch.cuda.synchronize(dev)
+            entry["fp64_s_per_estimate"] = round(time.perf_counter() - t0, 3)
+            keys = (('bk_raw', 'bk_shot') if kind == 'bispec'
+                    else ('zeta_raw', 'zeta_shot'))
+            entry["max_rel_err_fp32mixed"] = per_bin_err_keys(r32, r64, keys)
+            cnt = 'nmodes_1' if kind == 'bispec' else 'npairs_1'
+            entry["counts_equal"] = bool(np.array_equal(r32[cnt], r64[cnt]))
+        out[name] = entry
+        print(f"# {name}: {json.dumps(entry)}", file=sys.stderr, flush=True)
+    line = {
+        "metric": "large-mesh estimates s/estimate (1024^3, 2e7 lognormal "
+                  "particles, PCS)",
+        "value": out['B000']['s_per_estimate'], "unit": "s/estimate",
+        "higher_is_better": False, "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 meshes / float-float transforms, f64 "
+                 "offsets/reductions",
+        "data": "synthetic lognormal-Poisson box generated on the GPU",
+        "config": {"workload": (f"{n} lognormal-Poisson particles, L=2000 "
+                                "Mpc/h, 1024^3 mesh, PCS; B_000 and B_202 "
+                                "full 40 lin bins 0.005-0.3 h/Mpc; zeta_000 "
+                                "and zeta_110 diag 30 lin bins 10-150 "
+                                "Mpc/h")},
+        "estimates": out,
     }
     print(json.dumps(line), flush=True)
 
@@ -882,6 +1048,8 @@ def main():
         run_mocks(args)
     elif args.workload == 'survey':
         run_survey(args)
+    elif args.workload == 'large':
+        run_large(args)
     else:
         run_gb300(args)
 

@@ -399,6 +399,22 @@ int trvg_bispec_gpp_adjoint(
   const trvg_binning* kbinning, double norm_factor, const double* cotangent,
   double* grad_mesh, double* grad_w, double* grad_pos, trvg_threept_out* out);
 
+/* Vector-Jacobian product of the periodic-box B_000 (degrees 0, 0, 0),
+ * raw AND shot noise; the reference has no derivatives.  The input is
+ * either the particles `data` (mesh = NULL) or a count mesh `mesh` (data
+ * = NULL): ngrid[0] * ngrid[1] * ngrid[2] FP32 values in DEVICE memory,
+ * z fastest, the weight per cell the assignment deposits; its fluctuation
+ * is taken about its own mean, and it has no shot noise.  cot_raw[2 i] =
+ * dL / d Re(raw_i) and, for particles, cot_shot[2 i] = dL / d Re(shot_i)
+ * (NULL: shot noise not differentiated).  Outputs as for
+ * trvg_bispec_gpp_adjoint; grad_mesh in device memory for a mesh input;
+ * grad_w and grad_pos must be NULL for a mesh input. */
+int trvg_bispec_gpp_vjp(
+  trvg_context* ctx, const trvg_params* params, const trvg_catalogue* data,
+  const float* mesh, const trvg_binning* kbinning, double norm_factor,
+  const double* cot_raw, const double* cot_shot, double* grad_mesh,
+  double* grad_w, double* grad_pos, trvg_threept_out* out);
+
 int trvg_compute_bispec_in_gpp_box_batch(
   trvg_context* ctx, const trvg_params* params,
   const trvg_catalogue* particles, int n_mocks, const int64_t* offsets,

@@ -41,6 +41,7 @@ EXPORTED = [
     "trvg_kernel_time_count", "trvg_kernel_time_get",
     "trvg_calc_grid_based_powlaw_norm_noalloc",
     "trvg_compute_bispec_in_gpp_box_batch", "trvg_bispec_gpp_adjoint",
+    "trvg_bispec_gpp_vjp",
     "trvg_compute_3pcf_window", "trvg_tuned_count", "trvg_tuned_get",
     "trvg_hankel_create", "trvg_hankel_info", "trvg_hankel_transform",
     "trvg_hankel_destroy",
@@ -205,6 +206,9 @@ def _declare(lib):
     lib.trvg_bispec_gpp_adjoint.argtypes = [
         vp, P(Params), P(Catalogue), P(BinningC), dp, P(dp), vp, vp, vp,
         P(ThreeptOut)]
+    lib.trvg_bispec_gpp_vjp.argtypes = [
+        vp, P(Params), P(Catalogue), vp, P(BinningC), dp, P(dp), P(dp), vp,
+        vp, vp, P(ThreeptOut)]
     lib.trvg_calc_grid_based_powlaw_norm_noalloc.argtypes = [
         P(Params), P(Catalogue), ip, vp, P(dp)]
     lib.trvg_wigner_3j.argtypes = [ip] * 6

@@ -153,7 +153,82 @@ gather_grad_kernel(Geom g, DevCatalogue cat, const Real* grad, double* gw,
   }
 }
 
+// The weight field of the uncoupled shot-noise terms S_ab = vol_cell
+// sum_x xi(x) j_0(k_a |x|) j_0(k_b |x|) of every pair:
+// W(x) = sum_p mu_p j_0(k_a |x|) j_0(k_b |x|), from a table over the
+// integer keys sx^2 + sy^2 + sz^2 (cubic cells) or evaluated per cell.
+__global__ void shot_weight_table_kernel(int nkeys, double dr,
+                                         SplineTable sj, int np,
+                                         const double* ka, const double* kb,
+                                         const double* mu, double* table) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nkeys;
+       t += gridDim.x * blockDim.x) {
+    const double r = sqrt(double(t)) * dr;
+    double acc = 0.;
+    for (int p = 0; p < np; ++p)
+      acc += mu[p] * spline_eval(sj, ka[p] * r) * spline_eval(sj, kb[p] * r);
+    table[t] = acc;
+  }
+}
+
+template <class Real>
+__global__ void shot_weight_field_kernel(Geom g, const double* table,
+                                         SplineTable sj, int np,
+                                         const double* ka, const double* kb,
+                                         const double* mu, Real* W) {
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.n[2]);
+    const int j = int((t / g.n[2]) % g.n[1]);
+    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
+    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
+              sz = shift_index(k, g.n[2]);
+    if (table != nullptr) {
+      W[t] = Real(table[sx * sx + sy * sy + sz * sz]);
+      continue;
+    }
+    const double rx = double(sx) * g.dr[0], ry = double(sy) * g.dr[1],
+                 rz = double(sz) * g.dr[2];
+    const double r = sqrt(rx * rx + ry * ry + rz * rz);
+    double acc = 0.;
+    for (int p = 0; p < np; ++p)
+      acc += mu[p] * spline_eval(sj, ka[p] * r) * spline_eval(sj, kb[p] * r);
+    W[t] = Real(acc);
+  }
+}
+
 }  // namespace
+
+template <class Real>
+void launch_shot_weight_field(Context& ctx, const Geom& g,
+                              const SplineTable& sj, int np,
+                              const double* ka, const double* kb,
+                              const double* mu, double* table, Real* W) {
+  const bool cubic = g.dr[0] == g.dr[1] && g.dr[1] == g.dr[2];
+  const int nkeys = (g.n[0] / 2) * (g.n[0] / 2) + (g.n[1] / 2) * (g.n[1] / 2) +
+                    (g.n[2] / 2) * (g.n[2] / 2) + 1;
+  if (cubic) {
+    TRVG_KBEGIN(ctx, "shot_weight_table_kernel");
+    shot_weight_table_kernel<<<grid_for(nkeys, 128), 128, 0, ctx.stream>>>(
+        nkeys, g.dr[0], sj, np, ka, kb, mu, table);
+    TRVG_LAUNCHED(ctx);
+  }
+  TRVG_KBEGIN(ctx, "shot_weight_field_kernel");
+  shot_weight_field_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0,
+                                   ctx.stream>>>(g, cubic ? table : nullptr,
+                                                 sj, np, ka, kb, mu, W);
+  TRVG_LAUNCHED(ctx);
+}
+
+template void launch_shot_weight_field<float>(Context&, const Geom&,
+                                              const SplineTable&, int,
+                                              const double*, const double*,
+                                              const double*, double*, float*);
+template void launch_shot_weight_field<double>(Context&, const Geom&,
+                                               const SplineTable&, int,
+                                               const double*, const double*,
+                                               const double*, double*,
+                                               double*);
 
 template <class FR>
 void launch_adjoint_fields(Context& ctx, int64_t ncell, const FR* G,

@@ -2319,8 +2319,91 @@ struct Engine {
   // count mesh m (what the assignment deposits), and the gathered
   // gradients of the particle weights and positions (caller's order).
   // The shell fields are recomputed, not stored from a forward call.
-  void bispec_adjoint(const trvg_catalogue* data, const trvg_binning* kb,
-                      double norm, const double* cot, double* grad_mesh,
+  // Adds the shot-noise part of the mesh gradient's half spectrum to U:
+  // for the cotangents mu_p of norm * shot_p, shot_p = N + S_a(row) +
+  // S_a(col) + S_ab(row, col) (threept.cpp:1974-2140 for degrees 0, 0, 0),
+  // S_a = mean over the statistics modes of bin a of |delta|^2 / C_1 - N
+  // and S_ab = vol_cell sum_x xi(x) j_0(k_a |x|) j_0(k_b |x|).
+  void shot_adjoint(const HostBins& hb, const vector<Pair>& pairs,
+                    const vector<double>& keff, const FieldSpec<Real>& dn,
+                    const FieldSpec<Real>& nf, double norm,
+                    const double* cot_shot, C* U) {
+    const int ndv = int(pairs.size());
+    vector<double> mu(ndv), ca(hb.nb, 0.);
+    for (int i = 0; i < ndv; ++i) {
+      mu[i] = cot_shot[2 * i] * norm;
+      ca[pairs[i].row] += mu[i];
+      ca[pairs[i].col] += mu[i];
+    }
+    // Single-leg terms through the statistics plan of the forward estimate.
+    vector<int> smin, smax;
+    const double dk_sample = 1.e-5;
+    sample_ranges(hb, dk_sample, 1000000, smin, smax);
+    const int smax_all = *std::max_element(smax.begin(), smax.end());
+    const Cube cube = make_cube(double(smax_all + 1) * dk_sample);
+    const StatsPlan& sp = stats_plan(hb, smin, smax, cube, 0, 0);
+    vector<double> fac(hb.nb, 0.);
+    for (int b = 0; b < hb.nb; ++b)
+      if (sp.nmodes[b] != 0) fac[b] = ca[b] / double(sp.nmodes[b]);
+    launch_adjoint_stats<Real, Real>(
+        ctx, g, cube, dn, nf, hb.nb, sp.max_count,
+        static_cast<const int*>(ctx.buffers[sp.tag + ".off"].ptr),
+        static_cast<const uint32_t*>(ctx.buffers[sp.tag + ".list"].ptr),
+        static_cast<const double2*>(ctx.buffers[sp.tag + ".coef"].ptr),
+        upload("adj.sfac", fac), U);
+    // Pair terms: the weight field of all pairs, its spectrum, then U.
+    vector<double> ka(ndv), kbv(ndv);
+    for (int i = 0; i < ndv; ++i) {
+      ka[i] = keff[pairs[i].row];
+      kbv[i] = keff[pairs[i].col];
+    }
+    const int nkeys = (g.n[0] / 2) * (g.n[0] / 2) +
+                      (g.n[1] / 2) * (g.n[1] / 2) +
+                      (g.n[2] / 2) * (g.n[2] / 2) + 1;
+    double* table = ctx.buf<double>("adj.wtab", size_t(nkeys));
+    Real* W = ctx.buf<Real>("adj.W", size_t(g.nmesh));
+    launch_shot_weight_field<Real>(ctx, g, spline(0), ndv,
+                                   upload("adj.ka", ka), upload("adj.kb", kbv),
+                                   upload("adj.mu", mu), table, W);
+    C* Wh = ctx.buf<C>("adj.Wh", size_t(g.nhalf));
+    cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
+    TRVG_CUFFT(cufftSetStream(h, ctx.stream));
+    ctx.kbegin("cufft.r2c.adj");
+    FFT<Real>::r2c(h, W, Wh);
+    ctx.kend();
+    ctx.fft_launches++;
+    launch_adjoint_xi<Real>(ctx, g, Wh, dn, nf, ax, g.vol_cell / g.vol, U);
+  }
+
+  // The count mesh of `mesh_in` (device, FP32, n0 n1 n2 cells of
+  // deposited weight) as a field: its spectrum and its exact sum.
+  Field field_from_mesh(const float* mesh_in) {
+    Field f;
+    Real* m = ctx.buf<Real>("mesh.in", size_t(g.nmesh));
+    launch_mesh_copy<Real>(ctx, mesh_in, g.nmesh, m);
+    double* s = ctx.buf<double>("mesh.in.sum", 1);
+    zero(s, sizeof(double));
+    launch_mesh_sum_pow<Real>(ctx, m, g.nmesh, 1, s);
+    f.sums[0] = download(s, 1)[0];
+    cufftHandle h = ctx.plan(FFT<Real>::kR2C, g.n, 1);
+    C* o = ctx.buf<C>("mesh.in.spec", size_t(g.nhalf));
+    TRVG_CUFFT(cufftSetStream(h, ctx.stream));
+    ctx.kbegin("cufft.r2c.mesh");
+    FFT<Real>::r2c(h, m, o);
+    ctx.kend();
+    ctx.fft_launches++;
+    f.spec.re = o;
+    ++ctx.mesh_gen;
+    return f;
+  }
+
+  // Vector-Jacobian product of the periodic-box B_000 (raw and shot noise)
+  // with respect to the count mesh, the particle weights and positions.
+  // Input: particles (`data`) or a count mesh (`mesh_in`, raw only: the
+  // mesh's own mean is subtracted, so the mesh gradient has zero mean).
+  void bispec_adjoint(const trvg_catalogue* data, const float* mesh_in,
+                      const trvg_binning* kb, double norm, const double* cot,
+                      const double* cot_shot, double* grad_mesh,
                       double* grad_w, double* grad_pos,
                       trvg_threept_out* out) {
     const HostBins hb = host_bins(kb);
@@ -2330,18 +2413,38 @@ struct Engine {
                   "The bispectrum adjoint covers degrees (0, 0, 0) only.");
     if (cot == nullptr)
       throw_error(TRVG_ERR_INVALID_PARAMETER, "Null cotangent.");
+    if ((data == nullptr) == (mesh_in == nullptr))
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "Give either particles or a count mesh.");
+    if (mesh_in != nullptr &&
+        (cot_shot != nullptr || grad_w != nullptr || grad_pos != nullptr))
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "A count mesh has no shot noise or particle gradients.");
+    if (mesh_in != nullptr && interlace)
+      throw_error(TRVG_ERR_INVALID_PARAMETER,
+                  "A count mesh input has no interlacing shadow.");
     const vector<Pair> pairs = dv_pairs(p.shape, hb.nb, p.idx_bin);
     const int ndv = int(pairs.size());
     if (out != nullptr && out->dim != ndv)
       throw_error(TRVG_ERR_INVALID_PARAMETER,
                   "Output data vector has dimension %d, expected %d.",
                   out->dim, ndv);
-    const DevCatalogue raw = upload_catalogue(data, "data", false, false);
-    const DevCatalogue dd = spatially_sorted(raw, "data");
-    TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
-    Field base = make_field("N", {{dd, WeightSpec()}}, false);
-    const double nbar = double(dd.n) / g.vol;
-    const FieldSpec<Real> dn = k0_view(base, -nbar * g.vol);
+    DevCatalogue raw, dd;
+    Field base;
+    FieldSpec<Real> dn, nf;
+    if (mesh_in == nullptr) {
+      raw = upload_catalogue(data, "data", false, false);
+      dd = spatially_sorted(raw, "data");
+      TRVG_CUDA(cudaEventRecord(ctx.ev_h2d, ctx.stream));
+      base = make_field("N", {{dd, WeightSpec()}}, false);
+      const double nbar = double(dd.n) / g.vol;
+      dn = k0_view(base, -nbar * g.vol);
+      nf = k0_view(base, 0.);
+    } else {
+      base = field_from_mesh(mesh_in);
+      dn = k0_view(base, -base.sums[0]);
+      nf = k0_view(base, 0.);
+    }
 
     vector<long long> nmodes;
     vector<double> keff;
@@ -2445,6 +2548,11 @@ struct Engine {
     launch_adjoint_spectrum<Real, Real>(ctx, g, M, K, Kg, Hh, Qh,
                                         upload("adj.lo", lo),
                                         upload("adj.hi", hi), nbl, ax, U);
+    // A count mesh enters through its fluctuation about its own mean: the
+    // k = 0 mode carries no gradient.
+    if (mesh_in != nullptr) zero(U, sizeof(C));
+    if (cot_shot != nullptr)
+      shot_adjoint(hb, pairs, keff, dn, nf, norm, cot_shot, U);
     Real* gm = ctx.buf<Real>("adj.grad", size_t(g.nmesh));
     {
       cufftHandle h = ctx.plan(FFT<Real>::kC2R, g.n, 1);
@@ -2454,8 +2562,9 @@ struct Engine {
       ctx.fft_launches++;
     }
 
-    // Outputs, in the memory kind of the particle arrays.
-    const bool on_dev = data->memory == TRVG_MEM_DEVICE;
+    // Outputs, in the memory kind of the particle arrays (device for a
+    // count mesh input).
+    const bool on_dev = data == nullptr || data->memory == TRVG_MEM_DEVICE;
     const size_t n = size_t(raw.n);
     auto deliver = [&](const double* src, double* dst, size_t count) {
       if (dst == nullptr || count == 0) return;
@@ -2898,9 +3007,25 @@ int trvg_bispec_gpp_adjoint(trvg_context* ctx, const trvg_params* params,
                             double* grad_w, double* grad_pos,
                             trvg_threept_out* out) {
   TRVG_API_BEGIN
+  if (data == nullptr)
+    trvg::throw_error(TRVG_ERR_INVALID_PARAMETER, "Null catalogue.");
   run(ctx, params, false, [&](auto& e) {
-    e.bispec_adjoint(data, kbinning, norm_factor, cotangent, grad_mesh,
-                     grad_w, grad_pos, out);
+    e.bispec_adjoint(data, nullptr, kbinning, norm_factor, cotangent,
+                     nullptr, grad_mesh, grad_w, grad_pos, out);
+  });
+  TRVG_API_END
+}
+
+int trvg_bispec_gpp_vjp(trvg_context* ctx, const trvg_params* params,
+                        const trvg_catalogue* data, const float* mesh,
+                        const trvg_binning* kbinning, double norm_factor,
+                        const double* cot_raw, const double* cot_shot,
+                        double* grad_mesh, double* grad_w, double* grad_pos,
+                        trvg_threept_out* out) {
+  TRVG_API_BEGIN
+  run(ctx, params, false, [&](auto& e) {
+    e.bispec_adjoint(data, mesh, kbinning, norm_factor, cot_raw, cot_shot,
+                     grad_mesh, grad_w, grad_pos, out);
   });
   TRVG_API_END
 }

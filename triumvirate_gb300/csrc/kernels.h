@@ -482,6 +482,29 @@ template <class Real>
 void launch_gather_grad(Context& ctx, const Geom& g, int order,
                         const DevCatalogue& cat, const Real* grad, double* gw,
                         double* gx, double* gy, double* gz);
+// Shot-noise adjoint (ell = 0).  Single-leg terms: U += fac[a] coef d for
+// the listed modes of each two-point statistics bin a (stats plan lists).
+template <class Real, class UR>
+void launch_adjoint_stats(Context& ctx, const Geom& g, const Cube& cube,
+                          const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                          int nbins, int max_count, const int* off,
+                          const uint32_t* list, const double2* coef,
+                          const double* fac, typename CplxOf<UR>::type* U);
+// W(x) = sum_p mu_p j_0(ka_p |x|) j_0(kb_p |x|) on the full mesh (`table`:
+// scratch of one double per integer key for cubic cells).
+template <class Real>
+void launch_shot_weight_field(Context& ctx, const Geom& g,
+                              const SplineTable& sj, int np,
+                              const double* ka, const double* kb,
+                              const double* mu, double* table, Real* W);
+// Pair terms: U += 2 scale FFT[W](k) / C_1(k) delta(k) on the half
+// spectrum (k = 0: the legs' k = 0 values).
+template <class Real>
+void launch_adjoint_xi(Context& ctx, const Geom& g,
+                       const typename CplxOf<Real>::type* Wh,
+                       const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                       const AxisTablesDev& ax, double scale,
+                       typename CplxOf<Real>::type* U);
 
 template <class Real>
 void launch_radial_hist(Context& ctx, const Geom& g, const Real* xi_re,

@@ -1220,6 +1220,109 @@ template void launch_wide_angle<float2>(Context&, const Geom&, float2*,
 template void launch_wide_angle<double2>(Context&, const Geom&, double2*,
                                          double);
 
+// Adjoint of the single-leg shot-noise terms S_a = sum_{k in a} coef(k)
+// fa(k) fb(k)^* / n_a for ell = 0: with fa = fb = delta away from k = 0,
+// dS_a / dm(x) = 2 sum_k coef delta_k e^{ikx} / n_a, so every listed mode
+// of the half spectrum (kz >= 0) adds 2 fac[a] coef(k) delta_k to U, and
+// k = 0 adds fac[a] coef (fa + fb) (the two legs' k = 0 values, which the
+// count mesh moves one for one).  Bins list disjoint modes.
+template <class Modes, class UR>
+__global__ void adjoint_stats_kernel(Geom g, Cube cube, Modes modes,
+                                     const int* off, const uint32_t* list,
+                                     const double2* coef, const double* fac,
+                                     typename CplxOf<UR>::type* U) {
+  const int q = blockIdx.y;
+  const double f = fac[q];
+  if (f == 0.) return;
+  for (int e = off[q] + blockIdx.x * blockDim.x + threadIdx.x; e < off[q + 1];
+       e += gridDim.x * blockDim.x) {
+    const uint32_t t = list[e];
+    int sx, sy, sz;
+    cube_mode(g, cube, t, sx, sy, sz);
+    if (sz < 0) continue;
+    cd va, vb;
+    modes.values(g, sx, sy, sz, va, vb);
+    const double c = coef[t].x;
+    const cd d = (sx == 0 && sy == 0 && sz == 0)
+                     ? cd{va.re + vb.re, va.im + vb.im}
+                     : cd{2. * va.re, 2. * va.im};
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]);
+    auto& u = U[(int64_t(i) * g.n[1] + j) * g.nzh + sz];
+    u.x += UR(f * c * d.re);
+    u.y += UR(f * c * d.im);
+  }
+}
+
+template <class Real, class UR>
+void launch_adjoint_stats(Context& ctx, const Geom& g, const Cube& cube,
+                          const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                          int nbins, int max_count, const int* off,
+                          const uint32_t* list, const double2* coef,
+                          const double* fac, typename CplxOf<UR>::type* U) {
+  if (nbins <= 0 || max_count <= 0) return;
+  const int bx = int(std::min<int64_t>((max_count + 255) / 256, 64));
+  TRVG_KBEGIN(ctx, "adjoint_stats_kernel");
+  adjoint_stats_kernel<SpectrumModes<Real>, UR>
+      <<<dim3(bx, nbins), 256, 0, ctx.stream>>>(
+          g, cube, SpectrumModes<Real>{fa, fb}, off, list, coef, fac, U);
+  TRVG_LAUNCHED(ctx);
+}
+
+template void launch_adjoint_stats<float, float>(
+    Context&, const Geom&, const Cube&, const FieldSpec<float>&,
+    const FieldSpec<float>&, int, int, const int*, const uint32_t*,
+    const double2*, const double*, float2*);
+template void launch_adjoint_stats<double, double>(
+    Context&, const Geom&, const Cube&, const FieldSpec<double>&,
+    const FieldSpec<double>&, int, int, const int*, const uint32_t*,
+    const double2*, const double*, double2*);
+
+// U(k) += 2 scale Wh(k) / C_1(k) delta(k) on the half spectrum: the
+// adjoint of sum_p mu_p S_ab through xi = IFFT[(|delta|^2 / C_1 - S) / V];
+// at k = 0 the two legs' k = 0 values (a0 + b0) replace 2 delta.
+template <class Real>
+__global__ void adjoint_xi_kernel(Geom g,
+                                  const typename CplxOf<Real>::type* Wh,
+                                  FieldSpec<Real> fa, FieldSpec<Real> fb,
+                                  AxisTablesDev ax, double scale,
+                                  typename CplxOf<Real>::type* U) {
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+       t < g.nhalf; t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t % g.nzh);
+    const int j = int((t / g.nzh) % g.n[1]);
+    const int i = int(t / (int64_t(g.nzh) * g.n[1]));
+    const cd va = field_value(fa, g, i, j, k), vb = field_value(fb, g, i, j, k);
+    const cd d = (t == 0) ? cd{va.re + vb.re, va.im + vb.im}
+                          : cd{2. * va.re, 2. * va.im};
+    const double c = scale * double(Wh[t].x) / alias_sn(ax, i, j, k);
+    U[t].x += Real(c * d.re);
+    U[t].y += Real(c * d.im);
+  }
+}
+
+template <class Real>
+void launch_adjoint_xi(Context& ctx, const Geom& g,
+                       const typename CplxOf<Real>::type* Wh,
+                       const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
+                       const AxisTablesDev& ax, double scale,
+                       typename CplxOf<Real>::type* U) {
+  TRVG_KBEGIN(ctx, "adjoint_xi_kernel");
+  adjoint_xi_kernel<Real><<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+      g, Wh, fa, fb, ax, scale, U);
+  TRVG_LAUNCHED(ctx);
+}
+
+template void launch_adjoint_xi<float>(Context&, const Geom&, const float2*,
+                                       const FieldSpec<float>&,
+                                       const FieldSpec<float>&,
+                                       const AxisTablesDev&, double, float2*);
+template void launch_adjoint_xi<double>(Context&, const Geom&,
+                                        const double2*,
+                                        const FieldSpec<double>&,
+                                        const FieldSpec<double>&,
+                                        const AxisTablesDev&, double,
+                                        double2*);
+
 void launch_stats_pk_cube(Context& ctx, const Geom& g, const Cube& cube,
                           const float4* ffcube, int Kc, cd k0a, cd k0b,
                           int nbins, int max_count, const int* off,
