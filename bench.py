@@ -916,9 +916,12 @@ def per_bin_err_keys(a, b, keys):
         mod = np.abs(y)
         rel = np.abs(x - y) / mod
         i = int(np.argmax(rel))
+        big = mod >= 1e-3 * mod.max()
         out[k] = {"max": float(rel[i]), "entry": i,
                   "modulus_over_max": float(mod[i] / mod.max()),
-                  "normwise": float(np.max(np.abs(x - y)) / mod.max())}
+                  "normwise": float(np.max(np.abs(x - y)) / mod.max()),
+                  # entries not 1000x below the largest one
+                  "max_above_1e-3_of_max": float(np.max(rel[big]))}
     return out
 
 
