@@ -608,7 +608,7 @@ __device__ __forceinline__ bool fast_particle(const AssignArgs& a,
 // SH: the interlacing shadow is deposited too (sre != nullptr).  COMP: FP32
 // meshes with compensation meshes (a.lo_off).
 template <int ORDER, class Real, bool SH, bool COMP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, COMP ? 2 : 3)
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
   cd acc = {0., 0.}, acc_s = {0., 0.};
@@ -974,7 +974,7 @@ ylm_weight_sums_kernel(DevCatalogue cat, YlmTargets ts, double* out) {
 }
 
 template <int ORDER, bool SH, bool COMP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, COMP ? 2 : 1)
 assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
   const int64_t np = a.cat.count(), p0 = a.cat.first();
   for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
