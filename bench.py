@@ -74,6 +74,12 @@ def parse_args():
     ap.add_argument('--mesh-comp', type=int, default=2, choices=[0, 1, 2],
                     help='compensated FP32 mesh deposit (library option '
                          '"mesh_comp")')
+    ap.add_argument('--seed', type=int, default=42,
+                    help='seed of the uniform catalogue (metric workload)')
+    ap.add_argument('--ff-transforms', type=int, default=1, choices=[0, 1, 2],
+                    help='float-float transforms of the shell fields: 1 both '
+                         'directions, 2 the forward transform only, 0 none '
+                         '(library option "ff_transforms")')
     ap.add_argument('--assign-path', type=int, default=0, choices=[0, 1, 2],
                     help='deposit of sorted catalogues: 0 autotuned, '
                          '1 shared-memory tiled, 2 per-particle atomics')
@@ -292,7 +298,7 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     box, n, N = args.boxsize, args.npart, args.ngrid
-    x, y, z = make_particles(n, box, seed=42 + rank)
+    x, y, z = make_particles(n, box, seed=args.seed + rank)
     binning = Binning('fourier', 'lin', 0.005, 0.205, args.nbins)
     nbar = n / box ** 3
     norm = 1. / (n * nbar ** 2)        # threept.cpp:96-136, alpha = 1
@@ -300,6 +306,7 @@ def run_gb300(args):
     ctx = _lib.Context(local)
     ctx.set_option('assign_path', args.assign_path)
     ctx.set_option('mesh_comp', args.mesh_comp)
+    ctx.set_option('ff_transforms', args.ff_transforms)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
 
@@ -397,6 +404,7 @@ def run_gb300(args):
     cold = _lib.Context(local)
     cold.set_option('assign_path', args.assign_path)
     cold.set_option('mesh_comp', args.mesh_comp)
+    cold.set_option('ff_transforms', args.ff_transforms)
     cold.set_stream(stream.cuda_stream)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -997,6 +1005,12 @@ def run_large(args):
         dom = max(mine, key=lambda k: mine[k][0])
         dom_ms = mine[dom][0] / mine[dom][1]
         alg = algorithmic_bytes(dom, fa, 4) if kind == 'bispec' else None
+        if dom == 'reduce_pairs_tiled_kernel' and kind == 'bispec':
+            # FP32 real fields on the evaluation grid: G and every field of
+            # both legs (one set when the legs are equal) read once.
+            mc = int(np.prod(ctx.stats()['pruned_grid']))
+            nf = 40 if deg[0] == deg[1] else 80
+            alg = 4 * mc * (1 + nf)
         roof = {"kernel": dom, "ms_per_launch": round(dom_ms, 4)}
         if alg is not None:
             ach = alg / (dom_ms * 1e-3) / 1e9

@@ -205,9 +205,16 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           compensated fields in FP64 (default FP32);
  *   "sort_catalogue"   0/1: order catalogues of >= 65536 particles by mesh
  *                           tile before the deposit (default 1);
- *   "ff_transforms"    0/1: FP32-mixed: compute the spectrum modes of the
- *                           shell fields and the evaluation-grid transforms
- *                           in float-float arithmetic (default 1);
+ *   "ff_transforms"    FP32-mixed periodic-box bispectra with real shell
+ *                           fields: 1 (default) compute the spectrum modes
+ *                           of the shell fields and the evaluation-grid
+ *                           transforms in float-float arithmetic, 2 only
+ *                           the forward transform of the mesh (rounded once
+ *                           to FP32 before FP32 inverse transforms), 0
+ *                           neither;
+ *   "gram_per_pair"    0/1: FP32 shell-field pair sums one data-vector
+ *                           entry per thread instead of the register-tiled
+ *                           Gram form (default 0);
  *   "graph_batch"      0/1: FP32-mixed batches: capture one mock as a CUDA
  *                           graph and replay it for the others (default 1;
  *                           off while profiling);

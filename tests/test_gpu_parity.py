@@ -243,6 +243,10 @@ GPP_CASES = [
     ('3pcf', 'tsc', 32, (0, 0, 0), 'diag', None, (40., 160., 4)),
     ('3pcf', 'cic', 32, (2, 0, 2), 'row', 1, (40., 160., 4)),
     ('3pcf', 'tsc', 32, (1, 1, 0), 'full', None, (40., 160., 3)),
+    # the large-mesh 3PCF's path (PCS, j_l-weighted fields on the full
+    # mesh from the key table, zeta_110 diag) at 64^3
+    ('3pcf', 'pcs', 64, (1, 1, 0), 'diag', None, (20., 150., 5)),
+    ('3pcf', 'pcs', 64, (0, 0, 0), 'diag', None, (20., 150., 5)),
 ]
 
 
@@ -750,6 +754,11 @@ def test_float_float_transforms_match_fp64(bins, degrees, form):
     assert_per_bin(ff, ref, 'bk_raw')
     assert err_ff < 1e-6, err_ff
     assert err_ff < 2. * err_32 + 1e-7, (err_ff, err_32)
+    # Forward transform only in float-float (FP32 inverse transforms).
+    fwd = run('fp32mixed', 2)
+    err_fwd = np.max(np.abs(fwd - ref)) / scale
+    assert err_fwd < 2. * err_32 + 1e-7, (err_fwd, err_32)
+    assert_per_bin(fwd, ref, 'bk_raw', RTOL_FP32_FFT)
 
 
 # ---------------------------------------------------------------------------
@@ -968,3 +977,62 @@ def test_side_stream_shot_noise_matches_one_stream():
     for k in ('bk_raw', 'bk_shot'):
         assert_per_bin(two[k], one[k], k, 2 * RTOL_FP32)
         assert_per_bin(two[k], ref[k], k)
+
+
+# ---------------------------------------------------------------------------
+# Register-tiled Gram form of the FP32 pair sums
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("case", ['survey_b202_full', 'gpp_b000_full_fp32fft',
+                                  'gpp_b202_full_fp32fft', 'gpp_zeta000_diag',
+                                  'gpp_zeta110_full'])
+def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
+    """FP32 pair sums in the register-tiled Gram form (complex survey fields,
+    real periodic-box fields with FP32 transforms, the 3PCF's j_l-weighted
+    fields) equal the one-entry-per-thread form; forms full, triu and diag
+    exercise tiles that hold one, some and all of their field pairs."""
+    ctx = _lib.default_context(None)
+    rng = np.random.default_rng(71)
+    pos = rng.uniform(0., 800., size=(20000, 3))
+    d = rng.uniform(-500., 500., size=(5000, 3))
+    r = rand_catalogue_array
+    kb = Binning('fourier', 'lin', 0.01, 0.12, 11)
+    rb = Binning('config', 'lin', 40., 160., 6)
+
+    def est():
+        if case == 'survey_b202_full':
+            return compute_bispec(
+                ParticleCatalogue(*d.T, nz=3e-9),
+                ParticleCatalogue(r[:, 0], r[:, 1], r[:, 2], nz=r[:, 3]),
+                degrees=(2, 0, 2), binning=kb, form='full',
+                sampling_params=_sampling('fp32mixed', 32, 'pcs'))
+        cat = ParticleCatalogue(*pos.T, nz=len(pos) / 800. ** 3)
+        samp = _sampling('fp32mixed', 48, 'tsc', box=800.)
+        if case.startswith('gpp_b'):
+            deg = (0, 0, 0) if 'b000' in case else (2, 0, 2)
+            return compute_bispec_in_gpp_box(cat, degrees=deg, binning=kb,
+                                             form='full',
+                                             sampling_params=samp)
+        deg = (0, 0, 0) if 'zeta000' in case else (1, 1, 0)
+        form = 'diag' if 'diag' in case else 'full'
+        return compute_3pcf_in_gpp_box(cat, degrees=deg, binning=rb,
+                                       form=form, sampling_params=samp)
+
+    def run(per_pair):
+        ctx.set_option('gram_per_pair', per_pair)
+        ctx.set_option('ff_transforms', 0)
+        try:
+            return est()
+        finally:
+            ctx.set_option('gram_per_pair', 0)
+            ctx.set_option('ff_transforms', 1)
+    tiled, pair = run(0), run(1)
+    keys = ('bk_raw', 'bk_shot') if 'zeta' not in case \
+        else ('zeta_raw', 'zeta_shot')
+    # The two runs deposit the FP32 mesh with atomics in different orders
+    # and transform it with FP32 FFTs: per entry within the FP32-FFT bound,
+    # and normwise to 1e-6 (a wrong tile or slot would differ at O(1)).
+    for k in keys:
+        assert_per_bin(tiled[k], pair[k], (case, k), RTOL_FP32_FFT)
+        scale = np.max(np.abs(pair[k]))
+        assert np.max(np.abs(tiled[k] - pair[k])) <= 1e-6 * scale, (case, k)

@@ -303,7 +303,12 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
   } else if (k == "sort_catalogue") {
     ctx->impl.sort_catalogue = value != 0;
   } else if (k == "ff_transforms") {
-    ctx->impl.ff_transforms = value != 0;
+    if (value < 0 || value > 2)
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "ff_transforms must be 0, 1 or 2.");
+    ctx->impl.ff_transforms = int(value);
+  } else if (k == "gram_per_pair") {
+    ctx->impl.gram_per_pair = value != 0;
   } else if (k == "graph_batch") {
     ctx->impl.graph_batch = value != 0;
   } else if (k == "autotune") {

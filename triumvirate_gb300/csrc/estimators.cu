@@ -74,6 +74,61 @@ struct FFT<double> {
   }
 };
 
+// Transforms per cuFFT plan of a batch of equal 3-d transforms.  cuFFT
+// fails to build a batched plan once the batch holds 2^31 or more padded
+// elements (three 1024^3 C2R transforms return CUFFT_INTERNAL_ERROR), so a
+// larger batch runs as consecutive slices, each under its own cached plan.
+inline int fft_chunk(const int M[3], int nb) {
+  const double n = double(M[0]) * M[1] * (2 * (M[2] / 2 + 1));
+  const int c = int(2147483647.0 / n);
+  return std::max(1, std::min(nb, c));
+}
+
+// nb inverse C2C transforms in place, consecutive fields of M[0] M[1] M[2]
+// modes.  Returns the number of cuFFT executions.
+template <class FR>
+int c2c_inv_batched(Context& ctx, const int M[3], int nb,
+                    typename CplxOf<FR>::type* io) {
+  const size_t Mc = size_t(M[0]) * M[1] * M[2];
+  const int c = fft_chunk(M, nb);
+  int n = 0;
+  for (int b0 = 0; b0 < nb; b0 += c, ++n) {
+    cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, std::min(c, nb - b0));
+    FFT<FR>::c2c_inv(h, io + size_t(b0) * Mc);
+  }
+  return n;
+}
+
+// nb C2R transforms from half spectra to real fields.
+template <class FR>
+int c2r_batched(Context& ctx, const int M[3], int nb,
+                typename CplxOf<FR>::type* in, FR* out) {
+  const size_t Mc = size_t(M[0]) * M[1] * M[2];
+  const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  const int c = fft_chunk(M, nb);
+  int n = 0;
+  for (int b0 = 0; b0 < nb; b0 += c, ++n) {
+    cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, std::min(c, nb - b0));
+    FFT<FR>::c2r(h, in + size_t(b0) * Mh, out + size_t(b0) * Mc);
+  }
+  return n;
+}
+
+// nb R2C transforms from real fields to half spectra.
+template <class FR>
+int r2c_batched(Context& ctx, const int M[3], int nb, FR* in,
+                typename CplxOf<FR>::type* out) {
+  const size_t Mc = size_t(M[0]) * M[1] * M[2];
+  const size_t Mh = size_t(M[0]) * M[1] * (M[2] / 2 + 1);
+  const int c = fft_chunk(M, nb);
+  int n = 0;
+  for (int b0 = 0; b0 < nb; b0 += c, ++n) {
+    cufftHandle h = ctx.plan(FFT<FR>::kR2C, M, std::min(c, nb - b0));
+    FFT<FR>::r2c(h, in + size_t(b0) * Mc, out + size_t(b0) * Mh);
+  }
+  return n;
+}
+
 // ---------------------------------------------------------------------------
 // Host helpers.
 // ---------------------------------------------------------------------------
@@ -1440,11 +1495,33 @@ struct Engine {
       launch_build_F<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo,
                                dhi, nb, hmax, out, disjoint(lo, hi));
     }
-    cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, nb);
     ctx.kbegin("cufft.c2c.F");
-    FFT<FR>::c2c_inv(h, out);
+    ctx.fft_launches += c2c_inv_batched<FR>(ctx, M, nb, out);
     ctx.kend();
-    ctx.fft_launches++;
+  }
+
+  // Tiles of the register-tiled Gram form that hold at least one pair
+  // (pa[q], pb[q]) and the entry of each field pair; false when the form
+  // does not apply (fields beyond its staged chunk, a repeated pair).
+  static bool gram_tile_list(bool cplx, int na, int nb, const vector<int>& pa,
+                             const vector<int>& pb, vector<int2>& tiles,
+                             vector<int>& slot) {
+    if (!gram_tiled_fits(cplx, na, nb)) return false;
+    const GramTile t = gram_tile(cplx);
+    const int ta = (na + t.ti - 1) / t.ti, tb = (nb + t.tj - 1) / t.tj;
+    slot.assign(size_t(na) * nb, -1);
+    vector<char> used(size_t(ta) * tb, 0);
+    for (size_t q = 0; q < pa.size(); ++q) {
+      int& s = slot[size_t(pa[q]) * nb + pb[q]];
+      if (s >= 0) return false;
+      s = int(q);
+      used[size_t(pa[q] / t.ti) * tb + pb[q] / t.tj] = 1;
+    }
+    tiles.clear();
+    for (int i = 0; i < ta; ++i)
+      for (int j = 0; j < tb; ++j)
+        if (used[size_t(i) * tb + j]) tiles.push_back(make_int2(i, j));
+    return !tiles.empty();
   }
 
   // True when no two bins [lo, hi) overlap.
@@ -1550,11 +1627,9 @@ struct Engine {
         launch_build_F_half<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m,
                                       dlo, dhi, nb, hmax, H);
     }
-    cufftHandle h = ctx.plan(FFT<FR>::kC2R, M, nb);
     ctx.kbegin("cufft.c2r.F");
-    FFT<FR>::c2r(h, H, out);
+    ctx.fft_launches += c2r_batched<FR>(ctx, M, nb, H, out);
     ctx.kend();
-    ctx.fft_launches++;
   }
 
   // Shell fields and G are real when both legs have m = 0 and even ell and
@@ -1628,16 +1703,9 @@ struct Engine {
     int64_t gen = -1;
   } ff_cube;
 
-  // Pair sums with float-float transforms: the source mesh's spectrum on
-  // the cube |s| <= 2K, G and the shell fields of both legs evaluated from
-  // it, then the same real-field reduction.
-  vector<cplx> pair_sums_ff(const FieldSpec<Real>& src, const Leg& la,
-                            const Leg& lb, const vector<Pair>& pairs,
-                            const HostBins& hb, const int M[3],
-                            const int K[3]) {
-    const int k = K[0], kg = 2 * k;
-    const int np = int(pairs.size());
-    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+  // Spectrum of the source's FP32 mesh on the cube |sx|, |sy| <= kg,
+  // 0 <= sz <= kg by the float-float z, y and x passes.
+  const float4* ff_forward(const FieldSpec<Real>& src, int kg) {
     float4* T1 = ctx.buf<float4>(
         "ff.T1", size_t(g.n[0]) * (kg + 1) * g.n[1]);
     float4* T2 = ctx.buf<float4>(
@@ -1648,6 +1716,38 @@ struct Engine {
                            reinterpret_cast<const float*>(src.mesh_lo), kg,
                            T1, T2, cube);
     ff_cube = {cube, kg, src.re, src.mesh_gen};
+    return cube;
+  }
+
+  // The source with its spectrum replaced by the float-float forward
+  // transform rounded once to FP32 (the modes |s| <= 2K the shell fields and
+  // G read), for the FP32 inverse transforms of ff_transforms = 2.
+  FieldSpec<Real> ff_spectrum_f32(const FieldSpec<Real>& src, const int K[3]) {
+    FieldSpec<Real> s = src;
+    if constexpr (sizeof(Real) == 4) {
+      const int kg = 2 * K[0];
+      const float4* cube = ff_forward(src, kg);
+      float2* h = ctx.buf<float2>("ffwd.spec", size_t(g.nhalf));
+      launch_ff_cube_to_half(ctx, g, cube, kg, h);
+      s.re = h;
+      s.mesh = nullptr;
+      s.mesh_lo = nullptr;
+      s.mesh_gen = -1;
+    }
+    return s;
+  }
+
+  // Pair sums with float-float transforms: the source mesh's spectrum on
+  // the cube |s| <= 2K, G and the shell fields of both legs evaluated from
+  // it, then the same real-field reduction.
+  vector<cplx> pair_sums_ff(const FieldSpec<Real>& src, const Leg& la,
+                            const Leg& lb, const vector<Pair>& pairs,
+                            const HostBins& hb, const int M[3],
+                            const int K[3]) {
+    const int k = K[0], kg = 2 * k;
+    const int np = int(pairs.size());
+    const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
+    const float4* cube = ff_forward(src, kg);
 
     const bool shared = la.ell == lb.ell && la.m == lb.m;
     vector<int> A, B;
@@ -1759,8 +1859,15 @@ struct Engine {
     vector<cplx> res(np, cplx(0., 0.));
     const bool real = real_fields(src, gsrc, la, lb, M);
     if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
-      if (real && ff_applicable(src, gsrc, la, lb, pairs, hb, M, K))
+      if (real && ff_applicable(src, gsrc, la, lb, pairs, hb, M, K)) {
+        if (ctx.ff_transforms == 2) {
+          // Forward transform only in float-float; batches run eagerly
+          // (ff_taken stays false).
+          const FieldSpec<Real> s2 = ff_spectrum_f32(src, K);
+          return pair_sums_t<FR>(s2, s2, la, lb, pairs, hb, radii, M, K, Kg);
+        }
         return pair_sums_ff(src, la, lb, pairs, hb, M, K);
+      }
     }
     if (replay == nullptr) ff_taken = false;
     const FC* G = real ? nullptr : build_G<FR>(gsrc, M, Kg);
@@ -1867,7 +1974,28 @@ struct Engine {
         const int* dpb = upload("pairs.b", pb);
         double* dout = ctx.buf<double>("pairs.out", 2 * idx.size());
         zero(dout, 2 * idx.size() * sizeof(double));
-        if (real)
+        bool tiled = false;
+        if constexpr (sizeof(FR) == 4) {
+          vector<int2> tl;
+          vector<int> slot;
+          if (!ctx.gram_per_pair &&
+              gram_tile_list(!real, int(bA.size()), int(bB.size()), pa, pb,
+                             tl, slot)) {
+            const int2* dt = upload("gram.tiles", tl);
+            const int* ds = upload("gram.slot", slot);
+            launch_reduce_pairs_tiled(
+                ctx, Mc, !real,
+                real ? Gr : reinterpret_cast<const float*>(G),
+                real ? FAr : reinterpret_cast<const float*>(FA),
+                int(bA.size()),
+                real ? FBr : reinterpret_cast<const float*>(FB),
+                int(bB.size()), dt, int(tl.size()), ds, dout);
+            tiled = true;
+          }
+        }
+        if (tiled)
+          ;
+        else if (real)
           launch_reduce_pairs_real<FR>(ctx, Mc, Gr, FAr, FBr, dpa, dpb,
                                        int(idx.size()), dout, int(bA.size()),
                                        int(bB.size()));
@@ -2528,15 +2656,14 @@ struct Engine {
     C* Hh = ctx.buf<C>("adj.Hh", size_t(nbl) * Mh);
     C* Qh = ctx.buf<C>("adj.Qh", Mh);
     {
-      cufftHandle h = ctx.plan(FFT<Real>::kR2C, M, nbl);
       ctx.kbegin("cufft.r2c.adj");
-      FFT<Real>::r2c(h, H, Hh);
+      ctx.fft_launches += r2c_batched<Real>(ctx, M, nbl, H, Hh);
       ctx.kend();
       cufftHandle h1 = ctx.plan(FFT<Real>::kR2C, M, 1);
       ctx.kbegin("cufft.r2c.adj");
       FFT<Real>::r2c(h1, Q, Qh);
       ctx.kend();
-      ctx.fft_launches += 2;
+      ctx.fft_launches += 1;
     }
     vector<double> lo(nbl), hi(nbl);
     for (int a = 0; a < nbl; ++a) {

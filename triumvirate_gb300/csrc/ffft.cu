@@ -893,6 +893,33 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
   });
 }
 
+// The cube's modes rounded once to FP32, written at their places in a half
+// spectrum of the mesh (the R2C output layout); entries off the cube are
+// left as they are.
+__global__ void ff_cube_to_half_kernel(Geom g, const float4* cube, int Kg,
+                                       float2* h) {
+  const int w = 2 * Kg + 1;
+  const int64_t count = int64_t(w) * w * (Kg + 1);
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int sz = int(t % (Kg + 1));
+    const int64_t r = t / (Kg + 1);
+    const int sy = int(r % w) - Kg, sx = int(r / w) - Kg;
+    const float4 v = cube[t];
+    h[(int64_t(wrapi(sx, g.n[0])) * g.n[1] + wrapi(sy, g.n[1])) * g.nzh +
+      sz] = make_float2(v.x + v.y, v.z + v.w);
+  }
+}
+
+void launch_ff_cube_to_half(Context& ctx, const Geom& g, const float4* cube,
+                            int Kg, float2* h) {
+  const int64_t count = int64_t(2 * Kg + 1) * (2 * Kg + 1) * (Kg + 1);
+  TRVG_KBEGIN(ctx, "ff_cube_to_half_kernel");
+  ff_cube_to_half_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, cube, Kg, h);
+  TRVG_LAUNCHED(ctx);
+}
+
 void launch_ff_build_G(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, const float2* const iw[3],
                        cd k0, float4* E, const double* k0_dev) {

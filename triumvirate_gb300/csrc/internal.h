@@ -140,8 +140,12 @@ struct Context {
   bool shell_fields_fp64 = false;
   // Order large catalogues by mesh tile before the deposit.
   bool sort_catalogue = true;
-  // FP32-mixed: float-float transforms of the shell fields.
-  bool ff_transforms = true;
+  // FP32-mixed: float-float transforms of the shell fields (0 none, 1 both
+  // directions, 2 the forward transform of the mesh only).
+  int ff_transforms = 1;
+  // FP32 pair sums one pair per thread instead of the register-tiled Gram
+  // form (a comparison switch; both accumulate in float-float).
+  bool gram_per_pair = false;
   // Batches: replay one captured mock as a CUDA graph (batch.cu).
   bool graph_batch = true;
   // Autotuner: launch shapes picked by timing (tile side of the catalogue

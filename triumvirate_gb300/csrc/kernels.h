@@ -348,6 +348,24 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
                               double* out /* 2 * npairs, imaginary 0 */, int na = 0,
                               int nb = 0);
 
+// Register-tiled Gram form for FP32 fields (real: float, complex: float2
+// stored as float pairs).  One thread accumulates a tile of ti leg-a by tj
+// leg-b fields; `tiles` lists the (a / ti, b / tj) tiles that hold at least
+// one data-vector entry and slot[a * nb + b] is the entry of field pair
+// (a, b), -1 when it has none.
+struct GramTile {
+  int ti, tj;
+};
+inline GramTile gram_tile(bool cplx) {
+  return cplx ? GramTile{2, 4} : GramTile{4, 8};
+}
+bool gram_tiled_fits(bool cplx, int na, int nb);
+void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
+                               const float* G, const float* Fa, int na,
+                               const float* Fb, int nb, const int2* tiles,
+                               int ntiles, const int* slot,
+                               double* out /* 2 per entry */);
+
 // ---- ffft.cu -------------------------------------------------------------
 // Float-float transforms of the shell fields: a plan is the radix list of
 // the length and its twiddle table (cos, sin of 2 pi k / n, float-float).
@@ -371,6 +389,10 @@ struct FFPlan {
   const float4* tw;
 };
 bool ff_length_ok(int n);
+// The cube's modes (|sx|, |sy| <= Kg, 0 <= sz <= Kg) rounded to FP32 into
+// the half spectrum h of the mesh (other entries untouched).
+void launch_ff_cube_to_half(Context& ctx, const Geom& g, const float4* cube,
+                            int Kg, float2* h);
 FFPlan ff_plan(Context& ctx, int n);
 // Spectrum of the FP32 mesh on the cube |sx|, |sy| <= Kg, 0 <= sz <= Kg:
 // cube[sx + Kg][sy + Kg][sz] (T1, T2: scratch of n0 (Kg+1) n1 and

@@ -268,6 +268,152 @@ reduce_pairs_gram_real_kernel(int64_t ncell, const float* G, const float* Fa,
   }
 }
 
+// Register-tiled Gram form of the pair sums for FP32 fields.  A block
+// stages CELLS cells of every leg-a field (F_a) and of every leg-b field
+// times G (F_b G) in shared memory, cell-major, so that a thread reads the
+// TI leg-a and TJ leg-b values of one cell as 16-byte vectors and updates a
+// TI x TJ tile of field pairs from them (TI + TJ loads for TI TJ products;
+// the per-pair form needs two loads per product).  Every field is read
+// from HBM once per launch.  The products of kGramRun cells are summed in
+// FP32 and then added to float-float accumulators (TwoSum), so the
+// accumulated sum keeps the error of an FP32 sum of kGramRun terms per run
+// rather than of the whole grid.  The threads of a tile split the chunk's
+// cells into slices; the slices are summed in FP64 at the end and each
+// data-vector entry gets one atomic add per block.
+constexpr int kGramRun = 8;
+constexpr int kGramThreads = 256;
+
+template <bool CPLX, int TI, int TJ, int CELLS>
+__global__ void __launch_bounds__(kGramThreads, 2)
+reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
+                          const float* __restrict__ Fa, int na, int rsa,
+                          const float* __restrict__ Fb, int nb, int rsb,
+                          const int2* __restrict__ tiles, int ntiles,
+                          const int* __restrict__ slot, double* out) {
+  constexpr int W = CPLX ? 2 : 1;  // floats per value
+  constexpr int NP = TI * TJ * W;  // partial sums per thread
+  extern __shared__ float4 gsm4[];
+  float* As = reinterpret_cast<float*>(gsm4);  // [CELLS][rsa] values
+  float* Bs = As + CELLS * rsa * W;            // [CELLS][rsb] values
+  const int g0 = blockIdx.y * kGramThreads;    // this block's tile group
+  const int T = min(kGramThreads, ntiles - g0);
+  const int S = kGramThreads / T;
+  const int tid = threadIdx.x;
+  const bool active = tid < S * T;
+  const int tile = tid % T, slice = tid / T;
+  int i0 = 0, j0 = 0;
+  if (active) {
+    const int2 tl = tiles[g0 + tile];
+    i0 = tl.x * TI;
+    j0 = tl.y * TJ;
+  }
+  float p[NP];
+  FF acc[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    p[q] = 0.f;
+    acc[q] = ff_zero();
+  }
+  int run = 0;
+  const int nrow = rsa + rsb;
+  for (int64_t c0 = int64_t(blockIdx.x) * CELLS; c0 < ncell;
+       c0 += int64_t(gridDim.x) * CELLS) {
+    __syncthreads();  // the previous chunk is consumed
+    for (int w = tid; w < nrow * CELLS; w += kGramThreads) {
+      const int row = w / CELLS, c = w - row * CELLS;
+      const int64_t cell = c0 + c;
+      if constexpr (CPLX) {
+        float2 v = make_float2(0.f, 0.f);
+        if (row < rsa) {
+          if (row < na && cell < ncell)
+            v = reinterpret_cast<const float2*>(Fa)[int64_t(row) * ncell +
+                                                    cell];
+          reinterpret_cast<float2*>(As)[c * rsa + row] = v;
+        } else {
+          const int r = row - rsa;
+          if (r < nb && cell < ncell)
+            v = cmulc(
+                reinterpret_cast<const float2*>(Fb)[int64_t(r) * ncell + cell],
+                reinterpret_cast<const float2*>(G)[cell]);
+          reinterpret_cast<float2*>(Bs)[c * rsb + r] = v;
+        }
+      } else {
+        float v = 0.f;
+        if (row < rsa) {
+          if (row < na && cell < ncell) v = Fa[int64_t(row) * ncell + cell];
+          As[c * rsa + row] = v;
+        } else {
+          const int r = row - rsa;
+          if (r < nb && cell < ncell)
+            v = Fb[int64_t(r) * ncell + cell] * G[cell];
+          Bs[c * rsb + r] = v;
+        }
+      }
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cend = ncell - c0 < CELLS ? int(ncell - c0) : CELLS;
+    for (int c = slice; c < cend; c += S) {
+      float a[TI * W], b[TJ * W];
+      const float4* va =
+          reinterpret_cast<const float4*>(As + (c * rsa + i0) * W);
+      const float4* vb =
+          reinterpret_cast<const float4*>(Bs + (c * rsb + j0) * W);
+#pragma unroll
+      for (int v = 0; v < TI * W / 4; ++v)
+        reinterpret_cast<float4*>(a)[v] = va[v];
+#pragma unroll
+      for (int v = 0; v < TJ * W / 4; ++v)
+        reinterpret_cast<float4*>(b)[v] = vb[v];
+#pragma unroll
+      for (int i = 0; i < TI; ++i)
+#pragma unroll
+        for (int j = 0; j < TJ; ++j) {
+          if constexpr (CPLX) {
+            float& re = p[2 * (i * TJ + j)];
+            float& im = p[2 * (i * TJ + j) + 1];
+            re = fmaf(a[2 * i], b[2 * j], re);
+            re = fmaf(-a[2 * i + 1], b[2 * j + 1], re);
+            im = fmaf(a[2 * i], b[2 * j + 1], im);
+            im = fmaf(a[2 * i + 1], b[2 * j], im);
+          } else {
+            p[i * TJ + j] = fmaf(a[i], b[j], p[i * TJ + j]);
+          }
+        }
+      if (++run == kGramRun) {
+        run = 0;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          ff_add(acc[q], p[q]);
+          p[q] = 0.f;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q) ff_add(acc[q], p[q]);
+  __syncthreads();  // the staging buffer becomes the slice table
+  double* red = reinterpret_cast<double*>(gsm4);  // [S][T][NP]
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+      red[(slice * T + tile) * NP + q] = ff_value(acc[q]);
+  }
+  __syncthreads();
+  for (int w = tid; w < T * NP; w += kGramThreads) {
+    const int tl = w / NP, q = w - tl * NP;
+    double s = 0.;
+    for (int u = 0; u < S; ++u) s += red[(u * T + tl) * NP + q];
+    const int2 tt = tiles[g0 + tl];
+    const int pr = q / W, comp = q - pr * W;
+    const int i = tt.x * TI + pr / TJ, j = tt.y * TJ + pr % TJ;
+    if (i < na && j < nb) {
+      const int sl = slot[int64_t(i) * nb + j];
+      if (sl >= 0) atomicAdd(out + 2 * int64_t(sl) + comp, s);
+    }
+  }
+}
+
 // Real fields: sum_x F_a F_b G; the imaginary part of the output is left
 // at zero.
 template <class Real>
@@ -1021,6 +1167,75 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
   reduce_pairs_real_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
       ncell, G, Fa, Fb, pa, pb, npairs, out);
   TRVG_LAUNCHED(ctx);
+}
+
+namespace {
+
+// Cells per staged chunk, values per staged row and shared memory of the
+// tiled Gram form.
+int gram_cells(bool cplx) { return cplx ? 64 : 128; }
+
+void gram_rows(bool cplx, int na, int nb, int& rsa, int& rsb) {
+  const GramTile t = gram_tile(cplx);
+  // Rows padded to whole tiles and 16-byte vectors.
+  const int va = cplx ? 2 : 4;
+  rsa = (na + t.ti - 1) / t.ti * t.ti;
+  rsa = (rsa + va - 1) / va * va;
+  rsb = (nb + t.tj - 1) / t.tj * t.tj;
+  rsb = (rsb + va - 1) / va * va;
+}
+
+size_t gram_smem(bool cplx, int na, int nb) {
+  int rsa, rsb;
+  gram_rows(cplx, na, nb, rsa, rsb);
+  const GramTile t = gram_tile(cplx);
+  const int w = cplx ? 2 : 1;
+  const size_t stage = size_t(gram_cells(cplx)) * (rsa + rsb) * w * 4;
+  const size_t red = size_t(kGramThreads) * t.ti * t.tj * w * 8;
+  return std::max(stage, red);
+}
+
+constexpr size_t kGramSmemMax = 112 * 1024;  // two blocks per SM
+
+}  // namespace
+
+bool gram_tiled_fits(bool cplx, int na, int nb) {
+  return na > 0 && nb > 0 && gram_smem(cplx, na, nb) <= kGramSmemMax;
+}
+
+void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
+                               const float* G, const float* Fa, int na,
+                               const float* Fb, int nb, const int2* tiles,
+                               int ntiles, const int* slot, double* out) {
+  if (ntiles <= 0 || ncell <= 0) return;
+  if (!gram_tiled_fits(cplx, na, nb))
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Tiled pair sums: %d x %d fields exceed the staged chunk.",
+                na, nb);
+  int rsa, rsb;
+  gram_rows(cplx, na, nb, rsa, rsb);
+  const size_t smem = gram_smem(cplx, na, nb);
+  const int cells = gram_cells(cplx);
+  const int64_t chunks = (ncell + cells - 1) / cells;
+  dim3 grid(unsigned(std::min<int64_t>(chunks, 152 * 2)),
+            unsigned((ntiles + kGramThreads - 1) / kGramThreads));
+  auto go = [&](auto kernel) {
+    static bool configured[64] = {};
+    if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+      TRVG_CUDA(cudaFuncSetAttribute(
+          kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+          int(kGramSmemMax)));
+      if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+    }
+    TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
+    kernel<<<grid, kGramThreads, smem, ctx.stream>>>(
+        ncell, G, Fa, na, rsa, Fb, nb, rsb, tiles, ntiles, slot, out);
+    TRVG_LAUNCHED(ctx);
+  };
+  if (cplx)
+    go(reduce_pairs_tiled_kernel<true, 2, 4, 64>);
+  else
+    go(reduce_pairs_tiled_kernel<false, 4, 8, 128>);
 }
 
 void launch_reduce_pairs_ff(Context& ctx, int64_t ncell, int64_t ld,

@@ -720,6 +720,76 @@ __global__ void build_F_sjl_half_kernel(Geom g, FieldSpec<Real> f,
   }
 }
 
+// FP32 fields of meshes whose three axes share one fundamental frequency
+// dk: |k| = dk sqrt(key), key = sx^2 + sy^2 + sz^2, so j_l(k r_q) is one
+// table entry per (key, radius) instead of one spline evaluation (FP64,
+// with the upward recurrence beyond the spline) per mode and radius.
+__global__ void sjl_key_table_kernel(double dk, int64_t nkeys, SjlArgs sa,
+                                     float* jt /* [nkeys][nb] */) {
+  const int64_t count = nkeys * sa.nb;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t key = t / sa.nb;
+    const int q = int(t - key * sa.nb);
+    const double k = dk * sqrt(double(key));
+    jt[t] = float(spline_eval(sa.sj, k * sa.radii[q]));
+  }
+}
+
+// j_l(k r_q) y_lm(k) f(k) / W(k) / V from the key table: the mode's value
+// is formed in FP64 and rounded once, each field entry is one FP32 product.
+template <class Real, bool HALF>
+__global__ void build_F_sjl_key_kernel(Geom g, FieldSpec<Real> f,
+                                       AxisTablesDev ax, int ell, int m,
+                                       int nb, const float* __restrict__ jt,
+                                       double inv_vol, float2* out) {
+  const int64_t count = HALF ? g.nhalf : g.nmesh;
+  const int nz = HALF ? g.nzh : g.n[2];
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int kk = int(t % nz);
+    const int j = int((t / nz) % g.n[1]);
+    const int i = int(t / (int64_t(nz) * g.n[1]));
+    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
+              sz = shift_index(kk, g.n[2]);
+    const double kx = dmul(double(sx), g.dk[0]);
+    const double ky = dmul(double(sy), g.dk[1]);
+    const double kz = dmul(double(sz), g.dk[2]);
+    const cd v = field_value(f, g, i, j, kk);
+    const double w = window_pow(ax, i, j, kk);
+    const cd y = reduced_ylm(ell, m, kx, ky, kz);
+    const cd val = y * cdivr(v, w);
+    const float vr = float(val.re * inv_vol), vi = float(val.im * inv_vol);
+    const int64_t key = int64_t(sx) * sx + int64_t(sy) * sy + int64_t(sz) * sz;
+    const float* row = jt + key * nb;
+    for (int q = 0; q < nb; ++q) {
+      const float jl = row[q];
+      out[int64_t(q) * count + t] = make_float2(vr * jl, vi * jl);
+    }
+  }
+}
+
+// Key-table form: FP32 fields, one fundamental frequency on all axes.
+template <class Real, class FR>
+bool sjl_key_form(Context& ctx, const Geom& g, const SplineTable& sj,
+                  const double* radii, int nb, int64_t& nkeys, float*& jt) {
+  if constexpr (sizeof(FR) != 4) {
+    return false;
+  } else {
+    if (g.dk[0] != g.dk[1] || g.dk[1] != g.dk[2]) return false;
+    nkeys = 1;
+    for (int a = 0; a < 3; ++a) nkeys += int64_t(g.n[a] / 2) * (g.n[a] / 2);
+    if (nkeys * nb > (int64_t(1) << 30)) return false;
+    jt = ctx.buf<float>("sjl.keys", size_t(nkeys) * nb);
+    SjlArgs sa{sj, radii, nb};
+    TRVG_KBEGIN(ctx, "sjl_key_table_kernel");
+    sjl_key_table_kernel<<<grid_for(nkeys * nb, 256), 256, 0, ctx.stream>>>(
+        g.dk[0], nkeys, sa, jt);
+    TRVG_LAUNCHED(ctx);
+    return true;
+  }
+}
+
 // Fine-binned two-point statistics (field.cpp:2586-2702).  Each mode goes
 // to fine sample int(k / 1e-5); bin b collects samples i with
 // lo_b <= i * 1e-5 < hi_b (precomputed as [smin_b, smax_b)).
@@ -1073,6 +1143,17 @@ void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const AxisTablesDev& ax, int ell, int m,
                         const SplineTable& sj, const double* radii, int nb,
                         typename CplxOf<FR>::type* out) {
+  int64_t nkeys = 0;
+  float* jt = nullptr;
+  if (sjl_key_form<Real, FR>(ctx, g, sj, radii, nb, nkeys, jt)) {
+    TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
+    build_F_sjl_key_kernel<Real, false>
+        <<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+            g, f, ax, ell, m, nb, jt, 1. / g.vol,
+            reinterpret_cast<float2*>(out));
+    TRVG_LAUNCHED(ctx);
+    return;
+  }
   SjlArgs sa{sj, radii, nb};
   TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
   build_F_sjl_kernel<Real, FR><<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
@@ -1419,6 +1500,17 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
                              int ell, int m, const SplineTable& sj,
                              const double* radii, int nb,
                              typename CplxOf<FR>::type* out) {
+  int64_t nkeys = 0;
+  float* jt = nullptr;
+  if (sjl_key_form<Real, FR>(ctx, g, sj, radii, nb, nkeys, jt)) {
+    TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
+    build_F_sjl_key_kernel<Real, true>
+        <<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+            g, f, ax, ell, m, nb, jt, 1. / g.vol,
+            reinterpret_cast<float2*>(out));
+    TRVG_LAUNCHED(ctx);
+    return;
+  }
   SjlArgs sa{sj, radii, nb};
   TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
   build_F_sjl_half_kernel<Real, FR><<<grid_for(g.nhalf, 256), 256, 0,
