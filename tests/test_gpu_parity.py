@@ -757,7 +757,7 @@ def test_float_float_transforms_match_fp64(bins, degrees, form):
     # Forward transform only in float-float (FP32 inverse transforms).
     fwd = run('fp32mixed', 2)
     err_fwd = np.max(np.abs(fwd - ref)) / scale
-    assert err_fwd < 2. * err_32 + 1e-7, (err_fwd, err_32)
+    assert err_fwd < 1e-6, (err_fwd, err_32)
     assert_per_bin(fwd, ref, 'bk_raw', RTOL_FP32_FFT)
 
 
@@ -1019,20 +1019,27 @@ def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
                                        form=form, sampling_params=samp)
 
     def run(per_pair):
+        # Compensated, renormalised deposits: both runs transform the same
+        # correctly rounded FP32 meshes whatever the order of the atomics.
         ctx.set_option('gram_per_pair', per_pair)
         ctx.set_option('ff_transforms', 0)
+        ctx.set_option('mesh_comp', 1)
+        ctx.set_option('mesh_renorm', 1)
         try:
             return est()
         finally:
             ctx.set_option('gram_per_pair', 0)
             ctx.set_option('ff_transforms', 1)
+            ctx.set_option('mesh_comp', 2)
+            ctx.set_option('mesh_renorm', 0)
     tiled, pair = run(0), run(1)
     keys = ('bk_raw', 'bk_shot') if 'zeta' not in case \
         else ('zeta_raw', 'zeta_shot')
-    # The two runs deposit the FP32 mesh with atomics in different orders
-    # and transform it with FP32 FFTs: per entry within the FP32-FFT bound,
-    # and normwise to 1e-6 (a wrong tile or slot would differ at O(1)).
+    # The forms differ in the FP32 partial sums of the tiled one: per entry
+    # within the FP32-FFT bound, normwise to 2e-6 (a wrong tile or slot
+    # would differ at O(1)).
     for k in keys:
         assert_per_bin(tiled[k], pair[k], (case, k), RTOL_FP32_FFT)
         scale = np.max(np.abs(pair[k]))
-        assert np.max(np.abs(tiled[k] - pair[k])) <= 1e-6 * scale, (case, k)
+        assert np.max(np.abs(tiled[k] - pair[k])) <= 2e-6 * scale, (
+            case, k, float(np.max(np.abs(tiled[k] - pair[k])) / scale))

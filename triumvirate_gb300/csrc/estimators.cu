@@ -1453,7 +1453,14 @@ struct Engine {
     using FC = typename CplxOf<FR>::type;
     const int64_t Mc = int64_t(M[0]) * M[1] * M[2];
     FC* G = ctx.buf<FC>("G", size_t(Mc));
-    launch_build_G<Real, FR>(ctx, g, M, Kg, f, ax, G);
+    bool done = false;
+    if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
+      if (f.re_s == nullptr) {
+        launch_build_G_f32(ctx, g, M, Kg, f, inv_win_f, G);
+        done = true;
+      }
+    }
+    if (!done) launch_build_G<Real, FR>(ctx, g, M, Kg, f, ax, G);
     cufftHandle h = ctx.plan(FFT<FR>::kC2C, M, 1);
     ctx.kbegin("cufft.c2c.G");
     FFT<FR>::c2c_inv(h, G);
@@ -1481,7 +1488,7 @@ struct Engine {
       for (int i = 0; i < nb; ++i) r[i] = radii[bins[i]];
       const double* dr = upload(tag + ".r", r);
       launch_build_F_sjl<Real, FR>(ctx, g, src, ax, leg.ell, leg.m, leg.sj,
-                                   dr, nb, out);
+                                   dr, nb, out, inv_win_f);
     } else {
       vector<double> lo(nb), hi(nb);
       double hmax = 0.;
@@ -1492,8 +1499,19 @@ struct Engine {
       }
       const double* dlo = upload(tag + ".lo", lo);
       const double* dhi = upload(tag + ".hi", hi);
-      launch_build_F<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo,
-                               dhi, nb, hmax, out, disjoint(lo, hi));
+      bool done = false;
+      if constexpr (sizeof(Real) == 4 && sizeof(FR) == 4) {
+        if (src.re_s == nullptr && leg.ell <= kMaxYlmDegree &&
+            disjoint(lo, hi)) {
+          const int16_t* tab = shell_table(M, K, lo, hi, dlo, dhi, hmax);
+          launch_build_F_tab_f32(ctx, g, M, tab, src, inv_win_f, leg.ell,
+                                 leg.m, nb, out);
+          done = true;
+        }
+      }
+      if (!done)
+        launch_build_F<Real, FR>(ctx, g, M, K, src, ax, leg.ell, leg.m, dlo,
+                                 dhi, nb, hmax, out, disjoint(lo, hi));
     }
     ctx.kbegin("cufft.c2c.F");
     ctx.fft_launches += c2c_inv_batched<FR>(ctx, M, nb, out);
@@ -1602,7 +1620,7 @@ struct Engine {
       for (int i = 0; i < nb; ++i) r[i] = radii[bins[i]];
       const double* dr = upload(tag + ".r", r);
       launch_build_F_sjl_half<Real, FR>(ctx, g, src, ax, leg.ell, leg.m,
-                                        leg.sj, dr, nb, H);
+                                        leg.sj, dr, nb, H, inv_win_f);
     } else {
       vector<double> lo(nb), hi(nb);
       double hmax = 0.;
@@ -2145,22 +2163,51 @@ struct Engine {
           Ms.push_back(t.M);
       // L = M = 0: delta n_00 and N_00 are the fields built above.
       const bool reuse = p.ELL == 0;
-      vector<YlmField> ts;
+      // With real weights y_{L,-M} = (-1)^M conj y_LM, so delta n_{L,-M}
+      // and N_{L,-M} are (-1)^M times the conjugates of the order-M meshes:
+      // only orders M >= 0 are deposited (fp32mixed; the FP64 path deposits
+      // every order, as the reference does).
+      const bool mirror_m = sizeof(Real) == 4 && !reuse;
+      vector<int> Md;
       for (int M : Ms) {
-        const std::string sfx = "." + std::to_string(M);
-        if (!reuse) {
+        const int d = mirror_m ? std::abs(M) : M;
+        if (std::find(Md.begin(), Md.end(), d) == Md.end()) Md.push_back(d);
+      }
+      vector<YlmField> ts;
+      if (!reuse)
+        for (int M : Md) {
+          const std::string sfx = "." + std::to_string(M);
           ts.push_back({"dnLM" + sfx, M, 1, false, 1., -alpha, M != 0});
           ts.push_back({"NLM" + sfx, M, 2, true, 1., alpha * alpha, M != 0});
         }
+      const size_t nmesh_t = ts.size();
+      for (int M : Ms)
         ts.push_back({"", M, 3, false, 1., alpha * alpha * alpha, false});
-      }
       const vector<Field> fs = make_ylm_fields(p.ELL, &dd, &dr, ts);
-      const size_t per = reuse ? 1 : 3;
       for (size_t j = 0; j < Ms.size(); ++j) {
-        dn_of[Ms[j]] = reuse ? dn : k0_view(fs[per * j], 0.);
-        N_of[Ms[j]] = reuse ? nf : k0_view(fs[per * j + 1], 0.);
-        const Field& sb = fs[per * j + per - 1];
-        sbar_of[Ms[j]] = cplx(sb.sums[0], sb.sums[1]);
+        const int M = Ms[j];
+        if (reuse) {
+          dn_of[M] = dn;
+          N_of[M] = nf;
+        } else {
+          const int d = mirror_m ? std::abs(M) : M;
+          const size_t jd = size_t(
+              std::find(Md.begin(), Md.end(), d) - Md.begin());
+          FieldSpec<Real> a = k0_view(fs[2 * jd], 0.);
+          FieldSpec<Real> b = k0_view(fs[2 * jd + 1], 0.);
+          if (d != M) {
+            const double sg = (M % 2 != 0) ? -1. : 1.;
+            for (FieldSpec<Real>* v : {&a, &b}) {
+              v->sign *= sg;
+              v->im_sign = -v->im_sign;
+              v->k0 = cd{sg * v->k0.re, -sg * v->k0.im};
+            }
+          }
+          dn_of[M] = a;
+          N_of[M] = b;
+        }
+        const Field& sb = fs[nmesh_t + j];
+        sbar_of[M] = cplx(sb.sums[0], sb.sums[1]);
       }
     }
 

@@ -120,6 +120,11 @@ struct FieldSpec {
   // Its compensation mesh (compensated FP32 deposit), or nullptr.
   const Real* mesh_lo = nullptr;
   int64_t mesh_gen = -1;
+  // The field is sign * (FFT[re] + i im_sign FFT[im]) away from k = 0: a
+  // conjugated view (im_sign = -1) gives the order -M of a Y_lm-weighted
+  // field from the meshes of order M.
+  double sign = 1.;
+  double im_sign = 1.;
 };
 
 // Device copies of the per-axis Fourier factor tables.
@@ -240,10 +245,13 @@ void launch_build_F(Context& ctx, const Geom& g, const int M[3],
                     bool disjoint_bins = false);
 
 template <class Real, class FR>
+// iw: per-axis FP32 1 / W factors (FP32 mode values on meshes with one
+// fundamental frequency), or entries nullptr.
 void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const AxisTablesDev& ax, int ell, int m,
                         const SplineTable& sj, const double* radii, int nb,
-                        typename CplxOf<FR>::type* out);
+                        typename CplxOf<FR>::type* out,
+                        const float* const iw[3]);
 
 // Half-spectrum builders for real fields (C2R on the evaluation grid).
 template <class Real, class FR>
@@ -262,7 +270,8 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
                              const FieldSpec<Real>& f, const AxisTablesDev& ax,
                              int ell, int m, const SplineTable& sj,
                              const double* radii, int nb,
-                             typename CplxOf<FR>::type* out);
+                             typename CplxOf<FR>::type* out,
+                             const float* const iw[3]);
 
 // FP32-mixed builders of real fields without interlacing (values FP32,
 // shell membership from a table of the exact FP64 test).
@@ -272,6 +281,17 @@ void launch_shell_table(Context& ctx, const Geom& g, const int M[3],
 void launch_build_G_half_f32(Context& ctx, const Geom& g, const int M[3],
                              const int Kg[3], const float2* f, cd k0,
                              const float* const iw[3], float2* out);
+// G on the full evaluation grid for FP32 spectra without interlacing, in
+// FP32.
+void launch_build_G_f32(Context& ctx, const Geom& g, const int M[3],
+                        const int Kg[3], const FieldSpec<float>& f,
+                        const float* const iw[3], float2* out);
+// Complex FP32 shell spectra on the full evaluation grid from the half-grid
+// shell table of disjoint bins (FP32 fields without interlacing).
+void launch_build_F_tab_f32(Context& ctx, const Geom& g, const int M[3],
+                            const int16_t* tab, const FieldSpec<float>& f,
+                            const float* const iw[3], int ell, int m, int nb,
+                            float2* out);
 void launch_build_F_half_f32(Context& ctx, const Geom& g, const int M[3],
                              const int16_t* tab, const float2* f, cd k0,
                              const float* const iw[3], int ell, int nb,

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "ff.cuh"
@@ -269,33 +270,70 @@ reduce_pairs_gram_real_kernel(int64_t ncell, const float* G, const float* Fa,
 }
 
 // Register-tiled Gram form of the pair sums for FP32 fields.  A block
-// stages CELLS cells of every leg-a field (F_a) and of every leg-b field
-// times G (F_b G) in shared memory, cell-major, so that a thread reads the
-// TI leg-a and TJ leg-b values of one cell as 16-byte vectors and updates a
-// TI x TJ tile of field pairs from them (TI + TJ loads for TI TJ products;
-// the per-pair form needs two loads per product).  Every field is read
-// from HBM once per launch.  The products of kGramRun cells are summed in
-// FP32 and then added to float-float accumulators (TwoSum), so the
-// accumulated sum keeps the error of an FP32 sum of kGramRun terms per run
-// rather than of the whole grid.  The threads of a tile split the chunk's
-// cells into slices; the slices are summed in FP64 at the end and each
-// data-vector entry gets one atomic add per block.
+// stages CELLS cells of every leg-a field (F_a), of every leg-b field (F_b)
+// and of G in shared memory, cell-major, with asynchronous copies
+// (cp.async) into one of two buffers while it reduces the other; F_b is
+// then multiplied by G in shared memory (when both legs are one field set,
+// F_b G is formed from the staged F_a and nothing more is read).  A thread
+// reads the TI leg-a and TJ leg-b values of one cell as 16-byte vectors and
+// updates a TI x TJ tile of field pairs from them (TI + TJ loads for TI TJ
+// products).  Every field is read from HBM once per launch.  The products
+// of kGramRun cells are summed in FP32 and then added to float-float
+// accumulators (TwoSum), so the accumulated sum keeps the error of an FP32
+// sum of kGramRun terms per run rather than of the whole grid.  The
+// threads of a tile split the chunk's cells into slices; the slices are
+// summed in FP64 at the end and each data-vector entry gets one atomic add
+// per block.
 constexpr int kGramRun = 8;
 constexpr int kGramThreads = 256;
+
+__device__ __forceinline__ void cp_async_val(float* s, const float* g) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a),
+               "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_val(float2* s, const float2* g) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a),
+               "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ float gram_zero(float) { return 0.f; }
+__device__ __forceinline__ float2 gram_zero(float2) {
+  return make_float2(0.f, 0.f);
+}
+__device__ __forceinline__ float gram_mul(float a, float b) { return a * b; }
+__device__ __forceinline__ float2 gram_mul(float2 a, float2 b) {
+  return cmulc(a, b);
+}
 
 template <bool CPLX, int TI, int TJ, int CELLS>
 __global__ void __launch_bounds__(kGramThreads, 2)
 reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
                           const float* __restrict__ Fa, int na, int rsa,
                           const float* __restrict__ Fb, int nb, int rsb,
-                          const int2* __restrict__ tiles, int ntiles,
-                          const int* __restrict__ slot, double* out) {
+                          bool same, const int2* __restrict__ tiles,
+                          int ntiles, const int* __restrict__ slot,
+                          double* out) {
+  using V = typename std::conditional<CPLX, float2, float>::type;
   constexpr int W = CPLX ? 2 : 1;  // floats per value
   constexpr int NP = TI * TJ * W;  // partial sums per thread
   extern __shared__ float4 gsm4[];
-  float* As = reinterpret_cast<float*>(gsm4);  // [CELLS][rsa] values
-  float* Bs = As + CELLS * rsa * W;            // [CELLS][rsb] values
-  const int g0 = blockIdx.y * kGramThreads;    // this block's tile group
+  V* const sbase = reinterpret_cast<V*>(gsm4);
+  const int stage = CELLS * (rsa + rsb + 1);  // values per buffer
+  const V* fa = reinterpret_cast<const V*>(Fa);
+  const V* fb = reinterpret_cast<const V*>(Fb);
+  const V* gv = reinterpret_cast<const V*>(G);
+  const int g0 = blockIdx.y * kGramThreads;  // this block's tile group
   const int T = min(kGramThreads, ntiles - g0);
   const int S = kGramThreads / T;
   const int tid = threadIdx.x;
@@ -315,84 +353,100 @@ reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
     acc[q] = ff_zero();
   }
   int run = 0;
-  const int nrow = rsa + rsb;
-  for (int64_t c0 = int64_t(blockIdx.x) * CELLS; c0 < ncell;
-       c0 += int64_t(gridDim.x) * CELLS) {
-    __syncthreads();  // the previous chunk is consumed
-    for (int w = tid; w < nrow * CELLS; w += kGramThreads) {
+  // Rows fetched per chunk: leg a, leg b (unless one field set), G.
+  const int nfetch = rsa + (same ? 0 : rsb) + 1;
+  auto issue = [&](int64_t c0, int buf) {
+    V* As = sbase + buf * stage;
+    V* Bs = As + CELLS * rsa;
+    V* Gs = Bs + CELLS * rsb;
+    for (int w = tid; w < nfetch * CELLS; w += kGramThreads) {
       const int row = w / CELLS, c = w - row * CELLS;
       const int64_t cell = c0 + c;
-      if constexpr (CPLX) {
-        float2 v = make_float2(0.f, 0.f);
-        if (row < rsa) {
-          if (row < na && cell < ncell)
-            v = reinterpret_cast<const float2*>(Fa)[int64_t(row) * ncell +
-                                                    cell];
-          reinterpret_cast<float2*>(As)[c * rsa + row] = v;
-        } else {
-          const int r = row - rsa;
-          if (r < nb && cell < ncell)
-            v = cmulc(
-                reinterpret_cast<const float2*>(Fb)[int64_t(r) * ncell + cell],
-                reinterpret_cast<const float2*>(G)[cell]);
-          reinterpret_cast<float2*>(Bs)[c * rsb + r] = v;
-        }
+      V* dst;
+      const V* src = nullptr;
+      if (row < rsa) {
+        dst = As + c * rsa + row;
+        if (row < na && cell < ncell) src = fa + int64_t(row) * ncell + cell;
+      } else if (row == nfetch - 1) {
+        dst = Gs + c;
+        if (cell < ncell) src = gv + cell;
       } else {
-        float v = 0.f;
-        if (row < rsa) {
-          if (row < na && cell < ncell) v = Fa[int64_t(row) * ncell + cell];
-          As[c * rsa + row] = v;
-        } else {
-          const int r = row - rsa;
-          if (r < nb && cell < ncell)
-            v = Fb[int64_t(r) * ncell + cell] * G[cell];
-          Bs[c * rsb + r] = v;
-        }
+        const int r = row - rsa;
+        dst = Bs + c * rsb + r;
+        if (r < nb && cell < ncell) src = fb + int64_t(r) * ncell + cell;
       }
+      if (src != nullptr) cp_async_val(dst, src);
+      else *dst = gram_zero(V());
+    }
+    cp_async_commit();
+  };
+  const int64_t step = int64_t(gridDim.x) * CELLS;
+  int64_t c0 = int64_t(blockIdx.x) * CELLS;
+  int buf = 0;
+  if (c0 < ncell) issue(c0, 0);
+  for (; c0 < ncell; c0 += step, buf ^= 1) {
+    if (c0 + step < ncell) issue(c0 + step, buf ^ 1);
+    else cp_async_commit();  // an empty group keeps the count uniform
+    cp_async_wait<1>();      // this chunk's copies have landed
+    __syncthreads();
+    V* As = sbase + buf * stage;
+    V* Bs = As + CELLS * rsa;
+    const V* Gs = Bs + CELLS * rsb;
+    for (int w = tid; w < rsb * CELLS; w += kGramThreads) {
+      const int c = w / rsb, r = w - c * rsb;
+      V b;
+      if (same) b = r < na ? As[c * rsa + r] : gram_zero(V());
+      else b = Bs[c * rsb + r];
+      Bs[c * rsb + r] = gram_mul(b, Gs[c]);
     }
     __syncthreads();
-    if (!active) continue;
-    const int cend = ncell - c0 < CELLS ? int(ncell - c0) : CELLS;
-    for (int c = slice; c < cend; c += S) {
-      float a[TI * W], b[TJ * W];
-      const float4* va =
-          reinterpret_cast<const float4*>(As + (c * rsa + i0) * W);
-      const float4* vb =
-          reinterpret_cast<const float4*>(Bs + (c * rsb + j0) * W);
+    if (active) {
+      const int cend = ncell - c0 < CELLS ? int(ncell - c0) : CELLS;
+      const float* af = reinterpret_cast<const float*>(As);
+      const float* bf = reinterpret_cast<const float*>(Bs);
+      for (int c = slice; c < cend; c += S) {
+        float a[TI * W], b[TJ * W];
+        const float4* va =
+            reinterpret_cast<const float4*>(af + (c * rsa + i0) * W);
+        const float4* vb =
+            reinterpret_cast<const float4*>(bf + (c * rsb + j0) * W);
 #pragma unroll
-      for (int v = 0; v < TI * W / 4; ++v)
-        reinterpret_cast<float4*>(a)[v] = va[v];
+        for (int v = 0; v < TI * W / 4; ++v)
+          reinterpret_cast<float4*>(a)[v] = va[v];
 #pragma unroll
-      for (int v = 0; v < TJ * W / 4; ++v)
-        reinterpret_cast<float4*>(b)[v] = vb[v];
+        for (int v = 0; v < TJ * W / 4; ++v)
+          reinterpret_cast<float4*>(b)[v] = vb[v];
 #pragma unroll
-      for (int i = 0; i < TI; ++i)
+        for (int i = 0; i < TI; ++i)
 #pragma unroll
-        for (int j = 0; j < TJ; ++j) {
-          if constexpr (CPLX) {
-            float& re = p[2 * (i * TJ + j)];
-            float& im = p[2 * (i * TJ + j) + 1];
-            re = fmaf(a[2 * i], b[2 * j], re);
-            re = fmaf(-a[2 * i + 1], b[2 * j + 1], re);
-            im = fmaf(a[2 * i], b[2 * j + 1], im);
-            im = fmaf(a[2 * i + 1], b[2 * j], im);
-          } else {
-            p[i * TJ + j] = fmaf(a[i], b[j], p[i * TJ + j]);
+          for (int j = 0; j < TJ; ++j) {
+            if constexpr (CPLX) {
+              float& re = p[2 * (i * TJ + j)];
+              float& im = p[2 * (i * TJ + j) + 1];
+              re = fmaf(a[2 * i], b[2 * j], re);
+              re = fmaf(-a[2 * i + 1], b[2 * j + 1], re);
+              im = fmaf(a[2 * i], b[2 * j + 1], im);
+              im = fmaf(a[2 * i + 1], b[2 * j], im);
+            } else {
+              p[i * TJ + j] = fmaf(a[i], b[j], p[i * TJ + j]);
+            }
           }
-        }
-      if (++run == kGramRun) {
-        run = 0;
+        if (++run == kGramRun) {
+          run = 0;
 #pragma unroll
-        for (int q = 0; q < NP; ++q) {
-          ff_add(acc[q], p[q]);
-          p[q] = 0.f;
+          for (int q = 0; q < NP; ++q) {
+            ff_add(acc[q], p[q]);
+            p[q] = 0.f;
+          }
         }
       }
     }
+    __syncthreads();  // the buffer is refilled two chunks on
   }
+  cp_async_wait<0>();
 #pragma unroll
   for (int q = 0; q < NP; ++q) ff_add(acc[q], p[q]);
-  __syncthreads();  // the staging buffer becomes the slice table
+  __syncthreads();  // the staging buffers become the slice table
   double* red = reinterpret_cast<double*>(gsm4);  // [S][T][NP]
   if (active) {
 #pragma unroll
@@ -1190,7 +1244,9 @@ size_t gram_smem(bool cplx, int na, int nb) {
   gram_rows(cplx, na, nb, rsa, rsb);
   const GramTile t = gram_tile(cplx);
   const int w = cplx ? 2 : 1;
-  const size_t stage = size_t(gram_cells(cplx)) * (rsa + rsb) * w * 4;
+  // Two staging buffers of leg a, leg b and G.
+  const size_t stage =
+      2 * size_t(gram_cells(cplx)) * (rsa + rsb + 1) * w * 4;
   const size_t red = size_t(kGramThreads) * t.ti * t.tj * w * 8;
   return std::max(stage, red);
 }
@@ -1215,6 +1271,8 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
   int rsa, rsb;
   gram_rows(cplx, na, nb, rsa, rsb);
   const size_t smem = gram_smem(cplx, na, nb);
+  // One field set for both legs: stage it once.
+  const bool same = Fa == Fb && na == nb;
   const int cells = gram_cells(cplx);
   const int64_t chunks = (ncell + cells - 1) / cells;
   dim3 grid(unsigned(std::min<int64_t>(chunks, 152 * 2)),
@@ -1229,7 +1287,7 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
     }
     TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
     kernel<<<grid, kGramThreads, smem, ctx.stream>>>(
-        ncell, G, Fa, na, rsa, Fb, nb, rsb, tiles, ntiles, slot, out);
+        ncell, G, Fa, na, rsa, Fb, nb, rsb, same, tiles, ntiles, slot, out);
     TRVG_LAUNCHED(ctx);
   };
   if (cplx)

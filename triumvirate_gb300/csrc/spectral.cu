@@ -34,11 +34,12 @@ __device__ __forceinline__ cd half_value(const C* h, const Geom& g, int i,
 
 template <class C>
 __device__ __forceinline__ cd pair_value(const C* re, const C* im,
-                                         const Geom& g, int i, int j, int k) {
+                                         const Geom& g, int i, int j, int k,
+                                         double im_sign) {
   cd v = half_value(re, g, i, j, k);
   if (im != nullptr) {
     const cd b = half_value(im, g, i, j, k);
-    v = v + cd{-b.im, b.re};  // v + i b
+    v = v + cd{-im_sign * b.im, im_sign * b.re};  // v + i im_sign b
   }
   return v;
 }
@@ -49,9 +50,9 @@ __device__ __forceinline__ cd field_value(const FieldSpec<Real>& f,
                                           const Geom& g, int i, int j,
                                           int k) {
   if (f.k0_set && i == 0 && j == 0 && k == 0) return f.k0;
-  cd v = pair_value(f.re, f.im, g, i, j, k);
+  cd v = pair_value(f.re, f.im, g, i, j, k, f.im_sign);
   if (f.re_s != nullptr) {
-    const cd vs = pair_value(f.re_s, f.im_s, g, i, j, k);
+    const cd vs = pair_value(f.re_s, f.im_s, g, i, j, k, f.im_sign);
     const double mx = (i < g.n[0] / 2) ? double(i) / g.n[0]
                                        : double(i) / g.n[0] - 1;
     const double my = (j < g.n[1] / 2) ? double(j) / g.n[1]
@@ -64,6 +65,7 @@ __device__ __forceinline__ cd field_value(const FieldSpec<Real>& f,
     v = cd{(v.re + (ca * vs.re - sa * vs.im)) / 2.,
            (v.im + (sa * vs.re + ca * vs.im)) / 2.};
   }
+  if (f.sign != 1.) v = cd{f.sign * v.re, f.sign * v.im};
   return v;
 }
 
@@ -83,11 +85,18 @@ __device__ __forceinline__ float2 field_value_f(const FieldSpec<Real>& f,
   };
   float2 v = half(reinterpret_cast<const float2*>(f.re));
   if (f.im != nullptr) {
-    const float2 b = half(reinterpret_cast<const float2*>(f.im));
+    float2 b = half(reinterpret_cast<const float2*>(f.im));
+    if (f.im_sign != 1.) b = make_float2(-b.x, -b.y);
     v = make_float2(v.x - b.y, v.y + b.x);  // v + i b
   }
+  if (f.sign != 1.) v = make_float2(-v.x, -v.y);
   return v;
 }
+
+// Per-axis FP32 factors of 1 / W (1 / sinc^order).
+struct InvWinF {
+  const float* w[3];
+};
 
 // ylm_lean in FP32 (cnm = cnorm[|m|] of ylm_all_norms).
 __device__ __forceinline__ float2 ylm_lean_f(int ell, int m, float cnm,
@@ -219,6 +228,35 @@ __global__ void build_G_kernel(Geom g, int M0, int M1, int M2, int Kg0,
       const cd r = cdivr(cdivr(v, w), g.vol);
       o.x = FR(r.re);
       o.y = FR(r.im);
+    }
+    out[t] = o;
+  }
+}
+
+// build_G_kernel for FP32 spectra without interlacing, in FP32 (1 / W from
+// the per-axis tables).
+__global__ void build_G_f32_kernel(Geom g, int M0, int M1, int M2, int Kg0,
+                                   int Kg1, int Kg2, FieldSpec<float> f,
+                                   InvWinF iw, float inv_vol, float2* out) {
+  const uint32_t count = uint32_t(M0) * M1 * M2;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(M2));
+    const uint32_t row = t / uint32_t(M2);
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const bool in = (M0 == g.n[0] || abs(sx) <= Kg0) &&
+                    (M1 == g.n[1] || abs(sy) <= Kg1) &&
+                    (M2 == g.n[2] || abs(sz) <= Kg2);
+    float2 o = make_float2(0.f, 0.f);
+    if (in) {
+      const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+                k = wrap(sz, g.n[2]);
+      const float2 v = field_value_f(f, g, i, j, k);
+      const float w = iw.w[0][i] * iw.w[1][j] * iw.w[2][k] * inv_vol;
+      o = make_float2(v.x * w, v.y * w);
     }
     out[t] = o;
   }
@@ -553,9 +591,6 @@ __device__ __forceinline__ float2 half_value_f(const float2* h, const Geom& g,
   return v;
 }
 
-struct InvWinF {
-  const float* w[3];
-};
 
 // Shell index of every half-spectrum mode of the evaluation grid (-1: in
 // no shell), bins disjoint.
@@ -652,6 +687,50 @@ __global__ void build_F_half_f32_kernel(Geom g, int M0, int M1, int M2,
   }
 }
 
+// Complex FP32 shell spectra on the full evaluation grid from the half-grid
+// shell table: |k| depends on sz only through sz^2, so mode (a, b, c) with
+// c > M2 / 2 reads entry (a, b, M2 - c).  Modes of shell q get
+// y_lm(k) f(k) / W(k) with FP32 factors (1 / W from the per-axis tables);
+// the others stay zero (`out` is zeroed beforehand).
+__global__ void build_F_tab_f32_kernel(Geom g, int M0, int M1, int M2,
+                                       const int16_t* tab,
+                                       FieldSpec<float> f, InvWinF iw,
+                                       int ell, int m, float cnm,
+                                       float2* out) {
+  const int Mh = M2 / 2 + 1;
+  const uint32_t count = uint32_t(M0) * M1 * M2;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const int c = int(t % uint32_t(M2));
+    const uint32_t row = t / uint32_t(M2);
+    const int q = tab[int64_t(row) * Mh + (c < Mh ? c : M2 - c)];
+    if (q < 0) continue;
+    const int b = int(row % uint32_t(M1));
+    const int a = int(row / uint32_t(M1));
+    const int sx = shift_index(a, M0), sy = shift_index(b, M1),
+              sz = shift_index(c, M2);
+    const int i = wrap(sx, g.n[0]), j = wrap(sy, g.n[1]),
+              kk = wrap(sz, g.n[2]);
+    const float2 v = field_value_f(f, g, i, j, kk);
+    const float w = iw.w[0][i] * iw.w[1][j] * iw.w[2][kk];
+    float2 y = make_float2(1.f, 0.f);
+    if (ell > 0) {
+      const float kx = float(sx) * float(g.dk[0]);
+      const float ky = float(sy) * float(g.dk[1]);
+      const float kz = float(sz) * float(g.dk[2]);
+      const float k = sqrtf(kx * kx + ky * ky + kz * kz);
+      y = make_float2(0.f, 0.f);
+      if (k > 0.f) {
+        const float ik = 1.f / k;
+        y = ylm_lean_f(ell, m, cnm, kz * ik, make_float2(kx * ik, -ky * ik));
+      }
+    }
+    const float2 vw = make_float2(v.x * w, v.y * w);
+    out[int64_t(q) * count + t] =
+        make_float2(y.x * vw.x - y.y * vw.y, y.x * vw.y + y.y * vw.x);
+  }
+}
+
 struct SjlArgs {
   SplineTable sj;
   const double* radii;
@@ -736,12 +815,15 @@ __global__ void sjl_key_table_kernel(double dk, int64_t nkeys, SjlArgs sa,
   }
 }
 
-// j_l(k r_q) y_lm(k) f(k) / W(k) / V from the key table: the mode's value
-// is formed in FP64 and rounded once, each field entry is one FP32 product.
-template <class Real, bool HALF>
+// j_l(k r_q) y_lm(k) f(k) / W(k) / V from the key table, each field entry
+// one FP32 product.  With F32 (FP32 spectra without interlacing) the
+// mode's value is formed in FP32 (1 / W from the per-axis tables, y_lm from
+// the FP32 direction), otherwise in FP64 and rounded once.
+template <class Real, bool HALF, bool F32>
 __global__ void build_F_sjl_key_kernel(Geom g, FieldSpec<Real> f,
-                                       AxisTablesDev ax, int ell, int m,
-                                       int nb, const float* __restrict__ jt,
+                                       AxisTablesDev ax, InvWinF iw,
+                                       float cnm, int ell, int m, int nb,
+                                       const float* __restrict__ jt,
                                        double inv_vol, float2* out) {
   const int64_t count = HALF ? g.nhalf : g.nmesh;
   const int nz = HALF ? g.nzh : g.n[2];
@@ -752,14 +834,37 @@ __global__ void build_F_sjl_key_kernel(Geom g, FieldSpec<Real> f,
     const int i = int(t / (int64_t(nz) * g.n[1]));
     const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
               sz = shift_index(kk, g.n[2]);
-    const double kx = dmul(double(sx), g.dk[0]);
-    const double ky = dmul(double(sy), g.dk[1]);
-    const double kz = dmul(double(sz), g.dk[2]);
-    const cd v = field_value(f, g, i, j, kk);
-    const double w = window_pow(ax, i, j, kk);
-    const cd y = reduced_ylm(ell, m, kx, ky, kz);
-    const cd val = y * cdivr(v, w);
-    const float vr = float(val.re * inv_vol), vi = float(val.im * inv_vol);
+    float vr, vi;
+    if constexpr (F32) {
+      const float2 v = field_value_f(f, g, i, j, kk);
+      const float w =
+          iw.w[0][i] * iw.w[1][j] * iw.w[2][kk] * float(inv_vol);
+      float2 y = make_float2(1.f, 0.f);
+      if (ell > 0) {
+        const float kx = float(sx) * float(g.dk[0]);
+        const float ky = float(sy) * float(g.dk[1]);
+        const float kz = float(sz) * float(g.dk[2]);
+        const float k = sqrtf(kx * kx + ky * ky + kz * kz);
+        y = make_float2(0.f, 0.f);
+        if (k > 0.f) {
+          const float ik = 1.f / k;
+          y = ylm_lean_f(ell, m, cnm, kz * ik,
+                         make_float2(kx * ik, -ky * ik));
+        }
+      }
+      vr = (y.x * v.x - y.y * v.y) * w;
+      vi = (y.x * v.y + y.y * v.x) * w;
+    } else {
+      const double kx = dmul(double(sx), g.dk[0]);
+      const double ky = dmul(double(sy), g.dk[1]);
+      const double kz = dmul(double(sz), g.dk[2]);
+      const cd v = field_value(f, g, i, j, kk);
+      const double w = window_pow(ax, i, j, kk);
+      const cd y = reduced_ylm(ell, m, kx, ky, kz);
+      const cd val = y * cdivr(v, w);
+      vr = float(val.re * inv_vol);
+      vi = float(val.im * inv_vol);
+    }
     const int64_t key = int64_t(sx) * sx + int64_t(sy) * sy + int64_t(sz) * sz;
     const float* row = jt + key * nb;
     for (int q = 0; q < nb; ++q) {
@@ -1142,15 +1247,28 @@ template <class Real, class FR>
 void launch_build_F_sjl(Context& ctx, const Geom& g, const FieldSpec<Real>& f,
                         const AxisTablesDev& ax, int ell, int m,
                         const SplineTable& sj, const double* radii, int nb,
-                        typename CplxOf<FR>::type* out) {
+                        typename CplxOf<FR>::type* out,
+                        const float* const iw[3]) {
   int64_t nkeys = 0;
   float* jt = nullptr;
   if (sjl_key_form<Real, FR>(ctx, g, sj, radii, nb, nkeys, jt)) {
+    InvWinF w{{iw[0], iw[1], iw[2]}};
+    double cn[kMaxYlmDegree + 1] = {};
+    const bool f32 = sizeof(Real) == 4 && f.re_s == nullptr &&
+                     ell <= kMaxYlmDegree && iw[0] != nullptr;
+    if (ell <= kMaxYlmDegree) ylm_all_norms(ell, cn);
+    const float cnm = ell <= kMaxYlmDegree ? float(cn[std::abs(m)]) : 0.f;
     TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
-    build_F_sjl_key_kernel<Real, false>
-        <<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
-            g, f, ax, ell, m, nb, jt, 1. / g.vol,
-            reinterpret_cast<float2*>(out));
+    if (f32)
+      build_F_sjl_key_kernel<Real, false, true>
+          <<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+              g, f, ax, w, cnm, ell, m, nb, jt, 1. / g.vol,
+              reinterpret_cast<float2*>(out));
+    else
+      build_F_sjl_key_kernel<Real, false, false>
+          <<<grid_for(g.nmesh, 256), 256, 0, ctx.stream>>>(
+              g, f, ax, w, cnm, ell, m, nb, jt, 1. / g.vol,
+              reinterpret_cast<float2*>(out));
     TRVG_LAUNCHED(ctx);
     return;
   }
@@ -1462,6 +1580,39 @@ void launch_build_F_half_f32(Context& ctx, const Geom& g, const int M[3],
   TRVG_LAUNCHED(ctx);
 }
 
+void launch_build_G_f32(Context& ctx, const Geom& g, const int M[3],
+                        const int Kg[3], const FieldSpec<float>& f,
+                        const float* const iw[3], float2* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  InvWinF w{{iw[0], iw[1], iw[2]}};
+  TRVG_KBEGIN(ctx, "build_G_kernel");
+  build_G_f32_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], Kg[0], Kg[1], Kg[2], f, w, float(1. / g.vol), out);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_build_F_tab_f32(Context& ctx, const Geom& g, const int M[3],
+                            const int16_t* tab, const FieldSpec<float>& f,
+                            const float* const iw[3], int ell, int m, int nb,
+                            float2* out) {
+  const int64_t count = int64_t(M[0]) * M[1] * M[2];
+  if (count >= (int64_t(1) << 32))
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Evaluation grid too large.");
+  if (ell > kMaxYlmDegree)
+    throw_error(TRVG_ERR_INVALID_PARAMETER, "Degree above the FP32 builder.");
+  TRVG_CUDA(cudaMemsetAsync(out, 0, size_t(nb) * count * sizeof(float2),
+                            ctx.stream));
+  double cn[kMaxYlmDegree + 1] = {};
+  ylm_all_norms(ell, cn);
+  InvWinF w{{iw[0], iw[1], iw[2]}};
+  TRVG_KBEGIN(ctx, "build_F_kernel");
+  build_F_tab_f32_kernel<<<grid_for(count, 256), 256, 0, ctx.stream>>>(
+      g, M[0], M[1], M[2], tab, f, w, ell, m, float(cn[std::abs(m)]), out);
+  TRVG_LAUNCHED(ctx);
+}
+
 template <class Real, class FR>
 void launch_build_G_half(Context& ctx, const Geom& g, const int M[3],
                          const int Kg[3], const FieldSpec<Real>& f,
@@ -1499,15 +1650,28 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
                              const FieldSpec<Real>& f, const AxisTablesDev& ax,
                              int ell, int m, const SplineTable& sj,
                              const double* radii, int nb,
-                             typename CplxOf<FR>::type* out) {
+                             typename CplxOf<FR>::type* out,
+                             const float* const iw[3]) {
   int64_t nkeys = 0;
   float* jt = nullptr;
   if (sjl_key_form<Real, FR>(ctx, g, sj, radii, nb, nkeys, jt)) {
+    InvWinF w{{iw[0], iw[1], iw[2]}};
+    double cn[kMaxYlmDegree + 1] = {};
+    const bool f32 = sizeof(Real) == 4 && f.re_s == nullptr &&
+                     ell <= kMaxYlmDegree && iw[0] != nullptr;
+    if (ell <= kMaxYlmDegree) ylm_all_norms(ell, cn);
+    const float cnm = ell <= kMaxYlmDegree ? float(cn[std::abs(m)]) : 0.f;
     TRVG_KBEGIN(ctx, "build_F_sjl_kernel");
-    build_F_sjl_key_kernel<Real, true>
-        <<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
-            g, f, ax, ell, m, nb, jt, 1. / g.vol,
-            reinterpret_cast<float2*>(out));
+    if (f32)
+      build_F_sjl_key_kernel<Real, true, true>
+          <<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+              g, f, ax, w, cnm, ell, m, nb, jt, 1. / g.vol,
+              reinterpret_cast<float2*>(out));
+    else
+      build_F_sjl_key_kernel<Real, true, false>
+          <<<grid_for(g.nhalf, 256), 256, 0, ctx.stream>>>(
+              g, f, ax, w, cnm, ell, m, nb, jt, 1. / g.vol,
+              reinterpret_cast<float2*>(out));
     TRVG_LAUNCHED(ctx);
     return;
   }
@@ -1528,7 +1692,8 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
       double, CplxOf<F>::type*, bool);                                       \
   template void launch_build_F_sjl<R, F>(                                    \
       Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
-      int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
+      int, const SplineTable&, const double*, int, CplxOf<F>::type*,         \
+      const float* const*);                                                  \
   template void launch_build_G_half<R, F>(                                   \
       Context&, const Geom&, const int*, const int*, const FieldSpec<R>&,    \
       const AxisTablesDev&, CplxOf<F>::type*);                               \
@@ -1538,7 +1703,8 @@ void launch_build_F_sjl_half(Context& ctx, const Geom& g,
       double, CplxOf<F>::type*);                                             \
   template void launch_build_F_sjl_half<R, F>(                               \
       Context&, const Geom&, const FieldSpec<R>&, const AxisTablesDev&, int, \
-      int, const SplineTable&, const double*, int, CplxOf<F>::type*);        \
+      int, const SplineTable&, const double*, int, CplxOf<F>::type*,         \
+      const float* const*);                                                  \
   template void launch_twopt_field<R, F>(                                    \
       Context&, const Geom&, const FieldSpec<R>&, const FieldSpec<R>&, cd,   \
       const AxisTablesDev&, CplxOf<F>::type*, CplxOf<F>::type*);
