@@ -1043,3 +1043,34 @@ def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
         scale = np.max(np.abs(pair[k]))
         assert np.max(np.abs(tiled[k] - pair[k])) <= 2e-6 * scale, (
             case, k, float(np.max(np.abs(tiled[k] - pair[k])) / scale))
+
+
+def test_tiled_gram_complex_then_real_in_fresh_process():
+    """A fresh process whose first tiled reduction is complex and whose next
+    one is real (survey B_202: terms of order M != 0, then M = 0) opts both
+    kernels in to their shared memory."""
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np\n"
+        "from triumvirate_gb300.catalogue import ParticleCatalogue\n"
+        "from triumvirate_gb300.dataobjs import Binning\n"
+        "from triumvirate_gb300.threept import compute_bispec\n"
+        "rng = np.random.default_rng(5)\n"
+        "d = rng.uniform(-300., 300., size=(3000, 3)) + [0., 0., 800.]\n"
+        "r = rng.uniform(-300., 300., size=(12000, 3)) + [0., 0., 800.]\n"
+        "res = compute_bispec(ParticleCatalogue(*d.T, nz=1e-4),\n"
+        "                     ParticleCatalogue(*r.T, nz=1e-4),\n"
+        "                     degrees=(2, 0, 2),\n"
+        "                     binning=Binning('fourier', 'lin', 0.01, 0.1, 6),\n"
+        "                     form='full',\n"
+        "                     sampling_params={'boxsize': [1000.] * 3,\n"
+        "                                      'ngrid': [32] * 3,\n"
+        "                                      'assignment': 'tsc',\n"
+        "                                      'precision': 'fp32mixed'})\n"
+        "assert np.all(np.isfinite(res['bk_raw']))\n")
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    p = subprocess.run([sys.executable, "-c", code], cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]

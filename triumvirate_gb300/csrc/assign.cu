@@ -330,26 +330,34 @@ __device__ __forceinline__ void red_run4(float* row, int z0, const float* v) {
   if (off + ORDER > 4) atomicAdd(p + 1, make_float4(q[4], q[5], q[6], q[7]));
 }
 
+// FP32 window k of a stencil (a float-float window rounded once).
 template <int ORDER>
-__device__ __forceinline__ void deposit_f(const AssignArgs& a,
-                                          const StencilF<ORDER>& sx,
-                                          const StencilF<ORDER>& sy,
-                                          const StencilF<ORDER>& sz, float wgt,
-                                          float* mesh) {
+__device__ __forceinline__ float win_f(const StencilF<ORDER>& s, int k) {
+  return s.win[k];
+}
+template <int ORDER>
+__device__ __forceinline__ float win_f(const StencilFF<ORDER>& s, int k) {
+  return __fadd_rn(s.win[k].hi, s.win[k].lo);
+}
+
+template <int ORDER, class St>
+__device__ __forceinline__ void deposit_f(const AssignArgs& a, const St& sx,
+                                          const St& sy, const St& sz,
+                                          float wgt, float* mesh) {
   bool run = a.vec4;
 #pragma unroll
   for (int k = 1; k < ORDER; ++k) run = run && (sz.idx[k] == sz.idx[0] + k);
 #pragma unroll
   for (int i = 0; i < ORDER; ++i) {
-    const float wi = sx.win[i] * wgt;
+    const float wi = win_f(sx, i) * wgt;
 #pragma unroll
     for (int j = 0; j < ORDER; ++j) {
       float* row =
           mesh + (int64_t(sx.idx[i]) * a.n[1] + sy.idx[j]) * a.n[2];
-      const float wij = wi * sy.win[j];
+      const float wij = wi * win_f(sy, j);
       float v[ORDER];
 #pragma unroll
-      for (int k = 0; k < ORDER; ++k) v[k] = wij * sz.win[k];
+      for (int k = 0; k < ORDER; ++k) v[k] = wij * win_f(sz, k);
       if (run) {
         red_run4<ORDER>(row, sz.idx[0], v);
       } else {
@@ -1005,6 +1013,21 @@ assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
       const YlmTarget& u = ts.t[t];
       if (u.re == nullptr) continue;
       const cd wgt = target_weight(u, wpow, ypos, ts.ell);
+      if constexpr (COMP) {
+        // Targets whose sums do not cancel: plain FP32 atomics with the
+        // float-float windows rounded once.
+        if (fast && !u.comp) {
+          deposit_f<ORDER>(a, sx, sy, sz, float(wgt.re), u.re);
+          if (u.im != nullptr)
+            deposit_f<ORDER>(a, sx, sy, sz, float(wgt.im), u.im);
+          if constexpr (SH) {
+            deposit_f<ORDER>(a, hx, hy, hz, float(wgt.re), u.sre);
+            if (u.sim != nullptr)
+              deposit_f<ORDER>(a, hx, hy, hz, float(wgt.im), u.sim);
+          }
+          continue;
+        }
+      }
       if (fast) {
         if constexpr (COMP) {
           const FF wr = ff_from_double(wgt.re), wi = ff_from_double(wgt.im);

@@ -641,7 +641,12 @@ struct Engine {
   Field make_field(const std::string& name, const vector<Part>& parts,
                    bool cplx, bool defer_r2c = false) {
     Field f;
-    const int64_t lo = mesh_lo_off(parts.size() > 1);
+    // Compensation meshes where the parts' sums can cancel: parts whose
+    // scales differ in sign (data minus alpha randoms).
+    bool cancel = false;
+    for (const Part& part : parts)
+      cancel = cancel || (part.ws.scale * parts[0].ws.scale < 0.);
+    const int64_t lo = mesh_lo_off(cancel);
     const size_t cells = size_t(g.nmesh + lo);
     Real* mre = ctx.buf<Real>("mesh.re", cells);
     Real* mim = cplx ? ctx.buf<Real>("mesh.im", cells) : nullptr;
@@ -680,7 +685,7 @@ struct Engine {
                           i == 0 ? &fill : nullptr, lo);
     // Several parts (data minus alpha randoms) cancel in the sum: the FP32
     // meshes the FFTs read become the correctly rounded compensated sums.
-    if (lo != 0 && (parts.size() > 1 || ctx.mesh_renorm))
+    if (lo != 0 && (cancel || ctx.mesh_renorm))
       for (Real* m : {mre, mim, sre, sim})
         if (m != nullptr)
           launch_mesh_renorm(ctx, reinterpret_cast<float*>(m), g.nmesh, lo);
@@ -792,6 +797,10 @@ struct Engine {
       u.power = ts[i].power;
       u.conj = ts[i].conj;
       u.sums = sums + 4 * i;
+      // Data and randoms of opposite signs cancel; a target whose parts
+      // add (N_LM: alpha^2 randoms plus data) deposits plain FP32 sums
+      // unless every mesh is compensated.
+      u.comp = ctx.mesh_comp == 1 || ts[i].scale_d * ts[i].scale_r < 0.;
       if (ts[i].name.empty()) continue;
       const std::string& nm = ts[i].name;
       const size_t cells = size_t(g.nmesh + mesh_lo_off(dd && dr));
@@ -1409,8 +1418,9 @@ struct Engine {
     } else {
       // Cells of unequal sides: keyed by (|s_x|, |s_y|, |s_z|), which fixes
       // |r|, with the radius of each key in a table.
-      const int64_t nkeys = int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) *
-                            (g.n[2] / 2 + 1);
+      const int64_t nkeys = int64_t(g.n[0] - g.n[0] / 2 + 1) *
+                            (g.n[1] - g.n[1] / 2 + 1) *
+                            (g.n[2] - g.n[2] / 2 + 1);
       double* hist = ctx.buf<double>("sn.hist", 2 * size_t(nkeys));
       double* rkey = ctx.buf<double>("sn.rkey", size_t(nkeys));
       zero(hist, 2 * nkeys * sizeof(double));

@@ -73,6 +73,10 @@ struct YlmTarget {
   float* sre = nullptr;
   float* sim = nullptr;
   double* sums = nullptr;  // [4]: landed weight (re, im, shadow re, im)
+  // Compensated deposit (launches with compensation meshes): the target's
+  // catalogues enter with opposite signs, so its sums cancel.  Other
+  // targets deposit plain FP32 sums into the same meshes.
+  bool comp = true;
 };
 
 struct YlmTargets {

@@ -1040,56 +1040,92 @@ pair_bessel_gram_ff_kernel(int64_t nkeys, double dr, const double* rkey,
   }
 }
 
-// Cells of any shape grouped by (|s_x|, |s_y|, |s_z|), which fixes |r|:
-// hist[key] += xi y_a y_b, key = (|s_x| D_y + |s_y|) D_z + |s_z| with
-// D = n/2 + 1 per axis, and rkey[key] = |r| (the sign of s does not change
-// a product s dr, so every cell of a key has this radius).
-template <class Real>
-__global__ void __launch_bounds__(256)
-octant_cell_hist_kernel(Geom g, const Real* xi_re, const Real* xi_im,
-                        int ell_a, int m_a, int ell_b, int m_b, double cna,
-                        double cnb, double* hist) {
-  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
-  const int dy = g.n[1] / 2 + 1, dz = g.n[2] / 2 + 1;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-       t < g.nmesh; t += int64_t(gridDim.x) * blockDim.x) {
-    const int k = int(t % g.n[2]);
-    const int j = int((t / g.n[2]) % g.n[1]);
-    const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
-    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
-              sz = shift_index(k, g.n[2]);
-    const int64_t key = (int64_t(abs(sx)) * dy + abs(sy)) * dz + abs(sz);
-    cd v = {double(xi_re[t]), xi_im != nullptr ? double(xi_im[t]) : 0.};
-    if (!trivial) {
-      // y_a y_b from the form of reduced_ylm_all (cna, cnb: the norms of
-      // |m_a|, |m_b|); zero at r = 0 unless a degree is 0.
-      const double rx = dmul(double(sx), g.dr[0]);
-      const double ry = dmul(double(sy), g.dr[1]);
-      const double rz = dmul(double(sz), g.dr[2]);
-      const double r = dsqrt(dadd(dadd(dmul(rx, rx), dmul(ry, ry)),
-                                  dmul(rz, rz)));
-      if (fabs(r) < 1.e-9) {
-        v = cd{0., 0.};
-      } else {
-        const double inv = 1.0 / r;
-        const cd u = cmk(rx * inv, -ry * inv);
-        v = v * (ylm_lean(ell_a, m_a, cna, rz * inv, u) *
-                 ylm_lean(ell_b, m_b, cnb, rz * inv, u));
-      }
-    }
-    if (v.re != 0.) atomicAdd(hist + 2 * key, v.re);
-    if (v.im != 0.) atomicAdd(hist + 2 * key + 1, v.im);
-  }
-}
 
-__global__ void octant_radius_kernel(Geom g, double* rkey) {
-  const int dx = g.n[0] / 2 + 1, dy = g.n[1] / 2 + 1, dz = g.n[2] / 2 + 1;
+// Cells of any shape grouped by (|s_x|, |s_y|, |s_z|), which fixes |r|:
+// hist[key] = sum of xi y_a y_b over the key's cells, key = (|s_x| D_y +
+// |s_y|) D_z + |s_z| with D = n - n/2 + 1 per axis (|s| reaches n/2 + 1 on
+// an odd axis, where index n/2 has frequency -(n/2 + 1)), and rkey[key] =
+// |r| (the sign of s does not change a product s dr).  One thread per key:
+// its (up to eight) cells are summed in the thread and the bin is written
+// once, without atomics.  Along an axis, key a holds cell a when a < n/2
+// (shift a) and cell n - a when 1 <= a <= n - n/2 (shift -a).  FP32 fields
+// take y_a y_b in FP32.
+template <class Real>
+__global__ void octant_key_hist_kernel(Geom g, const Real* xi_re,
+                                       const Real* xi_im, int ell_a, int m_a,
+                                       int ell_b, int m_b, double cna,
+                                       double cnb, double* hist,
+                                       double* rkey) {
+  const bool trivial = (ell_a == 0 && m_a == 0 && ell_b == 0 && m_b == 0);
+  const int dx = g.n[0] - g.n[0] / 2 + 1, dy = g.n[1] - g.n[1] / 2 + 1,
+            dz = g.n[2] - g.n[2] / 2 + 1;
   const int64_t nk = int64_t(dx) * dy * dz;
+  // Cell of key index a along an axis of n cells: side 0 is cell a, side 1
+  // cell n - a; -1 where the side holds none.
+  auto cell_of = [](int a, int n, int side) {
+    if (side == 0) return a < n / 2 ? a : -1;
+    return (a >= 1 && a <= n - n / 2) ? n - a : -1;
+  };
   for (int64_t key = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
        key < nk; key += int64_t(gridDim.x) * blockDim.x) {
     const int c = int(key % dz);
     const int b = int((key / dz) % dy);
     const int a = int(key / (int64_t(dz) * dy));
+    double sre = 0., sim = 0.;
+    for (int fx = 0; fx < 2; ++fx) {
+      const int i = cell_of(a, g.n[0], fx);
+      if (i < 0) continue;
+      const int sx = shift_index(i, g.n[0]);
+      for (int fy = 0; fy < 2; ++fy) {
+        const int j = cell_of(b, g.n[1], fy);
+        if (j < 0) continue;
+        const int sy = shift_index(j, g.n[1]);
+        for (int fz = 0; fz < 2; ++fz) {
+          const int k = cell_of(c, g.n[2], fz);
+          if (k < 0) continue;
+          const int sz = shift_index(k, g.n[2]);
+          const int64_t t = (int64_t(i) * g.n[1] + j) * g.n[2] + k;
+          const double vr = double(xi_re[t]);
+          const double vi = xi_im != nullptr ? double(xi_im[t]) : 0.;
+          if (trivial) {
+            sre += vr;
+            sim += vi;
+            continue;
+          }
+          if constexpr (sizeof(Real) == 4) {
+            const float rx = float(sx) * float(g.dr[0]);
+            const float ry = float(sy) * float(g.dr[1]);
+            const float rz = float(sz) * float(g.dr[2]);
+            const float r = sqrtf(rx * rx + ry * ry + rz * rz);
+            if (r < 1.e-9f) continue;
+            const float inv = 1.f / r;
+            const float2 u = make_float2(rx * inv, -ry * inv);
+            const float2 ya = ylm_lean_f(ell_a, m_a, float(cna), rz * inv, u);
+            const float2 yb = ylm_lean_f(ell_b, m_b, float(cnb), rz * inv, u);
+            const float2 y = make_float2(ya.x * yb.x - ya.y * yb.y,
+                                         ya.x * yb.y + ya.y * yb.x);
+            const float fr = float(vr), fi = float(vi);
+            sre += double(fr * y.x - fi * y.y);
+            sim += double(fr * y.y + fi * y.x);
+          } else {
+            const double rx = dmul(double(sx), g.dr[0]);
+            const double ry = dmul(double(sy), g.dr[1]);
+            const double rz = dmul(double(sz), g.dr[2]);
+            const double r = dsqrt(dadd(dadd(dmul(rx, rx), dmul(ry, ry)),
+                                        dmul(rz, rz)));
+            if (fabs(r) < 1.e-9) continue;
+            const double inv = 1.0 / r;
+            const cd u = cmk(rx * inv, -ry * inv);
+            const cd y = ylm_lean(ell_a, m_a, cna, rz * inv, u) *
+                         ylm_lean(ell_b, m_b, cnb, rz * inv, u);
+            sre += vr * y.re - vi * y.im;
+            sim += vr * y.im + vi * y.re;
+          }
+        }
+      }
+    }
+    hist[2 * key] = sre;
+    hist[2 * key + 1] = sim;
     rkey[key] = vec3_mag(dmul(double(a), g.dr[0]), dmul(double(b), g.dr[1]),
                          dmul(double(c), g.dr[2]));
   }
@@ -1277,13 +1313,18 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
   const int64_t chunks = (ncell + cells - 1) / cells;
   dim3 grid(unsigned(std::min<int64_t>(chunks, 152 * 2)),
             unsigned((ntiles + kGramThreads - 1) / kGramThreads));
+  // Both kernels have one function-pointer type, so the opt-in flags are
+  // kept per form (real, complex) and device.
+  static bool configured[2][64] = {};
   auto go = [&](auto kernel) {
-    static bool configured[64] = {};
-    if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
+    bool* done = (ctx.device >= 0 && ctx.device < 64)
+                     ? &configured[cplx ? 1 : 0][ctx.device]
+                     : nullptr;
+    if (done == nullptr || !*done) {
       TRVG_CUDA(cudaFuncSetAttribute(
           kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
           int(kGramSmemMax)));
-      if (ctx.device >= 0 && ctx.device < 64) configured[ctx.device] = true;
+      if (done != nullptr) *done = true;
     }
     TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
     kernel<<<grid, kGramThreads, smem, ctx.stream>>>(
@@ -1426,8 +1467,8 @@ template <class Real>
 void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
                              const Real* xi_im, int ell_a, int m_a, int ell_b,
                              int m_b, double* hist, double* rkey) {
-  const int64_t nk = int64_t(g.n[0] / 2 + 1) * (g.n[1] / 2 + 1) *
-                     (g.n[2] / 2 + 1);
+  const int64_t nk = int64_t(g.n[0] - g.n[0] / 2 + 1) *
+                     (g.n[1] - g.n[1] / 2 + 1) * (g.n[2] - g.n[2] / 2 + 1);
   double na[kMaxYlmDegree + 1], nb[kMaxYlmDegree + 1];
   if (ell_a > kMaxYlmDegree || ell_b > kMaxYlmDegree)
     throw_error(TRVG_ERR_INVALID_PARAMETER, "Degree above %d.",
@@ -1435,13 +1476,9 @@ void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
   ylm_all_norms(ell_a, na);
   ylm_all_norms(ell_b, nb);
   TRVG_KBEGIN(ctx, "orbit_rows_kernel");
-  octant_cell_hist_kernel<Real><<<grid_for(g.nmesh, 256), 256, 0,
-                                  ctx.stream>>>(
+  octant_key_hist_kernel<Real><<<grid_for(nk, 256), 256, 0, ctx.stream>>>(
       g, xi_re, xi_im, ell_a, m_a, ell_b, m_b, na[std::abs(m_a)],
-      nb[std::abs(m_b)], hist);
-  TRVG_LAUNCHED(ctx);
-  TRVG_KBEGIN(ctx, "orbit_rows_kernel");
-  octant_radius_kernel<<<grid_for(nk, 256), 256, 0, ctx.stream>>>(g, rkey);
+      nb[std::abs(m_b)], hist, rkey);
   TRVG_LAUNCHED(ctx);
 }
 

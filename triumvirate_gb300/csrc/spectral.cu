@@ -98,33 +98,6 @@ struct InvWinF {
   const float* w[3];
 };
 
-// ylm_lean in FP32 (cnm = cnorm[|m|] of ylm_all_norms).
-__device__ __forceinline__ float2 ylm_lean_f(int ell, int m, float cnm,
-                                             float mu, float2 u) {
-  const int am = m < 0 ? -m : m;
-  float2 e = make_float2(1.f, 0.f);
-  for (int i = 0; i < am; ++i)
-    e = make_float2(e.x * u.x - e.y * u.y, e.x * u.y + e.y * u.x);
-  float q1 = 0.f, q = 1.f;
-  if (ell > am) {
-    q1 = 1.f;
-    q = float(2 * am + 1) * mu;
-    for (int l = am + 2; l <= ell; ++l) {
-      const float qn =
-          (float(2 * l - 1) * mu * q - float(l + am - 1) * q1) / float(l - am);
-      q1 = q;
-      q = qn;
-    }
-  }
-  const float c = cnm * q;
-  float2 v = make_float2(c * e.x, c * e.y);
-  if (m < 0) {
-    v.y = -v.y;
-    if (am & 1) v = make_float2(-v.x, -v.y);
-  }
-  return v;
-}
-
 // Shot-noise aliasing C_1(k) (field.cpp:3463-3509).
 __device__ __forceinline__ double alias_sn(const AxisTablesDev& ax, int i,
                                            int j, int k) {
