@@ -1284,9 +1284,20 @@ struct Engine {
       if (replay != nullptr)
         throw_error(TRVG_ERR_INVALID_PARAMETER,
                     "Batch replay covers the FP32 real shot-noise field only.");
-      launch_twopt_field<Real, XR>(ctx, g, fa, fb,
-                                   cd{shot.real(), shot.imag()}, ax, hre,
-                                   him);
+      bool done = false;
+      if constexpr (sizeof(Real) == 4 && sizeof(XR) == 4) {
+        if (!interlace && fa.re_s == nullptr && fb.re_s == nullptr) {
+          launch_twopt_field_f32(
+              ctx, g, fa, fb,
+              make_float2(float(shot.real()), float(shot.imag())),
+              inv_alias_f, hre, him);
+          done = true;
+        }
+      }
+      if (!done)
+        launch_twopt_field<Real, XR>(ctx, g, fa, fb,
+                                     cd{shot.real(), shot.imag()}, ax, hre,
+                                     him);
     }
     cufftHandle h = ctx.plan(FFT<XR>::kC2R, g.n, 1);
     TRVG_CUFFT(cufftSetStream(h, ctx.stream));

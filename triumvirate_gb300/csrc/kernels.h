@@ -285,6 +285,14 @@ void launch_shell_table(Context& ctx, const Geom& g, const int M[3],
 void launch_build_G_half_f32(Context& ctx, const Geom& g, const int M[3],
                              const int Kg[3], const float2* f, cd k0,
                              const float* const iw[3], float2* out);
+// The shot-noise field spectrum (|f_a f_b^*| / C_1 - S) / V of FP32 spectra
+// without interlacing, in FP32; out_im: the imaginary part's spectrum when
+// the field is complex (nullptr: real).
+void launch_twopt_field_f32(Context& ctx, const Geom& g,
+                            const FieldSpec<float>& fa,
+                            const FieldSpec<float>& fb, float2 shot,
+                            const float* const inv_alias[3], float2* out_re,
+                            float2* out_im);
 // G on the full evaluation grid for FP32 spectra without interlacing, in
 // FP32.
 void launch_build_G_f32(Context& ctx, const Geom& g, const int M[3],
@@ -576,7 +584,8 @@ bool launch_pair_bessel_gram(Context& ctx, const Geom& g, int64_t nkeys,
                              const int* pa, const int* pb, int npairs,
                              double* out, const double* rkey = nullptr);
 // Sums of xi y_a y_b over cells of any shape, keyed by (|s_x|, |s_y|,
-// |s_z|) on (n/2 + 1)^3 keys, with each key's radius in rkey.
+// |s_z|) on (n - n/2 + 1)^3 keys (per axis), with each key's radius in
+// rkey.
 template <class Real>
 void launch_octant_cell_hist(Context& ctx, const Geom& g, const Real* xi_re,
                              const Real* xi_im, int ell_a, int m_a, int ell_b,

@@ -278,13 +278,13 @@ reduce_pairs_gram_real_kernel(int64_t ncell, const float* G, const float* Fa,
 // reads the TI leg-a and TJ leg-b values of one cell as 16-byte vectors and
 // updates a TI x TJ tile of field pairs from them (TI + TJ loads for TI TJ
 // products).  Every field is read from HBM once per launch.  The products
-// of kGramRun cells are summed in FP32 and then added to float-float
+// of kGramRun (16) cells are summed in FP32 and then added to float-float
 // accumulators (TwoSum), so the accumulated sum keeps the error of an FP32
 // sum of kGramRun terms per run rather than of the whole grid.  The
 // threads of a tile split the chunk's cells into slices; the slices are
 // summed in FP64 at the end and each data-vector entry gets one atomic add
 // per block.
-constexpr int kGramRun = 8;
+constexpr int kGramRun = 16;
 constexpr int kGramThreads = 256;
 
 __device__ __forceinline__ void cp_async_val(float* s, const float* g) {
@@ -321,9 +321,9 @@ __global__ void __launch_bounds__(kGramThreads, 2)
 reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
                           const float* __restrict__ Fa, int na, int rsa,
                           const float* __restrict__ Fb, int nb, int rsb,
-                          bool same, const int2* __restrict__ tiles,
-                          int ntiles, const int* __restrict__ slot,
-                          double* out) {
+                          unsigned mrsb, bool same,
+                          const int2* __restrict__ tiles, int ntiles,
+                          const int* __restrict__ slot, double* out) {
   using V = typename std::conditional<CPLX, float2, float>::type;
   constexpr int W = CPLX ? 2 : 1;  // floats per value
   constexpr int NP = TI * TJ * W;  // partial sums per thread
@@ -393,7 +393,8 @@ reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
     V* Bs = As + CELLS * rsa;
     const V* Gs = Bs + CELLS * rsb;
     for (int w = tid; w < rsb * CELLS; w += kGramThreads) {
-      const int c = w / rsb, r = w - c * rsb;
+      // w / rsb by the multiplier ceil(2^32 / rsb) (exact: w < 2^16).
+      const int c = int(__umulhi(unsigned(w), mrsb)), r = w - c * rsb;
       V b;
       if (same) b = r < na ? As[c * rsa + r] : gram_zero(V());
       else b = Bs[c * rsb + r];
@@ -1021,14 +1022,19 @@ pair_bessel_gram_ff_kernel(int64_t nkeys, double dr, const double* rkey,
       if (!on[u]) continue;
       const float2* ja = J + ia[u] * kGramRow;
       const float2* jb = J + ib[u] * kGramRow;
+      // Unnormalised float-float sums over the chunk (the next operation
+      // splits the leading words again), normalised once per chunk.
+      FF sr = acc[2 * u], si = acc[2 * u + 1];
       for (int k = 0; k < kGramKeys; ++k) {
         const float4 h = H[k];
         if (h.x == 0.f && h.z == 0.f) continue;
         const float2 a = ja[k], b = jb[k];
         const FF w = ffmul(FF{a.x, a.y}, FF{b.x, b.y});
-        ff_merge(acc[2 * u], ffnorm(ffmul(w, FF{h.x, h.y})));
-        ff_merge(acc[2 * u + 1], ffnorm(ffmul(w, FF{h.z, h.w})));
+        sr = ffadd(sr, ffmul(w, FF{h.x, h.y}));
+        si = ffadd(si, ffmul(w, FF{h.z, h.w}));
       }
+      acc[2 * u] = ffnorm(sr);
+      acc[2 * u + 1] = ffnorm(si);
     }
   }
 #pragma unroll
@@ -1309,6 +1315,9 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
   const size_t smem = gram_smem(cplx, na, nb);
   // One field set for both legs: stage it once.
   const bool same = Fa == Fb && na == nb;
+  // Multiplier of the division by rsb in the F_b G pass (rsb < 2^8, the
+  // dividend below rsb * cells < 2^16).
+  const unsigned mrsb = unsigned((uint64_t(1) << 32) / unsigned(rsb) + 1);
   const int cells = gram_cells(cplx);
   const int64_t chunks = (ncell + cells - 1) / cells;
   dim3 grid(unsigned(std::min<int64_t>(chunks, 152 * 2)),
@@ -1328,7 +1337,8 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
     }
     TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
     kernel<<<grid, kGramThreads, smem, ctx.stream>>>(
-        ncell, G, Fa, na, rsa, Fb, nb, rsb, same, tiles, ntiles, slot, out);
+        ncell, G, Fa, na, rsa, Fb, nb, rsb, mrsb, same, tiles, ntiles, slot,
+        out);
     TRVG_LAUNCHED(ctx);
   };
   if (cplx)

@@ -1011,6 +1011,44 @@ twopt_field_kernel(Geom g, FieldSpec<Real> fa, FieldSpec<Real> fb, cd shot,
   }
 }
 
+// twopt_field_kernel for FP32 spectra without interlacing, in FP32 (1 / C_1
+// from the per-axis FP32 tables): the complex survey fields.
+__device__ __forceinline__ float2 twopt_mode_f32(const Geom& g,
+                                                 const FieldSpec<float>& fa,
+                                                 const FieldSpec<float>& fb,
+                                                 float2 shot, const InvWinF& ia,
+                                                 int i, int j, int k) {
+  const float2 va = field_value_f(fa, g, i, j, k);
+  const float2 vb = field_value_f(fb, g, i, j, k);
+  const float inv = ia.w[0][i] * ia.w[1][j] * ia.w[2][k];
+  return make_float2((va.x * vb.x + va.y * vb.y) * inv - shot.x,
+                     (va.y * vb.x - va.x * vb.y) * inv - shot.y);
+}
+
+__global__ void __launch_bounds__(256)
+twopt_field_f32_kernel(Geom g, FieldSpec<float> fa, FieldSpec<float> fb,
+                       float2 shot, InvWinF ia, float inv_vol, float2* out_re,
+                       float2* out_im) {
+  const int row = blockIdx.x;
+  const int i = row / g.n[1], j = row - (row / g.n[1]) * g.n[1];
+  for (int k = threadIdx.x; k < g.nzh; k += blockDim.x) {
+    const int64_t t = int64_t(row) * g.nzh + k;
+    const float2 p = twopt_mode_f32(g, fa, fb, shot, ia, i, j, k);
+    if (out_im == nullptr) {
+      out_re[t] = make_float2(p.x * inv_vol, p.y * inv_vol);
+    } else {
+      const int ii = (i == 0) ? 0 : g.n[0] - i;
+      const int jj = (j == 0) ? 0 : g.n[1] - j;
+      const int kk = (k == 0) ? 0 : g.n[2] - k;
+      float2 q = twopt_mode_f32(g, fa, fb, shot, ia, ii, jj, kk);
+      q.y = -q.y;
+      const float h = 0.5f * inv_vol;
+      out_re[t] = make_float2((p.x + q.x) * h, (p.y + q.y) * h);
+      out_im[t] = make_float2((p.y - q.y) * h, -(p.x - q.x) * h);
+    }
+  }
+}
+
 // FP32 fast path for two real-mesh spectra without interlacing:
 // P = (fa fb^* / C_1 - S) / V in float, the k = 0 mode given exactly.
 // One element of the FP32 shot-noise field at flat half-spectrum index t.
@@ -1275,6 +1313,18 @@ void launch_twopt_field(Context& ctx, const Geom& g, const FieldSpec<Real>& fa,
   TRVG_KBEGIN(ctx, "twopt_field_kernel");
   twopt_field_kernel<Real, XR><<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
       g, fa, fb, shot, ax, out_re, out_im);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_twopt_field_f32(Context& ctx, const Geom& g,
+                            const FieldSpec<float>& fa,
+                            const FieldSpec<float>& fb, float2 shot,
+                            const float* const inv_alias[3], float2* out_re,
+                            float2* out_im) {
+  InvWinF ia{{inv_alias[0], inv_alias[1], inv_alias[2]}};
+  TRVG_KBEGIN(ctx, "twopt_field_kernel");
+  twopt_field_f32_kernel<<<g.n[0] * g.n[1], 256, 0, ctx.stream>>>(
+      g, fa, fb, shot, ia, float(1. / g.vol), out_re, out_im);
   TRVG_LAUNCHED(ctx);
 }
 
