@@ -75,6 +75,9 @@ def parse_args():
     ap.add_argument('--mesh-comp', type=int, default=2, choices=[0, 1, 2],
                     help='compensated FP32 mesh deposit (library option '
                          '"mesh_comp")')
+    ap.add_argument('--side-priority', type=int, default=0, choices=[0, 1],
+                    help='priority of the second stream (library option '
+                         '"side_priority")')
     ap.add_argument('--seed', type=int, default=42,
                     help='seed of the uniform catalogue (metric workload)')
     ap.add_argument('--ff-transforms', type=int, default=1, choices=[0, 1, 2],
@@ -308,6 +311,7 @@ def run_gb300(args):
     ctx.set_option('assign_path', args.assign_path)
     ctx.set_option('mesh_comp', args.mesh_comp)
     ctx.set_option('ff_transforms', args.ff_transforms)
+    ctx.set_option('side_priority', args.side_priority)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
 
@@ -406,6 +410,7 @@ def run_gb300(args):
     cold.set_option('assign_path', args.assign_path)
     cold.set_option('mesh_comp', args.mesh_comp)
     cold.set_option('ff_transforms', args.ff_transforms)
+    cold.set_option('side_priority', args.side_priority)
     cold.set_stream(stream.cuda_stream)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()

@@ -226,6 +226,8 @@ int trvg_context_set_stream(trvg_context* ctx, void* stream);
  *                           periodic-box bispectrum on a second stream next
  *                           to the float-float shell fields (default 1; off
  *                           while profiling and in batch replays);
+ *   "side_priority"    0/1: create the second stream at the default (0)
+ *                           or the device's greatest priority (1);
  *   "xi_octant"        0/1: FP32 periodic-box bispectra with m = 0 legs of
  *                           even total degree: keep the shot-noise field
  *                           averaged over sign flips on one octant (three

@@ -121,7 +121,16 @@ cudaEvent_t next_event(Context& c) {
 
 cudaStream_t Context::side_stream() {
   if (side == nullptr) {
-    TRVG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    int prio = 0;
+    if (side_priority != 0) {
+      int least = 0, greatest = 0;
+      TRVG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      prio = greatest;
+    }
+    TRVG_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking,
+                                           prio));
+  }
+  if (ev_fork == nullptr) {
     TRVG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     TRVG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   }
@@ -316,6 +325,16 @@ int trvg_set_option(trvg_context* ctx, const char* key, int64_t value) {
     if (value == 0) ctx->impl.tuned.clear();
   } else if (k == "overlap") {
     ctx->impl.overlap = value != 0;
+  } else if (k == "side_priority") {
+    if (value < 0 || value > 1)
+      trvg::throw_error(TRVG_ERR_INVALID_PARAMETER,
+                        "side_priority must be 0 or 1.");
+    if (ctx->impl.side != nullptr && ctx->impl.side_priority != int(value)) {
+      TRVG_CUDA(cudaStreamSynchronize(ctx->impl.side));
+      TRVG_CUDA(cudaStreamDestroy(ctx->impl.side));
+      ctx->impl.side = nullptr;
+    }
+    ctx->impl.side_priority = int(value);
   } else if (k == "xi_octant") {
     ctx->impl.xi_octant = value != 0;
   } else if (k == "fused_ylm") {

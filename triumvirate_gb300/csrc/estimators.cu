@@ -1745,6 +1745,11 @@ struct Engine {
   // Spectrum of the source's FP32 mesh on the cube |sx|, |sy| <= kg,
   // 0 <= sz <= kg by the float-float z, y and x passes.
   const float4* ff_forward(const FieldSpec<Real>& src, int kg) {
+    // Already transformed in this estimate (not while capturing a batch).
+    if (replay == nullptr && ff_cube.cube != nullptr && ff_cube.half == kg &&
+        ff_cube.spec == src.re && ff_cube.gen == src.mesh_gen &&
+        src.mesh_gen == ctx.mesh_gen)
+      return ff_cube.cube;
     float4* T1 = ctx.buf<float4>(
         "ff.T1", size_t(g.n[0]) * (kg + 1) * g.n[1]);
     float4* T2 = ctx.buf<float4>(
@@ -2153,6 +2158,10 @@ struct Engine {
           ff_applicable(dn, dn, la0, lb0, pairs, hb, M, K)) {
         const cudaStream_t main = ctx.stream, side = ctx.side_stream();
         TRVG_CUDA(cudaEventRecord(ctx.ev_fork, main));
+        // The float-float forward transform of the mesh is submitted before
+        // the side work (which waits only for the deposit), so that the
+        // side kernels fill the SMs the transform's blocks leave.
+        ff_forward(dn, 2 * K[0]);
         TRVG_CUDA(cudaStreamWaitEvent(side, ctx.ev_fork, 0));
         ctx.stream = side;
         try {

@@ -125,6 +125,9 @@ struct Context {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool overlap = true;
+  // Priority of the second stream: 0 the default, 1 the device's greatest
+  // (its blocks are dispatched first whenever an SM has room).
+  int side_priority = 0;
   cudaStream_t side_stream();
   int verbose = 0;
   // Counters of the current / last call.
