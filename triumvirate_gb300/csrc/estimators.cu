@@ -2018,11 +2018,19 @@ struct Engine {
         const int* dpb = upload("pairs.b", pb);
         double* dout = ctx.buf<double>("pairs.out", 2 * idx.size());
         zero(dout, 2 * idx.size() * sizeof(double));
+        // FP32 fields: the register-tiled Gram form when the pairs fill
+        // its tiles (several pairs per field), otherwise (diagonal forms)
+        // the streaming form, which reads every field once and holds a few
+        // pairs per thread.
         bool tiled = false;
+        const int nmax = int(std::max(bA.size(), bB.size()));
+        const bool dense = int(idx.size()) >= 2 * nmax;
+        int na_gram = int(bA.size()), nb_gram = int(bB.size());
         if constexpr (sizeof(FR) == 4) {
           vector<int2> tl;
           vector<int> slot;
-          if (!ctx.gram_per_pair &&
+          if (!ctx.gram_per_pair && !dense) na_gram = nb_gram = 0;
+          if (!ctx.gram_per_pair && dense &&
               gram_tile_list(!real, int(bA.size()), int(bB.size()), pa, pb,
                              tl, slot)) {
             const int2* dt = upload("gram.tiles", tl);
@@ -2041,12 +2049,11 @@ struct Engine {
           ;
         else if (real)
           launch_reduce_pairs_real<FR>(ctx, Mc, Gr, FAr, FBr, dpa, dpb,
-                                       int(idx.size()), dout, int(bA.size()),
-                                       int(bB.size()));
+                                       int(idx.size()), dout, na_gram,
+                                       nb_gram);
         else
           launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb,
-                                  int(idx.size()), dout, int(bA.size()),
-                                  int(bB.size()));
+                                  int(idx.size()), dout, na_gram, nb_gram);
         vector<double> h = download(dout, 2 * idx.size());
         for (size_t q = 0; q < idx.size(); ++q)
           res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);
