@@ -469,6 +469,213 @@ reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
   }
 }
 
+// The same register-tiled Gram form with row-major staging, for fields
+// whose rows start on 16-byte boundaries: a chunk of CELLS cells of every
+// leg-a row, leg-b row and G is copied with 16-byte cp.async into rows of
+// CELLS values (plus 16 bytes of padding), F_b G is formed with vector
+// operations, and a thread updates its TI x TJ tile from two cells per
+// step (one 8-byte load per real row, one 16-byte load per complex row).
+// The copies and the F_b G pass cost a quarter of the per-element
+// transposing form's instructions and write shared memory without bank
+// conflicts.
+template <bool CPLX, int TI, int TJ, int CELLS>
+__global__ void __launch_bounds__(kGramThreads, 2)
+reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
+                         const float* __restrict__ Fa, int na, int rsa,
+                         const float* __restrict__ Fb, int nb, int rsb,
+                         bool same, const int2* __restrict__ tiles,
+                         int ntiles, const int* __restrict__ slot,
+                         double* out) {
+  constexpr int W = CPLX ? 2 : 1;          // floats per value
+  constexpr int NP = TI * TJ * W;          // partial sums per thread
+  constexpr int ROW = CELLS * W + 4;       // floats per staged row
+  constexpr int VPR = CELLS * W / 4;       // 16-byte vectors per row
+  constexpr int STEPS = CELLS / 2;         // two cells per step
+  extern __shared__ float4 gsm4[];
+  float* const sbase = reinterpret_cast<float*>(gsm4);
+  const int stage = (rsa + rsb + 1) * ROW;  // floats per buffer
+  const int g0 = blockIdx.y * kGramThreads;
+  const int T = min(kGramThreads, ntiles - g0);
+  const int S = kGramThreads / T;
+  const int tid = threadIdx.x;
+  const bool active = tid < S * T;
+  const int tile = tid % T, slice = tid / T;
+  int i0 = 0, j0 = 0;
+  if (active) {
+    const int2 tl = tiles[g0 + tile];
+    i0 = tl.x * TI;
+    j0 = tl.y * TJ;
+  }
+  float p[NP];
+  FF acc[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    p[q] = 0.f;
+    acc[q] = ff_zero();
+  }
+  int run = 0;
+  const int64_t nfl = ncell * W;  // floats per field
+  // Rows fetched per chunk: leg a, leg b (unless one field set), G.
+  const int nfetch = rsa + (same ? 0 : rsb) + 1;
+  auto issue = [&](int64_t c0, int buf) {
+    float* base = sbase + buf * stage;
+    const int64_t f0 = c0 * W;  // first float of the chunk in a row
+    for (int w = tid; w < nfetch * VPR; w += kGramThreads) {
+      const int row = w / VPR, v = w - row * VPR;
+      const float* src;
+      float* dst;
+      bool valid;
+      if (row < rsa) {
+        dst = base + row * ROW;
+        valid = row < na;
+        src = Fa + int64_t(row) * nfl;
+      } else if (row == nfetch - 1) {
+        dst = base + (rsa + rsb) * ROW;
+        valid = true;
+        src = G;
+      } else {
+        const int r = row - rsa;
+        dst = base + (rsa + r) * ROW;
+        valid = r < nb;
+        src = Fb + int64_t(r) * nfl;
+      }
+      dst += 4 * v;
+      const int64_t e = f0 + 4 * v;  // first float of the vector
+      if (valid && e + 4 <= nfl) {
+        const unsigned a =
+            static_cast<unsigned>(__cvta_generic_to_shared(dst));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a),
+                     "l"(src + e)
+                     : "memory");
+      } else {
+        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {  // the tail of the last chunk
+          float t[4] = {0.f, 0.f, 0.f, 0.f};
+          for (int k = 0; k < 4; ++k)
+            if (e + k < nfl) t[k] = src[e + k];
+          z = make_float4(t[0], t[1], t[2], t[3]);
+        }
+        *reinterpret_cast<float4*>(dst) = z;
+      }
+    }
+    cp_async_commit();
+  };
+  const int64_t step = int64_t(gridDim.x) * CELLS;
+  int64_t c0 = int64_t(blockIdx.x) * CELLS;
+  int buf = 0;
+  if (c0 < ncell) issue(c0, 0);
+  for (; c0 < ncell; c0 += step, buf ^= 1) {
+    if (c0 + step < ncell) issue(c0 + step, buf ^ 1);
+    else cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    float* As = sbase + buf * stage;
+    float* Bs = As + rsa * ROW;
+    const float* Gs = Bs + rsb * ROW;
+    // F_b G in place (from the staged F_a when both legs are one set).
+    for (int w = tid; w < rsb * VPR; w += kGramThreads) {
+      const int r = w / VPR, v = w - r * VPR;
+      float4 b;
+      if (same)
+        b = r < na ? reinterpret_cast<const float4*>(As + r * ROW)[v]
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+      else
+        b = reinterpret_cast<const float4*>(Bs + r * ROW)[v];
+      const float4 gg = reinterpret_cast<const float4*>(Gs)[v];
+      float4 o;
+      if constexpr (CPLX) {
+        o = make_float4(b.x * gg.x - b.y * gg.y, b.x * gg.y + b.y * gg.x,
+                        b.z * gg.z - b.w * gg.w, b.z * gg.w + b.w * gg.z);
+      } else {
+        o = make_float4(b.x * gg.x, b.y * gg.y, b.z * gg.z, b.w * gg.w);
+      }
+      reinterpret_cast<float4*>(Bs + r * ROW)[v] = o;
+    }
+    __syncthreads();
+    if (active) {
+      const int cend = ncell - c0 < CELLS ? int(ncell - c0) : CELLS;
+      const int send = (cend + 1) / 2;  // the padding cell of an odd tail is 0
+      for (int st = slice; st < send; st += S) {
+        // Two cells: a[i] (and b[j]) hold cell 2 st then cell 2 st + 1.
+        float a[TI][2 * W], b[TJ][2 * W];
+#pragma unroll
+        for (int i = 0; i < TI; ++i) {
+          const float* r = As + (i0 + i) * ROW + 2 * W * st;
+          if constexpr (CPLX) {
+            const float4 v = *reinterpret_cast<const float4*>(r);
+            a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
+          } else {
+            const float2 v = *reinterpret_cast<const float2*>(r);
+            a[i][0] = v.x; a[i][1] = v.y;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < TJ; ++j) {
+          const float* r = Bs + (j0 + j) * ROW + 2 * W * st;
+          if constexpr (CPLX) {
+            const float4 v = *reinterpret_cast<const float4*>(r);
+            b[j][0] = v.x; b[j][1] = v.y; b[j][2] = v.z; b[j][3] = v.w;
+          } else {
+            const float2 v = *reinterpret_cast<const float2*>(r);
+            b[j][0] = v.x; b[j][1] = v.y;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < TI; ++i)
+#pragma unroll
+          for (int j = 0; j < TJ; ++j) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              if constexpr (CPLX) {
+                float& re = p[2 * (i * TJ + j)];
+                float& im = p[2 * (i * TJ + j) + 1];
+                re = fmaf(a[i][2 * k], b[j][2 * k], re);
+                re = fmaf(-a[i][2 * k + 1], b[j][2 * k + 1], re);
+                im = fmaf(a[i][2 * k], b[j][2 * k + 1], im);
+                im = fmaf(a[i][2 * k + 1], b[j][2 * k], im);
+              } else {
+                p[i * TJ + j] = fmaf(a[i][k], b[j][k], p[i * TJ + j]);
+              }
+            }
+          }
+        run += 2;
+        if (run >= kGramRun) {
+          run = 0;
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            ff_add(acc[q], p[q]);
+            p[q] = 0.f;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+#pragma unroll
+  for (int q = 0; q < NP; ++q) ff_add(acc[q], p[q]);
+  __syncthreads();
+  double* red = reinterpret_cast<double*>(gsm4);  // [S][T][NP]
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+      red[(slice * T + tile) * NP + q] = ff_value(acc[q]);
+  }
+  __syncthreads();
+  for (int w = tid; w < T * NP; w += kGramThreads) {
+    const int tl = w / NP, q = w - tl * NP;
+    double sum = 0.;
+    for (int u = 0; u < S; ++u) sum += red[(u * T + tl) * NP + q];
+    const int2 tt = tiles[g0 + tl];
+    const int pr = q / W, comp = q - pr * W;
+    const int i = tt.x * TI + pr / TJ, j = tt.y * TJ + pr % TJ;
+    if (i < na && j < nb) {
+      const int sl = slot[int64_t(i) * nb + j];
+      if (sl >= 0) atomicAdd(out + 2 * int64_t(sl) + comp, sum);
+    }
+  }
+}
+
 // Real fields: sum_x F_a F_b G; the imaginary part of the output is left
 // at zero.
 template <class Real>
@@ -1341,6 +1548,37 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
         out);
     TRVG_LAUNCHED(ctx);
   };
+  // Row-major staging with 16-byte copies when every row starts on a
+  // 16-byte boundary (cells per row a multiple of 4 / floats per value).
+  const int w = cplx ? 2 : 1;
+  const size_t smem_rows =
+      std::max(2 * size_t(rsa + rsb + 1) * (cells * w + 4) * 4,
+               size_t(kGramThreads) * gram_tile(cplx).ti *
+                   gram_tile(cplx).tj * w * 8);
+  if (!ctx.gram_per_pair && (ncell * w) % 4 == 0 &&
+      smem_rows <= kGramSmemMax) {
+    static bool rows_configured[2][64] = {};
+    bool* done = (ctx.device >= 0 && ctx.device < 64)
+                     ? &rows_configured[cplx ? 1 : 0][ctx.device]
+                     : nullptr;
+    auto rows = [&](auto kernel) {
+      if (done == nullptr || !*done) {
+        TRVG_CUDA(cudaFuncSetAttribute(
+            kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            int(kGramSmemMax)));
+        if (done != nullptr) *done = true;
+      }
+      TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
+      kernel<<<grid, kGramThreads, smem_rows, ctx.stream>>>(
+          ncell, G, Fa, na, rsa, Fb, nb, rsb, same, tiles, ntiles, slot, out);
+      TRVG_LAUNCHED(ctx);
+    };
+    if (cplx)
+      rows(reduce_pairs_rows_kernel<true, 2, 4, 64>);
+    else
+      rows(reduce_pairs_rows_kernel<false, 4, 8, 128>);
+    return;
+  }
   if (cplx)
     go(reduce_pairs_tiled_kernel<true, 2, 4, 64>);
   else
