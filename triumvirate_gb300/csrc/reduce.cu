@@ -493,7 +493,11 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
   constexpr int STEPS = CELLS / 2;         // two cells per step
   extern __shared__ float4 gsm4[];
   float* const sbase = reinterpret_cast<float*>(gsm4);
-  const int stage = (rsa + rsb + 1) * ROW;  // floats per buffer
+  // Staged row R (leg a, then leg b, then G) starts at off(R): rows eight
+  // apart (the B rows of neighbouring tiles) fall 16 bytes apart in the
+  // banks instead of on the same bank.
+  auto off = [](int R) { return R * ROW + 4 * ((R >> 3) & 7); };
+  const int stage = (rsa + rsb + 1) * ROW + 32;  // floats per buffer
   const int g0 = blockIdx.y * kGramThreads;
   const int T = min(kGramThreads, ntiles - g0);
   const int S = kGramThreads / T;
@@ -526,16 +530,16 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
       float* dst;
       bool valid;
       if (row < rsa) {
-        dst = base + row * ROW;
+        dst = base + off(row);
         valid = row < na;
         src = Fa + int64_t(row) * nfl;
       } else if (row == nfetch - 1) {
-        dst = base + (rsa + rsb) * ROW;
+        dst = base + off(rsa + rsb);
         valid = true;
         src = G;
       } else {
         const int r = row - rsa;
-        dst = base + (rsa + r) * ROW;
+        dst = base + off(rsa + r);
         valid = r < nb;
         src = Fb + int64_t(r) * nfl;
       }
@@ -569,18 +573,18 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    float* As = sbase + buf * stage;
-    float* Bs = As + rsa * ROW;
-    const float* Gs = Bs + rsb * ROW;
+    float* const base = sbase + buf * stage;
+    const float* Gs = base + off(rsa + rsb);
     // F_b G in place (from the staged F_a when both legs are one set).
     for (int w = tid; w < rsb * VPR; w += kGramThreads) {
       const int r = w / VPR, v = w - r * VPR;
+      float* brow = base + off(rsa + r);
       float4 b;
       if (same)
-        b = r < na ? reinterpret_cast<const float4*>(As + r * ROW)[v]
+        b = r < na ? reinterpret_cast<const float4*>(base + off(r))[v]
                    : make_float4(0.f, 0.f, 0.f, 0.f);
       else
-        b = reinterpret_cast<const float4*>(Bs + r * ROW)[v];
+        b = reinterpret_cast<const float4*>(brow)[v];
       const float4 gg = reinterpret_cast<const float4*>(Gs)[v];
       float4 o;
       if constexpr (CPLX) {
@@ -589,7 +593,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
       } else {
         o = make_float4(b.x * gg.x, b.y * gg.y, b.z * gg.z, b.w * gg.w);
       }
-      reinterpret_cast<float4*>(Bs + r * ROW)[v] = o;
+      reinterpret_cast<float4*>(brow)[v] = o;
     }
     __syncthreads();
     if (active) {
@@ -600,7 +604,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
         float a[TI][2 * W], b[TJ][2 * W];
 #pragma unroll
         for (int i = 0; i < TI; ++i) {
-          const float* r = As + (i0 + i) * ROW + 2 * W * st;
+          const float* r = base + off(i0 + i) + 2 * W * st;
           if constexpr (CPLX) {
             const float4 v = *reinterpret_cast<const float4*>(r);
             a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
@@ -611,7 +615,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
         }
 #pragma unroll
         for (int j = 0; j < TJ; ++j) {
-          const float* r = Bs + (j0 + j) * ROW + 2 * W * st;
+          const float* r = base + off(rsa + j0 + j) + 2 * W * st;
           if constexpr (CPLX) {
             const float4 v = *reinterpret_cast<const float4*>(r);
             b[j][0] = v.x; b[j][1] = v.y; b[j][2] = v.z; b[j][3] = v.w;
@@ -1552,7 +1556,7 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
   // 16-byte boundary (cells per row a multiple of 4 / floats per value).
   const int w = cplx ? 2 : 1;
   const size_t smem_rows =
-      std::max(2 * size_t(rsa + rsb + 1) * (cells * w + 4) * 4,
+      std::max(2 * (size_t(rsa + rsb + 1) * (cells * w + 4) + 32) * 4,
                size_t(kGramThreads) * gram_tile(cplx).ti *
                    gram_tile(cplx).tj * w * 8);
   if (!ctx.gram_per_pair && (ncell * w) % 4 == 0 &&
