@@ -2899,6 +2899,15 @@ struct Engine {
     vector<int> smin, smax;
     sample_ranges(hb, 1., 100000, smin, smax);
     BinsDev bd = bins_dev("rb", hb, &smin, &smax);
+    {
+      // A cell of r >= the last bin's end (sample step 1) is in no bin, and
+      // r >= min(dr) sqrt(s_x^2 + s_y^2 + s_z^2).
+      int smax_max = 0;
+      for (int v : smax) smax_max = std::max(smax_max, v);
+      const double drmin = std::min(g.dr[0], std::min(g.dr[1], g.dr[2]));
+      const double q = double(smax_max) / drmin;
+      bd.key_max = int64_t(std::ceil(q * q * (1. + 1e-6))) + 1;
+    }
 
     vector<cplx> zeta(ndv, 0.), sn(ndv, 0.);
     vector<long long> npairs(hb.nb, 0);

@@ -154,6 +154,9 @@ struct BinsDev {
   const double* hi = nullptr;
   const int* smin = nullptr;   // first fine sample index in the bin
   const int* smax = nullptr;   // one past the last
+  // Cells with s_x^2 + s_y^2 + s_z^2 above key_max lie beyond every bin
+  // (-1: no such bound).
+  int64_t key_max = -1;
 };
 
 // ---- shot-noise field on one octant (spectral.cu, reduce.cu) --------------

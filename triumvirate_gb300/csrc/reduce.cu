@@ -1369,9 +1369,15 @@ shotnoise_3pcf_kernel(Geom g, const Real* xi_re, const Real* xi_im, int ell_a,
     const int k = int(t % g.n[2]);
     const int j = int((t / g.n[2]) % g.n[1]);
     const int i = int(t / (int64_t(g.n[2]) * g.n[1]));
-    const double rx = dmul(double(shift_index(i, g.n[0])), g.dr[0]);
-    const double ry = dmul(double(shift_index(j, g.n[1])), g.dr[1]);
-    const double rz = dmul(double(shift_index(k, g.n[2])), g.dr[2]);
+    const int sx = shift_index(i, g.n[0]), sy = shift_index(j, g.n[1]),
+              sz = shift_index(k, g.n[2]);
+    // Beyond every bin by an integer test (no FP64 for most cells).
+    if (bins.key_max >= 0 &&
+        int64_t(sx) * sx + int64_t(sy) * sy + int64_t(sz) * sz > bins.key_max)
+      continue;
+    const double rx = dmul(double(sx), g.dr[0]);
+    const double ry = dmul(double(sy), g.dr[1]);
+    const double rz = dmul(double(sz), g.dr[2]);
     const double r = vec3_mag(rx, ry, rz);
     const int idx_r = int(ddiv(r, 1.));
     if (idx_r < 0 || idx_r >= n_sample) continue;
