@@ -1047,6 +1047,27 @@ def run_large(args):
             entry["max_rel_err_fp32mixed"] = per_bin_err_keys(r32, r64, keys)
             cnt = 'nmodes_1' if kind == 'bispec' else 'npairs_1'
             entry["counts_equal"] = bool(np.array_equal(r32[cnt], r64[cnt]))
+            if kind == 'bispec':
+                # The same estimate with FP32 cuFFT shell fields (option
+                # ff_transforms = 0) instead of the float-float transforms.
+                ctx.set_option('ff_transforms', 0)
+                try:
+                    est('fp32mixed')
+                    t32 = []
+                    for _ in range(2):
+                        torch.cuda.synchronize(dev)
+                        e0 = torch.cuda.Event(enable_timing=True)
+                        e1 = torch.cuda.Event(enable_timing=True)
+                        e0.record(stream)
+                        rf = est('fp32mixed')
+                        e1.record(stream)
+                        torch.cuda.synchronize(dev)
+                        t32.append(e0.elapsed_time(e1) / 1e3)
+                finally:
+                    ctx.set_option('ff_transforms', 1)
+                entry["fp32_fft_variant"] = {
+                    "s_per_estimate": round(statistics.median(t32), 4),
+                    "max_rel_err_vs_fp64": per_bin_err_keys(rf, r64, keys)}
         out[name] = entry
         print(f"# {name}: {json.dumps(entry)}", file=sys.stderr, flush=True)
     line = {

@@ -1726,7 +1726,17 @@ struct Engine {
     if (replay != nullptr) return ff_taken;  // as in the warm-up estimate
     size_t free_b = 0, total_b = 0;
     TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    return bytes < 0.6 * double(free_b);
+    // Buffers of an earlier float-float estimate are reused, not added.
+    double have = 0.;
+    for (const auto& kv : ctx.buffers)
+      if (kv.first.compare(0, 3, "ff.") == 0 ||
+          kv.first.compare(0, 4, "ffA.") == 0 ||
+          kv.first.compare(0, 4, "ffB.") == 0)
+        have += double(kv.second.bytes);
+    if (bytes < 0.6 * (double(free_b) + have)) return true;
+    ctx.log(10, "float-float shell fields need %.1f GB, %.1f GB free: FP32 "
+            "transforms", bytes / 1e9, (double(free_b) + have) / 1e9);
+    return false;
   }
 
   // 3PCF window with wide-angle corrections: G(x) *= r^-wide_angle_power.
@@ -1855,20 +1865,40 @@ struct Engine {
       pb[i] = int(std::lower_bound(B.begin(), B.end(), pairs[i].col) -
                   B.begin());
     }
-    const int* dpa = upload("pairs.a", pa);
-    const int* dpb = upload("pairs.b", pb);
     double* dout = ctx.buf<double>("pairs.out", 2 * size_t(np));
-    char key[96];
-    std::snprintf(key, sizeof(key), "pair_bin_batch.%dx%dx%d.pairs%d.%s",
-                  M[0], M[1], M[2], np, shared ? "shared" : "two");
-    const int ppb = tuned(key, {8, 4, 16}, [&](int c) {
+    // Pair lists with several pairs per field (full and upper-triangle
+    // forms) take the register-tiled Gram form on the hi words: rounding a
+    // field to FP32 perturbs each cell independently, far below the
+    // transforms' rounding, while the float-float products cost some 30
+    // FP32 instructions per pair and cell.  Diagonal lists keep the
+    // float-float streaming form.
+    const int nmax = int(std::max(A.size(), B.size()));
+    vector<int2> tl;
+    vector<int> slot;
+    if (!ctx.gram_per_pair && np >= 2 * nmax &&
+        gram_tile_list(false, int(A.size()), int(B.size()), pa, pb, tl,
+                       slot)) {
+      const int2* dt = upload("gram.tiles", tl);
+      const int* ds = upload("gram.slot", slot);
+      zero(dout, 2 * np * sizeof(double));
+      launch_reduce_pairs_tiled(ctx, Mc, false, G, FA, int(A.size()), FB,
+                                int(B.size()), dt, int(tl.size()), ds, dout,
+                                ld);
+    } else {
+      const int* dpa = upload("pairs.a", pa);
+      const int* dpb = upload("pairs.b", pb);
+      char key[96];
+      std::snprintf(key, sizeof(key), "pair_bin_batch.%dx%dx%d.pairs%d.%s",
+                    M[0], M[1], M[2], np, shared ? "shared" : "two");
+      const int ppb = tuned(key, {8, 4, 16}, [&](int c) {
+        zero(dout, 2 * np * sizeof(double));
+        launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa,
+                               dpb, np, dout, c);
+      });
       zero(dout, 2 * np * sizeof(double));
       launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb,
-                             np, dout, c);
-    });
-    zero(dout, 2 * np * sizeof(double));
-    launch_reduce_pairs_ff(ctx, Mc, ld, G, Gl, FA, FAl, FB, FBl, dpa, dpb, np,
-                           dout, ppb);
+                             np, dout, ppb);
+    }
     ff_taken = true;
     dev_pairs = dout;
     if (replay != nullptr) return vector<cplx>(np, cplx(0., 0.));

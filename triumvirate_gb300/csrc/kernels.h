@@ -387,7 +387,8 @@ void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,
 // stored as float pairs).  One thread accumulates a tile of ti leg-a by tj
 // leg-b fields; `tiles` lists the (a / ti, b / tj) tiles that hold at least
 // one data-vector entry and slot[a * nb + b] is the entry of field pair
-// (a, b), -1 when it has none.
+// (a, b), -1 when it has none.  Field r of a leg starts ld values after
+// field r - 1 (ld = 0: ncell).
 struct GramTile {
   int ti, tj;
 };
@@ -399,7 +400,8 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
                                const float* G, const float* Fa, int na,
                                const float* Fb, int nb, const int2* tiles,
                                int ntiles, const int* slot,
-                               double* out /* 2 per entry */);
+                               double* out /* 2 per entry */,
+                               int64_t ld = 0);
 
 // ---- ffft.cu -------------------------------------------------------------
 // Float-float transforms of the shell fields: a plan is the radix list of

@@ -323,7 +323,8 @@ reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
                           const float* __restrict__ Fb, int nb, int rsb,
                           unsigned mrsb, bool same,
                           const int2* __restrict__ tiles, int ntiles,
-                          const int* __restrict__ slot, double* out) {
+                          const int* __restrict__ slot, double* out,
+                          int64_t ld) {
   using V = typename std::conditional<CPLX, float2, float>::type;
   constexpr int W = CPLX ? 2 : 1;  // floats per value
   constexpr int NP = TI * TJ * W;  // partial sums per thread
@@ -366,14 +367,14 @@ reduce_pairs_tiled_kernel(int64_t ncell, const float* __restrict__ G,
       const V* src = nullptr;
       if (row < rsa) {
         dst = As + c * rsa + row;
-        if (row < na && cell < ncell) src = fa + int64_t(row) * ncell + cell;
+        if (row < na && cell < ncell) src = fa + int64_t(row) * ld + cell;
       } else if (row == nfetch - 1) {
         dst = Gs + c;
         if (cell < ncell) src = gv + cell;
       } else {
         const int r = row - rsa;
         dst = Bs + c * rsb + r;
-        if (r < nb && cell < ncell) src = fb + int64_t(r) * ncell + cell;
+        if (r < nb && cell < ncell) src = fb + int64_t(r) * ld + cell;
       }
       if (src != nullptr) cp_async_val(dst, src);
       else *dst = gram_zero(V());
@@ -485,7 +486,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
                          const float* __restrict__ Fb, int nb, int rsb,
                          bool same, const int2* __restrict__ tiles,
                          int ntiles, const int* __restrict__ slot,
-                         double* out) {
+                         double* out, int64_t ld) {
   constexpr int W = CPLX ? 2 : 1;          // floats per value
   constexpr int NP = TI * TJ * W;          // partial sums per thread
   constexpr int ROW = CELLS * W + 4;       // floats per staged row
@@ -493,11 +494,13 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
   constexpr int STEPS = CELLS / 2;         // two cells per step
   extern __shared__ float4 gsm4[];
   float* const sbase = reinterpret_cast<float*>(gsm4);
-  // Staged row R (leg a, then leg b, then G) starts at off(R): rows eight
-  // apart (the B rows of neighbouring tiles) fall 16 bytes apart in the
-  // banks instead of on the same bank.
-  auto off = [](int R) { return R * ROW + 4 * ((R >> 3) & 7); };
-  const int stage = (rsa + rsb + 1) * ROW + 32;  // floats per buffer
+  // Staged row R (leg a, then leg b, then G) starts at off(R): every eighth
+  // row is moved 16 bytes further, so that rows eight apart (the B rows of
+  // neighbouring tiles) fall 16 bytes apart in the banks instead of on the
+  // same bank.  The offsets only grow (rows never overlap).
+  auto off = [](int R) { return R * ROW + 4 * (R >> 3); };
+  const int nrow_all = rsa + rsb + 1;
+  const int stage = nrow_all * ROW + 4 * (nrow_all >> 3) + 4;  // floats
   const int g0 = blockIdx.y * kGramThreads;
   const int T = min(kGramThreads, ntiles - g0);
   const int S = kGramThreads / T;
@@ -519,6 +522,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
   }
   int run = 0;
   const int64_t nfl = ncell * W;  // floats per field
+  const int64_t rfl = ld * W;     // floats between fields
   // Rows fetched per chunk: leg a, leg b (unless one field set), G.
   const int nfetch = rsa + (same ? 0 : rsb) + 1;
   auto issue = [&](int64_t c0, int buf) {
@@ -532,7 +536,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
       if (row < rsa) {
         dst = base + off(row);
         valid = row < na;
-        src = Fa + int64_t(row) * nfl;
+        src = Fa + int64_t(row) * rfl;
       } else if (row == nfetch - 1) {
         dst = base + off(rsa + rsb);
         valid = true;
@@ -541,7 +545,7 @@ reduce_pairs_rows_kernel(int64_t ncell, const float* __restrict__ G,
         const int r = row - rsa;
         dst = base + off(rsa + r);
         valid = r < nb;
-        src = Fb + int64_t(r) * nfl;
+        src = Fb + int64_t(r) * rfl;
       }
       dst += 4 * v;
       const int64_t e = f0 + 4 * v;  // first float of the vector
@@ -1521,8 +1525,14 @@ bool gram_tiled_fits(bool cplx, int na, int nb) {
 void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
                                const float* G, const float* Fa, int na,
                                const float* Fb, int nb, const int2* tiles,
-                               int ntiles, const int* slot, double* out) {
+                               int ntiles, const int* slot, double* out,
+                               int64_t ld) {
   if (ntiles <= 0 || ncell <= 0) return;
+  if (ld == 0) ld = ncell;
+  if (ld < ncell)
+    throw_error(TRVG_ERR_INVALID_PARAMETER,
+                "Tiled pair sums: field stride %lld below %lld cells.",
+                (long long)ld, (long long)ncell);
   if (!gram_tiled_fits(cplx, na, nb))
     throw_error(TRVG_ERR_INVALID_PARAMETER,
                 "Tiled pair sums: %d x %d fields exceed the staged chunk.",
@@ -1555,17 +1565,19 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
     TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
     kernel<<<grid, kGramThreads, smem, ctx.stream>>>(
         ncell, G, Fa, na, rsa, Fb, nb, rsb, mrsb, same, tiles, ntiles, slot,
-        out);
+        out, ld);
     TRVG_LAUNCHED(ctx);
   };
   // Row-major staging with 16-byte copies when every row starts on a
-  // 16-byte boundary (cells per row a multiple of 4 / floats per value).
+  // 16-byte boundary (field stride a multiple of 4 / floats per value).
   const int w = cplx ? 2 : 1;
+  const int nrow_all = rsa + rsb + 1;
   const size_t smem_rows =
-      std::max(2 * (size_t(rsa + rsb + 1) * (cells * w + 4) + 32) * 4,
+      std::max(2 * (size_t(nrow_all) * (cells * w + 4) +
+                    4 * size_t(nrow_all >> 3) + 4) * 4,
                size_t(kGramThreads) * gram_tile(cplx).ti *
                    gram_tile(cplx).tj * w * 8);
-  if (!ctx.gram_per_pair && (ncell * w) % 4 == 0 &&
+  if (!ctx.gram_per_pair && (ld * w) % 4 == 0 &&
       smem_rows <= kGramSmemMax) {
     static bool rows_configured[2][64] = {};
     bool* done = (ctx.device >= 0 && ctx.device < 64)
@@ -1580,7 +1592,8 @@ void launch_reduce_pairs_tiled(Context& ctx, int64_t ncell, bool cplx,
       }
       TRVG_KBEGIN(ctx, "reduce_pairs_tiled_kernel");
       kernel<<<grid, kGramThreads, smem_rows, ctx.stream>>>(
-          ncell, G, Fa, na, rsa, Fb, nb, rsb, same, tiles, ntiles, slot, out);
+          ncell, G, Fa, na, rsa, Fb, nb, rsb, same, tiles, ntiles, slot, out,
+          ld);
       TRVG_LAUNCHED(ctx);
     };
     if (cplx)
