@@ -997,6 +997,10 @@ def run_large(args):
             pp = params(deg, shape, precision)
             return _engine.call_threept(fn, ctx, pp, cat, binning, norm,
                                         kind, shape=shape)
+        # Each estimate starts from a context without the cached buffers of
+        # the previous ones, as a single call would (the float-float shell
+        # fields of B_202 need about 104 GB).
+        ctx.release_workspace()
         est('fp32mixed')
         times = []
         for _ in range(max(1, min(args.steps, 3))):
@@ -1022,6 +1026,20 @@ def run_large(args):
             mc = int(np.prod(ctx.stats()['pruned_grid']))
             nf = 40 if deg[0] == deg[1] else 80
             alg = 4 * mc * (1 + nf)
+        if alg is not None and dom.startswith('ff_inv_'):
+            # The table's mean counts two inverse launches (G, one leg of
+            # float-float fields).  Two legs make three; and the full forms
+            # reduce the fields in the tiled Gram form, which reads hi words
+            # only, so the z pass writes 4 B per cell, not 8.
+            g_half = algorithmic_bytes(
+                dom, argparse.Namespace(**{**vars(fa), 'nbins': 0}), 4)
+            ig, i_f = 2 * g_half, 2 * alg - 2 * g_half
+            if dom == 'ff_inv_z_kernel':
+                mc = int(np.prod(ctx.stats()['pruned_grid']))
+                ig -= 4 * mc
+                i_f -= 4 * mc * fa.nbins
+            legs = 1 if deg[0] == deg[1] else 2
+            alg = (ig + legs * i_f) / (1 + legs)
         roof = {"kernel": dom, "ms_per_launch": round(dom_ms, 4)}
         if alg is not None:
             ach = alg / (dom_ms * 1e-3) / 1e9
@@ -1036,7 +1054,9 @@ def run_large(args):
                  "top_kernels_ms": {k: round(v[0], 3) for k, v in sorted(
                      kt.items(), key=lambda kv: -kv[1][0])[:6]},
                  "roofline_dominant": roof,
-                 "evaluation_grid": list(ctx.stats()['pruned_grid'])}
+                 "evaluation_grid": list(ctx.stats()['pruned_grid']),
+                 "shell_transforms": ("float-float" if any(
+                     k.startswith('ff_') for k in kt) else "FP32 cuFFT")}
         if not args.no_fp64:
             t0 = time.perf_counter()
             r64 = est('fp64')

@@ -1714,15 +1714,40 @@ struct Engine {
     e.erase(std::unique(e.begin(), e.end()), e.end());
     for (size_t i = 1; i < e.size(); ++i)
       if (e[i].first < e[i - 1].second) return false;
-    // Device memory of the transforms (float4 scratch, float fields).
+    // Device memory of the transforms, as pair_sums_ff allocates it: the
+    // spectrum cube (float4), G's and each field's half spectrum, two
+    // scratch sets of planes, and the real fields (hi words, plus lo words
+    // unless the tiled Gram form reduces them).
     const int kg = 2 * K[0];
-    const double mc = double(M[0]) * M[1] * M[2];
+    const bool shared = la.ell == lb.ell && la.m == lb.m;
+    vector<int> A, B;
+    for (const Pair& q : pairs) {
+      A.push_back(q.row);
+      B.push_back(q.col);
+    }
+    if (shared) {
+      A.insert(A.end(), B.begin(), B.end());
+      B = A;
+    }
+    for (vector<int>* v : {&A, &B}) {
+      std::sort(v->begin(), v->end());
+      v->erase(std::unique(v->begin(), v->end()), v->end());
+    }
+    const double na = double(A.size()), nb = double(B.size());
+    const double nmax = std::max(na, nb);
+    const bool tiled = !ctx.gram_per_pair && double(pairs.size()) >= 2 * nmax &&
+                       gram_tiled_fits(false, int(na), int(nb));
+    const double plane_g = double(kg + 1) * M[1] * M[0];
+    const double plane_f = double(K[0] + 1) * M[1] * M[0];
+    const double nfields = na + (shared ? 0. : nb);
+    const double ld = double(ff_field_stride(int64_t(M[0]) * M[1] * M[2]));
     const double bytes =
         16. * (double(g.n[0]) * (kg + 1) * g.n[1] +
                double(2 * kg + 1) * (kg + 1) * g.n[0] +
                double(2 * kg + 1) * (2 * kg + 1) * (kg + 1)) +
-        16. * 3. * double(hb.nb) * (K[0] + 1) * M[0] * M[1] * 2. +
-        8. * mc * (2. * hb.nb + 1.);
+        16. * (plane_g + nfields * plane_f +
+               2. * std::max(plane_g, nmax * plane_f)) +
+        4. * ld * (tiled ? 1. : 2.) * (1. + nfields);
     if (replay != nullptr) return ff_taken;  // as in the warm-up estimate
     size_t free_b = 0, total_b = 0;
     TRVG_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -1823,15 +1848,38 @@ struct Engine {
     float4* Y1 = ctx.buf<float4>("ff.Y1", yn);
     float4* Y2 = ctx.buf<float4>("ff.Y2", yn);
 
+    vector<int> pa(np), pb(np);
+    for (int i = 0; i < np; ++i) {
+      pa[i] = int(std::lower_bound(A.begin(), A.end(), pairs[i].row) -
+                  A.begin());
+      pb[i] = int(std::lower_bound(B.begin(), B.end(), pairs[i].col) -
+                  B.begin());
+    }
+    // Pair lists with several pairs per field (full and upper-triangle
+    // forms) take the register-tiled Gram form on the hi words: rounding a
+    // field to FP32 perturbs each cell independently, far below the
+    // transforms' rounding, while the float-float products cost some 30
+    // FP32 instructions per pair and cell.  Diagonal lists keep the
+    // float-float streaming form.  The tiled form reads no lo words, so
+    // none are written.
+    const int nmax = int(std::max(A.size(), B.size()));
+    vector<int2> tl;
+    vector<int> slot;
+    const bool tiled =
+        !ctx.gram_per_pair && np >= 2 * nmax &&
+        gram_tile_list(false, int(A.size()), int(B.size()), pa, pb, tl, slot);
+    const size_t words = tiled ? 1 : 2;
+
     float4* EG = ctx.buf<float4>("ff.EG", plane_g);
     launch_ff_build_G(ctx, g, M, cube, kg, inv_win_ff, src.k0, EG,
                       src.k0_dev);
     const int64_t ld = ff_field_stride(Mc);
     float* G = ctx.buf<float>("ff.G", size_t(ld));
-    float* Gl = ctx.buf<float>("ff.G.lo", size_t(ld));
+    float* Gl = tiled ? nullptr : ctx.buf<float>("ff.G.lo", size_t(ld));
     launch_ff_inverse(ctx, M, 1, kg, kg, EG, Y1, Y2, G, Gl, ld);
 
-    // Float-float fields of one leg: hi words, lo words after nb * Mc.
+    // Float-float fields of one leg: hi words, lo words (when kept) after
+    // nb * ld.
     auto leg_fields = [&](const Leg& leg, const vector<int>& bins,
                           const std::string& tag) -> float* {
       const int nb = int(bins.size());
@@ -1848,36 +1896,18 @@ struct Engine {
       float4* E = ctx.buf<float4>(tag + ".E", size_t(nb) * plane_f);
       launch_ff_build_F(ctx, g, M, cube, kg, k, tab, nb, leg.ell, inv_win_ff,
                         src.k0, E, src.k0_dev);
-      float* out = ctx.buf<float>(tag + ".F", 2 * size_t(nb) * ld);
+      float* out = ctx.buf<float>(tag + ".F", words * size_t(nb) * ld);
       launch_ff_inverse(ctx, M, nb, k, k, E, Y1, Y2, out,
-                        out + size_t(nb) * ld, ld);
+                        tiled ? nullptr : out + size_t(nb) * ld, ld);
       return out;
     };
     const float* FA = leg_fields(la, A, "ffA");
     const float* FB = shared ? FA : leg_fields(lb, B, "ffB");
-    const float* FAl = FA + A.size() * size_t(ld);
-    const float* FBl = FB + B.size() * size_t(ld);
+    const float* FAl = tiled ? nullptr : FA + A.size() * size_t(ld);
+    const float* FBl = tiled ? nullptr : FB + B.size() * size_t(ld);
 
-    vector<int> pa(np), pb(np);
-    for (int i = 0; i < np; ++i) {
-      pa[i] = int(std::lower_bound(A.begin(), A.end(), pairs[i].row) -
-                  A.begin());
-      pb[i] = int(std::lower_bound(B.begin(), B.end(), pairs[i].col) -
-                  B.begin());
-    }
     double* dout = ctx.buf<double>("pairs.out", 2 * size_t(np));
-    // Pair lists with several pairs per field (full and upper-triangle
-    // forms) take the register-tiled Gram form on the hi words: rounding a
-    // field to FP32 perturbs each cell independently, far below the
-    // transforms' rounding, while the float-float products cost some 30
-    // FP32 instructions per pair and cell.  Diagonal lists keep the
-    // float-float streaming form.
-    const int nmax = int(std::max(A.size(), B.size()));
-    vector<int2> tl;
-    vector<int> slot;
-    if (!ctx.gram_per_pair && np >= 2 * nmax &&
-        gram_tile_list(false, int(A.size()), int(B.size()), pa, pb, tl,
-                       slot)) {
+    if (tiled) {
       const int2* dt = upload("gram.tiles", tl);
       const int* ds = upload("gram.slot", slot);
       zero(dout, 2 * np * sizeof(double));

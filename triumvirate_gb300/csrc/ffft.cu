@@ -639,7 +639,8 @@ ff_inv_y_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* Y1,
 }
 
 // C2R along z of the half lines Y2[f][a][b][0..Kcf] (zero above), two
-// lines per complex transform; writes the real fields out[f][a][b][z].
+// lines per complex transform; writes the real fields out[f][a][b][z]
+// (hi words, correctly rounded) and their lo words unless out_lo is null.
 template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
@@ -691,10 +692,10 @@ ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
       const float4 v = A[l * ls + pidx(z)];
       const FF re = ffnorm(FF{v.x, v.y}), im = ffnorm(FF{v.z, v.w});
       out[o0 + z] = re.hi;
-      out_lo[o0 + z] = re.lo;
+      if (out_lo != nullptr) out_lo[o0 + z] = re.lo;
       if (two) {
         out[o1 + z] = im.hi;
-        out_lo[o1 + z] = im.lo;
+        if (out_lo != nullptr) out_lo[o1 + z] = im.lo;
       }
     }
   }

@@ -449,7 +449,8 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                        float4* E, const double* k0_dev = nullptr);
 // Real fields on the M grid of nf half spectra E with planes c <= Kcf and
 // band |sx|, |sy| <= Kf, as float-float words: field f at out + f ld (hi)
-// and out_lo + f ld, cells [a][b][z] (Y1, Y2: scratch of
+// and out_lo + f ld (not written when out_lo is null), cells [a][b][z]
+// (Y1, Y2: scratch of
 // nf (Kcf+1) M0 M1 float4 each).
 void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
                        const float4* E, float4* Y1, float4* Y2, float* out,
