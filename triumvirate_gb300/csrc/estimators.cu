@@ -1896,9 +1896,39 @@ struct Engine {
       float4* E = ctx.buf<float4>(tag + ".E", size_t(nb) * plane_f);
       launch_ff_build_F(ctx, g, M, cube, kg, k, tab, nb, leg.ell, inv_win_ff,
                         src.k0, E, src.k0_dev);
+      // A shell field is zero on the x lines (sy, kz) outside its disc
+      // (sy dk_y)^2 + (kz dk_z)^2 < hi^2 (the line's point nearest k = 0
+      // is sx = 0) and on the planes above hi / dk_z: the inverse passes
+      // skip those lines (included with a margin: an extra line only costs
+      // time).
+      const int kc = k + 1, nbx = 2 * k + 1;
+      vector<int> bm(size_t(nb) * kc, -1), kz(nb, 0), xl;
+      vector<int64_t> yoff(nb + 1, 0);
+      for (int f = 0; f < nb; ++f) {
+        const double h2 = hi[f] * hi[f] * (1. + 1e-9);
+        for (int c = 0; c < kc; ++c) {
+          const double z2 = (c * g.dk[2]) * (c * g.dk[2]);
+          if (c > 0 && z2 > h2) break;
+          int m = 0;
+          while (m < k && ((m + 1) * g.dk[1]) * ((m + 1) * g.dk[1]) + z2 <= h2)
+            ++m;
+          bm[size_t(f) * kc + c] = m;
+          kz[f] = c;
+          for (int sy = -m; sy <= m; ++sy)
+            xl.push_back((f * kc + c) * nbx + sy + k);
+        }
+        yoff[f + 1] = yoff[f] + int64_t(M[0]) * (kz[f] + 1);
+      }
+      FFBand band;
+      band.xl = upload(tag + ".xl", xl);
+      band.nxl = int64_t(xl.size());
+      band.bm = upload(tag + ".bm", bm);
+      band.kz = upload(tag + ".kz", kz);
+      band.yoff = upload(tag + ".yoff", yoff);
+      band.nyl = yoff[nb];
       float* out = ctx.buf<float>(tag + ".F", words * size_t(nb) * ld);
       launch_ff_inverse(ctx, M, nb, k, k, E, Y1, Y2, out,
-                        tiled ? nullptr : out + size_t(nb) * ld, ld);
+                        tiled ? nullptr : out + size_t(nb) * ld, ld, band);
       return out;
     };
     const float* FA = leg_fields(la, A, "ffA");

@@ -560,24 +560,29 @@ __global__ void ff_build_F_kernel(Geom g, FFBuild bd, int M2, const float4* cube
 // ---- Inverse transforms of a group of fields -------------------------------
 // nf fields, each with planes c in [0, Kcf] and band |sx|, |sy| <= Kf.
 
-// x lines (f, c, b in band) of E[f][c][b][a]; writes Y1[f][c][a][b].
+// x lines (f, c, b in band; only the listed ones when band.xl is set) of
+// E[f][c][b][a]; writes Y1[f][c][a][b].
 template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_x_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* E,
-                __grid_constant__ const FFPlan P, int LB, float4* Y1) {
+                __grid_constant__ const FFPlan P, int LB, float4* Y1,
+                FFBand band) {
   extern __shared__ float4 smem[];
   __shared__ int64_t ibase[kMaxLines], obase[kMaxLines];
   const int ls = line_stride(M0);
   float4* A = smem;
   const float4* tw = stage_twiddles(smem, LB, ls, P);
   const int nb = 2 * Kf + 1;
-  const int64_t nlines = int64_t(nf) * (Kcf + 1) * nb;
+  const int64_t nlines =
+      band.xl != nullptr ? band.nxl : int64_t(nf) * (Kcf + 1) * nb;
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   if (threadIdx.x < nl) {
-    const int64_t line = l0 + threadIdx.x;
+    const int64_t line = band.xl != nullptr
+                             ? int64_t(band.xl[l0 + threadIdx.x])
+                             : l0 + threadIdx.x;
     const int64_t fc = line / nb;  // f (Kcf + 1) + c
     const int b = wrapi(int(line - fc * nb) - Kf, M1);
     ibase[threadIdx.x] = (fc * M1 + b) * M0;
@@ -597,35 +602,62 @@ ff_inv_x_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* E,
   }
 }
 
-// y lines of Y1 (entries outside the band are zero), ordered
-// (f M0 + a) (Kcf + 1) + c; writes Y2[f][a][b][c].
+// y lines of Y1 (entries outside the band, or outside the x lines that
+// band lists, are zero), ordered (f M0 + a) (Kcf + 1) + c, or with
+// band.yoff set field by field over the planes c <= kz[f]; writes
+// Y2[f][a][b][c].
 template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_y_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* Y1,
-                __grid_constant__ const FFPlan P, int LB, float4* Y2) {
+                __grid_constant__ const FFPlan P, int LB, float4* Y2,
+                FFBand band) {
   extern __shared__ float4 smem[];
   __shared__ int64_t ibase[kMaxLines], obase[kMaxLines];
+  __shared__ int lbm[kMaxLines];
   const int ls = line_stride(M1);
   float4* A = smem;
   const float4* tw = stage_twiddles(smem, LB, ls, P);
-  const int64_t nlines = int64_t(nf) * (Kcf + 1) * M0;
+  const int64_t nlines =
+      band.yoff != nullptr ? band.nyl : int64_t(nf) * (Kcf + 1) * M0;
   const int64_t l0 = int64_t(blockIdx.x) * LB;
   const int nl = min_lines(LB, nlines - l0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   if (threadIdx.x < nl) {
     const int64_t line = l0 + threadIdx.x;
-    const int64_t fa = line / (Kcf + 1);
-    const int64_t c = line - fa * (Kcf + 1);
-    const int64_t f = fa / M0, a = fa - f * M0;
+    int64_t f, a, c;
+    int bmax = Kf;
+    if (band.yoff != nullptr) {
+      // The last field whose lines start at or before this one (a field
+      // has at least its plane c = 0, so it owns the line).
+      int lo = 0, hi = nf;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (band.yoff[mid] <= line) lo = mid;
+        else hi = mid;
+      }
+      f = lo;
+      const int64_t r = line - band.yoff[f];
+      const int64_t kc = band.kz[f] + 1;
+      a = r / kc;
+      c = r - a * kc;
+      bmax = band.bm[f * (Kcf + 1) + c];
+    } else {
+      const int64_t fa = line / (Kcf + 1);
+      c = line - fa * (Kcf + 1);
+      f = fa / M0;
+      a = fa - f * M0;
+    }
     ibase[threadIdx.x] = ((f * (Kcf + 1) + c) * M0 + a) * M1;
-    obase[threadIdx.x] = fa * M1 * (Kcf + 1) + c;
+    obase[threadIdx.x] = (f * M0 + a) * M1 * (Kcf + 1) + c;
+    lbm[threadIdx.x] = bmax;
   }
   __syncthreads();
   for (int l = warp; l < nl; l += nw) {
     const float4* src = Y1 + ibase[l];
+    const int bmax = lbm[l];
     for (int b = lane; b < M1; b += 32)
-      A[l * ls + pidx(b)] = (abs(sym_shift(b, M1)) <= Kf)
+      A[l * ls + pidx(b)] = (abs(sym_shift(b, M1)) <= bmax)
                                 ? src[b]
                                 : make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -645,7 +677,7 @@ template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
                 __grid_constant__ const FFPlan P, int LB, float* out,
-                float* out_lo, int64_t ld) {
+                float* out_lo, int64_t ld, const int* kz) {
   extern __shared__ float4 smem[];
   const int ls = line_stride(M2);
   float4* A = smem;
@@ -656,19 +688,26 @@ ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
   const int nl = min_lines(LB, npair - p0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
+  const int64_t plane = int64_t(M0) * M1;  // lines per field
   for (int l = warp; l < nl; l += nw) {
     const int64_t line0 = 2 * (p0 + l);
     const bool two = line0 + 1 < nlines;
     const float4* h1 = Y2 + line0 * (Kcf + 1);
     const float4* h2 = h1 + (Kcf + 1);
+    // Planes above a field's last shell plane were not written (zero).
+    int kz1 = Kcf, kz2 = Kcf;
+    if (kz != nullptr) {
+      kz1 = kz[line0 / plane];
+      if (two) kz2 = kz[(line0 + 1) / plane];
+    }
     for (int k = lane; k < M2; k += 32) {
       // Hermitian extension of the half lines; Z = H1 + i H2.
       const bool up = k <= M2 / 2;
       const int kk = up ? k : M2 - k;
       FFC a = ffc_zero(), b = ffc_zero();
       if (kk <= Kcf) {
-        a = ffc_load(h1 + kk);
-        if (two) b = ffc_load(h2 + kk);
+        if (kk <= kz1) a = ffc_load(h1 + kk);
+        if (two && kk <= kz2) b = ffc_load(h2 + kk);
         if (!up) {
           a = ffc_conj(a);
           b = ffc_conj(b);
@@ -679,7 +718,6 @@ ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
     }
   }
   ff_fft_lines<+1, MASK>(A, nl, ls, P, tw);
-  const int64_t plane = int64_t(M0) * M1;  // lines per field
   auto offset = [&](int64_t line) {
     const int64_t f = line / plane;
     return f * ld + (line - f * plane) * M2;
@@ -953,30 +991,36 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
 
 void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
                        const float4* E, float4* Y1, float4* Y2, float* out,
-                       float* out_lo, int64_t ld) {
+                       float* out_lo, int64_t ld, const FFBand& band) {
   const FFPlan Px = ff_plan(ctx, M[0]);
   const FFPlan Py = ff_plan(ctx, M[1]);
   const FFPlan Pz = ff_plan(ctx, M[2]);
   with_grid_radix_set(Px, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Px);
-    const int64_t nl = int64_t(nf) * (Kcf + 1) * (2 * Kf + 1);
+    const int64_t nl = band.xl != nullptr
+                           ? band.nxl
+                           : int64_t(nf) * (Kcf + 1) * (2 * Kf + 1);
+    if (nl == 0) return;
     allow_smem(ff_inv_x_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_inv_x_kernel");
     ff_inv_x_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(M[0], lb), ctx.stream>>>(
-        M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1);
+        M[0], M[1], nf, Kf, Kcf, E, Px, lb, Y1, band);
     TRVG_LAUNCHED(ctx);
   });
   with_grid_radix_set(Py, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);
-    const int64_t nl = int64_t(nf) * (Kcf + 1) * M[0];
+    const int64_t nl = band.yoff != nullptr
+                           ? band.nyl
+                           : int64_t(nf) * (Kcf + 1) * M[0];
+    if (nl == 0) return;
     allow_smem(ff_inv_y_kernel<MASK>);
     TRVG_KBEGIN(ctx, "ff_inv_y_kernel");
     ff_inv_y_kernel<MASK><<<int((nl + lb - 1) / lb), 256,
                             smem_bytes(M[1], lb), ctx.stream>>>(
-        M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2);
+        M[0], M[1], nf, Kf, Kcf, Y1, Py, lb, Y2, band);
     TRVG_LAUNCHED(ctx);
   });
   with_grid_radix_set(Pz, [&](auto set) {
@@ -987,7 +1031,7 @@ void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
     TRVG_KBEGIN(ctx, "ff_inv_z_kernel");
     ff_inv_z_kernel<MASK><<<int((np + lb - 1) / lb), 256,
                             smem_bytes(M[2], lb), ctx.stream>>>(
-        M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb, out, out_lo, ld);
+        M[0], M[1], M[2], nf, Kcf, Y2, Pz, lb, out, out_lo, ld, band.kz);
     TRVG_LAUNCHED(ctx);
   });
 }

@@ -447,6 +447,21 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
                        const float4* cube, int Kg, int K, const int16_t* tab,
                        int nq, int ell, const float2* const iw[3], cd k0,
                        float4* E, const double* k0_dev = nullptr);
+// Lines of the inverse passes that can hold modes when each field of a
+// group is a shell (null pointers: every line of the band box).  x lines
+// are listed by code (f (Kcf + 1) + c) (2 Kf + 1) + sy + Kf; bm[f (Kcf + 1)
+// + c] is the largest |sy| of plane c of field f (-1: none), kz[f] the
+// largest plane of field f, and field f owns the y lines [yoff[f],
+// yoff[f + 1]), M0 (kz[f] + 1) of them.
+struct FFBand {
+  const int* xl = nullptr;
+  int64_t nxl = 0;
+  const int* bm = nullptr;
+  const int* kz = nullptr;
+  const int64_t* yoff = nullptr;
+  int64_t nyl = 0;
+};
+
 // Real fields on the M grid of nf half spectra E with planes c <= Kcf and
 // band |sx|, |sy| <= Kf, as float-float words: field f at out + f ld (hi)
 // and out_lo + f ld (not written when out_lo is null), cells [a][b][z]
@@ -454,7 +469,8 @@ void launch_ff_build_F(Context& ctx, const Geom& g, const int M[3],
 // nf (Kcf+1) M0 M1 float4 each).
 void launch_ff_inverse(Context& ctx, const int M[3], int nf, int Kf, int Kcf,
                        const float4* E, float4* Y1, float4* Y2, float* out,
-                       float* out_lo, int64_t ld);
+                       float* out_lo, int64_t ld,
+                       const FFBand& band = FFBand());
 // Field stride of the reductions: cells rounded up to whole float4 quads.
 inline int64_t ff_field_stride(int64_t ncell) { return (ncell + 3) / 4 * 4; }
 // sum_x F_a F_b G of float-float fields (hi, lo words; field q of a leg at
