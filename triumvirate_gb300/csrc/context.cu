@@ -108,6 +108,28 @@ cufftHandle Context::plan1d(int type, int n, int batch) {
   return h;
 }
 
+cufftHandle Context::plan_xy(int n0, int n1, int nz) {
+  PlanKey key{-int(CUFFT_C2C), {n0, n1, nz}, nz};
+  auto it = plans.find(key);
+  if (it != plans.end()) return it->second;
+  cufftHandle h;
+  TRVG_CUFFT(cufftCreate(&h));
+  TRVG_CUFFT(cufftSetStream(h, stream));
+  long long nn[2] = {n0, n1};
+  const long long plane = (long long)n0 * n1;
+  size_t work = 0;
+  cufftResult r = cufftMakePlanMany64(h, 2, nn, nullptr, 1, plane, nullptr,
+                                      1, plane, CUFFT_C2C, nz, &work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    throw_error(r == CUFFT_ALLOC_FAILED ? TRVG_ERR_ALLOC : TRVG_ERR_CUFFT,
+                "cuFFT x-y plan (%d x %d, %d planes) failed: %d", n0, n1, nz,
+                int(r));
+  }
+  plans[key] = h;
+  return h;
+}
+
 namespace {
 cudaEvent_t next_event(Context& c) {
   if (c.events_used == c.event_pool.size()) {

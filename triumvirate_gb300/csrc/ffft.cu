@@ -360,12 +360,14 @@ __device__ __forceinline__ int lines_shift(int nl) {
 }
 
 // z lines of the real mesh, two rows per complex line; keeps kz in [0, Kz]
-// into T1[x][kz][y].
+// into T1[x][kz][y] and, when `full` is set, every kz in [0, n2 / 2] of
+// every row rounded to FP32 into full[kz][x][y] (planes of the mesh's
+// transform along z, which batched x-y transforms complete).
 template <int MASK>
 __global__ void __launch_bounds__(256, 2)
 ff_fwd_z_kernel(Geom g, const float* mesh, const float* mesh_lo,
                 __grid_constant__ const FFPlan P, int LB, int Kz,
-                float4* T1) {
+                float4* T1, float2* full) {
   extern __shared__ float4 smem[];
   __shared__ int64_t obase[2 * kMaxLines];
   const int n2 = g.n[2], ls = line_stride(n2);
@@ -407,6 +409,25 @@ ff_fwd_z_kernel(Geom g, const float* mesh, const float* mesh_lo,
     const FFC v = (t & 1) ? ffc_scale2(ffc_muli(ffc_sub(z, zm), -1), 0.5f)
                           : ffc_scale2(ffc_add(z, zm), 0.5f);
     T1[obase[t] + int64_t(kz) * g.n[1]] = ffc_pack(v);
+  }
+  if (full != nullptr) {
+    // Both rows of line l at kz, from Z(k) and conj Z(-k) rounded to FP32,
+    // plane by plane: full[kz][row]; consecutive threads write the block's
+    // consecutive rows of one plane.
+    const int nzh = n2 / 2 + 1;
+    const int64_t nrows = int64_t(g.n[0]) * g.n[1];
+    for (int w = threadIdx.x; w < nzh << sh; w += blockDim.x) {
+      const int t = w & ((1 << sh) - 1), kz = w >> sh;
+      if (t >= 2 * nl) continue;
+      const int l = t >> 1;
+      const float4 a = A[l * ls + pidx(kz)];
+      const float4 b = A[l * ls + pidx(kz == 0 ? 0 : n2 - kz)];
+      const float zr = a.x + a.y, zi = a.z + a.w;
+      const float mr = b.x + b.y, mi = -(b.z + b.w);
+      full[int64_t(kz) * nrows + 2 * p0 + t] =
+          (t & 1) ? make_float2(0.5f * (zi - mi), -0.5f * (zr - mr))
+                  : make_float2(0.5f * (zr + mr), 0.5f * (zi + mi));
+    }
   }
 }
 
@@ -891,9 +912,43 @@ void with_grid_radix_set(const FFPlan& P, F&& f) {
 
 }  // namespace
 
+// spec[x][y][kz] = planes[kz][x][y] (kz < nz): 32 x 32 tiles of (kz, y)
+// per x through shared memory, both sides coalesced.
+__global__ void __launch_bounds__(256)
+planes_to_half_kernel(int n0, int n1, int nz, const float2* __restrict__ planes,
+                      float2* __restrict__ spec) {
+  __shared__ float2 tile[32][33];
+  const int x = blockIdx.z;
+  const int y0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const int64_t plane = int64_t(n0) * n1;
+  for (int j = ty; j < 32; j += 8) {
+    const int z = z0 + j, y = y0 + tx;
+    if (z < nz && y < n1)
+      tile[j][tx] = planes[int64_t(z) * plane + int64_t(x) * n1 + y];
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int y = y0 + j, z = z0 + tx;
+    if (z < nz && y < n1)
+      spec[(int64_t(x) * n1 + y) * nz + z] = tile[tx][j];
+  }
+}
+
+void launch_planes_to_half(Context& ctx, const Geom& g, const float2* planes,
+                           float2* spec) {
+  const int nz = g.n[2] / 2 + 1;
+  dim3 grid((g.n[1] + 31) / 32, (nz + 31) / 32, g.n[0]);
+  TRVG_KBEGIN(ctx, "planes_to_half_kernel");
+  planes_to_half_kernel<<<grid, 256, 0, ctx.stream>>>(g.n[0], g.n[1], nz,
+                                                      planes, spec);
+  TRVG_LAUNCHED(ctx);
+}
+
 void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
                             const float* mesh_lo, int Kg, float4* T1,
-                            float4* T2, float4* cube) {
+                            float4* T2, float4* cube, float2* full,
+                            cudaEvent_t after_z) {
   const FFPlan Pz = ff_plan(ctx, g.n[2]);
   const FFPlan Py = ff_plan(ctx, g.n[1]);
   const FFPlan Px = ff_plan(ctx, g.n[0]);
@@ -905,9 +960,10 @@ void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
     TRVG_KBEGIN(ctx, "ff_fwd_z_kernel");
     ff_fwd_z_kernel<MASK><<<int((npair + lb - 1) / lb), 256,
                             smem_bytes(g.n[2], lb), ctx.stream>>>(
-        g, mesh, mesh_lo, Pz, lb, Kg, T1);
+        g, mesh, mesh_lo, Pz, lb, Kg, T1, full);
     TRVG_LAUNCHED(ctx);
   });
+  if (after_z != nullptr) TRVG_CUDA(cudaEventRecord(after_z, ctx.stream));
   with_mesh_radix_set(Py, [&](auto set) {
     constexpr int MASK = decltype(set)::value;
     const int lb = lines_per_block(Py);

@@ -206,6 +206,10 @@ struct Context {
   cufftHandle plan(int type, const int n[3], int batch);
   // Batched 1-D plan of length n (cached with the 3-D ones).
   cufftHandle plan1d(int type, int n, int batch);
+  // In-place C2C of nz contiguous n0 x n1 planes (element (z, x, y) at
+  // (z n0 + x) n1 + y): the x and y transforms that complete an R2C whose
+  // z transform is done.
+  cufftHandle plan_xy(int n0, int n1, int nz);
   void release();
   void log(int level, const char* fmt, ...) const;
 };

@@ -433,10 +433,16 @@ void launch_ff_cube_to_half(Context& ctx, const Geom& g, const float4* cube,
 FFPlan ff_plan(Context& ctx, int n);
 // Spectrum of the FP32 mesh on the cube |sx|, |sy| <= Kg, 0 <= sz <= Kg:
 // cube[sx + Kg][sy + Kg][sz] (T1, T2: scratch of n0 (Kg+1) n1 and
-// (2Kg+1)(Kg+1) n0 float4).
+// (2Kg+1)(Kg+1) n0 float4).  With `full` set the z pass also writes every
+// row's transform along z in FP32, plane by plane (full[kz][x][y], kz <=
+// n2/2), and `after_z` is recorded on the stream after that pass.
 void launch_ff_forward_cube(Context& ctx, const Geom& g, const float* mesh,
                             const float* mesh_lo, int Kg, float4* T1,
-                            float4* T2, float4* cube);
+                            float4* T2, float4* cube, float2* full = nullptr,
+                            cudaEvent_t after_z = nullptr);
+// spec[x][y][kz] (the R2C layout, kz <= n2/2) from planes[kz][x][y].
+void launch_planes_to_half(Context& ctx, const Geom& g, const float2* planes,
+                           float2* spec);
 // Evaluation-grid half spectra E[c][b][a] of G (planes c <= Kg) and
 // E[q][c][b][a] of nq shell fields (planes c <= K) from the cube.
 // k0_dev (re, im in device memory), when given, replaces the host k0.
