@@ -255,8 +255,12 @@ def algorithmic_bytes(kernel, args, real_bytes):
     ig, i_f = inv(1, Kg), inv(args.nbins, K)
     table = {
         # float-float mesh transforms: the FP32 mesh read, z-pass spectrum
-        # rows (kz <= 2K) written; then the kept y and x bands.
-        'ff_fwd_z_kernel': real_bytes * nm + f4 * N * (Kg + 1) * N,
+        # rows (kz <= 2K) written, and the FP32 planes of every row's z
+        # transform (8 B per half-spectrum mode) that complete the mesh's
+        # R2C; then the kept y and x bands.
+        'ff_fwd_z_kernel': real_bytes * nm + f4 * N * (Kg + 1) * N + c * nh,
+        # the planes read and the R2C-layout spectrum written.
+        'planes_to_half_kernel': 2 * c * nh,
         'ff_fwd_y_kernel': f4 * N * (Kg + 1) * (N + 2 * Kg + 1),
         'ff_fwd_x_kernel': f4 * (2 * Kg + 1) * (Kg + 1) * (N + 2 * Kg + 1),
         'ff_inv_x_kernel': (ig[0] + i_f[0]) / 2,

@@ -412,21 +412,22 @@ ff_fwd_z_kernel(Geom g, const float* mesh, const float* mesh_lo,
   }
   if (full != nullptr) {
     // Both rows of line l at kz, from Z(k) and conj Z(-k) rounded to FP32,
-    // plane by plane: full[kz][row]; consecutive threads write the block's
-    // consecutive rows of one plane.
+    // plane by plane: full[kz][row].  The two rows are adjacent in a plane
+    // (one 16-byte store); consecutive threads write the block's
+    // consecutive lines of one plane.
     const int nzh = n2 / 2 + 1;
     const int64_t nrows = int64_t(g.n[0]) * g.n[1];
-    for (int w = threadIdx.x; w < nzh << sh; w += blockDim.x) {
-      const int t = w & ((1 << sh) - 1), kz = w >> sh;
-      if (t >= 2 * nl) continue;
-      const int l = t >> 1;
+    const int shl = lines_shift(nl);
+    for (int w = threadIdx.x; w < nzh << shl; w += blockDim.x) {
+      const int l = w & ((1 << shl) - 1), kz = w >> shl;
+      if (l >= nl) continue;
       const float4 a = A[l * ls + pidx(kz)];
       const float4 b = A[l * ls + pidx(kz == 0 ? 0 : n2 - kz)];
       const float zr = a.x + a.y, zi = a.z + a.w;
       const float mr = b.x + b.y, mi = -(b.z + b.w);
-      full[int64_t(kz) * nrows + 2 * p0 + t] =
-          (t & 1) ? make_float2(0.5f * (zi - mi), -0.5f * (zr - mr))
-                  : make_float2(0.5f * (zr + mr), 0.5f * (zi + mi));
+      reinterpret_cast<float4*>(full + int64_t(kz) * nrows)[p0 + l] =
+          make_float4(0.5f * (zr + mr), 0.5f * (zi + mi), 0.5f * (zi - mi),
+                      -0.5f * (zr - mr));
     }
   }
 }
