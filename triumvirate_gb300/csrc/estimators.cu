@@ -2215,8 +2215,10 @@ struct Engine {
     // delta n_00 and N_00 (gpp: one unit-weight assignment serves both).
     FieldSpec<Real> dn, nf;
     if (!survey && replay != nullptr) {
-      // The mock's k = 0 modes are formed on the device (batch.cu).
-      Field base = make_field("N", {{dd, WeightSpec()}}, false);
+      // The mock's k = 0 modes are formed on the device (batch.cu); the
+      // mesh's R2C is deferred as in the warm-up estimate.
+      Field base = make_field("N", {{dd, WeightSpec()}}, false,
+                              sizeof(Real) == 4);
       dn = base.spec;
       nf = base.spec;
       dn.k0_set = nf.k0_set = true;
@@ -2278,13 +2280,15 @@ struct Engine {
       // batched x-y transforms of the planes plus a transpose complete the
       // mesh's R2C (0.35 + 0.2 ms at 512^3 against 0.82 ms for cuFFT's R2C,
       // whose x-y passes on the R2C layout are slower than on planes).
+      // A captured batch replays the same path as its eager warm-up, which
+      // created the plan and the planes buffer (ff_applicable returns the
+      // warm-up's choice); it runs on one stream.
       const bool fuse = sizeof(Real) == 4 && pending_r2c.mesh != nullptr &&
-                        octant && replay == nullptr &&
-                        real_fields(dn, dn, la0, lb0, M) &&
+                        octant && real_fields(dn, dn, la0, lb0, M) &&
                         ff_applicable(dn, dn, la0, lb0, pairs, hb, M, K);
       float2* zfull =
           fuse ? ctx.buf<float2>("mesh.zplanes", size_t(g.nhalf)) : nullptr;
-      if (fuse && ctx.overlap && !ctx.profiling) {
+      if (fuse && ctx.overlap && !ctx.profiling && replay == nullptr) {
         const cudaStream_t main = ctx.stream, side = ctx.side_stream();
         // The float-float forward transform of the mesh is submitted first;
         // the x-y transforms and the octant shot-noise field (memory-bound)
