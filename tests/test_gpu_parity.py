@@ -988,7 +988,8 @@ def test_side_stream_shot_noise_matches_one_stream():
                                   'gpp_zeta110_full', 'gpp_b000_full_36bins',
                                   'gpp_b202_full_36bins',
                                   'gpp_b000_full_ff_36bins',
-                                  'gpp_b202_full_ff_36bins'])
+                                  'gpp_b202_full_ff_36bins',
+                                  'gpp_b220_diag'])
 def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
     """FP32 pair sums in the register-tiled Gram form (complex survey fields,
     real periodic-box fields with FP32 transforms, the hi words of
@@ -996,7 +997,9 @@ def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
     one-entry-per-thread form (float-float products for float-float
     fields); forms full, triu and diag exercise tiles that hold one, some
     and all of their field pairs, and the 36-bin cases stage more than 64
-    rows per chunk."""
+    rows per chunk.  B_220 diag: legs of orders m and -m read one set of
+    fields, leg b conjugated, against leg b transformed (the per-pair
+    form)."""
     ctx = _lib.default_context(None)
     rng = np.random.default_rng(71)
     pos = rng.uniform(0., 800., size=(20000, 3))
@@ -1022,10 +1025,12 @@ def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
                          96 if case.endswith('36bins') else 48,
                          'tsc', box=800.)
         if case.startswith('gpp_b'):
-            deg = (0, 0, 0) if 'b000' in case else (2, 0, 2)
-            return compute_bispec_in_gpp_box(cat, degrees=deg, binning=kb,
-                                             form='full',
-                                             sampling_params=samp)
+            deg = ((0, 0, 0) if 'b000' in case else
+                   (2, 2, 0) if 'b220' in case else (2, 0, 2))
+            return compute_bispec_in_gpp_box(
+                cat, degrees=deg, binning=kb,
+                form='diag' if case.endswith('diag') else 'full',
+                sampling_params=samp)
         deg = (0, 0, 0) if 'zeta000' in case else (1, 1, 0)
         form = 'diag' if 'diag' in case else 'full'
         return compute_3pcf_in_gpp_box(cat, degrees=deg, binning=rb,
@@ -1054,9 +1059,9 @@ def test_tiled_gram_matches_per_pair(case, rand_catalogue_array):
     # 2e-6 (a wrong tile or slot would differ at O(1)).  B_202 has entries
     # near 1e-5 of the largest whose FP32 sums cancel; there both forms lie
     # some 3e-3 from FP64 and 5e-4 from each other, so its per-entry check
-    # covers the entries above 1e-3 of the largest.
+    # (and B_220's) covers the entries above 1e-3 of the largest.
     rtol = RTOL_FP32 if 'b000' in case else RTOL_FP32_FFT
-    floor = 1e-3 if 'b202' in case else 0.
+    floor = 1e-3 if ('b202' in case or 'b220' in case) else 0.
     for k in keys:
         t, q = np.asarray(tiled[k]), np.asarray(pair[k])
         scale = np.max(np.abs(q))

@@ -2039,7 +2039,25 @@ struct Engine {
       else
         launch_wide_angle(ctx, g, const_cast<FC*>(G), wide_angle_power);
     }
-    const bool shared = la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl;
+    // Shell legs of orders m and -m of one degree over a real mesh: with
+    // delta(-k) = conj delta(k), the windows even in k and
+    // y_lm(-k) = (-1)^l y_lm(k), F_{l,-m} = (-1)^(l+m) conj(F_{l,m}) as long
+    // as every mode's partner -k is a mode of the grid, i.e. the band stays
+    // below the Nyquist index (the 3PCF's j_l-weighted fields reach it).  A
+    // diagonal pair list then reads leg a's fields for both legs (the
+    // streaming kernel conjugates leg b) instead of transforming leg b.
+    bool diagonal = true;
+    for (const Pair& q : pairs) diagonal = diagonal && q.row == q.col;
+    bool below_nyquist = true;
+    for (int a = 0; a < 3; ++a)
+      below_nyquist = below_nyquist && 2 * K[a] < M[a];
+    const bool mirror = !real && diagonal && !ctx.gram_per_pair &&
+                        !la.sjl && !lb.sjl && below_nyquist &&
+                        la.ell == lb.ell && la.m == -lb.m && la.m != 0 &&
+                        src.im == nullptr && src.im_s == nullptr;
+    const double mirror_sign = ((la.ell + la.m) & 1) ? -1. : 1.;
+    const bool shared =
+        mirror || (la.ell == lb.ell && la.m == lb.m && la.sjl == lb.sjl);
     vector<int> A, B;
     for (const Pair& q : pairs) {
       A.push_back(q.row);
@@ -2167,10 +2185,12 @@ struct Engine {
                                        nb_gram);
         else
           launch_reduce_pairs<FR>(ctx, Mc, G, FA, FB, dpa, dpb,
-                                  int(idx.size()), dout, na_gram, nb_gram);
+                                  int(idx.size()), dout, na_gram, nb_gram,
+                                  mirror);
         vector<double> h = download(dout, 2 * idx.size());
+        const double sgn = mirror ? mirror_sign : 1.;
         for (size_t q = 0; q < idx.size(); ++q)
-          res[idx[q]] += cplx(h[2 * q], h[2 * q + 1]);
+          res[idx[q]] += sgn * cplx(h[2 * q], h[2 * q + 1]);
       }
     }
     return res;

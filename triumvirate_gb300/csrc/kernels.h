@@ -374,7 +374,9 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
                          const typename CplxOf<Real>::type* Fb,
                          const int* pa, const int* pb, int npairs,
                          double* out /* 2 * npairs */, int na = 0,
-                         int nb = 0 /* fields per leg: FP32 tiled form */);
+                         int nb = 0 /* fields per leg: FP32 tiled form */,
+                         bool conj_b = false /* leg b read conjugated
+                                                (streaming form only) */);
 
 template <class Real>
 void launch_reduce_pairs_real(Context& ctx, int64_t ncell, const Real* G,

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256)
 reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
                     const typename CplxOf<Real>::type* Fa,
                     const typename CplxOf<Real>::type* Fb, const int* pa,
-                    const int* pb, int npairs, double* out) {
+                    const int* pb, int npairs, double* out, bool conj_b) {
   using C = typename CplxOf<Real>::type;
   __shared__ double red[2 * kPairChunk * 32];
   const int p0 = blockIdx.y * kPairChunk;
@@ -141,7 +141,8 @@ reduce_pairs_kernel(int64_t ncell, const typename CplxOf<Real>::type* G,
     for (int q = 0; q < kPairChunk; ++q) {
       if (!ok[q]) continue;
       const C a = Fa[int64_t(ia[q]) * ncell + t];
-      const C b = Fb[int64_t(ib[q]) * ncell + t];
+      C b = Fb[int64_t(ib[q]) * ncell + t];
+      if (conj_b) b.y = -b.y;
       const C p = cmulc(cmulc(a, b), g);
       acc[2 * q].add(p.x);
       acc[2 * q + 1].add(p.y);
@@ -1420,11 +1421,11 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
                          const typename CplxOf<Real>::type* Fa,
                          const typename CplxOf<Real>::type* Fb,
                          const int* pa, const int* pb, int npairs,
-                         double* out, int na, int nb) {
+                         double* out, int na, int nb, bool conj_b) {
   if (npairs <= 0) return;
   if constexpr (sizeof(Real) == 4) {
     const size_t smem = size_t(na + nb) * kRedRow * sizeof(float2);
-    if (na > 0 && nb > 0 && smem <= 200 * 1024) {
+    if (!conj_b && na > 0 && nb > 0 && smem <= 200 * 1024) {
       static bool configured[64] = {};
       if (ctx.device < 0 || ctx.device >= 64 || !configured[ctx.device]) {
         TRVG_CUDA(cudaFuncSetAttribute(
@@ -1446,8 +1447,8 @@ void launch_reduce_pairs(Context& ctx, int64_t ncell,
   const int chunks = (npairs + kPairChunk - 1) / kPairChunk;
   dim3 grid(grid_for(ncell, 256, 152 * 8), chunks);
   TRVG_KBEGIN(ctx, "reduce_pairs_kernel");
-  reduce_pairs_kernel<Real><<<grid, 256, 0, ctx.stream>>>(ncell, G, Fa, Fb,
-                                                          pa, pb, npairs, out);
+  reduce_pairs_kernel<Real><<<grid, 256, 0, ctx.stream>>>(
+      ncell, G, Fa, Fb, pa, pb, npairs, out, conj_b);
   TRVG_LAUNCHED(ctx);
 }
 
@@ -1772,7 +1773,8 @@ void launch_shotnoise_3pcf_bins(Context& ctx, const Geom& g, const Real* xi_re,
                                        const CplxOf<R>::type*,                \
                                        const CplxOf<R>::type*,                \
                                        const CplxOf<R>::type*, const int*,    \
-                                       const int*, int, double*, int, int);   \
+                                       const int*, int, double*, int, int,    \
+                                       bool);                                 \
   template void launch_reduce_pairs_real<R>(Context&, int64_t, const R*,     \
                                             const R*, const R*, const int*,   \
                                             const int*, int, double*, int,    \
