@@ -147,6 +147,12 @@ __host__ __device__ __forceinline__ int line_stride(int n) {
 // Lines per block at most (per-line offsets are kept in shared memory).
 constexpr int kMaxLines = 16;
 
+// Radix sets of a plan (bit per radix); kernels specialised for a set
+// inline its stages, the generic ones (kRadixAll) call them out of line, so
+// that each stage keeps its own register allocation.
+constexpr int kRadix8 = 1, kRadix4 = 2, kRadix2 = 4, kRadix3 = 8,
+              kRadix5 = 16, kRadixAll = 31;
+
 // Butterflies one thread keeps in registers per stage.
 template <int R>
 struct StageItems {
@@ -206,18 +212,21 @@ __device__ __forceinline__ void ff_stage_body(float4* A, int nl, int ln,
   __syncthreads();
 }
 
-// Butterflies per lane when one warp transforms a line.
-template <int R>
+// Butterflies per lane when one warp transforms a line: two of radix 8 in
+// plans of radix 8 alone (n = 512 has 64 per stage), where the kernels
+// still fit 128 registers without spills; one in mixed plans.
+template <int R, int MASK>
 struct WarpItems {
-  static constexpr int value = (R == 8 || R == 5) ? 1 : (R == 2 ? 3 : 2);
+  static constexpr int value =
+      R == 8 ? (MASK == kRadix8 ? 2 : 1) : (R == 5 ? 1 : (R == 2 ? 3 : 2));
 };
 
 // One stage of radix R over the line L of this warp (same indexing as
 // ff_stage, butterfly j = lane + 32 it), synchronised within the warp only.
-template <int R, int D>
+template <int R, int D, int MASK>
 __device__ __forceinline__ void ff_stage_warp_body(float4* L, const FFPlan& P,
                                                    int s, const float4* tw) {
-  constexpr int IMAX = WarpItems<R>::value;
+  constexpr int IMAX = WarpItems<R, MASK>::value;
   const int nb = P.nb[s], Ns = P.ns[s];
   const unsigned mns = P.mns[s];
   const int lane = threadIdx.x & 31;
@@ -255,11 +264,6 @@ __device__ __forceinline__ void ff_stage_warp_body(float4* L, const FFPlan& P,
 
 // Transforms the nl lines of A (line stride ln) in place, direction D,
 // with the twiddle table tw (n entries, usually a shared-memory copy).
-// Radix sets of a plan (bit per radix); kernels specialised for a set
-// inline its stages, the generic ones (kRadixAll) call them out of line, so
-// that each stage keeps its own register allocation.
-constexpr int kRadix8 = 1, kRadix4 = 2, kRadix2 = 4, kRadix3 = 8,
-              kRadix5 = 16, kRadixAll = 31;
 
 template <int R, int D>
 __device__ __noinline__ void ff_stage_call(float4* A, int nl, int ln,
@@ -270,7 +274,7 @@ __device__ __noinline__ void ff_stage_call(float4* A, int nl, int ln,
 template <int R, int D>
 __device__ __noinline__ void ff_stage_warp_call(float4* L, const FFPlan& P,
                                                 int s, const float4* tw) {
-  ff_stage_warp_body<R, D>(L, P, s, tw);
+  ff_stage_warp_body<R, D, kRadixAll>(L, P, s, tw);
 }
 
 template <int R, int D, int MASK>
@@ -284,7 +288,7 @@ template <int R, int D, int MASK>
 __device__ __forceinline__ void ff_stage_warp(float4* L, const FFPlan& P,
                                               int s, const float4* tw) {
   if constexpr (MASK == kRadixAll) ff_stage_warp_call<R, D>(L, P, s, tw);
-  else ff_stage_warp_body<R, D>(L, P, s, tw);
+  else ff_stage_warp_body<R, D, MASK>(L, P, s, tw);
 }
 
 // Transforms the nl lines of A (line stride ln) in place, direction D,
@@ -820,9 +824,12 @@ FFPlan ff_plan(Context& ctx, int n) {
     P.mns[s] = magic(ns);
   }
   P.warp_lines = true;
+  bool pure8 = true;
+  for (int s = 0; s < P.nstage; ++s) pure8 = pure8 && P.radix[s] == 8;
   for (int s = 0; s < P.nstage; ++s) {
     const int R = P.radix[s];
-    const int items = (R == 8 || R == 5) ? 1 : (R == 2 ? 3 : 2);  // WarpItems
+    // WarpItems of the kernel this plan's radix set selects.
+    const int items = R == 8 ? (pure8 ? 2 : 1) : (R == 5 ? 1 : (R == 2 ? 3 : 2));
     if (P.nb[s] > 32 * items) P.warp_lines = false;
   }
   // Stage-major twiddle table: sum over stages of (radix - 1) ns = n - 1
@@ -903,8 +910,10 @@ void with_mesh_radix_set(const FFPlan& P, F&& f) {
 
 template <class F>
 void with_grid_radix_set(const FFPlan& P, F&& f) {
+  // Plans of radix 8 alone take the kRadix8 kernels here too: their warp
+  // form keeps two butterflies per lane (WarpItems), which ff_plan assumes.
   dispatch_radix(radix_mask(P), f,
-                 RadixSets<kRadix3 | kRadix5, kRadix2 | kRadix3,
+                 RadixSets<kRadix8, kRadix3 | kRadix5, kRadix2 | kRadix3,
                            kRadix8 | kRadix4 | kRadix5,
                            kRadix4 | kRadix3 | kRadix5,
                            kRadix8 | kRadix2 | kRadix3,
