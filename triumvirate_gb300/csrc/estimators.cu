@@ -894,9 +894,9 @@ struct Engine {
 
   // The deferred R2C of the mesh whose transform along z the float-float z
   // pass has written plane by plane into `planes`: the x and y transforms
-  // of the planes (contiguous, batched, in place), then the planes
-  // transposed into the spectrum buffer's R2C layout.
-  void finish_pending_r2c_xy(float2* planes) {
+  // of the planes (contiguous, batched, in place), then (unless no reader
+  // needs it) the planes transposed into the spectrum buffer's R2C layout.
+  void finish_pending_r2c_xy(float2* planes, bool to_half = true) {
     if constexpr (sizeof(Real) == 4) {
       cufftHandle h = ctx.plan_xy(g.n[0], g.n[1], g.nzh);
       TRVG_CUFFT(cufftSetStream(h, ctx.stream));
@@ -906,8 +906,9 @@ struct Engine {
                               CUFFT_FORWARD));
       ctx.kend();
       ctx.fft_launches++;
-      launch_planes_to_half(ctx, g, planes,
-                            reinterpret_cast<float2*>(pending_r2c.out));
+      if (to_half)
+        launch_planes_to_half(ctx, g, planes,
+                              reinterpret_cast<float2*>(pending_r2c.out));
     }
     pending_r2c = PendingR2C{};
   }
@@ -1022,9 +1023,10 @@ struct Engine {
 
   // Fine-binned two-point statistics (field.cpp:2511-2703): the field
   // products over a mode list cached per mesh, binning and degrees.
-  Stats twopt_stats(const HostBins& hb, const FieldSpec<Real>& fa,
-                    const FieldSpec<Real>& fb, cplx shot, int ell, int m) {
-    vector<int> smin, smax;
+  // Sample ranges of the bins and the mode cube of the fine-binned
+  // statistics; false when two bins share a mode (the direct form).
+  bool stats_ranges(const HostBins& hb, vector<int>& smin,
+                    vector<int>& smax, Cube& cube) {
     const double dk_sample = 1.e-5;
     sample_ranges(hb, dk_sample, 1000000, smin, smax);
     // Each mode must fall in at most one bin.
@@ -1033,10 +1035,27 @@ struct Engine {
       if (smax[b] > smin[b]) r.push_back({smin[b], smax[b]});
     std::sort(r.begin(), r.end());
     for (size_t i = 1; i < r.size(); ++i)
-      if (r[i].first < r[i - 1].second)
-        return twopt_stats_direct(hb, fa, fb, shot, ell, m);
+      if (r[i].first < r[i - 1].second) return false;
     const int smax_all = *std::max_element(smax.begin(), smax.end());
-    const Cube cube = make_cube(double(smax_all + 1) * dk_sample);
+    cube = make_cube(double(smax_all + 1) * dk_sample);
+    return true;
+  }
+
+  // True when twopt_stats of fa and fb reads the float-float spectrum
+  // cube, not the fields' FP32 spectra.
+  bool stats_read_cube(const HostBins& hb, const FieldSpec<Real>& fa,
+                       const FieldSpec<Real>& fb) {
+    vector<int> smin, smax;
+    Cube cube;
+    return stats_ranges(hb, smin, smax, cube) && cube_covers(fa, fb, cube);
+  }
+
+  Stats twopt_stats(const HostBins& hb, const FieldSpec<Real>& fa,
+                    const FieldSpec<Real>& fb, cplx shot, int ell, int m) {
+    vector<int> smin, smax;
+    Cube cube;
+    if (!stats_ranges(hb, smin, smax, cube))
+      return twopt_stats_direct(hb, fa, fb, shot, ell, m);
     const StatsPlan& sp = stats_plan(hb, smin, smax, cube, ell, m);
     // One sum buffer per degree: a replayed term reads both legs' sums.
     double* dpk = ctx.buf<double>("st.pk." + std::to_string(ell), 2 * hb.nb);
@@ -1235,8 +1254,10 @@ struct Engine {
   // Flip-averaged shot-noise field on the octant 0 <= a, b, c <= n/2:
   // three DCT-I passes of n/2 + 1 points, each a batched real FFT of length
   // n of the lines' even extensions, with tiled transposes between them.
+  // planes: the field's FP32 planes [kz][x][y] when its R2C-layout
+  // spectrum was not formed (both legs that field).
   Xi twopt_xi_octant(const FieldSpec<Real>& fa, const FieldSpec<Real>& fb,
-                     cplx shot) {
+                     cplx shot, const float2* planes = nullptr) {
     const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
     const int64_t l1 = int64_t(hx + 1) * (hy + 1);
     const int64_t l2 = int64_t(hx + 1) * (hz + 1);
@@ -1249,11 +1270,18 @@ struct Engine {
     float2* out = ctx.buf<float2>("xio.out", nout);
     const cplx a0(fa.k0.re, fa.k0.im), b0(fb.k0.re, fb.k0.im);
     const cplx p0 = (a0 * std::conj(b0) - shot) / g.vol;
-    launch_xi_octant_spectrum(
-        ctx, g, reinterpret_cast<const float2*>(fa.re),
-        reinterpret_cast<const float2*>(fb.re), inv_alias_f,
-        float(shot.real()), make_float2(float(p0.real()), float(p0.imag())),
-        fa.k0_dev, fb.k0_dev, replay ? replay->state->count_d : nullptr, ext);
+    if (planes != nullptr)
+      launch_xi_octant_planes(
+          ctx, g, planes, inv_alias_f, float(shot.real()),
+          make_float2(float(p0.real()), float(p0.imag())), fa.k0_dev,
+          fb.k0_dev, replay ? replay->state->count_d : nullptr, ext);
+    else
+      launch_xi_octant_spectrum(
+          ctx, g, reinterpret_cast<const float2*>(fa.re),
+          reinterpret_cast<const float2*>(fb.re), inv_alias_f,
+          float(shot.real()), make_float2(float(p0.real()), float(p0.imag())),
+          fa.k0_dev, fb.k0_dev, replay ? replay->state->count_d : nullptr,
+          ext);
     auto pass = [&](int n, int64_t lines) {
       cufftHandle h = ctx.plan1d(CUFFT_R2C, n, int(lines));
       TRVG_CUFFT(cufftSetStream(h, ctx.stream));
@@ -2308,6 +2336,22 @@ struct Engine {
                         ff_applicable(dn, dn, la0, lb0, pairs, hb, M, K);
       float2* zfull =
           fuse ? ctx.buf<float2>("mesh.zplanes", size_t(g.nhalf)) : nullptr;
+      // The octant shot-noise field is the only reader of the mesh's FP32
+      // spectrum when every term's legs take the float-float fields (which
+      // read the mesh) and the two-point statistics read the float-float
+      // cube: it then reads the planes, and the spectrum is not formed.
+      auto planes_only = [&]() {
+        if (dn.re != nf.re || ctx.shell_fields_fp64 ||
+            !stats_read_cube(hb, dn, nf))
+          return false;
+        for (const Term& t : terms) {
+          const Leg la{p.ell1, t.m1}, lb{p.ell2, t.m2};
+          if (!real_fields(dn, dn, la, lb, M) ||
+              !ff_applicable(dn, dn, la, lb, pairs, hb, M, K))
+            return false;
+        }
+        return true;
+      };
       if (fuse && ctx.overlap && !ctx.profiling && replay == nullptr) {
         const cudaStream_t main = ctx.stream, side = ctx.side_stream();
         // The float-float forward transform of the mesh is submitted first;
@@ -2315,11 +2359,12 @@ struct Engine {
         // follow its z pass on the second stream, next to its y and x
         // passes and the shell fields (FP32-issue-bound).
         ff_forward(dn, 2 * K[0], zfull, ctx.ev_fork);
+        const bool only = planes_only();
         TRVG_CUDA(cudaStreamWaitEvent(side, ctx.ev_fork, 0));
         ctx.stream = side;
         try {
-          finish_pending_r2c_xy(zfull);
-          xi = twopt_xi_octant(dn, nf, shot);
+          finish_pending_r2c_xy(zfull, !only);
+          xi = twopt_xi_octant(dn, nf, shot, only ? zfull : nullptr);
         } catch (...) {
           ctx.stream = main;
           throw;
@@ -2329,8 +2374,9 @@ struct Engine {
         forked = true;
       } else if (fuse) {
         ff_forward(dn, 2 * K[0], zfull);
-        finish_pending_r2c_xy(zfull);
-        xi = twopt_xi_octant(dn, nf, shot);
+        const bool only = planes_only();
+        finish_pending_r2c_xy(zfull, !only);
+        xi = twopt_xi_octant(dn, nf, shot, only ? zfull : nullptr);
       } else {
         run_pending_r2c();
         xi = octant ? twopt_xi_octant(dn, nf, shot) : twopt_xi(dn, nf, shot);

@@ -167,6 +167,12 @@ void launch_xi_octant_spectrum(Context& ctx, const Geom& g, const float2* fa,
                                float shot, float2 p0, const double* k0a,
                                const double* k0b, const double* shotp,
                                float* ext);
+// The same from one field's FP32 planes planes[kz][x][y] (both legs that
+// field).
+void launch_xi_octant_planes(Context& ctx, const Geom& g, const float2* planes,
+                             const float* const inv_alias[3], float shot,
+                             float2 p0, const double* k0a, const double* k0b,
+                             const double* shotp, float* ext);
 // dst[s dS + k dK + r] = dst[s dS + k dK + len - r] = src[s sS + r sR + k].x.
 void launch_octant_transpose(Context& ctx, const float2* src, int64_t sS,
                              int64_t sR, float* dst, int64_t dS, int64_t dK,

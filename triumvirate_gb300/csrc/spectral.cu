@@ -1174,6 +1174,63 @@ xi_octant_spectrum_kernel(int n0, int n1, int nzh, const float2* fa,
   }
 }
 
+// The same flip-averaged spectrum of one field from its FP32 planes
+// planes[r][x][y] (the mesh's z transform completed along x and y, before
+// any transpose into the R2C layout): per p a 32 (q) x 32 (r) tile is
+// read along y, averaged over the four (+-x, +-y) images and written along
+// z through shared memory.
+__global__ void __launch_bounds__(256)
+xi_octant_planes_kernel(int n0, int n1, int nzh, const float2* planes,
+                        const float* iax, const float* iay, const float* iaz,
+                        float shot, float inv_vol, float2 p0,
+                        const double* k0a, const double* k0b,
+                        const double* shotp, double vol, float* ext) {
+  __shared__ float tile[32][33];
+  if (k0a != nullptr) {
+    const double ar = k0a[0], ai = k0a[1], br = k0b[0], bi = k0b[1];
+    shot = float(shotp[0]);
+    p0 = make_float2(float((ar * br + ai * bi - shotp[0]) / vol),
+                     float((ai * br - ar * bi - shotp[1]) / vol));
+  }
+  const int hy = n1 / 2, hz = nzh - 1, nz = 2 * hz;
+  const int pp = blockIdx.z;
+  const int q0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t plane = int64_t(n0) * n1;
+  const int is[2] = {pp, (n0 - pp) % n0};
+  for (int k = ty; k < 32; k += 8) {
+    const int r = r0 + k, q = q0 + tx;
+    float v = 0.f;
+    if (r <= hz && q <= hy) {
+      const int js[2] = {q, (n1 - q) % n1};
+      float acc = 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = is[u >> 1], j = js[u & 1];
+        if (i == 0 && j == 0 && r == 0) {
+          acc += p0.x;
+        } else {
+          const float2 a = planes[int64_t(r) * plane + int64_t(i) * n1 + j];
+          const float inv = iax[i] * iay[j] * iaz[r];
+          acc += ((a.x * a.x + a.y * a.y) * inv - shot) * inv_vol;
+        }
+      }
+      v = 0.25f * acc;
+    }
+    tile[k][tx] = v;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int q = q0 + k, r = r0 + tx;
+    if (q <= hy && r <= hz) {
+      float* line = ext + (int64_t(pp) * (hy + 1) + q) * nz;
+      const float v = tile[tx][k];
+      line[r] = v;
+      if (r != 0 && r != hz) line[nz - r] = v;
+    }
+  }
+}
+
 // Real parts of R2C outputs, transposed into the even extensions of the
 // next axis: for slab s, src row r and column k,
 //   dst[s dS + k dK + r] = dst[s dS + k dK + (len - r)] = src[s sS + r sR + k].x
@@ -1355,6 +1412,19 @@ void launch_xi_octant_spectrum(Context& ctx, const Geom& g, const float2* fa,
   xi_octant_spectrum_kernel<<<grid_for(total, 256), 256, 0, ctx.stream>>>(
       g.n[0], g.n[1], g.nzh, fa, fb, inv_alias[0], inv_alias[1], inv_alias[2],
       shot, float(1. / g.vol), p0, k0a, k0b, shotp, g.vol, ext);
+  TRVG_LAUNCHED(ctx);
+}
+
+void launch_xi_octant_planes(Context& ctx, const Geom& g, const float2* planes,
+                             const float* const inv_alias[3], float shot,
+                             float2 p0, const double* k0a, const double* k0b,
+                             const double* shotp, float* ext) {
+  const int hx = g.n[0] / 2, hy = g.n[1] / 2, hz = g.n[2] / 2;
+  dim3 grid((hy + 1 + 31) / 32, (hz + 1 + 31) / 32, hx + 1);
+  TRVG_KBEGIN(ctx, "xi_octant_kernel");
+  xi_octant_planes_kernel<<<grid, 256, 0, ctx.stream>>>(
+      g.n[0], g.n[1], g.nzh, planes, inv_alias[0], inv_alias[1],
+      inv_alias[2], shot, float(1. / g.vol), p0, k0a, k0b, shotp, g.vol, ext);
   TRVG_LAUNCHED(ctx);
 }
 
