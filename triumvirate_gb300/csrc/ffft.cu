@@ -212,6 +212,17 @@ __device__ __forceinline__ void ff_stage_body(float4* A, int nl, int ln,
   __syncthreads();
 }
 
+// Blocks per SM the inverse passes are compiled for: the radix sets whose
+// kernels fit fewer registers without spills (checked with -Xptxas -v:
+// {3, 5} in 80 registers, its z pass in 64; {2, 3} in 79) run more warps
+// per SM; the others need up to 128 registers.
+template <int MASK, bool ZPASS>
+constexpr int inv_min_blocks() {
+  return MASK == (kRadix3 | kRadix5) ? (ZPASS ? 4 : 3)
+         : MASK == (kRadix2 | kRadix3) ? 3
+                                       : 2;
+}
+
 // Butterflies per lane when one warp transforms a line: two of radix 8 in
 // plans of radix 8 alone (n = 512 has 64 per stage), where the kernels
 // still fit 128 registers without spills; one in mixed plans.
@@ -589,7 +600,7 @@ __global__ void ff_build_F_kernel(Geom g, FFBuild bd, int M2, const float4* cube
 // x lines (f, c, b in band; only the listed ones when band.xl is set) of
 // E[f][c][b][a]; writes Y1[f][c][a][b].
 template <int MASK>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, inv_min_blocks<MASK, false>())
 ff_inv_x_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* E,
                 __grid_constant__ const FFPlan P, int LB, float4* Y1,
                 FFBand band) {
@@ -633,7 +644,7 @@ ff_inv_x_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* E,
 // band.yoff set field by field over the planes c <= kz[f]; writes
 // Y2[f][a][b][c].
 template <int MASK>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, inv_min_blocks<MASK, false>())
 ff_inv_y_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* Y1,
                 __grid_constant__ const FFPlan P, int LB, float4* Y2,
                 FFBand band) {
@@ -700,7 +711,7 @@ ff_inv_y_kernel(int M0, int M1, int nf, int Kf, int Kcf, const float4* Y1,
 // lines per complex transform; writes the real fields out[f][a][b][z]
 // (hi words, correctly rounded) and their lo words unless out_lo is null.
 template <int MASK>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, inv_min_blocks<MASK, true>())
 ff_inv_z_kernel(int M0, int M1, int M2, int nf, int Kcf, const float4* Y2,
                 __grid_constant__ const FFPlan P, int LB, float* out,
                 float* out_lo, int64_t ld, const int* kz) {
@@ -915,6 +926,7 @@ void with_grid_radix_set(const FFPlan& P, F&& f) {
   dispatch_radix(radix_mask(P), f,
                  RadixSets<kRadix8, kRadix3 | kRadix5, kRadix2 | kRadix3,
                            kRadix8 | kRadix4 | kRadix5,
+                           kRadix8 | kRadix2 | kRadix5,
                            kRadix4 | kRadix3 | kRadix5,
                            kRadix8 | kRadix2 | kRadix3,
                            kRadix2 | kRadix3 | kRadix5>{});
