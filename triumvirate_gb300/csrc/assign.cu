@@ -615,10 +615,11 @@ __device__ __forceinline__ bool fast_particle(const AssignArgs& a,
 
 // SH: the interlacing shadow is deposited too (sre != nullptr).  COMP: FP32
 // meshes with compensation meshes (a.lo_off).
-// Two blocks per SM: at three (85 registers) the TSC kernel spilled 104
-// bytes, and measured 6 % slower than with 128 registers and no spills.
+// TSC and PCS (and the compensated forms) at two blocks per SM: at three
+// (85 registers) the TSC kernel spilled 104 bytes and measured 6 % slower
+// than with 123 registers and no spills.  NGP and CIC fit 85 registers.
 template <int ORDER, class Real, bool SH, bool COMP>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, (COMP || ORDER >= 3) ? 2 : 3)
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
   cd acc = {0., 0.}, acc_s = {0., 0.};
