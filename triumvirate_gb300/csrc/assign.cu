@@ -615,11 +615,14 @@ __device__ __forceinline__ bool fast_particle(const AssignArgs& a,
 
 // SH: the interlacing shadow is deposited too (sre != nullptr).  COMP: FP32
 // meshes with compensation meshes (a.lo_off).
-// TSC and PCS (and the compensated forms) at two blocks per SM: at three
-// (85 registers) the TSC kernel spilled 104 bytes and measured 6 % slower
-// than with 123 registers and no spills.  NGP and CIC fit 85 registers.
+// Blocks per SM by the registers each form needs without spills: TSC and
+// PCS at two (at three, 85 registers, the TSC kernel spilled 104 bytes and
+// measured 6 % slower), their compensated forms at one (at two they
+// spilled 0.3-2 KB: 7 % slower for the survey's PCS deposit), NGP and CIC
+// at three (two when compensated).
 template <int ORDER, class Real, bool SH, bool COMP>
-__global__ void __launch_bounds__(256, (COMP || ORDER >= 3) ? 2 : 3)
+__global__ void __launch_bounds__(256, ORDER >= 3 ? (COMP ? 1 : 2)
+                                                  : (COMP ? 2 : 3))
 assign_kernel(AssignArgs a, Real* re, Real* im, Real* sre, Real* sim,
               double* sums) {
   cd acc = {0., 0.}, acc_s = {0., 0.};
@@ -984,8 +987,10 @@ ylm_weight_sums_kernel(DevCatalogue cat, YlmTargets ts, double* out) {
   }
 }
 
+// Compensated TSC / PCS forms at one block per SM: at two they spilled
+// 64-2080 bytes (3 % slower for the survey's B_202 deposit).
 template <int ORDER, bool SH, bool COMP>
-__global__ void __launch_bounds__(256, COMP ? 2 : 1)
+__global__ void __launch_bounds__(256, (COMP && ORDER <= 2) ? 2 : 1)
 assign_ylm_kernel(AssignArgs a, YlmTargets ts) {
   const int64_t np = a.cat.count(), p0 = a.cat.first();
   for (int64_t p = p0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
