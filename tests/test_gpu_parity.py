@@ -761,6 +761,32 @@ def test_float_float_transforms_match_fp64(bins, degrees, form):
     assert_per_bin(fwd, ref, 'bk_raw', RTOL_FP32_FFT)
 
 
+@pytest.mark.parametrize("degrees", [(0, 0, 0), (2, 0, 2)])
+def test_float_float_path_on_non_cubic_mesh(degrees):
+    """A cubic box on a 64 x 48 x 80 mesh keeps the float-float shell fields
+    (one band K on all axes, M = 30 below every mesh axis; forward passes
+    over lines of 64, 48 and 80 points), while its cells are not cubic, so
+    the shot-noise field is the full-mesh one (the octant form and the
+    z-pass planes need cubic cells, i.e. a cubic mesh here): both agree
+    with FP64 per bin."""
+    box, n = 800., 60000
+    pos = _uniform(n, box, seed=91)
+    binning = Binning('fourier', 'lin', 0.005, 0.05, 5)
+
+    def run(precision):
+        cat = ParticleCatalogue(*pos.T, nz=n / box ** 3)
+        return compute_bispec_in_gpp_box(
+            cat, degrees=degrees, binning=binning, form='diag',
+            sampling_params=_sampling(precision, [64, 48, 80], box=box))
+    got, ref = run('fp32mixed'), run('fp64')
+    assert np.array_equal(got['nmodes_1'], ref['nmodes_1'])
+    for k in ('bk_raw', 'bk_shot'):
+        scale = np.max(np.abs(ref[k]))
+        assert np.max(np.abs(got[k] - ref[k])) <= 1e-6 * scale, (
+            k, float(np.max(np.abs(got[k] - ref[k])) / scale))
+        assert_per_bin(got[k], ref[k], k, RTOL_FP32_FFT)
+
+
 # ---------------------------------------------------------------------------
 # Shared-memory tiled deposit (32^3 tiles) against the oracle and the
 # per-particle atomic deposit
