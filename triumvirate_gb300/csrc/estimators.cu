@@ -672,7 +672,12 @@ struct Engine {
         launch_weight_sum(ctx, part.cat, part.ws, wsum);
     }
     const double* wsum_im = (wsum != nullptr) ? wsum + 1 : nullptr;
-    launch_fill_offset<Real>(ctx, mre, g.nmesh, wsum, hsum, lo);
+    if (prefill_cells == int64_t(cells) && on_host && !cplx && !interlace &&
+        parts.size() == 1)
+      TRVG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.ev_join, 0));
+    else
+      launch_fill_offset<Real>(ctx, mre, g.nmesh, wsum, hsum, lo);
+    prefill_cells = 0;
     if (mim) launch_fill_offset<Real>(ctx, mim, g.nmesh, wsum_im, 0., lo);
     if (sre) launch_fill_offset<Real>(ctx, sre, g.nmesh, wsum, hsum, lo);
     if (sim) launch_fill_offset<Real>(ctx, sim, g.nmesh, wsum_im, 0., lo);
@@ -891,6 +896,10 @@ struct Engine {
     Real* mesh = nullptr;
     C* out = nullptr;
   } pending_r2c;
+  // The mesh buffer "mesh.re" already filled with the offset for a field
+  // of `prefill_cells` cells on the second stream (make_field waits for
+  // ctx.ev_join instead of filling it).
+  int64_t prefill_cells = 0;
 
   // The deferred R2C of the mesh whose transform along z the float-float z
   // pass has written plane by plane into `planes`: the x and y transforms
@@ -2243,6 +2252,32 @@ struct Engine {
     if (replay != nullptr && survey)
       throw_error(TRVG_ERR_INVALID_PARAMETER,
                   "Batch replay covers periodic-box bispectra only.");
+    // A periodic-box mesh of unit weights starts at minus its mean, which
+    // the particle count alone fixes: the second stream fills it while the
+    // catalogue is copied and sorted (after all earlier work on the
+    // context's stream, which may still read the buffer).
+    prefill_cells = 0;
+    if (sizeof(Real) == 4 && !survey && replay == nullptr && ctx.overlap &&
+        !ctx.profiling && !interlace && data != nullptr && data->n > 0 &&
+        data->w == nullptr) {
+      const int64_t lo = mesh_lo_off(false);
+      const int64_t cells = g.nmesh + lo;
+      Real* mre = ctx.buf<Real>("mesh.re", size_t(cells));
+      const cudaStream_t main = ctx.stream, side = ctx.side_stream();
+      TRVG_CUDA(cudaEventRecord(ctx.ev_fork, main));
+      TRVG_CUDA(cudaStreamWaitEvent(side, ctx.ev_fork, 0));
+      ctx.stream = side;
+      try {
+        launch_fill_offset<Real>(ctx, mre, g.nmesh, nullptr,
+                                 double(data->n), lo);
+      } catch (...) {
+        ctx.stream = main;
+        throw;
+      }
+      ctx.stream = main;
+      TRVG_CUDA(cudaEventRecord(ctx.ev_join, side));
+      prefill_cells = cells;
+    }
     const DevCatalogue dd = upload_catalogue(data, "data", survey);
     DevCatalogue dr;
     if (survey) dr = upload_catalogue(rand, "rand", true);
